@@ -1,0 +1,254 @@
+"""ctypes binding of ``lib/libctm_gb300.so`` (C ABI: ``include/ctm_gb300.h``).
+
+There is no fallback: if the library is missing or CUDA is unavailable, the
+first call raises.  Build the library with ``_build.build()`` (or
+``__graft_entry__.build()``).
+"""
+
+import ctypes
+import os
+
+import torch
+
+from . import _build
+
+CTM_OK, CTM_ERR_INVALID, CTM_ERR_UNSUPPORTED, CTM_ERR_WORKSPACE = 0, 1, 2, 3
+CTM_ERR_CUDA, CTM_ERR_NUMERIC, CTM_ERR_TIMEOUT = 4, 5, 6
+PREC = {"fp64": 0, "mixed": 1}
+PROJ = {"half-system": 0, "full-system": 1}
+SVD = {"rsvd": 0, "full-rank": 1}
+
+c_i64 = ctypes.c_int64
+c_i32 = ctypes.c_int32
+c_vp = ctypes.c_void_p
+c_sz_p = ctypes.POINTER(ctypes.c_size_t)
+
+
+class CtmSite(ctypes.Structure):
+    _fields_ = [("A", c_vp), ("C", c_vp * 4), ("E", c_vp * 4),
+                ("c_rows", c_i64 * 4), ("c_cols", c_i64 * 4),
+                ("e_rows", c_i64 * 4), ("e_cols", c_i64 * 4)]
+
+
+class CtmOpts(ctypes.Structure):
+    _fields_ = [("chi", c_i64), ("projectors", c_i32), ("svd_type", c_i32),
+                ("svd_cutoff", ctypes.c_double), ("rsvd_niter", c_i32),
+                ("rsvd_oversampling", c_i32), ("precision", c_i32), ("reserved", c_i32)]
+
+
+SITE_P = ctypes.POINTER(CtmSite)
+SITES_PP = ctypes.POINTER(SITE_P)
+
+_SIGNATURES = {
+    "ctm_version": ([], ctypes.c_char_p),
+    "ctm_last_error": ([], ctypes.c_char_p),
+    "ctm_device_status": ([ctypes.POINTER(ctypes.c_int), c_vp], ctypes.c_int),
+    "ctm_kernel_launches": ([], ctypes.c_ulonglong),
+    "ctm_profile_begin": ([], None),
+    "ctm_profile_end": ([], ctypes.c_int),
+    "ctm_profile_query": ([ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                           ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)],
+                          ctypes.c_int),
+    "ctm_quarter_tensor": ([SITE_P, c_i64, c_i64, c_i32, c_vp, ctypes.POINTER(c_i64), c_i32,
+                            c_vp, c_sz_p, c_vp], ctypes.c_int),
+    "ctm_calculate_projectors": ([SITES_PP, c_i64, c_i64, c_i32, ctypes.POINTER(CtmOpts), c_vp,
+                                  c_vp, c_vp, c_vp, c_vp, c_sz_p, c_vp], ctypes.c_int),
+    "ctm_projector_dims": ([SITES_PP, c_i64, c_i32, ctypes.POINTER(CtmOpts),
+                            ctypes.POINTER(c_i64), ctypes.POINTER(c_i64), ctypes.POINTER(c_i64),
+                            ctypes.POINTER(c_i64), ctypes.POINTER(c_i64)], ctypes.c_int),
+    "ctm_renormalize_boundary": ([SITE_P, c_i64, c_i64, c_i32, c_vp, c_i64, c_vp, c_i64, c_vp,
+                                  c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_sz_p,
+                                  c_vp], ctypes.c_int),
+    "ctm_site_rdm": ([SITE_P, c_i64, c_i64, c_vp, c_vp, c_sz_p, c_vp], ctypes.c_int),
+    "ctm_bond_rdm": ([SITE_P, SITE_P, c_i64, c_i64, c_i32, c_vp, c_vp, c_sz_p, c_vp],
+                     ctypes.c_int),
+    "ctm_svd_lowrank": ([c_vp, c_i64, c_i64, c_i64, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz_p,
+                         c_vp], ctypes.c_int),
+    "ctm_fused_matmul_svd_lowrank": ([c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_i32, c_vp, c_vp,
+                                      c_vp, c_vp, c_i32, c_vp, c_sz_p, c_vp], ctypes.c_int),
+    "ctm_fused_3matmul_svd_lowrank": ([c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_i64,
+                                       c_i64, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz_p, c_vp],
+                                      ctypes.c_int),
+    "ctm_svd_f64": ([c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp, c_sz_p, c_vp], ctypes.c_int),
+    "ctm_matmul": ([c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i32, c_vp, c_sz_p, c_vp],
+                   ctypes.c_int),
+}
+
+_lib = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load():
+    """Loads the library (once) and declares the C signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        raise RuntimeError(f"libctm_gb300.so not found at {path}; build it with "
+                           "__graft_entry__.build() (no CPU fallback exists)")
+    lib = ctypes.CDLL(path)
+    for name, (args, res) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return sorted(_SIGNATURES)
+
+
+def check(status, what=""):
+    if status == CTM_OK:
+        return
+    msg = load().ctm_last_error().decode(errors="replace")
+    text = f"{what}: {msg}" if what else msg
+    if status == CTM_ERR_INVALID:
+        raise ValueError(text)
+    raise RuntimeError(f"[ctm status {status}] {text}")
+
+
+def require_cuda(t, name="tensor"):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise ValueError(f"{name} must be a CUDA tensor (the gb300 backend has no CPU path)")
+    if t.dtype != torch.float64:
+        raise ValueError(f"{name} must be float64, got {t.dtype}")
+
+
+def ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def stream_handle(device=None):
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+class _Workspace:
+    """Per-device scratch buffer, grown on demand and reused stream-ordered."""
+
+    def __init__(self):
+        self.buf = {}
+
+    def get(self, nbytes, device):
+        key = torch.device(device).index
+        b = self.buf.get(key)
+        if b is None or b.numel() < nbytes:
+            size = max(int(nbytes * 1.25), 1 << 20)
+            b = torch.empty(size, dtype=torch.uint8, device=device)
+            self.buf[key] = b
+        return b
+
+
+WORKSPACE = _Workspace()
+_WS_CACHE = {}
+
+
+def call(name, args_before_ws, device, key=None, stream=None):
+    """Calls ``name(*args_before_ws, ws, &ws_bytes, stream)`` following the
+    workspace protocol (size query, then the real call)."""
+    lib = load()
+    fn = getattr(lib, name)
+    stream = stream_handle(device) if stream is None else stream
+    nbytes = _WS_CACHE.get(key) if key is not None else None
+    if nbytes is None:
+        sz = ctypes.c_size_t(0)
+        check(fn(*args_before_ws, None, ctypes.byref(sz), stream), name)
+        nbytes = sz.value
+        if key is not None:
+            _WS_CACHE[key] = nbytes
+    ws = WORKSPACE.get(nbytes, device)
+    sz = ctypes.c_size_t(ws.numel())
+    check(fn(*args_before_ws, ctypes.c_void_p(ws.data_ptr()), ctypes.byref(sz), stream), name)
+
+
+PROFILE_TAGS = {"gett_f64": 0, "tc_gemm": 1, "quarter_tc": 2, "other": 3}
+
+
+def profile_begin():
+    load().ctm_profile_begin()
+
+
+def profile_end():
+    """Returns {tag: (total_ms, total_work, launches)} of the profiled span."""
+    lib = load()
+    check(lib.ctm_profile_end(), "ctm_profile_end")
+    out = {}
+    for name, tag in PROFILE_TAGS.items():
+        ms, work, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+        check(lib.ctm_profile_query(tag, ctypes.byref(ms), ctypes.byref(work), ctypes.byref(n)),
+              "ctm_profile_query")
+        out[name] = (ms.value, work.value, n.value)
+    return out
+
+
+def kernel_launches():
+    return int(load().ctm_kernel_launches())
+
+
+def device_status(device=None):
+    flags = ctypes.c_int(0)
+    check(load().ctm_device_status(ctypes.byref(flags), stream_handle(device)), "ctm_device_status")
+    return flags.value
+
+
+class SiteRef:
+    """A ``CtmSite`` over a site's A, C[0..3], E[0..3] tensors (kept alive)."""
+
+    def __init__(self, site_tensor):
+        A = site_tensor["A"]
+        C = site_tensor["C"]
+        E = site_tensor["E"]
+        require_cuda(A, "A")
+        self.keep = [A.contiguous()]
+        self.D = A.shape[0]
+        self.d = A.shape[4]
+        s = CtmSite()
+        s.A = self.keep[0].data_ptr()
+        for k in range(4):
+            ck = C[k]
+            ek = E[k]
+            require_cuda(ck, f"C[{k}]")
+            require_cuda(ek, f"E[{k}]")
+            ck = ck.contiguous()
+            ek = ek.contiguous()
+            self.keep += [ck, ek]
+            s.C[k] = ck.data_ptr()
+            s.E[k] = ek.data_ptr()
+            s.c_rows[k], s.c_cols[k] = ck.shape
+            s.e_rows[k], s.e_cols[k] = ek.shape[0], ek.shape[1]
+        self.s = s
+        self.device = A.device
+
+    def shapes(self):
+        s = self.s
+        return tuple(tuple(x) for x in (s.c_rows, s.c_cols, s.e_rows, s.e_cols)) + (self.D, self.d)
+
+    @property
+    def pointer(self):
+        return ctypes.pointer(self.s)
+
+
+def opts_struct(config, chi, precision):
+    o = CtmOpts()
+    o.chi = int(chi)
+    proj = getattr(config, "projectors", "half-system")
+    proj = "full-system" if proj is None else proj
+    if proj not in PROJ:
+        raise ValueError(f"Invalid ctmrg projector type: {proj} provided.")
+    svd = getattr(config, "svd_type", "rsvd")
+    if svd not in SVD:
+        raise ValueError(f"Invalid svd type: {svd} provided.")
+    o.projectors = PROJ[proj]
+    o.svd_type = SVD[svd]
+    o.svd_cutoff = float(getattr(config, "svd_cutoff", 1e-12))
+    o.rsvd_niter = int(getattr(config, "rsvd_niter", 2))
+    o.rsvd_oversampling = int(getattr(config, "rsvd_oversampling", 2))
+    if precision not in PREC:
+        raise ValueError(f"Invalid precision: {precision} provided.")
+    o.precision = PREC[precision]
+    return o

@@ -1,0 +1,41 @@
+"""CTMRG configuration of the GB300 backend.
+
+Mirrors ``CTMRGConfig`` of the reference (acetn/ipeps/ipeps_config.py:16-24,
+documented in docs/source/input_settings.rst:45-54) and adds two fields:
+
+* ``backend``   -- "gb300" selects this library (the reference keeps "torch").
+* ``precision`` -- "fp64": every product in FP64, the drop-in path;
+                   "mixed": tensor-core range finder and split-precision
+                   products feeding the projectors (half-system rSVD only).
+
+Any object with the reference's attribute names works as a config; missing
+attributes take the defaults below.
+"""
+
+from dataclasses import dataclass
+from typing import Literal
+
+
+@dataclass
+class CTMRGConfig:
+    steps: int = 40
+    projectors: Literal["half-system", "full-system"] = "half-system"
+    svd_type: Literal["rsvd", "full-rank"] = "rsvd"
+    svd_cutoff: float = 1e-12
+    rsvd_niter: int = 2
+    rsvd_oversampling: int = 2
+    disable_progressbar: bool = False
+    backend: Literal["gb300"] = "gb300"
+    precision: Literal["fp64", "mixed"] = "fp64"
+
+
+def resolve(config):
+    """Returns a ``CTMRGConfig`` from a dict, a reference config object or None."""
+    if config is None:
+        return CTMRGConfig()
+    if isinstance(config, CTMRGConfig):
+        return config
+    if isinstance(config, dict):
+        return CTMRGConfig(**config)
+    fields = CTMRGConfig.__dataclass_fields__
+    return CTMRGConfig(**{k: getattr(config, k) for k in fields if hasattr(config, k)})

@@ -1,0 +1,48 @@
+// Internal operations of the CTMRG library (FP64 engine and helpers).
+#pragma once
+#include "ctm_common.cuh"
+
+namespace ctm {
+
+// C = alpha * einsum(spec, A, B) + beta * C for two-operand contractions whose
+// labels split into batch / row / column / contracted groups (no traces, no
+// outer-only labels).  All views are strided; nothing is copied.
+void einsum(Ctx& c, const char* spec, const View& A, const View& B, const View& C,
+            double alpha = 1.0, double beta = 0.0);
+
+// Deterministic reductions into a device scalar.
+void absmax(Ctx& c, const double* x, int64_t n, double* out);
+void sumsq(Ctx& c, const double* x, int64_t n, double* out);
+// x[i] = x[i] / s  (mode 0: s = *scal, mode 1: s = sqrt(*scal)) for i < n.
+void divide_by(Ctx& c, double* x, int64_t n, const double* scal, int mode);
+// dst (rows x cols, row-major, ld_dst) = src view (2-D strided)
+void copy2d(Ctx& c, const View& src, double* dst, int64_t ld_dst);
+void fill(Ctx& c, double* x, int64_t n, double v);
+
+// --- linear algebra (FP64) ---------------------------------------------------
+// Orthonormal basis of the columns of Y (n x q, row-major): Y := Q.
+// If R != nullptr it receives the q x q upper-triangular factor with Y_in = Q R.
+void orthonormalize(Ctx& c, double* Y, int64_t n, int64_t q, double* R);
+// Thin SVD of X (m x n, row-major, m >= n is not required):
+// X = U diag(S) V^T, U (m x r), S (r) descending, V (n x r), r = min(m, n).
+void svd_thin(Ctx& c, const double* X, int64_t m, int64_t n, double* U, double* S,
+              double* V);
+// Truncation of acetn/renormalization/projectors.py:163-167 on a descending
+// spectrum s (len r): chi_new = min(chi, #{s/s0 > cutoff}); f[i] = 1/sqrt(s_i/s_0)
+// for i < chi_new else 0 (i < cap).
+void truncation_factors(Ctx& c, const double* s, int64_t r, int64_t chi, double cutoff,
+                        double* f, int64_t cap, int64_t* chi_new);
+// x[r, c] *= f[c] for a (rows x cols) block with leading dimension ld.
+void scale_columns(Ctx& c, double* x, int64_t rows, int64_t cols, int64_t ld, const double* f);
+// out (rows x chi_new) contiguous = in (rows x cap, ld cap) * f (per column;
+// f == nullptr: no scaling), with chi_new read from device memory.
+void scale_columns_compact(Ctx& c, const double* in, int64_t rows, int64_t cap,
+                           const double* f, const int64_t* chi_new, double* out);
+
+const char* g_last_error_cstr();
+
+// Device-side failure flags (bit set by kernels: 1 = factorization failed,
+// 2 = iteration limit reached); read and cleared by ctm_device_status().
+int* status_flags(Ctx& c);
+
+}  // namespace ctm

@@ -1,0 +1,427 @@
+// FP64 tensor-contraction engine: a strided GETT kernel (no permute copies)
+// behind a two-operand einsum planner, plus deterministic reductions and
+// elementwise helpers.
+//
+// Every einsum of the reference's CTMRG path (acetn/renormalization/*.py,
+// acetn/measurement/rdm.py) is a two-operand contraction; the planner sorts
+// its labels into batch / row (M) / column (N) / contracted (K) groups,
+// merges modes that are adjacent in every operand, and launches one kernel
+// whose tile loaders decode multi-mode indices into strided addresses.
+#include "engine.cuh"
+
+#include <algorithm>
+#include <map>
+
+namespace ctm {
+
+namespace {
+
+constexpr int kMaxModes = 4;
+
+struct Mode {
+  int64_t ext;
+  int64_t s0;  // stride in the first operand of the pair
+  int64_t s1;  // stride in the second operand of the pair
+};
+
+struct Group {
+  int n;
+  Mode m[kMaxModes];
+};
+
+struct GettArgs {
+  const double* A;
+  const double* B;
+  double* C;
+  Group M, N, K;  // M: (A, C) strides, N: (B, C), K: (A, B)
+  int64_t Mt, Nt, Kt;
+  int64_t bext, bsa, bsb, bsc;
+  double alpha, beta;
+  int splitk;
+  int64_t kchunk;
+  double* part;
+};
+
+__device__ __forceinline__ void decode(const Group& g, int64_t idx, int64_t& o0, int64_t& o1) {
+  o0 = 0;
+  o1 = 0;
+#pragma unroll
+  for (int j = kMaxModes - 1; j >= 0; --j) {
+    if (j < g.n) {
+      const int64_t e = g.m[j].ext;
+      const int64_t r = idx % e;
+      idx /= e;
+      o0 += r * g.m[j].s0;
+      o1 += r * g.m[j].s1;
+    }
+  }
+}
+
+constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
+
+// One 64x64 output tile per CTA, 4x4 outputs per thread, K staged through
+// shared memory 16 at a time.  FP64 FMAs are the bound on this part, so the
+// loaders favour generality (any strides) over vector width.
+__global__ void __launch_bounds__(NT) gett_f64_kernel(const GettArgs p) {
+  __shared__ int64_t sAm[BM], sCm[BM], sBn[BN], sCn[BN];
+  __shared__ int64_t sAk[BK], sBk[BK];
+  __shared__ double As[BK][BM + 1];
+  __shared__ double Bs[BK][BN + 1];
+
+  const int tid = threadIdx.x;
+  const int64_t m0 = static_cast<int64_t>(blockIdx.x) * BM;
+  const int64_t n0 = static_cast<int64_t>(blockIdx.y) * BN;
+  const int64_t z = blockIdx.z;
+  const int64_t batch = z % p.bext;
+  const int64_t split = z / p.bext;
+  const double* A = p.A + batch * p.bsa;
+  const double* B = p.B + batch * p.bsb;
+
+  if (tid < BM) {
+    const int64_t m = m0 + tid;
+    if (m < p.Mt) decode(p.M, m, sAm[tid], sCm[tid]);
+    else { sAm[tid] = -1; sCm[tid] = -1; }
+  } else if (tid < BM + BN) {
+    const int t = tid - BM;
+    const int64_t n = n0 + t;
+    if (n < p.Nt) decode(p.N, n, sBn[t], sCn[t]);
+    else { sBn[t] = -1; sCn[t] = -1; }
+  }
+  const int64_t kb = split * p.kchunk;
+  const int64_t ke = min(kb + p.kchunk, p.Kt);
+
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+
+  const int tx = tid & 15, ty = tid >> 4;
+  for (int64_t k0 = kb; k0 < ke; k0 += BK) {
+    __syncthreads();
+    if (tid < BK) {
+      const int64_t k = k0 + tid;
+      if (k < ke) decode(p.K, k, sAk[tid], sBk[tid]);
+      else { sAk[tid] = -1; sBk[tid] = -1; }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < (BM * BK) / NT; ++e) {
+      const int lin = tid + e * NT;
+      const int mm = lin % BM, kk = lin / BM;
+      const int64_t am = sAm[mm], ak = sAk[kk];
+      As[kk][mm] = (am >= 0 && ak >= 0) ? A[am + ak] : 0.0;
+      const int64_t bn = sBn[mm], bk = sBk[kk];
+      Bs[kk][mm] = (bn >= 0 && bk >= 0) ? B[bk + bn] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+  }
+
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int mi = ty + 16 * i;
+    const int64_t m = m0 + mi;
+    if (m >= p.Mt) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int nj = tx + 16 * j;
+      const int64_t n = n0 + nj;
+      if (n >= p.Nt) continue;
+      if (p.splitk > 1) {
+        p.part[((split * p.bext + batch) * p.Mt + m) * p.Nt + n] = acc[i][j];
+      } else {
+        double* c = p.C + batch * p.bsc + sCm[mi] + sCn[nj];
+        const double v = p.alpha * acc[i][j];
+        *c = (p.beta != 0.0) ? fma(p.beta, *c, v) : v;
+      }
+    }
+  }
+}
+
+// Sums split-K partial tiles in a fixed order (deterministic) into C.
+__global__ void gett_splitk_reduce(const GettArgs p) {
+  const int64_t total = p.bext * p.Mt * p.Nt;
+  for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < total;
+       idx += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t n = idx % p.Nt;
+    const int64_t m = (idx / p.Nt) % p.Mt;
+    const int64_t b = idx / (p.Nt * p.Mt);
+    double s = 0.0;
+    for (int t = 0; t < p.splitk; ++t) s += p.part[((t * p.bext + b) * p.Mt + m) * p.Nt + n];
+    int64_t am, cm, bn, cn;
+    decode(p.M, m, am, cm);
+    decode(p.N, n, bn, cn);
+    double* c = p.C + b * p.bsc + cm + cn;
+    const double v = p.alpha * s;
+    *c = (p.beta != 0.0) ? fma(p.beta, *c, v) : v;
+  }
+}
+
+struct Label {
+  char ch;
+  int64_t ext;
+  int64_t sa, sb, sc;  // 0 when absent
+  bool ia, ib, ic;
+};
+
+// Merges modes (already ordered outer -> inner) that are contiguous in both
+// operands; drops unit extents.
+void merge(std::vector<Mode>& v) {
+  std::vector<Mode> out;
+  for (const Mode& md : v) {
+    if (md.ext == 1) continue;
+    if (!out.empty()) {
+      Mode& o = out.back();
+      if (o.s0 == md.ext * md.s0 && o.s1 == md.ext * md.s1) {
+        o.ext *= md.ext;
+        o.s0 = md.s0;
+        o.s1 = md.s1;
+        continue;
+      }
+    }
+    out.push_back(md);
+  }
+  v.swap(out);
+}
+
+Group to_group(std::vector<Mode> v, const char* what) {
+  merge(v);
+  CTM_REQUIRE(v.size() <= size_t(kMaxModes), CTM_ERR_UNSUPPORTED,
+              std::string("einsum: too many ") + what + " modes after merging");
+  Group g{};
+  g.n = static_cast<int>(v.size());
+  for (size_t i = 0; i < v.size(); ++i) g.m[i] = v[i];
+  return g;
+}
+
+int64_t group_size(const Group& g) {
+  int64_t s = 1;
+  for (int i = 0; i < g.n; ++i) s *= g.m[i].ext;
+  return s;
+}
+
+}  // namespace
+
+void einsum(Ctx& c, const char* spec, const View& A, const View& B, const View& C, double alpha,
+            double beta) {
+  std::string s(spec);
+  const size_t comma = s.find(','), arrow = s.find("->");
+  CTM_REQUIRE(comma != std::string::npos && arrow != std::string::npos, CTM_ERR_INVALID,
+              "einsum: bad spec " + s);
+  const std::string la = s.substr(0, comma), lb = s.substr(comma + 1, arrow - comma - 1),
+                    lc = s.substr(arrow + 2);
+  CTM_REQUIRE(int(la.size()) == A.nd && int(lb.size()) == B.nd && int(lc.size()) == C.nd,
+              CTM_ERR_INVALID, "einsum: rank mismatch in " + s);
+  std::map<char, Label> labels;
+  auto add = [&](const std::string& l, const View& v, int which) {
+    for (size_t i = 0; i < l.size(); ++i) {
+      Label& L = labels[l[i]];
+      if (L.ch == 0) {
+        L.ch = l[i];
+        L.ext = v.shape[i];
+      }
+      CTM_REQUIRE(L.ext == v.shape[i], CTM_ERR_INVALID,
+                  std::string("einsum: extent mismatch for label ") + l[i] + " in " + s);
+      if (which == 0) { L.ia = true; L.sa = v.stride[i]; }
+      if (which == 1) { L.ib = true; L.sb = v.stride[i]; }
+      if (which == 2) { L.ic = true; L.sc = v.stride[i]; }
+    }
+  };
+  add(la, A, 0);
+  add(lb, B, 1);
+  add(lc, C, 2);
+
+  std::vector<Label> bl, ml, nl, kl;
+  for (auto& kv : labels) {
+    const Label& L = kv.second;
+    if (L.ia && L.ib && L.ic) bl.push_back(L);
+    else if (L.ia && L.ic && !L.ib) ml.push_back(L);
+    else if (L.ib && L.ic && !L.ia) nl.push_back(L);
+    else if (L.ia && L.ib && !L.ic) kl.push_back(L);
+    else
+      CTM_REQUIRE(L.ext == 1, CTM_ERR_UNSUPPORTED,
+                  std::string("einsum: unsupported label pattern for ") + L.ch + " in " + s);
+  }
+  auto by = [](int64_t Label::*key) {
+    return [key](const Label& x, const Label& y) { return x.*key > y.*key; };
+  };
+  std::sort(ml.begin(), ml.end(), by(&Label::sc));
+  std::sort(nl.begin(), nl.end(), by(&Label::sc));
+  std::sort(kl.begin(), kl.end(), by(&Label::sa));
+  std::sort(bl.begin(), bl.end(), by(&Label::sc));
+
+  std::vector<Mode> mm, nn, kk, bb;
+  for (auto& L : ml) mm.push_back({L.ext, L.sa, L.sc});
+  for (auto& L : nl) nn.push_back({L.ext, L.sb, L.sc});
+  for (auto& L : kl) kk.push_back({L.ext, L.sa, L.sb});
+  GettArgs p{};
+  p.M = to_group(mm, "row");
+  p.N = to_group(nn, "column");
+  p.K = to_group(kk, "contracted");
+  // batch: at most one mode after merging (all three strides must merge)
+  int64_t bext = 1, bsa = 0, bsb = 0, bsc = 0;
+  {
+    std::vector<Label> bv;
+    for (auto& L : bl)
+      if (L.ext != 1) bv.push_back(L);
+    for (size_t i = 0; i < bv.size(); ++i) {
+      if (i == 0) {
+        bext = bv[0].ext; bsa = bv[0].sa; bsb = bv[0].sb; bsc = bv[0].sc;
+      } else {
+        const Label& L = bv[i];
+        CTM_REQUIRE(bsa == L.ext * L.sa && bsb == L.ext * L.sb && bsc == L.ext * L.sc,
+                    CTM_ERR_UNSUPPORTED, "einsum: non-mergeable batch modes in " + s);
+        bext *= L.ext; bsa = L.sa; bsb = L.sb; bsc = L.sc;
+      }
+    }
+  }
+  p.A = A.p;
+  p.B = B.p;
+  p.C = C.p;
+  p.Mt = group_size(p.M);
+  p.Nt = group_size(p.N);
+  p.Kt = group_size(p.K);
+  p.bext = bext; p.bsa = bsa; p.bsb = bsb; p.bsc = bsc;
+  p.alpha = alpha;
+  p.beta = beta;
+  if (p.Mt == 0 || p.Nt == 0) return;
+
+  const int64_t tiles = ((p.Mt + BM - 1) / BM) * ((p.Nt + BN - 1) / BN) * bext;
+  int splitk = 1;
+  const int64_t target = 2 * 152;
+  if (tiles < target && p.Kt >= 4 * BK) {
+    splitk = static_cast<int>(std::min<int64_t>((target + tiles - 1) / tiles, p.Kt / (4 * BK)));
+    splitk = std::max(splitk, 1);
+  }
+  p.kchunk = ((p.Kt + splitk - 1) / splitk + BK - 1) / BK * BK;
+  if (p.Kt == 0) p.kchunk = BK;
+  splitk = static_cast<int>(std::max<int64_t>(1, (p.Kt + p.kchunk - 1) / p.kchunk));
+  p.splitk = splitk;
+  Scope scope(c);
+  if (splitk > 1) p.part = c.alloc<double>(size_t(splitk) * bext * p.Mt * p.Nt);
+  if (c.sizing()) return;
+  dim3 grid(static_cast<unsigned>((p.Mt + BM - 1) / BM), static_cast<unsigned>((p.Nt + BN - 1) / BN),
+            static_cast<unsigned>(bext * splitk));
+  CTM_REQUIRE(grid.y <= 65535 && grid.z <= 65535, CTM_ERR_UNSUPPORTED, "einsum: grid too large");
+  {
+    KernelTimer timer(c.stream, kTagGettF64, 2.0 * double(p.Mt) * p.Nt * p.Kt * bext);
+    gett_f64_kernel<<<grid, NT, 0, c.stream>>>(p);
+    CTM_LAUNCH_CHECK();
+  }
+  if (splitk > 1) {
+    gett_splitk_reduce<<<grid_for(bext * p.Mt * p.Nt, 256), 256, 0, c.stream>>>(p);
+    CTM_LAUNCH_CHECK();
+  }
+}
+
+// ----------------------------------------------------------------- reductions
+namespace {
+
+constexpr int RT = 256;
+
+__device__ __forceinline__ double combine(double a, double b, int op) {
+  return op == 0 ? fmax(a, b) : a + b;
+}
+
+// Grid-stride partial reduction: op 0 = max |x|, op 1 = sum x^2.
+__global__ void reduce_partial(const double* __restrict__ x, int64_t n, double* part, int op) {
+  __shared__ double sh[RT];
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * int64_t(RT) + threadIdx.x; i < n; i += int64_t(gridDim.x) * RT) {
+    const double v = x[i];
+    acc = op == 0 ? fmax(acc, fabs(v)) : fma(v, v, acc);
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = RT / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = combine(sh[threadIdx.x], sh[threadIdx.x + s], op);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void reduce_final(const double* part, int nparts, double* out, int op) {
+  __shared__ double sh[RT];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += RT) acc = combine(acc, part[i], op);
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = RT / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = combine(sh[threadIdx.x], sh[threadIdx.x + s], op);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = sh[0];
+}
+
+void reduce(Ctx& c, const double* x, int64_t n, double* out, int op) {
+  const int blocks = grid_for(n, RT, 152 * 4);
+  Scope scope(c);
+  double* part = c.alloc<double>(blocks);
+  if (c.sizing()) return;
+  reduce_partial<<<blocks, RT, 0, c.stream>>>(x, n, part, op);
+  CTM_LAUNCH_CHECK();
+  reduce_final<<<1, RT, 0, c.stream>>>(part, blocks, out, op);
+  CTM_LAUNCH_CHECK();
+}
+
+__global__ void divide_kernel(double* x, int64_t n, const double* scal, int mode) {
+  const double s = mode == 0 ? scal[0] : sqrt(scal[0]);
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    x[i] = x[i] / s;
+}
+
+__global__ void copy2d_kernel(const double* src, int64_t rows, int64_t cols, int64_t s0,
+                              int64_t s1, double* dst, int64_t ld) {
+  const int64_t total = rows * cols;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < total;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t r = i / cols, q = i % cols;
+    dst[r * ld + q] = src[r * s0 + q * s1];
+  }
+}
+
+__global__ void fill_kernel(double* x, int64_t n, double v) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    x[i] = v;
+}
+
+}  // namespace
+
+void absmax(Ctx& c, const double* x, int64_t n, double* out) { reduce(c, x, n, out, 0); }
+void sumsq(Ctx& c, const double* x, int64_t n, double* out) { reduce(c, x, n, out, 1); }
+
+void divide_by(Ctx& c, double* x, int64_t n, const double* scal, int mode) {
+  if (c.sizing() || n == 0) return;
+  divide_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(x, n, scal, mode);
+  CTM_LAUNCH_CHECK();
+}
+
+void copy2d(Ctx& c, const View& src, double* dst, int64_t ld_dst) {
+  CTM_REQUIRE(src.nd == 2, CTM_ERR_INVALID, "copy2d: expects a 2-D view");
+  if (c.sizing() || src.numel() == 0) return;
+  copy2d_kernel<<<grid_for(src.numel(), 256), 256, 0, c.stream>>>(
+      src.p, src.shape[0], src.shape[1], src.stride[0], src.stride[1], dst, ld_dst);
+  CTM_LAUNCH_CHECK();
+}
+
+void fill(Ctx& c, double* x, int64_t n, double v) {
+  if (c.sizing() || n == 0) return;
+  fill_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(x, n, v);
+  CTM_LAUNCH_CHECK();
+}
+
+}  // namespace ctm

@@ -1,0 +1,539 @@
+// FP64 dense linear algebra for the projector construction:
+//  * orthonormalize(): QR of a tall-skinny matrix.  Shifted Cholesky-QR3
+//    (Fukaya, Kannan, Nakatsukasa, Yamamoto, Yanagisawa, SIAM J. Sci. Comput.
+//    42 (2020) A477) built on the GETT engine, with an orthogonality check
+//    and a one-CTA Householder QR that runs instead when the check fails
+//    (numerically rank-deficient input) or the problem is small.
+//  * svd_thin(): one-sided (Hestenes) Jacobi SVD with the round-robin pair
+//    ordering, run as a cooperative multi-CTA kernel with a bounded grid
+//    barrier (Demmel & Veselic, SIAM J. Matrix Anal. Appl. 13 (1992) 1204).
+//  * truncation of the singular spectrum and column scaling of the
+//    projectors (acetn/renormalization/projectors.py:163-167).
+#include "engine.cuh"
+
+#include <algorithm>
+#include <cmath>
+
+namespace ctm {
+
+namespace {
+
+__device__ int g_status_flags;
+
+constexpr int LT = 256;  // threads of one-CTA linear-algebra kernels
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum (all threads get the result).  sh must hold LT/32 doubles.
+__device__ double block_sum(double v, double* sh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int i = 0; i < int(blockDim.x >> 5); ++i) t += sh[i];
+  return t;
+}
+
+// ------------------------------------------------------------- Householder QR
+// One CTA.  Y (n x q, row-major) is overwritten by the explicit Q; R (q x q)
+// receives the triangular factor when non-null.  V (n x q) and beta (q) are
+// scratch.  Runs only when (flags == nullptr) or (*flags & 1) != 0.
+__global__ void __launch_bounds__(LT) householder_qr_kernel(double* Y, int64_t n, int64_t q,
+                                                            double* R, double* V, double* beta,
+                                                            const int* flags, int clear_bit) {
+  if (flags != nullptr && ((*flags) & clear_bit) == 0) return;
+  __shared__ double sh[LT / 32];
+  __shared__ double s_beta, s_alpha;
+  for (int64_t j = 0; j < q; ++j) {
+    // norm of the column below the diagonal
+    double part = 0.0;
+    for (int64_t i = j + threadIdx.x; i < n; i += LT) {
+      const double x = Y[i * q + j];
+      part = fma(x, x, part);
+    }
+    const double nrm2 = block_sum(part, sh);
+    if (threadIdx.x == 0) {
+      const double x0 = Y[j * q + j];
+      const double nrm = sqrt(nrm2);
+      if (nrm == 0.0) {
+        s_alpha = 0.0;
+        s_beta = 0.0;
+      } else {
+        const double alpha = x0 >= 0.0 ? -nrm : nrm;
+        const double v0 = x0 - alpha;
+        // v = x - alpha e1, stored with v0 in place; beta = 2 / (v^T v)
+        const double vtv = nrm2 - x0 * x0 + v0 * v0;
+        s_alpha = alpha;
+        s_beta = vtv > 0.0 ? 2.0 / vtv : 0.0;
+        Y[j * q + j] = v0;
+      }
+    }
+    __syncthreads();
+    const double bj = s_beta;
+    for (int64_t i = j + threadIdx.x; i < n; i += LT) V[i * q + j] = Y[i * q + j];
+    __syncthreads();
+    // trailing update Y[j:, j+1:] -= beta v (v^T Y)
+    for (int64_t c = j + 1; c < q; ++c) {
+      double d = 0.0;
+      for (int64_t i = j + threadIdx.x; i < n; i += LT) d = fma(V[i * q + j], Y[i * q + c], d);
+      const double w = block_sum(d, sh) * bj;
+      for (int64_t i = j + threadIdx.x; i < n; i += LT) Y[i * q + c] -= w * V[i * q + j];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      beta[j] = bj;
+      Y[j * q + j] = s_alpha;  // R diagonal
+    }
+    __syncthreads();
+  }
+  if (R != nullptr) {
+    for (int64_t idx = threadIdx.x; idx < q * q; idx += LT) {
+      const int64_t r = idx / q, c = idx % q;
+      R[idx] = (c >= r) ? Y[r * q + c] : 0.0;
+    }
+  }
+  __syncthreads();
+  // explicit Q = H_0 ... H_{q-1} [I; 0], applied right to left
+  for (int64_t idx = threadIdx.x; idx < n * q; idx += LT) {
+    const int64_t r = idx / q, c = idx % q;
+    Y[idx] = (r == c) ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  for (int64_t j = q - 1; j >= 0; --j) {
+    const double bj = beta[j];
+    if (bj == 0.0) continue;
+    for (int64_t c = j; c < q; ++c) {
+      double d = 0.0;
+      for (int64_t i = j + threadIdx.x; i < n; i += LT) d = fma(V[i * q + j], Y[i * q + c], d);
+      const double w = block_sum(d, sh) * bj;
+      for (int64_t i = j + threadIdx.x; i < n; i += LT) Y[i * q + c] -= w * V[i * q + j];
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------- Cholesky
+// One CTA.  G (q x q) -> Linv (q x q, lower-triangular inverse of the
+// Cholesky factor of G + shift I), Lt (q x q) = L^T (upper).  W is q x q
+// scratch.  shift = 11 (n q + q (q + 1)) u tr(G) when shifted != 0.
+__global__ void __launch_bounds__(LT) cholesky_inverse_kernel(const double* G, int64_t q,
+                                                              int64_t n, int shifted, double* W,
+                                                              double* Linv, double* Lt,
+                                                              int* flags) {
+  __shared__ double sh[LT / 32];
+  __shared__ double s_shift;
+  __shared__ int s_fail;
+  double tr = 0.0;
+  for (int64_t i = threadIdx.x; i < q; i += LT) tr += G[i * q + i];
+  tr = block_sum(tr, sh);
+  if (threadIdx.x == 0) {
+    const double u = 1.1102230246251565e-16;  // 2^-53
+    s_shift = shifted ? 11.0 * (double(n) * q + double(q) * (q + 1)) * u * tr : 0.0;
+    s_fail = 0;
+  }
+  __syncthreads();
+  for (int64_t idx = threadIdx.x; idx < q * q; idx += LT) {
+    const int64_t r = idx / q, c = idx % q;
+    W[idx] = (c <= r) ? G[idx] + ((r == c) ? s_shift : 0.0) : 0.0;
+  }
+  __syncthreads();
+  // right-looking Cholesky on the lower triangle of W
+  for (int64_t j = 0; j < q; ++j) {
+    if (threadIdx.x == 0) {
+      const double d = W[j * q + j];
+      if (!(d > 0.0)) s_fail = 1;
+      W[j * q + j] = d > 0.0 ? sqrt(d) : 1.0;
+    }
+    __syncthreads();
+    const double ljj = W[j * q + j];
+    for (int64_t i = j + 1 + threadIdx.x; i < q; i += LT) W[i * q + j] /= ljj;
+    __syncthreads();
+    const int64_t m = q - j - 1;
+    for (int64_t idx = threadIdx.x; idx < m * m; idx += LT) {
+      const int64_t i = j + 1 + idx / m, k = j + 1 + idx % m;
+      if (k <= i) W[i * q + k] -= W[i * q + j] * W[k * q + j];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && s_fail) atomicOr(flags, 1);
+  // Linv: forward substitution, one column per thread
+  for (int64_t c = threadIdx.x; c < q; c += LT) {
+    for (int64_t i = 0; i < q; ++i) {
+      double v;
+      if (i < c) {
+        v = 0.0;
+      } else {
+        double s = (i == c) ? 1.0 : 0.0;
+        for (int64_t k = c; k < i; ++k) s -= W[i * q + k] * Linv[k * q + c];
+        v = s / W[i * q + i];
+      }
+      Linv[i * q + c] = v;
+    }
+  }
+  if (Lt != nullptr) {
+    for (int64_t idx = threadIdx.x; idx < q * q; idx += LT) {
+      const int64_t r = idx / q, c = idx % q;
+      Lt[idx] = (c >= r) ? W[c * q + r] : 0.0;
+    }
+  }
+}
+
+// Sets flag bit 1 when max |G - I| exceeds tol (NaN counts as failure).
+__global__ void orthogonality_check_kernel(const double* G, int64_t q, double tol, int* flags) {
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int64_t idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
+    const int64_t r = idx / q, c = idx % q;
+    const double e = fabs(G[idx] - (r == c ? 1.0 : 0.0));
+    if (!(e <= tol)) bad = 1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && bad) atomicOr(flags, 1);
+}
+
+// ------------------------------------------------------------- Jacobi SVD
+struct JacobiArgs {
+  double* W;      // p x L, row j = column j being orthogonalised
+  double* J;      // p x p, row j = column j of the accumulated rotation
+  int64_t p, L;
+  int64_t pp;     // p rounded up to even
+  double tol;
+  int max_sweeps;
+  unsigned* bar;  // [0] arrival count, [1] generation, [2] abort, [3..4] sweep flags
+  int* flags;
+  int64_t spin_limit;
+};
+
+// Bounded grid barrier.  Returns false when this CTA gave up waiting (the
+// abort word is then set and the status flag records the timeout).
+__device__ bool grid_sync(const JacobiArgs& a) {
+  __syncthreads();
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    volatile unsigned* gen = a.bar + 1;
+    volatile unsigned* abort_w = a.bar + 2;
+    ok = 1;
+    const unsigned g = *gen;
+    __threadfence();
+    const unsigned arrived = atomicAdd(a.bar, 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(a.bar, 0u);
+      __threadfence();
+      atomicAdd(const_cast<unsigned*>(gen), 1u);
+    } else {
+      int64_t it = 0;
+      while (*gen == g) {
+        if (*abort_w != 0u || ++it > a.spin_limit) {
+          atomicExch(const_cast<unsigned*>(abort_w), 1u);
+          atomicOr(a.flags, 2);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+__device__ __forceinline__ int64_t rr_pos(int64_t i, int64_t r, int64_t pp) {
+  return i == 0 ? 0 : ((i - 1 + r) % (pp - 1)) + 1;
+}
+
+__global__ void __launch_bounds__(64) jacobi_sweeps_kernel(const JacobiArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps_per_cta = blockDim.x >> 5;
+  const int64_t gw = blockIdx.x * warps_per_cta + (threadIdx.x >> 5);
+  const int64_t total_w = gridDim.x * warps_per_cta;
+  const int64_t npairs = a.pp / 2;
+  for (int sweep = 0; sweep < a.max_sweeps; ++sweep) {
+    unsigned* rotated = a.bar + 3 + (sweep & 1);
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(a.bar + 3 + ((sweep + 1) & 1), 0u);
+    for (int64_t r = 0; r < a.pp - 1; ++r) {
+      for (int64_t k = gw; k < npairs; k += total_w) {
+        int64_t i = rr_pos(k, r, a.pp), j = rr_pos(a.pp - 1 - k, r, a.pp);
+        if (i > j) { const int64_t t = i; i = j; j = t; }
+        if (j >= a.p) continue;  // dummy partner
+        double* wi = a.W + i * a.L;
+        double* wj = a.W + j * a.L;
+        double al = 0.0, be = 0.0, ga = 0.0;
+        for (int64_t t = lane; t < a.L; t += 32) {
+          const double x = wi[t], y = wj[t];
+          al = fma(x, x, al);
+          be = fma(y, y, be);
+          ga = fma(x, y, ga);
+        }
+        al = warp_sum(al);
+        be = warp_sum(be);
+        ga = warp_sum(ga);
+        if (al == 0.0 || be == 0.0 || !(fabs(ga) > a.tol * sqrt(al) * sqrt(be))) continue;
+        const double zeta = (be - al) / (2.0 * ga);
+        const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(fma(zeta, zeta, 1.0)));
+        const double cs = 1.0 / sqrt(fma(t, t, 1.0));
+        const double sn = cs * t;
+        for (int64_t u = lane; u < a.L; u += 32) {
+          const double x = wi[u], y = wj[u];
+          wi[u] = cs * x - sn * y;
+          wj[u] = sn * x + cs * y;
+        }
+        double* ji = a.J + i * a.p;
+        double* jj = a.J + j * a.p;
+        for (int64_t u = lane; u < a.p; u += 32) {
+          const double x = ji[u], y = jj[u];
+          ji[u] = cs * x - sn * y;
+          jj[u] = sn * x + cs * y;
+        }
+        if (lane == 0) atomicExch(rotated, 1u);
+      }
+      if (!grid_sync(a)) return;
+    }
+    const unsigned any = *(volatile unsigned*)rotated;
+    if (!grid_sync(a)) return;
+    if (any == 0u) return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.flags, 2);
+}
+
+// Sorts the Jacobi result by descending column norm and writes U, S, V.
+// trans == 0: W rows are columns of X (m >= n): U = W_j / s_j, V = J.
+// trans == 1: W rows are rows of X (m < n):  U = J, V = W_j / s_j.
+__global__ void jacobi_finish_kernel(const double* W, const double* J, int64_t p, int64_t L,
+                                     int trans, double* U, double* S, double* V) {
+  const int64_t j = blockIdx.x;
+  if (j >= p) return;
+  __shared__ double sh[LT / 32];
+  __shared__ double s_norm;
+  __shared__ int64_t s_rank;
+  double part = 0.0;
+  for (int64_t t = threadIdx.x; t < L; t += blockDim.x) part = fma(W[j * L + t], W[j * L + t], part);
+  const double nj2 = block_sum(part, sh);
+  // rank: strictly larger norms (ties broken by index); norms recomputed per
+  // column so every block sees identical values
+  int64_t cnt = 0;
+  for (int64_t i = threadIdx.x; i < p; i += blockDim.x) {
+    if (i == j) continue;
+    double ni2 = 0.0;
+    for (int64_t t = 0; t < L; ++t) ni2 = fma(W[i * L + t], W[i * L + t], ni2);
+    if (ni2 > nj2 || (ni2 == nj2 && i < j)) ++cnt;
+  }
+  const double c = block_sum(double(cnt), sh);
+  if (threadIdx.x == 0) {
+    s_norm = sqrt(nj2);
+    s_rank = static_cast<int64_t>(c + 0.5);
+  }
+  __syncthreads();
+  const double sj = s_norm;
+  const int64_t rk = s_rank;
+  const double inv = sj > 0.0 ? 1.0 / sj : 0.0;
+  if (threadIdx.x == 0) S[rk] = sj;
+  if (trans == 0) {
+    for (int64_t t = threadIdx.x; t < L; t += blockDim.x) U[t * p + rk] = W[j * L + t] * inv;
+    for (int64_t t = threadIdx.x; t < p; t += blockDim.x) V[t * p + rk] = J[j * p + t];
+  } else {
+    for (int64_t t = threadIdx.x; t < p; t += blockDim.x) U[t * p + rk] = J[j * p + t];
+    for (int64_t t = threadIdx.x; t < L; t += blockDim.x) V[t * p + rk] = W[j * L + t] * inv;
+  }
+}
+
+__global__ void identity_kernel(double* X, int64_t p) {
+  for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < p * p;
+       idx += int64_t(gridDim.x) * blockDim.x)
+    X[idx] = (idx / p == idx % p) ? 1.0 : 0.0;
+}
+
+// ------------------------------------------------------------- truncation
+__global__ void truncation_kernel(const double* s, int64_t r, int64_t chi, double cutoff,
+                                  double* f, int64_t cap, int64_t* chi_new) {
+  __shared__ double sh[LT / 32];
+  const double s0 = s[0];
+  double cnt = 0.0;
+  for (int64_t i = threadIdx.x; i < r; i += LT) cnt += (s[i] / s0 > cutoff) ? 1.0 : 0.0;
+  cnt = block_sum(cnt, sh);
+  const int64_t count = static_cast<int64_t>(cnt + 0.5);
+  const int64_t cn = count < chi ? count : chi;
+  for (int64_t i = threadIdx.x; i < cap; i += LT)
+    f[i] = (i < cn) ? 1.0 / sqrt(s[i] / s0) : 0.0;
+  if (threadIdx.x == 0) *chi_new = cn;
+}
+
+__global__ void scale_compact_kernel(const double* in, int64_t rows, int64_t cap, const double* f,
+                                     const int64_t* chi_new, double* out) {
+  const int64_t cn = *chi_new;
+  const int64_t total = rows * cn;
+  for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < total;
+       idx += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t r = idx / cn, c = idx % cn;
+    out[idx] = f != nullptr ? in[r * cap + c] * f[c] : in[r * cap + c];
+  }
+}
+
+__global__ void restore_if_flagged_kernel(double* Y, const double* saved, int64_t n,
+                                          const int* flags) {
+  if (((*flags) & 1) == 0) return;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    Y[i] = saved[i];
+}
+
+}  // namespace
+
+int* status_flags(Ctx& c) {
+  (void)c;
+  int* p = nullptr;
+  CTM_CUDA(cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_status_flags));
+  return p;
+}
+
+void orthonormalize(Ctx& c, double* Y, int64_t n, int64_t q, double* R) {
+  CTM_REQUIRE(n >= q && q >= 1, CTM_ERR_INVALID, "orthonormalize: needs n >= q >= 1");
+  Scope scope(c);
+  double* V = c.alloc<double>(size_t(n) * q);
+  double* beta = c.alloc<double>(q);
+  const bool small = double(n) * q * q <= 4.0e6;
+  if (small) {
+    if (c.sizing()) return;
+    householder_qr_kernel<<<1, LT, 0, c.stream>>>(Y, n, q, R, V, beta, nullptr, 1);
+    CTM_LAUNCH_CHECK();
+    return;
+  }
+  // shifted Cholesky-QR3 with a Householder re-run when the check fails
+  double* X2 = c.alloc<double>(size_t(n) * q);
+  double* G = c.alloc<double>(size_t(q) * q);
+  double* Wk = c.alloc<double>(size_t(q) * q);
+  double* Li = c.alloc<double>(size_t(q) * q);
+  double* Lt = c.alloc<double>(size_t(q) * q);
+  double* Rt = c.alloc<double>(size_t(q) * q);
+  double* Rt2 = c.alloc<double>(size_t(q) * q);
+  int* flags = c.alloc<int>(1);
+  // keep the input for the fallback in V
+  if (!c.sizing()) {
+    CTM_CUDA(cudaMemcpyAsync(V, Y, sizeof(double) * n * q, cudaMemcpyDeviceToDevice, c.stream));
+    CTM_CUDA(cudaMemsetAsync(flags, 0, sizeof(int), c.stream));
+  }
+  double* cur = Y;
+  double* nxt = X2;
+  for (int stage = 0; stage < 3; ++stage) {
+    einsum(c, "ia,ib->ab", View(cur, {n, q}), View(cur, {n, q}), View(G, {q, q}));
+    if (!c.sizing()) {
+      cholesky_inverse_kernel<<<1, LT, 0, c.stream>>>(G, q, n, stage == 0 ? 1 : 0, Wk, Li, Lt,
+                                                      flags);
+      CTM_LAUNCH_CHECK();
+    }
+    // nxt = cur @ Linv^T
+    einsum(c, "ia,ba->ib", View(cur, {n, q}), View(Li, {q, q}), View(nxt, {n, q}));
+    if (R != nullptr) {
+      if (stage == 0) {
+        if (!c.sizing())
+          CTM_CUDA(cudaMemcpyAsync(Rt, Lt, sizeof(double) * q * q, cudaMemcpyDeviceToDevice,
+                                   c.stream));
+      } else {
+        einsum(c, "ab,bc->ac", View(Lt, {q, q}), View(Rt, {q, q}), View(Rt2, {q, q}));
+        std::swap(Rt, Rt2);
+      }
+    }
+    std::swap(cur, nxt);
+  }
+  // cur holds Q after the three stages; check it and fall back when needed
+  einsum(c, "ia,ib->ab", View(cur, {n, q}), View(cur, {n, q}), View(G, {q, q}));
+  double* hv = c.alloc<double>(size_t(n) * q);
+  if (c.sizing()) return;
+  orthogonality_check_kernel<<<1, LT, 0, c.stream>>>(G, q, 1e-11, flags);
+  CTM_LAUNCH_CHECK();
+  if (cur != Y)
+    CTM_CUDA(cudaMemcpyAsync(Y, cur, sizeof(double) * n * q, cudaMemcpyDeviceToDevice, c.stream));
+  if (R != nullptr)
+    CTM_CUDA(cudaMemcpyAsync(R, Rt, sizeof(double) * q * q, cudaMemcpyDeviceToDevice, c.stream));
+  restore_if_flagged_kernel<<<grid_for(n * q, 256), 256, 0, c.stream>>>(Y, V, n * q, flags);
+  CTM_LAUNCH_CHECK();
+  householder_qr_kernel<<<1, LT, 0, c.stream>>>(Y, n, q, R, hv, beta, flags, 1);
+  CTM_LAUNCH_CHECK();
+}
+
+void svd_thin(Ctx& c, const double* X, int64_t m, int64_t n, double* U, double* S, double* V) {
+  CTM_REQUIRE(m >= 1 && n >= 1, CTM_ERR_INVALID, "svd_thin: empty matrix");
+  const int trans = m >= n ? 0 : 1;
+  const int64_t p = std::min(m, n), L = std::max(m, n);
+  Scope scope(c);
+  double* W = c.alloc<double>(size_t(p) * L);
+  double* J = c.alloc<double>(size_t(p) * p);
+  unsigned* bar = c.alloc<unsigned>(8);
+  if (c.sizing()) return;
+  // W rows = columns of X (trans 0) or rows of X (trans 1)
+  if (trans == 0)
+    copy2d(c, View(X, {m, n}).permute({1, 0}), W, L);
+  else
+    CTM_CUDA(cudaMemcpyAsync(W, X, sizeof(double) * m * n, cudaMemcpyDeviceToDevice, c.stream));
+  identity_kernel<<<grid_for(p * p, 256), 256, 0, c.stream>>>(J, p);
+  CTM_LAUNCH_CHECK();
+  CTM_CUDA(cudaMemsetAsync(bar, 0, 8 * sizeof(unsigned), c.stream));
+  JacobiArgs a{};
+  a.W = W;
+  a.J = J;
+  a.p = p;
+  a.L = L;
+  a.pp = p + (p & 1);
+  a.tol = 2.220446049250313e-16 * std::sqrt(double(L));
+  a.max_sweeps = 60;
+  a.bar = bar;
+  a.flags = status_flags(c);
+  a.spin_limit = int64_t(20) * 1000 * 1000;  // ~1-2 s of 64 ns sleeps
+  if (p > 1) {
+    int dev = 0, sms = 0, per_sm = 0;
+    CTM_CUDA(cudaGetDevice(&dev));
+    CTM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int threads = 64;
+    CTM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_sweeps_kernel, threads, 0));
+    const int64_t npairs = a.pp / 2;
+    int64_t blocks = (npairs + 1) / 2;
+    blocks = std::min<int64_t>(blocks, int64_t(sms) * std::max(per_sm, 1));
+    blocks = std::min<int64_t>(blocks, sms);
+    blocks = std::max<int64_t>(blocks, 1);
+    void* args[] = {&a};
+    CTM_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(jacobi_sweeps_kernel),
+                                         dim3(unsigned(blocks)), dim3(threads), args, 0, c.stream));
+    CTM_LAUNCH_CHECK();
+  }
+  jacobi_finish_kernel<<<unsigned(p), LT, 0, c.stream>>>(W, J, p, L, trans, U, S, V);
+  CTM_LAUNCH_CHECK();
+}
+
+void truncation_factors(Ctx& c, const double* s, int64_t r, int64_t chi, double cutoff, double* f,
+                        int64_t cap, int64_t* chi_new) {
+  if (c.sizing()) return;
+  truncation_kernel<<<1, LT, 0, c.stream>>>(s, r, chi, cutoff, f, cap, chi_new);
+  CTM_LAUNCH_CHECK();
+}
+
+__global__ void scale_columns_kernel(double* x, int64_t rows, int64_t cols, int64_t ld,
+                                     const double* f) {
+  for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < rows * cols;
+       idx += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t r = idx / cols, c = idx % cols;
+    x[r * ld + c] *= f[c];
+  }
+}
+
+void scale_columns(Ctx& c, double* x, int64_t rows, int64_t cols, int64_t ld, const double* f) {
+  if (c.sizing() || rows * cols == 0) return;
+  scale_columns_kernel<<<grid_for(rows * cols, 256), 256, 0, c.stream>>>(x, rows, cols, ld, f);
+  CTM_LAUNCH_CHECK();
+}
+
+void scale_columns_compact(Ctx& c, const double* in, int64_t rows, int64_t cap, const double* f,
+                           const int64_t* chi_new, double* out) {
+  if (c.sizing() || rows * cap == 0) return;
+  scale_compact_kernel<<<grid_for(rows * cap, 256), 256, 0, c.stream>>>(in, rows, cap, f, chi_new,
+                                                                         out);
+  CTM_LAUNCH_CHECK();
+}
+
+}  // namespace ctm

@@ -1,0 +1,36 @@
+"""CTMRG driver on the GB300 library.
+
+Mirror of ``ctmrg(ipeps, config)`` (acetn/renormalization/ctmrg.py:4-31),
+non-distributed branch: ``config.steps`` iterations of left/right moves for
+every column followed by up/down moves for every row.
+"""
+
+from tqdm import tqdm
+
+from .config import resolve
+from .directional_mover import DirectionalMover
+
+
+def sweep_order(nx, ny):
+    """Move sequence of one iteration as (k, index) pairs (ctmrg.py:25-31)."""
+    order = []
+    for xi in range(nx):
+        order.append((0, xi))
+        order.append((2, (nx - xi + 1) % nx))
+    for yi in range(ny):
+        order.append((1, (ny - yi + 1) % ny))
+        order.append((3, yi))
+    return order
+
+
+def ctmrg(ipeps, config, omega_source=None, steps=None):
+    cfg = resolve(config)
+    mover = DirectionalMover(cfg, omega_source)
+    disable = cfg.disable_progressbar or getattr(ipeps, "rank", 0) != 0
+    pbar = tqdm(desc="Renormalizing boundary tensors", unit=" sweeps", disable=disable)
+    for _ in range(cfg.steps if steps is None else steps):
+        pbar.update(1)
+        for k, idx in sweep_order(ipeps.nx, ipeps.ny):
+            mover.move(ipeps, k, idx)
+    pbar.close()
+    return ipeps

@@ -1,0 +1,105 @@
+"""Randomized SVDs of ``acetn.linalg`` on the GB300 library.
+
+Same signatures and return conventions as the reference (U, S, V with
+A ~= U diag(S) V^T; q clamped to min(q, m, n)), plus an optional ``omega``
+argument: the (n x q) N(0,1) test matrix.  When it is None it is drawn with
+``torch.randn`` on the device, as the reference does
+(acetn/linalg/fused_matmul_svd_lowrank.py:32).
+"""
+
+import torch
+
+from . import _abi
+
+
+def _omega(omega, n, q, device):
+    if omega is None:
+        return torch.randn(n, q, dtype=torch.float64, device=device)
+    if omega.shape != (n, q):
+        raise ValueError(f"omega must have shape {(n, q)}, got {tuple(omega.shape)}")
+    return omega.to(device=device, dtype=torch.float64).contiguous()
+
+
+def svd_lowrank(A, q=6, niter=2, omega=None):
+    """acetn/linalg/svd_lowrank.py:4-44."""
+    _abi.require_cuda(A, "A")
+    A = A.contiguous()
+    m, n = A.shape
+    q = min(q, m, n)
+    om = _omega(omega, n, q, A.device)
+    U = torch.empty(m, q, dtype=torch.float64, device=A.device)
+    S = torch.empty(q, dtype=torch.float64, device=A.device)
+    V = torch.empty(n, q, dtype=torch.float64, device=A.device)
+    _abi.call("ctm_svd_lowrank", [_abi.ptr(A), m, n, q, niter, _abi.ptr(om), _abi.ptr(U),
+                                  _abi.ptr(S), _abi.ptr(V)], A.device)
+    return U, S, V
+
+
+def fused_matmul_svd_lowrank(A, B, q=6, niter=2, omega=None, precision="fp64"):
+    """acetn/linalg/fused_matmul_svd_lowrank.py:4-52."""
+    _abi.require_cuda(A, "A")
+    _abi.require_cuda(B, "B")
+    A = A.contiguous()
+    B = B.contiguous()
+    m, k = A.shape
+    k2, n = B.shape
+    if k != k2:
+        raise ValueError("A and B do not chain")
+    q = min(q, m, n)
+    om = _omega(omega, n, q, A.device)
+    U = torch.empty(m, q, dtype=torch.float64, device=A.device)
+    S = torch.empty(q, dtype=torch.float64, device=A.device)
+    V = torch.empty(n, q, dtype=torch.float64, device=A.device)
+    _abi.call("ctm_fused_matmul_svd_lowrank",
+              [_abi.ptr(A), _abi.ptr(B), m, k, n, q, niter, _abi.ptr(om), _abi.ptr(U),
+               _abi.ptr(S), _abi.ptr(V), _abi.PREC[precision]], A.device)
+    return U, S, V
+
+
+def fused_3matmul_svd_lowrank(A, B, C, D, q=6, niter=2, omega=None):
+    """acetn/linalg/fused_3matmul_svd_lowrank.py:4-56."""
+    for t, nm in ((A, "A"), (B, "B"), (C, "C"), (D, "D")):
+        _abi.require_cuda(t, nm)
+    A, B, C, D = (t.contiguous() for t in (A, B, C, D))
+    m, k1 = A.shape
+    if B.shape[0] != k1 or C.shape[0] != B.shape[1] or D.shape[0] != C.shape[1]:
+        raise ValueError("factors do not chain")
+    k2, k3, n = B.shape[1], C.shape[1], D.shape[1]
+    q = min(q, m, n)
+    om = _omega(omega, n, q, A.device)
+    U = torch.empty(m, q, dtype=torch.float64, device=A.device)
+    S = torch.empty(q, dtype=torch.float64, device=A.device)
+    V = torch.empty(n, q, dtype=torch.float64, device=A.device)
+    _abi.call("ctm_fused_3matmul_svd_lowrank",
+              [_abi.ptr(A), _abi.ptr(B), _abi.ptr(C), _abi.ptr(D), m, k1, k2, k3, n, q, niter,
+               _abi.ptr(om), _abi.ptr(U), _abi.ptr(S), _abi.ptr(V)], A.device)
+    return U, S, V
+
+
+def svd(A):
+    """Thin SVD (U, S, V) of an FP64 matrix with at most 4096 rows and columns."""
+    _abi.require_cuda(A, "A")
+    A = A.contiguous()
+    m, n = A.shape
+    r = min(m, n)
+    U = torch.empty(m, r, dtype=torch.float64, device=A.device)
+    S = torch.empty(r, dtype=torch.float64, device=A.device)
+    V = torch.empty(n, r, dtype=torch.float64, device=A.device)
+    _abi.call("ctm_svd_f64", [_abi.ptr(A), m, n, _abi.ptr(U), _abi.ptr(S), _abi.ptr(V)], A.device)
+    return U, S, V
+
+
+def matmul(A, B, precision="fp64"):
+    """A @ B with the library's FP64 or mixed-precision GEMM engine."""
+    _abi.require_cuda(A, "A")
+    _abi.require_cuda(B, "B")
+    A = A.contiguous()
+    B = B.contiguous()
+    M, K = A.shape
+    K2, N = B.shape
+    if K != K2:
+        raise ValueError("A and B do not chain")
+    C = torch.empty(M, N, dtype=torch.float64, device=A.device)
+    _abi.call("ctm_matmul", [_abi.ptr(A), _abi.ptr(B), _abi.ptr(C), M, N, K,
+                             _abi.PREC[precision]], A.device)
+    return C

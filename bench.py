@@ -1,0 +1,400 @@
+"""CTMRG moves/s of the GB300 library at D=6, chi=144 (Heisenberg J=1, 2x2 unit
+cell, d=2, half-system rSVD projectors, oversampling 16, 2 power iterations).
+
+A step is one directional move (projectors of both rows/columns of the move,
+then the boundary renormalization of both).  The environment is first grown
+to chi (two untimed CTMRG iterations), then W untimed moves, then K timed
+moves, each bracketed by CUDA events on the launching stream with an L2
+flush (a 256 MiB write) between moves outside the events.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+       [--precision fp64|mixed]
+Under torchrun every rank runs an independent replica (the path does not
+shard: "scaling": "weak"); rank 0 prints one JSON line.
+"""
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+D, CHI, PHYS, OVERSAMPLING, NITER, SEED = 6, 144, 2, 16, 2, 20250
+N_Q = CHI * D * D
+METRIC = "CTMRG moves/s at D=6, chi=144 (Heisenberg, 2x2, half-system rSVD os=16 niter=2)"
+
+
+def move_flops(D, chi, q, d=2, ny=2, niter=2):
+    """Algorithmic FLOPs of one move (GEMM-shaped work only; QR and the
+    q x N SVD excluded), per row: two quarter tensors, the rSVD GEMM chain,
+    the two projector products, and the boundary renormalization."""
+    n = chi * D * D
+    per_row = (2 * (2 * chi**3 * D**2 + 2 * chi**3 * D**4 + 4 * chi**2 * D**6 * d)
+               + 2 * n * n * q * (4 + 4 * niter)
+               + 4 * n * n * chi
+               + 4 * chi**3 * D**4 + 4 * chi**2 * D**6 * d + 8 * chi**3 * D**2)
+    return ny * per_row
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-i", str(self.index), "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names[1:], parts[5:9]):
+                if val.lower() in ("active", "1", "yes"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def package():
+    mod = importlib.import_module("ace-tn_gb300")
+    sys.modules.setdefault("acetn_gb300", mod)
+    return mod
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_model():
+    try:
+        with open("/proc/cpuinfo") as fh:
+            for line in fh:
+                if line.lower().startswith(("model name", "cpu part")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+# --------------------------------------------------------------------- oracle legs
+def oracle_moves(st_np, moves, seed=1):
+    """Times ``moves`` directional moves of the oracle (numpy, all host
+    threads) starting from a saturated state; returns seconds per move."""
+    from oracle import ctm_oracle as orc
+    cfg = dict(projectors="half-system", svd_type="rsvd", rsvd_oversampling=OVERSAMPLING,
+               rsvd_niter=NITER, svd_cutoff=1e-12)
+    mover = orc.Mover(cfg, orc.OmegaStream(seed))
+    order = orc.sweep_order(2, 2)
+    times = []
+    for i in range(moves):
+        k, idx = order[i % len(order)]
+        t0 = time.perf_counter()
+        mover.move(st_np, k, idx)
+        times.append(time.perf_counter() - t0)
+    return times
+
+
+def run_reference(args, rank):
+    """--impl reference: the reference's CPU path restated by the oracle
+    (numpy/LAPACK on the host cores), same config, metric and unit."""
+    if rank != 0:
+        return None
+    import numpy as np
+    from oracle import ctm_oracle as orc
+    st = orc.random_state(D, CHI, seed=SEED)
+    cfg = dict(projectors="half-system", svd_type="rsvd", rsvd_oversampling=OVERSAMPLING,
+               rsvd_niter=NITER, svd_cutoff=1e-12)
+    t0 = time.perf_counter()
+    orc.ctmrg(st, cfg, orc.OmegaStream(SEED), steps=2)  # grow the environment to chi
+    grow_s = time.perf_counter() - t0
+    oracle_moves(st, args.warmup, seed=SEED + 1)
+    times = oracle_moves(st, args.steps, seed=SEED + 2)
+    total = sum(times)
+    value = args.steps / total
+    q = CHI + OVERSAMPLING
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "moves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"heisenberg_2x2_D{D}_chi{CHI}_rsvd_os{OVERSAMPLING}_niter{NITER}",
+                   "D": D, "chi": CHI, "phys": PHYS, "projectors": "half-system",
+                   "svd_type": "rsvd", "seed": SEED},
+        "cpu_baseline": {"value": value, "unit": "moves/s", "cores": cpu_cores(), "kind": "port",
+                         "sample": f"{args.steps} moves after 2 growth iterations "
+                                   f"({grow_s:.1f} s) and {args.warmup} warm-up moves",
+                         "cpu_model": cpu_model()},
+        "e2e": {"value": value, "unit": "moves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "tflops": move_flops(D, CHI, q) / (total / args.steps) / 1e12,
+    }
+    return line
+
+
+# --------------------------------------------------------------------- gb300 arm
+def state_bytes(st):
+    n = 0
+    for s in st.site_list:
+        v = st[s]
+        n += v["A"].numel() * 8 + sum(t.numel() * 8 for t in v["C"]) + sum(t.numel() * 8 for t in v["E"])
+    return n
+
+
+def run_gb300(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    gb = package()
+    gb.build()
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+    cfg = gb.CTMRGConfig(projectors="half-system", svd_type="rsvd", rsvd_oversampling=OVERSAMPLING,
+                         rsvd_niter=NITER, svd_cutoff=1e-12, precision=args.precision,
+                         disable_progressbar=True)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(SEED + rank)
+
+    def omega(n, q, device):
+        return torch.randn(n, q, dtype=torch.float64, device=device, generator=gen)
+
+    st = gb.random_state(D, CHI, SEED, d=PHYS, device=dev)
+    mover = gb.DirectionalMover(cfg, omega_source=omega)
+    order = gb.sweep_order(2, 2)
+    for _ in range(2):  # grow the environment to chi
+        for k, idx in order:
+            mover.move(st, k, idx)
+    pos = 0
+    for _ in range(args.warmup):
+        k, idx = order[pos % len(order)]
+        mover.move(st, k, idx)
+        pos += 1
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    launches0 = gb._abi.kernel_launches()
+    gb._abi.profile_begin()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    torch.cuda.synchronize(dev)
+    for i in range(args.steps):
+        flush.zero_()
+        k, idx = order[pos % len(order)]
+        ev[i][0].record(stream)
+        mover.move(st, k, idx)
+        ev[i][1].record(stream)
+        pos += 1
+    torch.cuda.synchronize(dev)
+    prof = gb._abi.profile_end()
+    launches = gb._abi.kernel_launches() - launches0
+    clk = clocks.stop()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    total_s = sum(ms) / 1e3
+    t = torch.tensor([total_s], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    total_max = float(t.item())
+    value = world * args.steps / total_max
+
+    # ---- e2e: host buffers through the public API, copies inside the timed region
+    host = {s: {"A": st[s]["A"].cpu().pin_memory(),
+                "C": [c.cpu().pin_memory() for c in st[s]["C"]],
+                "E": [e.cpu().pin_memory() for e in st[s]["E"]]} for s in st.site_list}
+    e2e_steps = max(1, min(args.steps, 4))
+    h2d = d2h = 0
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        k, idx = order[pos % len(order)]
+        pos += 1
+        dst = gb.IpepsState(2, 2, st.dims, dev)
+        for s in st.site_list:
+            hs = host[s]
+            dst[s] = {"A": hs["A"].to(dev, non_blocking=True),
+                      "C": [c.to(dev, non_blocking=True) for c in hs["C"]],
+                      "E": [e.to(dev, non_blocking=True) for e in hs["E"]]}
+        h2d = state_bytes(dst)
+        mover.move(dst, k, idx)
+        # read back the tensors the move rewrote
+        moved = 0
+        for s in st.site_list:
+            outs = {"C": [c.to("cpu", non_blocking=True) for c in dst[s]["C"]],
+                    "E": [e.to("cpu", non_blocking=True) for e in dst[s]["E"]]}
+            moved += sum(c.numel() * 8 for c in outs["C"]) + sum(e.numel() * 8 for e in outs["E"])
+            host[s]["C"], host[s]["E"] = outs["C"], outs["E"]
+        torch.cuda.synchronize(dev)
+        for s in st.site_list:
+            host[s]["C"] = [c.pin_memory() for c in host[s]["C"]]
+            host[s]["E"] = [e.pin_memory() for e in host[s]["E"]]
+        d2h = moved
+    e2e_s = time.perf_counter() - t0
+    e2e_value = world * e2e_steps / e2e_s
+
+    gett_ms, gett_flops, gett_n = prof["gett_f64"]
+    tc_ms, tc_flops, tc_n = prof["tc_gemm"]
+    if tc_ms > gett_ms:
+        dom, dom_ms, dom_work, dom_n = "tc_gemm", tc_ms, tc_flops, tc_n
+    else:
+        dom, dom_ms, dom_work, dom_n = "gett_f64", gett_ms, gett_flops, gett_n
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except OSError:
+        pass
+    if dom == "tc_gemm":
+        peak = peaks.get("bf16_tflops_sustained") or 1700.0
+        peak_src = "MEASURED_PEAKS.json bf16_tflops_sustained" if peaks else "fallback 1.7 PF/s"
+        bound = "tensor"
+    else:
+        peak = fp64_peak_tflops(dev)
+        peak_src = "cuBLAS DGEMM 8192^3 measured by bench.py on this GPU (no FP64 entry in MEASURED_PEAKS.json)"
+        bound = "fp64"
+    achieved = (dom_work / (dom_ms / 1e3)) / 1e12 if dom_ms > 0 else None
+    q = CHI + OVERSAMPLING
+    line = None
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "moves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "bf16/3xbf16+f64",
+            "data": "synthetic",
+            "config": {"workload": f"heisenberg_2x2_D{D}_chi{CHI}_rsvd_os{OVERSAMPLING}_niter{NITER}",
+                       "D": D, "chi": CHI, "phys": PHYS, "projectors": "half-system",
+                       "svd_type": "rsvd", "precision": args.precision, "seed": SEED,
+                       "l2": "256 MiB flush between timed moves; quarter tensors 215 MB each",
+                       "parallelism": f"replicas x{world}"},
+            "tflops": move_flops(D, CHI, q) / (total_max / args.steps) / 1e12,
+            "roofline": {"bound": bound, "kernel": dom, "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
+                         "traffic": None, "launches": dom_n, "peak_source": peak_src,
+                         "share_of_step": dom_ms / (1e3 * total_s) if total_s else None},
+            "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+            "gpu_launches": int(launches),
+            "clocks": clk,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            st_np = type("S", (), {})
+            from oracle import ctm_oracle as orc
+            ost = orc.OracleState(
+                {s: {"A": st[s]["A"].cpu().numpy(), "C": [c.cpu().numpy() for c in st[s]["C"]],
+                     "E": [e.cpu().numpy() for e in st[s]["E"]]} for s in st.site_list}, 2, 2, CHI)
+            times = oracle_moves(ost, args.cpu_moves)
+            line["cpu_baseline"] = {"value": len(times) / sum(times), "unit": "moves/s",
+                                    "cores": cpu_cores(), "kind": "port",
+                                    "sample": f"{len(times)} oracle moves from the GPU run's "
+                                              f"saturated chi={CHI} state",
+                                    "cpu_model": cpu_model()}
+    return line
+
+
+_FP64_PEAK = {}
+
+
+def fp64_peak_tflops(dev):
+    import torch
+    if dev in _FP64_PEAK:
+        return _FP64_PEAK[dev]
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize(dev)
+    best = 1e9
+    for _ in range(3):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        torch.cuda.synchronize(dev)
+        best = min(best, s.elapsed_time(e) / 1e3)
+    _FP64_PEAK[dev] = 2.0 * n**3 / best / 1e12
+    return _FP64_PEAK[dev]
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--cpu-moves", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        line = run_reference(args, rank)
+    else:
+        if world > 1:
+            import torch
+            import torch.distributed as dist
+            torch.cuda.set_device(local_rank)
+            dist.init_process_group("nccl")
+        line = run_gb300(args, rank, world, local_rank)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,196 @@
+/*
+ * ctm_gb300.h - C ABI of the GB300 (sm_103a) CTMRG library.
+ *
+ * Every entry point takes device pointers to contiguous row-major tensors in
+ * the layouts of Ace-TN's torch tensors, plain integer sizes, a caller-owned
+ * device workspace and a cudaStream_t.  The library allocates no device
+ * memory besides a file-scope status word; all launches go to the given
+ * stream and only ctm_device_status() synchronizes (that stream).
+ *
+ * Workspace protocol: call with ws == NULL and *ws_bytes ignored; the entry
+ * point stores the bytes it needs in *ws_bytes and returns CTM_OK without
+ * launching anything.  Call again with a buffer of at least that size
+ * (256-byte aligned).
+ *
+ * Tensor layouts (reference: acetn/ipeps/site_tensor.py:41-83):
+ *   A    (D, D, D, D, d)          legs (left, up, right, down, phys)
+ *   C[k] (c_rows[k], c_cols[k])   k = 0 left, 1 up, 2 right, 3 down
+ *   E[k] (e_rows[k], e_cols[k], D, D)
+ *
+ * Status codes are returned by every function; ctm_last_error() gives the
+ * message of the last failure on the calling thread.
+ */
+#ifndef CTM_GB300_H
+#define CTM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* ctm_stream_t; /* == cudaStream_t */
+
+enum {
+  CTM_OK = 0,
+  CTM_ERR_INVALID = 1,      /* bad shape, size, pointer or option         */
+  CTM_ERR_UNSUPPORTED = 2,  /* valid request this library does not handle  */
+  CTM_ERR_WORKSPACE = 3,    /* workspace smaller than the queried size     */
+  CTM_ERR_CUDA = 4,         /* a CUDA runtime call failed                  */
+  CTM_ERR_NUMERIC = 5,      /* non-finite input or failed factorization    */
+  CTM_ERR_TIMEOUT = 6       /* a bounded device-side wait expired          */
+};
+
+/* Arithmetic of a projector computation. */
+enum {
+  CTM_PREC_FP64 = 0,   /* every product in FP64: the drop-in path                     */
+  CTM_PREC_MIXED = 1   /* tensor-core BF16 range finder, 3xBF16 products feeding the
+                          projectors, FP64 Rayleigh-Ritz SVD, truncation and scaling */
+};
+
+/* Projector construction (acetn/ipeps/ipeps_config.py:16-24 CTMRGConfig). */
+enum { CTM_PROJ_HALF = 0, CTM_PROJ_FULL = 1 };
+enum { CTM_SVD_RSVD = 0, CTM_SVD_FULL = 1 };
+
+typedef struct ctm_site_f64 {
+  const double* A;
+  const double* C[4];
+  const double* E[4];
+  int64_t c_rows[4], c_cols[4];
+  int64_t e_rows[4], e_cols[4];
+} ctm_site_f64;
+
+typedef struct ctm_ctmrg_opts {
+  int64_t chi;          /* dims["chi"]                                  */
+  int32_t projectors;   /* CTM_PROJ_HALF | CTM_PROJ_FULL                */
+  int32_t svd_type;     /* CTM_SVD_RSVD | CTM_SVD_FULL                  */
+  double svd_cutoff;    /* relative singular-value cutoff (1e-12)       */
+  int32_t rsvd_niter;   /* power iterations (2)                         */
+  int32_t rsvd_oversampling; /* q = chi + oversampling (2)              */
+  int32_t precision;    /* CTM_PREC_FP64 | CTM_PREC_MIXED               */
+  int32_t reserved;
+} ctm_ctmrg_opts;
+
+/* Library version string and message of the last failure on this thread. */
+const char* ctm_version(void);
+const char* ctm_last_error(void);
+
+/* Synchronizes `stream`, stores and clears the device-side failure flags of
+ * the current device: bit 0 = a factorization failed and its fallback ran,
+ * bit 1 = an iteration limit or a bounded wait expired.  No counterpart in
+ * the reference (its torch calls raise synchronously). */
+int ctm_device_status(int* flags, ctm_stream_t stream);
+
+/* Number of CUDA kernels this library has launched in the process (for
+ * launch accounting in benchmarks).  No counterpart in the reference. */
+unsigned long long ctm_kernel_launches(void);
+
+/* Live kernel timing for benchmarks.  Between ctm_profile_begin() and
+ * ctm_profile_end() the main kernels are bracketed by CUDA events on their
+ * stream; ctm_profile_end() waits for them and ctm_profile_query(tag, ...)
+ * returns total milliseconds, algorithmic work (FLOPs) and launch count of a
+ * kernel class: 0 = FP64 contraction (GETT), 1 = tensor-core GEMM,
+ * 2 = tensor-core quarter-tensor kernel, 3 = other.  No counterpart in the
+ * reference (its benchmarking decorators time whole Python calls). */
+void ctm_profile_begin(void);
+int ctm_profile_end(void);
+int ctm_profile_query(int tag, double* total_ms, double* total_work, long long* launches);
+
+/* Enlarged corner (quarter tensor) of one site in direction k, reshaped to a
+ * (rows x cols) matrix, rows = (c, r, R), cols = (e, d, D), divided by its
+ * largest |entry|.  qshape receives the six leg sizes.
+ * Reference: ProjectorCalculator.make_quarter_tensor,
+ * acetn/renormalization/projectors.py:35-60. */
+int ctm_quarter_tensor(const ctm_site_f64* site, int64_t D, int64_t d, int32_t k,
+                       double* Q, int64_t* qshape, int32_t precision,
+                       void* ws, size_t* ws_bytes, ctm_stream_t stream);
+
+/* Projector pair of one row/column of a directional move.
+ * sites[0..3] = (s1, s2, s3, s4) as built by calculate_{left,up,right,down}_projectors
+ * (acetn/renormalization/directional_mover.py:99-181).
+ * omega: (n x q) N(0,1) matrix for the rSVD (ignored for CTM_SVD_FULL); n is
+ * the column count of the last factor, q = min(chi + oversampling, m, n).
+ * P1 receives (e, D, D, chi_new) and P2 (c, D, D, chi_new), both written
+ * contiguously in the first rows*chi_new entries of buffers that must hold
+ * rows*min(chi, q) (rSVD) or rows*min(chi, n) (full-rank) doubles.
+ * chi_new (device int64) receives min(chi, #{s/s0 > cutoff}).
+ * Reference: ProjectorCalculator.calculate_half_system / calculate_full_system,
+ * acetn/renormalization/projectors.py:114-217. */
+int ctm_calculate_projectors(const ctm_site_f64* const* sites, int64_t D, int64_t d,
+                             int32_t k, const ctm_ctmrg_opts* opts, const double* omega,
+                             double* P1, double* P2, int64_t* chi_new,
+                             void* ws, size_t* ws_bytes, ctm_stream_t stream);
+
+/* Number of rows of P1/P2 and the sketch width q of ctm_calculate_projectors
+ * (host-side shape query, no device access). */
+int ctm_projector_dims(const ctm_site_f64* const* sites, int64_t D, int32_t k,
+                       const ctm_ctmrg_opts* opts, int64_t* p1_rows, int64_t* p2_rows,
+                       int64_t* omega_rows, int64_t* q, int64_t* chi_cap);
+
+/* Boundary renormalization of one row of a move: writes
+ *   Cout1 = renormalize_cj1(C[(3+k)%4], E[(2+k)%4], P1_i)   (rows_a x chi_i)
+ *   Cout2 = renormalize_cj2(C[k], E[k], P2_j)               (chi_j x cols)
+ *   Eout  = renormalize_ej(E[(3+k)%4], A perm k, P2_i, P1_j) (chi_i, chi_j, D, D)
+ * each divided by its Frobenius norm.  P*_x point to (rows, D, D, chi_x) tensors.
+ * Reference: DirectionalMover.renormalize_boundary / renormalize_cj1 /
+ * renormalize_cj2 / renormalize_ej, acetn/renormalization/directional_mover.py:273-366. */
+int ctm_renormalize_boundary(const ctm_site_f64* s1, int64_t D, int64_t d, int32_t k,
+                             const double* P1_i, int64_t chi_p1i,
+                             const double* P2_j, int64_t chi_p2j,
+                             const double* P2_i, int64_t chi_p2i,
+                             const double* P1_j, int64_t chi_p1j,
+                             double* Cout1, double* Cout2, double* Eout,
+                             int32_t precision, void* ws, size_t* ws_bytes,
+                             ctm_stream_t stream);
+
+/* Site reduced density matrix (d x d), not trace-normalised.
+ * Reference: RDM.build_site_rdm, acetn/measurement/rdm.py:35-67. */
+int ctm_site_rdm(const ctm_site_f64* site, int64_t D, int64_t d, double* rdm,
+                 void* ws, size_t* ws_bytes, ctm_stream_t stream);
+
+/* Bond reduced density matrix (d, d, d, d) of bond (s1, s2, k), not normalised.
+ * Reference: RDM.build_bond_rdm / build_bond_rdm_core_blocked,
+ * acetn/measurement/rdm.py:69-153. */
+int ctm_bond_rdm(const ctm_site_f64* s1, const ctm_site_f64* s2, int64_t D, int64_t d,
+                 int32_t k, double* rdm, void* ws, size_t* ws_bytes, ctm_stream_t stream);
+
+/* Randomized SVD of a (m x n), of a @ b (a: m x k, b: k x n), or of
+ * a @ b @ c @ e (shapes chained); omega (n x q) supplied by the caller.
+ * Writes U (m x q), S (q), V (n x q) with a @ ... ~= U diag(S) V^T.
+ * Reference: acetn/linalg/svd_lowrank.py:4-44,
+ * acetn/linalg/fused_matmul_svd_lowrank.py:4-52,
+ * acetn/linalg/fused_3matmul_svd_lowrank.py:4-56. */
+int ctm_svd_lowrank(const double* a, int64_t m, int64_t n, int64_t q, int32_t niter,
+                    const double* omega, double* U, double* S, double* V,
+                    void* ws, size_t* ws_bytes, ctm_stream_t stream);
+int ctm_fused_matmul_svd_lowrank(const double* a, const double* b, int64_t m, int64_t k,
+                                 int64_t n, int64_t q, int32_t niter, const double* omega,
+                                 double* U, double* S, double* V, int32_t precision,
+                                 void* ws, size_t* ws_bytes, ctm_stream_t stream);
+int ctm_fused_3matmul_svd_lowrank(const double* a, const double* b, const double* c,
+                                  const double* e, int64_t m, int64_t k1, int64_t k2,
+                                  int64_t k3, int64_t n, int64_t q, int32_t niter,
+                                  const double* omega, double* U, double* S, double* V,
+                                  void* ws, size_t* ws_bytes, ctm_stream_t stream);
+
+/* Thin SVD of an (m x n) FP64 matrix, m, n <= 4096: U (m x r), S (r), V (n x r),
+ * r = min(m, n), singular values descending.  Used by svd_type "full-rank"
+ * (acetn/renormalization/projectors.py:219-236). */
+int ctm_svd_f64(const double* a, int64_t m, int64_t n, double* U, double* S, double* V,
+                void* ws, size_t* ws_bytes, ctm_stream_t stream);
+
+/* Matrix product C = A @ B of FP64 row-major matrices, with the library's
+ * arithmetic: CTM_PREC_FP64 (exact FP64 FMAs) or CTM_PREC_MIXED (3xBF16
+ * split products on tcgen05 tensor cores, FP32 accumulation).
+ * No counterpart in the reference (torch.matmul); exposed to test and
+ * measure the GEMM engines behind every entry point above. */
+int ctm_matmul(const double* A, const double* B, double* C, int64_t M, int64_t N,
+               int64_t K, int32_t precision, void* ws, size_t* ws_bytes,
+               ctm_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CTM_GB300_H */

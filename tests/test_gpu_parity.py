@@ -1,0 +1,267 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle and with the
+reference's golden vectors.  Tolerances: 1e-10 relative on gauge-invariant
+quantities for every FP64 result that does not follow an rSVD trajectory
+over many iterations (those amplify rounding differences; see
+test_rsvd_trajectory_within_noise_floor)."""
+
+import numpy as np
+import pytest
+import torch
+
+import acetn_gb300 as gb
+from _golden import SITES_K, gpu_state, load, oracle_state, rel
+from oracle import ctm_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+CFG = dict(projectors="half-system", svd_type="rsvd", rsvd_oversampling=2, rsvd_niter=2,
+           svd_cutoff=1e-12)
+
+
+def omega_from(stream):
+    return lambda n, q, device: torch.from_numpy(stream(n, q)).to(device)
+
+
+def cfg_obj(**kw):
+    return gb.CTMRGConfig(**{**CFG, **kw})
+
+
+def energy_and_rdms(st, model):
+    m = gb.measure(st, model, verbose=False)
+    return float(m["Energy"])
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    gb.build()
+    assert torch.cuda.is_available()
+
+
+def test_quarter_tensors_match_golden():
+    z = load("move_d3_chi9.npz")
+    st = gpu_state(z, 9)
+    for k in range(4):
+        q, sh = gb.ProjectorCalculator.make_quarter_tensor(st[(0, 0)], k)
+        assert sh == (9, 3, 3, 9, 3, 3)
+        assert rel(q.cpu().numpy(), z[f"quarter_00_k{k}"]) < 1e-13
+
+
+@pytest.mark.parametrize("proj", ["half-system", "full-system"])
+@pytest.mark.parametrize("svd", ["rsvd", "full-rank"])
+def test_projector_pairs_match_golden(proj, svd):
+    z = load("move_d3_chi9.npz")
+    st = gpu_state(z, 9)
+    for k in range(4):
+        pc = gb.ProjectorCalculator(cfg_obj(projectors=proj, svd_type=svd),
+                                    omega_source=omega_from(orc.OmegaStream(1000 + k)))
+        p1, p2 = pc.calculate(st, SITES_K[k], k)
+        tag = f"proj_{proj[:4]}_{svd[:4]}_k{k}"
+        assert p1.shape[-1] == int(z[tag + "_chi"])
+        assert p1.shape[:3] == (9, 3, 3) and p2.shape[:3] == (9, 3, 3)
+        ob = (p2.reshape(-1, p2.shape[-1]) @ p1.reshape(-1, p1.shape[-1]).T).cpu().numpy()
+        assert rel(ob, z[tag + "_oblique"]) < TOL
+
+
+def test_rsvd_variants_match_golden():
+    z = load("move_d3_chi9.npz")
+    st = gpu_state(z, 9)
+    q1, _ = gb.ProjectorCalculator.make_quarter_tensor(st[(0, 0)], 0)
+    q4, _ = gb.ProjectorCalculator.make_quarter_tensor(st[(0, 1)], 3)
+    q2, _ = gb.ProjectorCalculator.make_quarter_tensor(st[(1, 0)], 1)
+    q3, _ = gb.ProjectorCalculator.make_quarter_tensor(st[(1, 1)], 2)
+    n = q4.shape[1]
+    om = torch.from_numpy(orc.OmegaStream(77)(n, 11)).cuda()
+    u, s, v = gb.fused_matmul_svd_lowrank(q1, q4, q=11, niter=2, omega=om)
+    assert rel(s.cpu().numpy(), z["rsvd_fused_s"]) < TOL
+    assert rel((u @ torch.diag(s) @ v.T).cpu().numpy(), z["rsvd_fused_usv"]) < TOL
+    om = torch.from_numpy(orc.OmegaStream(78)(q1.shape[1], 11)).cuda()
+    u, s, v = gb.svd_lowrank(q1, q=11, niter=2, omega=om)
+    assert rel(s.cpu().numpy(), z["rsvd_plain_s"]) < TOL
+    assert rel((u @ torch.diag(s) @ v.T).cpu().numpy(), z["rsvd_plain_usv"]) < TOL
+    om = torch.from_numpy(orc.OmegaStream(79)(q3.shape[1], 11)).cuda()
+    u, s, v = gb.fused_3matmul_svd_lowrank(q2, q1, q4, q3, q=11, niter=2, omega=om)
+    assert rel(s.cpu().numpy(), z["rsvd_fused3_s"]) < TOL
+    assert rel((u @ torch.diag(s) @ v.T).cpu().numpy(), z["rsvd_fused3_usv"]) < TOL
+
+
+@pytest.mark.parametrize("k,name", list(enumerate(("left", "up", "right", "down"))))
+def test_single_move_matches_golden(k, name):
+    z = load("move_d3_chi9.npz")
+    st = gpu_state(z, 9)
+    mover = gb.DirectionalMover(cfg_obj(), omega_source=omega_from(orc.OmegaStream(2000 + k)))
+    mover.move(st, k, 0)
+    e = energy_and_rdms(st, gb.HeisenbergModel(1.0))
+    e_ref = float(z[f"move_{name}_meas_Energy"])
+    assert abs(e - e_ref) <= TOL * abs(e_ref)
+    for s in st.site_list:
+        for kk in range(4):
+            sv = np.linalg.svd(st[s]["C"][kk].cpu().numpy(), compute_uv=False)
+            assert rel(sv / sv[0], z[f"move_{name}_spec_{s[0]}{s[1]}_C{kk}"]) < TOL
+    rdm = gb.RDM(st)
+    for s in st.site_list:
+        r = rdm[s].cpu().numpy()
+        assert np.abs(r / np.trace(r) - z[f"move_{name}_site_rdm_{s[0]}{s[1]}"]).max() < TOL
+    for b in st.bond_list:
+        r = rdm[b].cpu().numpy()
+        r = r / np.einsum("pqpq->", r)
+        tag = f"move_{name}_bond_rdm_{b.s1[0]}{b.s1[1]}_{b.s2[0]}{b.s2[1]}_{b.k}"
+        assert np.abs(r - z[tag]).max() < TOL
+
+
+def test_single_move_matches_oracle_elementwise_up_to_sign():
+    """A move on a random D=3 state: new C/E agree with the oracle entry by
+    entry up to the sign gauge of each projector column."""
+    ost = orc.random_state(3, 9, seed=21)
+    orc.ctmrg(ost, dict(CFG, svd_type="full-rank"), orc.OmegaStream(0), steps=1)
+    gst = gb.IpepsState.from_arrays(ost.copy().sites, 2, 2, 9)
+    orc.Mover(CFG, orc.OmegaStream(9)).move(ost, 0, 1)
+    gb.DirectionalMover(cfg_obj(), omega_source=omega_from(orc.OmegaStream(9))).move(gst, 0, 1)
+    for s in ost.sites:
+        for kk in range(4):
+            a = np.abs(gst[s]["C"][kk].cpu().numpy())
+            b = np.abs(ost[s]["C"][kk])
+            assert a.shape == b.shape and rel(a, b) < 1e-9
+            a = np.abs(gst[s]["E"][kk].cpu().numpy())
+            b = np.abs(ost[s]["E"][kk])
+            assert a.shape == b.shape and rel(a, b) < 1e-9
+
+
+@pytest.mark.parametrize("fname,chi,proj,steps,model", [
+    ("ctmrg_d2_chi20_fullrank.npz", 20, "half-system", 30, "heisenberg"),
+    ("ctmrg_ising_d3_chi12_full.npz", 12, "full-system", 10, "ising"),
+])
+def test_full_rank_ctmrg_matches_golden(fname, chi, proj, steps, model):
+    z = load(fname)
+    st = gpu_state(z, chi)
+    gb.ctmrg(st, cfg_obj(projectors=proj, svd_type="full-rank", steps=steps,
+                         disable_progressbar=True))
+    mdl = gb.HeisenbergModel(1.0) if model == "heisenberg" else gb.IsingModel(1.0, 3.0)
+    e = energy_and_rdms(st, mdl)
+    e_ref = float(z["out_meas_Energy"])
+    assert abs(e - e_ref) <= TOL * abs(e_ref)
+    rdm = gb.RDM(st)
+    for b in st.bond_list:
+        r = rdm[b].cpu().numpy()
+        r = r / np.einsum("pqpq->", r)
+        tag = f"out_bond_rdm_{b.s1[0]}{b.s1[1]}_{b.s2[0]}{b.s2[1]}_{b.k}"
+        assert np.abs(r - z[tag]).max() < TOL
+
+
+def test_rsvd_trajectory_within_noise_floor():
+    """30 rSVD iterations: FP64 implementations differing only in rounding
+    order diverge to ~1e-5 relative in E (the oracle vs the reference shows
+    the same); the GPU result must stay inside that band."""
+    z = load("ctmrg_d2_chi20_rsvd.npz")
+    st = gpu_state(z, 20)
+    gb.ctmrg(st, cfg_obj(steps=30, disable_progressbar=True),
+             omega_source=omega_from(orc.OmegaStream(5)))
+    e = energy_and_rdms(st, gb.HeisenbergModel(1.0))
+    e_ref = float(z["out_meas_Energy"])
+    assert abs(e - e_ref) <= 1e-3 * abs(e_ref)
+
+
+@pytest.mark.parametrize("case", ["ising_dims_2_20_dtau_001_hx_295",
+                                  "heisenberg_dims_3_16_dtau_001"])
+def test_ground_state_fixtures(case):
+    z = load(f"gs_{case}.npz")
+    chi = z["in_00_C0"].shape[0]
+    model = gb.IsingModel(1.0, 2.95) if case.startswith("ising") else gb.HeisenbergModel(1.0)
+    st = gpu_state(z, chi)
+    e_pub = float(z["published_energy"])
+    assert abs(energy_and_rdms(st, model) - e_pub) <= TOL * abs(e_pub)
+    gb.ctmrg(st, cfg_obj(svd_type="full-rank", steps=5, disable_progressbar=True))
+    e_ref = float(z["after5_full_meas_Energy"])
+    assert abs(energy_and_rdms(st, model) - e_ref) <= TOL * abs(e_ref)
+    st = gpu_state(z, chi)
+    gb.ctmrg(st, cfg_obj(steps=5, disable_progressbar=True),
+             omega_source=omega_from(orc.OmegaStream(31)))
+    e_ref = float(z["after5_rsvd_meas_Energy"])
+    assert abs(energy_and_rdms(st, model) - e_ref) <= 1e-7 * abs(e_ref)
+
+
+# ----------------------------------------------------------------- linalg
+# restated from the reference's rSVD unit tests (tests/unit/test_linalg.py)
+
+def _rand(m, n, seed):
+    g = torch.Generator().manual_seed(seed)
+    return torch.randn(m, n, generator=g, dtype=torch.float64).cuda()
+
+
+def test_svd_lowrank_properties():
+    A = _rand(100, 80, 42)
+    U, S, V = gb.svd_lowrank(A, q=20, niter=2)
+    assert U.shape == (100, 20) and S.shape == (20,) and V.shape == (80, 20)
+    assert torch.all(S >= 0) and torch.all(S[:-1] >= S[1:])
+    eye = torch.eye(20, dtype=torch.float64, device="cuda")
+    assert torch.allclose(U.T @ U, eye, atol=1e-10)
+    assert torch.allclose(V.T @ V, eye, atol=1e-10)
+    U, S, V = gb.svd_lowrank(A, q=40, niter=2)
+    assert torch.norm(A - U @ torch.diag(S) @ V.T) / torch.norm(A) < 0.5
+
+
+def test_low_rank_exact_recovery():
+    L = _rand(100, 10, 1) @ _rand(10, 80, 2)
+    U, S, V = gb.svd_lowrank(L, q=15, niter=3)
+    assert torch.norm(L - U @ torch.diag(S) @ V.T) / torch.norm(L) < 1e-10
+    A, B = _rand(100, 10, 3), _rand(10, 80, 4)
+    U, S, V = gb.fused_matmul_svd_lowrank(A, B, q=15, niter=3)
+    assert torch.norm(A @ B - U @ torch.diag(S) @ V.T) / torch.norm(A @ B) < 1e-10
+    A, B, C, D = _rand(60, 10, 5), _rand(10, 50, 6), _rand(50, 40, 7), _rand(40, 70, 8)
+    U, S, V = gb.fused_3matmul_svd_lowrank(A, B, C, D, q=15, niter=3)
+    P = A @ B @ C @ D
+    assert torch.norm(P - U @ torch.diag(S) @ V.T) / torch.norm(P) < 1e-10
+
+
+def test_rsvd_edge_cases():
+    A = _rand(30, 20, 9)
+    U, S, V = gb.svd_lowrank(A, q=50, niter=2)  # q clamped to min(m, n)
+    assert U.shape == (30, 20) and S.shape == (20,)
+    U, S, V = gb.svd_lowrank(A, q=5, niter=0)
+    assert U.shape == (30, 5)
+    U, S, V = gb.svd_lowrank(A.T.contiguous(), q=8, niter=1)  # wide
+    assert U.shape == (20, 8) and V.shape == (30, 8)
+    sv = torch.linalg.svdvals(A.cpu())
+    U, S, V = gb.svd_lowrank(A, q=20, niter=2)
+    assert torch.allclose(S.cpu(), sv, rtol=1e-10, atol=1e-12)
+
+
+def test_large_rank_deficient_rsvd_falls_back_and_stays_orthonormal():
+    """n q^2 above the Householder size switches to Cholesky-QR3; an exactly
+    rank-8 product makes its Gram singular, so the Householder re-run must
+    produce the orthonormal basis."""
+    A, B = _rand(3000, 8, 11), _rand(8, 2000, 12)
+    U, S, V = gb.fused_matmul_svd_lowrank(A, B, q=60, niter=2)
+    top = U[:, :8]
+    eye = torch.eye(8, dtype=torch.float64, device="cuda")
+    assert torch.allclose(top.T @ top, eye, atol=1e-10)
+    P = A @ B
+    assert torch.norm(P - U[:, :8] @ torch.diag(S[:8]) @ V[:, :8].T) / torch.norm(P) < 1e-10
+    assert S[8] / S[0] < 1e-12
+
+
+def test_thin_svd_matches_lapack():
+    for m, n in [(64, 64), (200, 37), (37, 200)]:
+        A = _rand(m, n, m + n)
+        U, S, V = gb.svd(A)
+        assert torch.allclose(S.cpu(), torch.linalg.svdvals(A.cpu()), rtol=1e-12, atol=1e-12)
+        r = min(m, n)
+        assert torch.allclose(U @ torch.diag(S) @ V.T, A, atol=1e-11)
+        assert torch.allclose(V.T @ V, torch.eye(r, dtype=torch.float64, device="cuda"), atol=1e-12)
+
+
+def test_fp64_matmul_exact_order_tolerance():
+    A, B = _rand(300, 257, 1), _rand(257, 129, 2)
+    C = gb.matmul(A, B)
+    assert torch.allclose(C, A @ B, rtol=1e-13, atol=1e-12)
+
+
+def test_errors_are_raised_not_hidden():
+    z = load("move_d3_chi9.npz")
+    st = gpu_state(z, 9)
+    pc = gb.ProjectorCalculator(cfg_obj())
+    with pytest.raises(ValueError):
+        pc.calculate(st, [(100, 100), (200, 200), (300, 300), (400, 400)], 0)
+    with pytest.raises(ValueError):
+        gb.svd_lowrank(torch.zeros(4, 4, dtype=torch.float32, device="cuda"))
+    assert gb._abi.device_status() == 0

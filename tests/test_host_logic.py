@@ -1,0 +1,70 @@
+"""Host-side logic of the package (no GPU): configuration, move order,
+site/bond bookkeeping and the state container."""
+
+import pytest
+import torch
+
+import acetn_gb300 as gb
+from oracle import ctm_oracle as orc
+
+
+def test_sweep_order_matches_reference_loop():
+    for nx, ny in [(2, 2), (3, 2), (2, 4)]:
+        assert gb.sweep_order(nx, ny) == orc.sweep_order(nx, ny)
+
+
+def test_site_and_bond_lists():
+    st = gb.IpepsState(2, 3, {"phys": 2, "bond": 2, "chi": 4}, device="cpu")
+    assert st.site_list == orc.build_site_list(2, 3)
+    assert [tuple(b) for b in st.bond_list] == orc.build_bond_list(2, 3)
+
+
+def test_config_defaults_and_validation():
+    cfg = gb.CTMRGConfig()
+    assert (cfg.steps, cfg.projectors, cfg.svd_type, cfg.svd_cutoff, cfg.rsvd_niter,
+            cfg.rsvd_oversampling) == (40, "half-system", "rsvd", 1e-12, 2, 2)
+    with pytest.raises(ValueError):
+        gb.ProjectorCalculator({"projectors": "quarter-system"})
+    with pytest.raises(TypeError):
+        gb.config.resolve({"no_such_field": 1})
+    pc = gb.ProjectorCalculator({"projectors": "full-system"})
+    assert pc.calculate == pc.calculate_full_system
+
+
+def test_reference_style_config_object_is_accepted():
+    class RefCfg:
+        steps = 3
+        projectors = "half-system"
+        svd_type = "full-rank"
+        svd_cutoff = 1e-10
+        rsvd_niter = 1
+        rsvd_oversampling = 4
+        disable_progressbar = True
+    cfg = gb.config.resolve(RefCfg())
+    assert cfg.svd_type == "full-rank" and cfg.rsvd_oversampling == 4 and cfg.precision == "fp64"
+
+
+def test_unknown_site_raises_value_error():
+    st = gb.IpepsState(2, 2, {"phys": 2, "bond": 2, "chi": 4}, device="cpu")
+    with pytest.raises(ValueError):
+        st[(3, 3)]
+
+
+def test_state_checkpoint_round_trip(tmp_path):
+    st = orc.random_state(2, 4, seed=3)
+    g = gb.IpepsState.from_arrays(st.sites, 2, 2, 4, device="cpu")
+    g.save(tmp_path / "s.pt")
+    h = gb.IpepsState.load(tmp_path / "s.pt", device="cpu")
+    for s in st.sites:
+        assert torch.equal(g[s]["A"], h[s]["A"])
+        for k in range(4):
+            assert torch.equal(g[s]["E"][k], h[s]["E"][k])
+
+
+def test_models_match_oracle_hamiltonians():
+    import numpy as np
+    h = gb.HeisenbergModel(1.0).two_site_hamiltonian(None).numpy()
+    assert np.allclose(h, orc.heisenberg_model(1.0)["two_site_ham"](None))
+    m = gb.IsingModel(1.0, 3.0)
+    assert np.allclose(m.two_site_hamiltonian(None).numpy(), orc.ising_model(1.0, 3.0)["two_site_ham"](None))
+    assert np.allclose(m.one_site_hamiltonian((0, 0)).numpy(), -3.0 * np.array([[0, 1], [1, 0]]))
