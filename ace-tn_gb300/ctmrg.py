@@ -5,7 +5,7 @@ non-distributed branch: ``config.steps`` iterations of left/right moves for
 every column followed by up/down moves for every row.
 """
 
-from tqdm import tqdm
+from ._progress import tqdm
 
 from .config import resolve
 from .directional_mover import DirectionalMover

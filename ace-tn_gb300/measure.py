@@ -8,7 +8,7 @@ reference's tables with tqdm.write.
 """
 
 import torch
-from tqdm import tqdm
+from ._progress import tqdm
 
 from .rdm import RDM
 
