@@ -14,7 +14,7 @@ from . import _build
 
 CTM_OK, CTM_ERR_INVALID, CTM_ERR_UNSUPPORTED, CTM_ERR_WORKSPACE = 0, 1, 2, 3
 CTM_ERR_CUDA, CTM_ERR_NUMERIC, CTM_ERR_TIMEOUT = 4, 5, 6
-PREC = {"fp64": 0, "mixed": 1}
+PREC = {"fp64": 0, "mixed": 1, "bf16": 2}
 PROJ = {"half-system": 0, "full-system": 1}
 SVD = {"rsvd": 0, "full-rank": 1}
 

@@ -6,6 +6,7 @@
 // strings are the reference's own index expressions, evaluated by the
 // strided GETT engine without permute copies.
 #include "engine.cuh"
+#include "tc_gemm.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -691,8 +692,22 @@ int ctm_matmul(const double* A, const double* B, double* C, int64_t M, int64_t N
     if (precision == CTM_PREC_FP64) {
       einsum(c, "ik,kj->ij", View(A, {M, K}), View(B, {K, N}), View(C, {M, N}));
     } else {
-      CTM_REQUIRE(precision == CTM_PREC_MIXED, CTM_ERR_INVALID, "bad precision");
-      CTM_REQUIRE(false, CTM_ERR_UNSUPPORTED, "mixed-precision matmul not built");
+      CTM_REQUIRE(precision == CTM_PREC_MIXED || precision == CTM_PREC_BF16, CTM_ERR_INVALID,
+                  "bad precision");
+      const bool x3 = precision == CTM_PREC_MIXED;
+      const int64_t lda = tc_ld(K);
+      Scope scope(c);
+      bf16* ah = c.alloc<bf16>(size_t(M) * lda);
+      bf16* al = x3 ? c.alloc<bf16>(size_t(M) * lda) : nullptr;
+      bf16* bh = c.alloc<bf16>(size_t(N) * lda);
+      bf16* bl = x3 ? c.alloc<bf16>(size_t(N) * lda) : nullptr;
+      split_bf16(c, A, M, K, K, false, ah, al, lda);
+      split_bf16(c, B, K, N, N, true, bh, bl, lda);
+      TcOperand a{ah, al, M, K, lda}, b{bh, bl, N, K, lda};
+      TcOut out;
+      out.f64 = C;
+      out.ld_f64 = N;
+      tc_gemm(c, a, b, x3 ? TcMode::kBf16x3 : TcMode::kBf16x1, out);
     }
   });
 }

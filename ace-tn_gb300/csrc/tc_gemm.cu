@@ -1,0 +1,493 @@
+// tcgen05 GEMM for sm_103a: TMA loads (128-byte swizzle) into a multi-stage
+// shared-memory ring, one thread issuing tcgen05.mma into a TMEM accumulator
+// (M = 128 rows per CTA, N up to 256 columns), split-K over the grid's z
+// dimension, and an epilogue reading TMEM with tcgen05.ld into FP32 partial
+// tiles that a second kernel reduces (fixed order) into the requested
+// output formats.
+//
+// Every mbarrier wait is bounded: on expiry the kernel records bit 2 in the
+// status word, stops issuing work, waits (bounded) for its own outstanding
+// copies and MMAs, frees its tensor memory and returns.
+#include <cuda.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "engine.cuh"
+#include "tc_gemm.cuh"
+
+namespace ctm {
+
+namespace {
+
+constexpr int kBM = 128;         // rows of A per CTA (MMA M)
+constexpr int kBK = 64;          // K per stage: 64 BF16 = 128 bytes = one swizzle row
+constexpr int kThreads = 128;    // 4 warps: TMEM lanes 0-127 in the epilogue
+constexpr uint32_t kTmemCols = 256;
+constexpr int64_t kSpinLimit = 4LL * 1000 * 1000;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n"
+      " .reg .pred P1;\n"
+      " mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n"
+      " selp.b32 %0, 1, 0, P1;\n"
+      "}\n"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Bounded wait on an mbarrier phase; false when the limit expired.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (int64_t i = 0; i < kSpinLimit; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (i > 32) __nanosleep(64);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle,
+// 8-row core-matrix groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t smem_desc(const void* p) {
+  const uint64_t addr = smem_u32(p);
+  uint64_t d = (addr >> 4) & 0x3FFFull;  // start address
+  d |= uint64_t(1) << 16;                // leading byte offset (unused with 128B swizzle)
+  d |= uint64_t(1024 >> 4) << 32;        // stride byte offset
+  d |= uint64_t(1) << 46;                // descriptor version (tcgen05)
+  d |= uint64_t(2) << 61;                // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B,
+// both K-major, shape M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n"
+      " .reg .pred p;\n"
+      " setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+      "}\n" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct GemmParams {
+  int ntile;         // MMA N (multiple of 16, <= 256)
+  int kb_total;      // 64-wide K blocks
+  int kb_per_split;
+  int stages;
+  int mode;          // 1 or 3
+  float* part;       // [split][m_pad][n_pad]
+  int m_pad, n_pad;
+  int* status;
+};
+
+__global__ void __launch_bounds__(kThreads, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tAl,
+                   const __grid_constant__ CUtensorMap tB, const __grid_constant__ CUtensorMap tBl,
+                   const GemmParams p) {
+  extern __shared__ uint8_t dyn_smem[];
+  uint8_t* base = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(dyn_smem) + 1023) & ~uintptr_t(1023));
+  const uint32_t a_bytes = kBM * kBK * 2;
+  const uint32_t b_bytes = uint32_t(p.ntile) * kBK * 2;
+  const uint32_t half_bytes = a_bytes + b_bytes;
+  const uint32_t stage_bytes = half_bytes * (p.mode == 3 ? 2 : 1);
+  uint64_t* full = reinterpret_cast<uint64_t*>(base + size_t(p.stages) * stage_bytes);
+  uint64_t* empty = full + p.stages;
+  uint64_t* tfull = empty + p.stages;
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(tfull + 1);
+  __shared__ int s_fail;
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    s_fail = 0;
+    for (int s = 0; s < p.stages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(tfull, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_holder)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_holder;
+
+  const int kb0 = blockIdx.z * p.kb_per_split;
+  const int kb1 = min(kb0 + p.kb_per_split, p.kb_total);
+  const int nkb = kb1 - kb0;
+  const int m0 = blockIdx.x * kBM;
+  const int n0 = blockIdx.y * p.ntile;
+  int issued_loads = 0;  // producer: stages handed to TMA
+
+  if (threadIdx.x == 0) {
+    // ---------------- TMA producer
+    for (int i = 0; i < nkb; ++i) {
+      const int s = i % p.stages;
+      const uint32_t ph = (i / p.stages) & 1;
+      if (!mbar_wait(&empty[s], ph ^ 1)) {
+        atomicOr(&s_fail, 1);
+        break;
+      }
+      uint8_t* st = base + size_t(s) * stage_bytes;
+      mbar_expect_tx(&full[s], stage_bytes);
+      const int x = (kb0 + i) * kBK;
+      tma_load_2d(st, &tA, x, m0, &full[s]);
+      tma_load_2d(st + a_bytes, &tB, x, n0, &full[s]);
+      if (p.mode == 3) {
+        tma_load_2d(st + half_bytes, &tAl, x, m0, &full[s]);
+        tma_load_2d(st + half_bytes + a_bytes, &tBl, x, n0, &full[s]);
+      }
+      issued_loads = i + 1;
+    }
+  } else if (threadIdx.x == 32) {
+    // ---------------- MMA issuer
+    const uint32_t idesc = idesc_bf16(kBM, p.ntile);
+    for (int i = 0; i < nkb; ++i) {
+      const int s = i % p.stages;
+      const uint32_t ph = (i / p.stages) & 1;
+      if (!mbar_wait(&full[s], ph)) {
+        atomicOr(&s_fail, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      uint8_t* st = base + size_t(s) * stage_bytes;
+#pragma unroll
+      for (int kk = 0; kk < kBK / 16; ++kk) {
+        const uint64_t ah = smem_desc(st + kk * 32);
+        const uint64_t bh = smem_desc(st + a_bytes + kk * 32);
+        mma_bf16(tmem, ah, bh, idesc, (i > 0 || kk > 0) ? 1u : 0u);
+        if (p.mode == 3) {
+          const uint64_t al = smem_desc(st + half_bytes + kk * 32);
+          const uint64_t bl = smem_desc(st + half_bytes + a_bytes + kk * 32);
+          mma_bf16(tmem, ah, bl, idesc, 1u);
+          mma_bf16(tmem, al, bh, idesc, 1u);
+        }
+      }
+      mma_commit(&empty[s]);
+    }
+    mma_commit(tfull);
+  }
+
+  // ---------------- epilogue: TMEM -> FP32 partial tile
+  bool ok = mbar_wait(tfull, 0);
+  if (!ok) atomicOr(&s_fail, 1);
+  __syncwarp();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const int row = m0 + warp * 32 + lane;
+  float* out = p.part + (size_t(blockIdx.z) * p.m_pad + row) * p.n_pad + n0;
+  if (ok) {
+    for (int c = 0; c < p.ntile; c += 16) {
+      float v[16];
+      tmem_ld16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c), v);
+      if (row < p.m_pad) {
+#pragma unroll
+        for (int j = 0; j < 16; j += 4)
+          *reinterpret_cast<float4*>(out + c + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+      }
+    }
+  }
+  // on failure: let in-flight copies land before the CTA's memory goes away
+  if (threadIdx.x == 0 && s_fail) {
+    for (int i = 0; i < issued_loads; ++i) {
+      const int s = i % p.stages;
+      (void)mbar_wait(&full[s], (i / p.stages) & 1);
+    }
+    atomicOr(p.status, 2);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols)
+                 : "memory");
+  }
+}
+
+// Sums the split-K partials in order and writes the requested outputs.
+struct ReduceParams {
+  const float* part;
+  int splits, m_pad, n_pad;
+  int64_t M, N;
+  double alpha;
+  double* f64;
+  int64_t ld_f64;
+  int f64_trans;
+  float* f32;
+  int64_t ld_f32;
+  bf16* hi_t;
+  bf16* lo_t;
+  int64_t ld_t;
+};
+
+__global__ void tc_reduce_kernel(const ReduceParams r) {
+  // 32 x 32 tile through shared memory so both row- and column-major
+  // destinations are written with contiguous warps
+  __shared__ double tile[32][33];
+  const int64_t m0 = int64_t(blockIdx.x) * 32, n0 = int64_t(blockIdx.y) * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+  for (int yy = ty; yy < 32; yy += 8) {
+    const int64_t m = m0 + yy, n = n0 + tx;
+    double s = 0.0;
+    if (m < r.M && n < r.N) {
+      for (int t = 0; t < r.splits; ++t)
+        s += double(r.part[(size_t(t) * r.m_pad + m) * r.n_pad + n]);
+      s *= r.alpha;
+      if (r.f64 != nullptr && !r.f64_trans) r.f64[m * r.ld_f64 + n] = s;
+      if (r.f32 != nullptr) r.f32[m * r.ld_f32 + n] = float(s);
+    }
+    tile[yy][tx] = s;
+  }
+  __syncthreads();
+  for (int yy = ty; yy < 32; yy += 8) {
+    const int64_t n = n0 + yy, m = m0 + tx;
+    if (m >= r.M || n >= r.N) continue;
+    const double s = tile[tx][yy];
+    if (r.f64 != nullptr && r.f64_trans) r.f64[n * r.ld_f64 + m] = s;
+    if (r.hi_t != nullptr) {
+      const bf16 h = __double2bfloat16(s);
+      r.hi_t[n * r.ld_t + m] = h;
+      if (r.lo_t != nullptr) r.lo_t[n * r.ld_t + m] = __double2bfloat16(s - double(__bfloat162float(h)));
+    }
+  }
+}
+
+__global__ void split_bf16_kernel(const double* src, int64_t rows, int64_t cols, int64_t ld_src,
+                                  int transpose, bf16* hi, bf16* lo, int64_t ld_dst) {
+  __shared__ double tile[32][33];
+  const int64_t r0 = int64_t(blockIdx.y) * 32, c0 = int64_t(blockIdx.x) * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  if (!transpose) {
+    for (int yy = ty; yy < 32; yy += 8) {
+      const int64_t r = r0 + yy, c = c0 + tx;
+      if (r < rows && c < cols) {
+        const double x = src[r * ld_src + c];
+        const bf16 h = __double2bfloat16(x);
+        hi[r * ld_dst + c] = h;
+        if (lo != nullptr) lo[r * ld_dst + c] = __double2bfloat16(x - double(__bfloat162float(h)));
+      }
+    }
+    return;
+  }
+  for (int yy = ty; yy < 32; yy += 8) {
+    const int64_t r = r0 + yy, c = c0 + tx;
+    tile[yy][tx] = (r < rows && c < cols) ? src[r * ld_src + c] : 0.0;
+  }
+  __syncthreads();
+  for (int yy = ty; yy < 32; yy += 8) {
+    const int64_t c = c0 + yy, r = r0 + tx;  // destination row c, column r
+    if (r < rows && c < cols) {
+      const double x = tile[tx][yy];
+      const bf16 h = __double2bfloat16(x);
+      hi[c * ld_dst + r] = h;
+      if (lo != nullptr) lo[c * ld_dst + r] = __double2bfloat16(x - double(__bfloat162float(h)));
+    }
+  }
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point, so the
+// library does not link libcuda (it still loads on machines without a driver).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  if (fn == nullptr) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    CTM_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                              cudaEnableDefault, &q));
+    CTM_REQUIRE(p != nullptr && q == cudaDriverEntryPointSuccess, CTM_ERR_CUDA,
+                "cuTensorMapEncodeTiled is not available from the driver");
+    fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+void make_map(CUtensorMap* map, const bf16* ptr, int64_t rows, int64_t k, int64_t ld,
+              uint32_t box_rows) {
+  CTM_REQUIRE(ptr != nullptr, CTM_ERR_INVALID, "tc_gemm: operand pointer is NULL");
+  CTM_REQUIRE((reinterpret_cast<uintptr_t>(ptr) & 15) == 0, CTM_ERR_INVALID,
+              "tc_gemm: operand must be 16-byte aligned");
+  CTM_REQUIRE(ld % 8 == 0 && ld >= k, CTM_ERR_INVALID, "tc_gemm: leading dimension");
+  const cuuint64_t dims[2] = {cuuint64_t(k), cuuint64_t(rows)};
+  const cuuint64_t strides[1] = {cuuint64_t(ld) * 2};
+  const cuuint32_t box[2] = {uint32_t(kBK), box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult res = encode_tiled()(
+      map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(ptr), dims, strides, box, estr,
+      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  CTM_REQUIRE(res == CUDA_SUCCESS, CTM_ERR_CUDA,
+              "cuTensorMapEncodeTiled failed with code " + std::to_string(int(res)));
+}
+
+int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    CTM_CUDA(cudaGetDevice(&dev));
+    CTM_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+  }
+  return n;
+}
+
+}  // namespace
+
+void split_bf16(Ctx& c, const double* src, int64_t rows, int64_t cols, int64_t ld_src,
+                bool transpose, bf16* hi, bf16* lo, int64_t ld_dst) {
+  if (c.sizing() || rows * cols == 0) return;
+  dim3 grid(unsigned((cols + 31) / 32), unsigned((rows + 31) / 32));
+  CTM_REQUIRE(grid.y <= 65535, CTM_ERR_UNSUPPORTED, "split_bf16: too many rows");
+  split_bf16_kernel<<<grid, 256, 0, c.stream>>>(src, rows, cols, ld_src, transpose ? 1 : 0, hi, lo,
+                                                ld_dst);
+  CTM_LAUNCH_CHECK();
+}
+
+void tc_gemm(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, const TcOut& out) {
+  CTM_REQUIRE(A.k == B.k && A.k >= 1 && A.rows >= 1 && B.rows >= 1, CTM_ERR_INVALID,
+              "tc_gemm: operand shapes");
+  const int imode = static_cast<int>(mode);
+  const int64_t M = A.rows, N = B.rows, K = A.k;
+  // N tiling: MMA N must be a multiple of 16 up to 256
+  const int64_t n_tiles = (N + 255) / 256;
+  int ntile = static_cast<int>(((N + n_tiles - 1) / n_tiles + 15) / 16 * 16);
+  ntile = std::max(ntile, 16);
+  const int64_t m_tiles = (M + kBM - 1) / kBM;
+  const int kb_total = static_cast<int>((K + kBK - 1) / kBK);
+  // split K so that the grid covers the SMs at least once
+  const int64_t base_ctas = m_tiles * n_tiles;
+  const int sms = c.sizing() ? 152 : sm_count();
+  int splits = static_cast<int>(std::min<int64_t>((sms + base_ctas - 1) / base_ctas,
+                                                  std::max(1, kb_total / 4)));
+  splits = std::max(splits, 1);
+  const int kb_per_split = (kb_total + splits - 1) / splits;
+  splits = (kb_total + kb_per_split - 1) / kb_per_split;
+  const int m_pad = static_cast<int>(m_tiles * kBM);
+  const int n_pad = static_cast<int>(n_tiles * ntile);
+  const uint32_t stage_bytes = uint32_t(kBM * kBK * 2 + ntile * kBK * 2) * (imode == 3 ? 2 : 1);
+  const int stages = std::max(2, std::min(6, int((200 * 1024) / stage_bytes)));
+  const size_t smem = size_t(stages) * stage_bytes + 1024 + 256;
+  Scope scope(c);
+  float* part = c.alloc<float>(size_t(splits) * m_pad * n_pad);
+  if (c.sizing()) return;
+  CTM_REQUIRE(imode == 1 || (A.lo != nullptr && B.lo != nullptr), CTM_ERR_INVALID,
+              "tc_gemm: 3xBF16 needs lo parts");
+  CTM_REQUIRE(m_tiles <= 0x7fffffff && n_tiles <= 65535 && splits <= 65535, CTM_ERR_UNSUPPORTED,
+              "tc_gemm: grid too large");
+  CUtensorMap tA, tAl, tB, tBl;
+  make_map(&tA, A.hi, A.rows, K, A.ld, kBM);
+  make_map(&tB, B.hi, B.rows, K, B.ld, uint32_t(ntile));
+  if (imode == 3) {
+    make_map(&tAl, A.lo, A.rows, K, A.ld, kBM);
+    make_map(&tBl, B.lo, B.rows, K, B.ld, uint32_t(ntile));
+  } else {
+    tAl = tA;
+    tBl = tB;
+  }
+  GemmParams p{};
+  p.ntile = ntile;
+  p.kb_total = kb_total;
+  p.kb_per_split = kb_per_split;
+  p.stages = stages;
+  p.mode = imode;
+  p.part = part;
+  p.m_pad = m_pad;
+  p.n_pad = n_pad;
+  p.status = status_flags(c);
+  CTM_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(smem)));
+  const dim3 grid(static_cast<unsigned>(m_tiles), static_cast<unsigned>(n_tiles),
+                  static_cast<unsigned>(splits));
+  {
+    KernelTimer timer(c.stream, kTagTcGemm, 2.0 * double(M) * N * K * imode);
+    tc_gemm_kernel<<<grid, kThreads, smem, c.stream>>>(tA, tAl, tB, tBl, p);
+    CTM_LAUNCH_CHECK();
+  }
+  ReduceParams r{};
+  r.part = part;
+  r.splits = splits;
+  r.m_pad = m_pad;
+  r.n_pad = n_pad;
+  r.M = M;
+  r.N = N;
+  r.alpha = out.alpha;
+  r.f64 = out.f64;
+  r.ld_f64 = out.ld_f64;
+  r.f64_trans = out.f64_trans ? 1 : 0;
+  r.f32 = out.f32;
+  r.ld_f32 = out.ld_f32;
+  r.hi_t = out.hi_t;
+  r.lo_t = out.lo_t;
+  r.ld_t = out.ld_t;
+  dim3 rg(unsigned((M + 31) / 32), unsigned((N + 31) / 32));
+  CTM_REQUIRE(rg.y <= 65535, CTM_ERR_UNSUPPORTED, "tc_gemm: output too wide");
+  tc_reduce_kernel<<<rg, 256, 0, c.stream>>>(r);
+  CTM_LAUNCH_CHECK();
+}
+
+}  // namespace ctm

@@ -45,8 +45,9 @@ enum {
 /* Arithmetic of a projector computation. */
 enum {
   CTM_PREC_FP64 = 0,   /* every product in FP64: the drop-in path                     */
-  CTM_PREC_MIXED = 1   /* tensor-core BF16 range finder, 3xBF16 products feeding the
+  CTM_PREC_MIXED = 1,  /* tensor-core BF16 range finder, 3xBF16 products feeding the
                           projectors, FP64 Rayleigh-Ritz SVD, truncation and scaling */
+  CTM_PREC_BF16 = 2    /* ctm_matmul only: one BF16 tensor-core pass, FP32 accumulation */
 };
 
 /* Projector construction (acetn/ipeps/ipeps_config.py:16-24 CTMRGConfig). */
@@ -181,8 +182,9 @@ int ctm_svd_f64(const double* a, int64_t m, int64_t n, double* U, double* S, dou
                 void* ws, size_t* ws_bytes, ctm_stream_t stream);
 
 /* Matrix product C = A @ B of FP64 row-major matrices, with the library's
- * arithmetic: CTM_PREC_FP64 (exact FP64 FMAs) or CTM_PREC_MIXED (3xBF16
- * split products on tcgen05 tensor cores, FP32 accumulation).
+ * arithmetic: CTM_PREC_FP64 (FP64 FMAs), CTM_PREC_MIXED (3xBF16 split
+ * products on tcgen05 tensor cores, FP32 accumulation) or CTM_PREC_BF16 (one
+ * BF16 tensor-core pass).
  * No counterpart in the reference (torch.matmul); exposed to test and
  * measure the GEMM engines behind every entry point above. */
 int ctm_matmul(const double* A, const double* B, double* C, int64_t M, int64_t N,
