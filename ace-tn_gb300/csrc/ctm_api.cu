@@ -19,20 +19,6 @@ namespace {
 
 thread_local std::string g_last_error;
 
-struct Site {
-  const ctm_site_f64* s;
-  int64_t D, d;
-  View A(int k) const { return bond_permute(s->A, D, d, k); }
-  View C(int k) const {
-    k = ((k % 4) + 4) % 4;
-    return View(s->C[k], {s->c_rows[k], s->c_cols[k]});
-  }
-  View E(int k) const {
-    k = ((k % 4) + 4) % 4;
-    return View(s->E[k], {s->e_rows[k], s->e_cols[k], D, D});
-  }
-};
-
 void check_site(const ctm_site_f64* s, int64_t D, int64_t d) {
   CTM_REQUIRE(s != nullptr && s->A != nullptr, CTM_ERR_INVALID, "site tensor A is NULL");
   CTM_REQUIRE(D >= 1 && d >= 1, CTM_ERR_INVALID, "bond and physical dimensions must be >= 1");
@@ -43,6 +29,8 @@ void check_site(const ctm_site_f64* s, int64_t D, int64_t d) {
                 CTM_ERR_INVALID, "corner/edge tensor with an empty dimension");
   }
 }
+
+}  // namespace
 
 // Quarter-tensor matrix dimensions of direction k: rows = (c, r, R), cols = (e, d, D).
 void quarter_dims(const Site& S, int k, int64_t& rows, int64_t& cols, int64_t sh[6]) {
@@ -61,7 +49,6 @@ void quarter_dims(const Site& S, int k, int64_t& rows, int64_t& cols, int64_t sh
   cols = sh[3] * S.D * S.D;
 }
 
-}  // namespace
 
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 
@@ -543,12 +530,17 @@ int ctm_quarter_tensor(const ctm_site_f64* site, int64_t D, int64_t d, int32_t k
                        ctm_stream_t stream) {
   return with_workspace(ws, ws_bytes, as_stream(stream), [&](Ctx& c) {
     check_site(site, D, d);
-    CTM_REQUIRE(precision == CTM_PREC_FP64, CTM_ERR_UNSUPPORTED,
-                "ctm_quarter_tensor: FP64 output only");
+    CTM_REQUIRE(precision == CTM_PREC_FP64 || precision == CTM_PREC_MIXED, CTM_ERR_INVALID,
+                "bad precision");
     Site S{site, D, d};
-    int64_t sh[6];
+    int64_t sh[6], rows, cols;
     if (!c.sizing()) CTM_REQUIRE(Q != nullptr, CTM_ERR_INVALID, "Q is NULL");
-    quarter_tensor(c, S, k, Q, sh);
+    if (precision == CTM_PREC_MIXED) {
+      quarter_dims(S, k, rows, cols, sh);
+      quarter_tensor_mixed_f64(c, S, k, Q);
+    } else {
+      quarter_tensor(c, S, k, Q, sh);
+    }
     if (qshape != nullptr)
       for (int i = 0; i < 6; ++i) qshape[i] = sh[i];
   });
@@ -594,9 +586,10 @@ int ctm_calculate_projectors(const ctm_site_f64* const* sites, int64_t D, int64_
       CTM_REQUIRE(opts->svd_type != CTM_SVD_RSVD || omega != nullptr, CTM_ERR_INVALID,
                   "omega is NULL for the randomized SVD");
     }
-    CTM_REQUIRE(opts->precision == CTM_PREC_FP64, CTM_ERR_UNSUPPORTED,
-                "mixed precision is not built yet");
-    calculate_projectors(c, S, k, *opts, omega, P1, P2, chi_new);
+    if (opts->precision == CTM_PREC_MIXED)
+      calculate_projectors_mixed(c, S, k, *opts, omega, P1, P2, chi_new);
+    else
+      calculate_projectors(c, S, k, *opts, omega, P1, P2, chi_new);
   });
 }
 
@@ -705,8 +698,7 @@ int ctm_matmul(const double* A, const double* B, double* C, int64_t M, int64_t N
       split_bf16(c, B, K, N, N, true, bh, bl, lda);
       TcOperand a{ah, al, M, K, lda}, b{bh, bl, N, K, lda};
       TcOut out;
-      out.f64 = C;
-      out.ld_f64 = N;
+      out.add(TcKind::kF64, C, TcLayout::rows(M, N, N));
       tc_gemm(c, a, b, x3 ? TcMode::kBf16x3 : TcMode::kBf16x1, out);
     }
   });

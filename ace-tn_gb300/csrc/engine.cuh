@@ -41,6 +41,31 @@ void scale_columns_compact(Ctx& c, const double* in, int64_t rows, int64_t cap,
 
 const char* g_last_error_cstr();
 
+// One site's tensors in the reference layouts (acetn/ipeps/site_tensor.py:41-83).
+struct Site {
+  const ctm_site_f64* s;
+  int64_t D, d;
+  View A(int k) const { return bond_permute(s->A, D, d, k); }
+  View C(int k) const {
+    k = ((k % 4) + 4) % 4;
+    return View(s->C[k], {s->c_rows[k], s->c_cols[k]});
+  }
+  View E(int k) const {
+    k = ((k % 4) + 4) % 4;
+    return View(s->E[k], {s->e_rows[k], s->e_cols[k], D, D});
+  }
+};
+
+// Quarter-tensor matrix shape of direction k: rows (c, r, R), cols (e, d, D).
+void quarter_dims(const Site& S, int k, int64_t& rows, int64_t& cols, int64_t sh[6]);
+// make_quarter_tensor in FP64 (acetn/renormalization/projectors.py:35-60).
+void quarter_tensor(Ctx& c, const Site& S, int k, double* Q, int64_t qshape[6]);
+// make_quarter_tensor on tensor cores (3xBF16), returned as FP64 hi + lo.
+void quarter_tensor_mixed_f64(Ctx& c, const Site& S, int k, double* Q);
+// Half-system rSVD projectors with tensor-core arithmetic (CTM_PREC_MIXED).
+void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg_opts& o,
+                                const double* omega, double* P1, double* P2, int64_t* chi_new);
+
 // Device-side failure flags (bit set by kernels: 1 = factorization failed,
 // 2 = iteration limit reached); read and cleared by ctm_device_status().
 int* status_flags(Ctx& c);

@@ -1,0 +1,279 @@
+// Mixed-precision projector construction (CTM_PREC_MIXED), half-system rSVD:
+//  * range finder (the power-iteration products) in one BF16 tensor-core
+//    pass with FP32 accumulation;
+//  * Rayleigh-Ritz products B = Q^T Q1 Q4 and the projector products
+//    P1 = Q1^T U, P2 = Q4 V in 3xBF16 split precision;
+//  * orthonormalization, the SVD of B, the truncation and the s^(-1/2)
+//    scaling in FP64.
+// Algorithm of acetn/renormalization/projectors.py:138-174 with
+// acetn/linalg/fused_matmul_svd_lowrank.py:4-52.
+#include "engine.cuh"
+#include "tc_gemm.cuh"
+
+#include <algorithm>
+
+namespace ctm {
+
+namespace {
+
+// BF16 operands of one quarter matrix Q (rows x cols): Q itself (K = cols)
+// and its transpose (K = rows), hi and lo parts.
+struct QOps {
+  bf16 *q_hi = nullptr, *q_lo = nullptr, *t_hi = nullptr, *t_lo = nullptr;
+  int64_t rows = 0, cols = 0, ld = 0, ldt = 0;
+  TcOperand q(bool lo) const { return TcOperand{q_hi, lo ? q_lo : nullptr, rows, cols, ld}; }
+  TcOperand t(bool lo) const { return TcOperand{t_hi, lo ? t_lo : nullptr, cols, rows, ldt}; }
+};
+
+QOps alloc_ops(Ctx& c, int64_t rows, int64_t cols) {
+  QOps o;
+  o.rows = rows;
+  o.cols = cols;
+  o.ld = tc_ld(cols);
+  o.ldt = tc_ld(rows);
+  o.q_hi = c.alloc<bf16>(size_t(rows) * o.ld);
+  o.q_lo = c.alloc<bf16>(size_t(rows) * o.ld);
+  o.t_hi = c.alloc<bf16>(size_t(cols) * o.ldt);
+  o.t_lo = c.alloc<bf16>(size_t(cols) * o.ldt);
+  return o;
+}
+
+int64_t round8(int64_t x) { return (x + 7) / 8 * 8; }
+
+// make_quarter_tensor (acetn/renormalization/projectors.py:35-60) on tensor
+// cores, 3xBF16 throughout.  The four einsums become
+//   t1 = C E_k (FP64, the small chi^3 D^2 step),
+//   t2[(c,u,U)][(e,l,L)] = sum_a t1[a][(c,u,U)] E_{k+3}[e][a][l][L],
+//   t3[(c,u,e,l)][(R,D,P)] = sum_(U,L) t2 A*[L][U][R][D][P],
+//   Q[(c,R,e,D)][(r,d)] = sum_(l,u,p) t3 A[l][u][r][d][p],
+// each GEMM's epilogue storing its result directly in the K-major layout of
+// the next GEMM's operand (the permutes of the reference's einsums folded
+// into the store addresses), and the last one writing Q / max|Q| and its
+// transpose as BF16 hi/lo operands.
+QOps quarter_mixed(Ctx& c, const Site& S, int k) {
+  int64_t sh[6], rows, cols;
+  quarter_dims(S, k, rows, cols, sh);
+  QOps o = alloc_ops(c, rows, cols);
+  const View ak = S.A(k), ck = S.C(k), ek1 = S.E(3 + k), ek2 = S.E(k);
+  const int64_t a = ck.shape[0], cc = sh[0], E = sh[3], D = S.D, d = S.d, D2 = D * D;
+  const TcMode x3 = TcMode::kBf16x3;
+  Scope scope(c);
+  double* absmax = c.alloc<double>(1);
+  // t1 = C E_k (a x (c,u,U)), FP64
+  double* t1 = c.alloc<double>(size_t(a) * cc * D2);
+  einsum(c, "ab,bcuU->acuU", ck, ek2, View(t1, {a, cc, D, D}));
+  // t2 operands: A2 = t1^T ((c,u,U) x a), B2 = E_{k+3} as ((e,l,L) x a)
+  const int64_t ld2 = tc_ld(a);
+  bf16* a2h = c.alloc<bf16>(size_t(cc) * D2 * ld2);
+  bf16* a2l = c.alloc<bf16>(size_t(cc) * D2 * ld2);
+  split_bf16(c, t1, a, cc * D2, cc * D2, true, a2h, a2l, ld2);
+  bf16* b2h = c.alloc<bf16>(size_t(E) * D2 * ld2);
+  bf16* b2l = c.alloc<bf16>(size_t(E) * D2 * ld2);
+  {
+    Gather g;
+    g.nr = 2;
+    g.re[0] = E; g.rs[0] = ek1.stride[0];
+    g.re[1] = D2; g.rs[1] = 1;
+    g.nk = 1;
+    g.ke[0] = a; g.ks[0] = ek1.stride[1];
+    gather_split_bf16(c, ek1.p, g, b2h, b2l, ld2);
+  }
+  // t2 -> T2p[(c,u,e,l)][(U,L)], ld3
+  const int64_t ld3 = round8(D2);
+  const int64_t rows3 = cc * D * E * D;
+  bf16* t2h = c.alloc<bf16>(size_t(rows3) * ld3);
+  bf16* t2l = c.alloc<bf16>(size_t(rows3) * ld3);
+  {
+    TcLayout l;
+    l.nm = 3;
+    l.me[0] = cc; l.ms[0] = D * E * D * ld3;
+    l.me[1] = D;  l.ms[1] = E * D * ld3;
+    l.me[2] = D;  l.ms[2] = D;
+    l.nn = 3;
+    l.ne[0] = E; l.ns[0] = D * ld3;
+    l.ne[1] = D; l.ns[1] = ld3;
+    l.ne[2] = D; l.ns[2] = 1;
+    TcOut out;
+    out.add(TcKind::kBf16Hi, t2h, l).add(TcKind::kBf16Lo, t2l, l);
+    tc_gemm(c, TcOperand{a2h, a2l, cc * D2, a, ld2}, TcOperand{b2h, b2l, E * D2, a, ld2}, x3, out);
+  }
+  // t3: B3[(R,D,P)][(U,L)] = A*[L][U][R][D][P]
+  bf16* b3h = c.alloc<bf16>(size_t(D2) * d * ld3);
+  bf16* b3l = c.alloc<bf16>(size_t(D2) * d * ld3);
+  {
+    Gather g;
+    g.nr = 3;
+    g.re[0] = D; g.rs[0] = ak.stride[2];
+    g.re[1] = D; g.rs[1] = ak.stride[3];
+    g.re[2] = d; g.rs[2] = ak.stride[4];
+    g.nk = 2;
+    g.ke[0] = D; g.ks[0] = ak.stride[1];
+    g.ke[1] = D; g.ks[1] = ak.stride[0];
+    gather_split_bf16(c, ak.p, g, b3h, b3l, ld3);
+  }
+  // t3 -> T3p[(c,R,e,D)][(l,u,p)], ld4
+  const int64_t ld4 = round8(D2 * d);
+  bf16* t3h = c.alloc<bf16>(size_t(rows3) * ld4);
+  bf16* t3l = c.alloc<bf16>(size_t(rows3) * ld4);
+  {
+    TcLayout l;
+    l.nm = 4;
+    l.me[0] = cc; l.ms[0] = D * E * D * ld4;
+    l.me[1] = D;  l.ms[1] = d;
+    l.me[2] = E;  l.ms[2] = D * ld4;
+    l.me[3] = D;  l.ms[3] = D * d;
+    l.nn = 3;
+    l.ne[0] = D; l.ns[0] = E * D * ld4;
+    l.ne[1] = D; l.ns[1] = ld4;
+    l.ne[2] = d; l.ns[2] = 1;
+    TcOut out;
+    out.add(TcKind::kBf16Hi, t3h, l).add(TcKind::kBf16Lo, t3l, l);
+    tc_gemm(c, TcOperand{t2h, t2l, rows3, D2, ld3}, TcOperand{b3h, b3l, D2 * d, D2, ld3}, x3, out);
+  }
+  // Q: B4[(r,d)][(l,u,p)] = A[l][u][r][d][p]
+  bf16* b4h = c.alloc<bf16>(size_t(D2) * ld4);
+  bf16* b4l = c.alloc<bf16>(size_t(D2) * ld4);
+  {
+    Gather g;
+    g.nr = 2;
+    g.re[0] = D; g.rs[0] = ak.stride[2];
+    g.re[1] = D; g.rs[1] = ak.stride[3];
+    g.nk = 3;
+    g.ke[0] = D; g.ks[0] = ak.stride[0];
+    g.ke[1] = D; g.ks[1] = ak.stride[1];
+    g.ke[2] = d; g.ks[2] = ak.stride[4];
+    gather_split_bf16(c, ak.p, g, b4h, b4l, ld4);
+  }
+  {
+    TcLayout lq;  // Q[(c,r,R)][(e,d,D)] row-major, ld
+    lq.nm = 4;
+    lq.me[0] = cc; lq.ms[0] = D * D * o.ld;
+    lq.me[1] = D;  lq.ms[1] = o.ld;
+    lq.me[2] = E;  lq.ms[2] = D * D;
+    lq.me[3] = D;  lq.ms[3] = 1;
+    lq.nn = 2;
+    lq.ne[0] = D; lq.ns[0] = D * o.ld;
+    lq.ne[1] = D; lq.ns[1] = D;
+    TcLayout lt;  // Q^T, ldt
+    lt.nm = 4;
+    lt.me[0] = cc; lt.ms[0] = D * D;
+    lt.me[1] = D;  lt.ms[1] = 1;
+    lt.me[2] = E;  lt.ms[2] = D * D * o.ldt;
+    lt.me[3] = D;  lt.ms[3] = o.ldt;
+    lt.nn = 2;
+    lt.ne[0] = D; lt.ns[0] = D;
+    lt.ne[1] = D; lt.ns[1] = D * o.ldt;
+    TcOut out;
+    out.add(TcKind::kBf16Hi, o.q_hi, lq).add(TcKind::kBf16Lo, o.q_lo, lq);
+    out.add(TcKind::kBf16Hi, o.t_hi, lt).add(TcKind::kBf16Lo, o.t_lo, lt);
+    tc_gemm_absmax_normalized(c, TcOperand{t3h, t3l, rows3, D2 * d, ld4},
+                              TcOperand{b4h, b4l, D2, D2 * d, ld4}, x3, out, absmax);
+  }
+  return o;
+}
+
+// Y^T as a BF16 operand (q x n) from Y (n x q, ld)
+TcOperand yt_operand(Ctx& c, const double* Y, int64_t n, int64_t q, int64_t ldy, bool lo) {
+  const int64_t ld = tc_ld(n);
+  bf16* hi = c.alloc<bf16>(size_t(q) * ld);
+  bf16* lw = lo ? c.alloc<bf16>(size_t(q) * ld) : nullptr;
+  split_bf16(c, Y, n, q, ldy, true, hi, lw, ld);
+  return TcOperand{hi, lw, q, n, ld};
+}
+
+// C = A @ B^T written as the next operand (C^T, BF16 hi [+ lo]).
+TcOperand gemm_to_operand(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, bool lo) {
+  const int64_t M = A.rows, N = B.rows;
+  const int64_t ld = tc_ld(M);
+  bf16* hi = c.alloc<bf16>(size_t(N) * ld);
+  bf16* lw = lo ? c.alloc<bf16>(size_t(N) * ld) : nullptr;
+  TcOut out;
+  out.add(TcKind::kBf16Hi, hi, TcLayout::cols(M, N, ld));
+  if (lo) out.add(TcKind::kBf16Lo, lw, TcLayout::cols(M, N, ld));
+  tc_gemm(c, A, B, mode, out);
+  return TcOperand{hi, lw, N, M, ld};
+}
+
+void gemm_to_f64(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, double* C,
+                 int64_t ldc, bool transposed) {
+  TcOut out;
+  out.add(TcKind::kF64, C,
+          transposed ? TcLayout::cols(A.rows, B.rows, ldc) : TcLayout::rows(A.rows, B.rows, ldc));
+  tc_gemm(c, A, B, mode, out);
+}
+
+}  // namespace
+
+void quarter_tensor_mixed_f64(Ctx& c, const Site& S, int k, double* Q) {
+  Scope scope(c);
+  const QOps o = quarter_mixed(c, S, k);
+  join_bf16(c, o.q_hi, o.q_lo, o.rows, o.cols, o.ld, Q);
+}
+
+void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg_opts& o,
+                                const double* omega, double* P1, double* P2, int64_t* chi_new) {
+  CTM_REQUIRE(o.projectors == CTM_PROJ_HALF && o.svd_type == CTM_SVD_RSVD, CTM_ERR_UNSUPPORTED,
+              "mixed precision is implemented for half-system rSVD projectors");
+  Scope scope(c);
+  int64_t sh1[6], sh4[6], r1, c1, r4, c4;
+  quarter_dims(*S[0], k, r1, c1, sh1);
+  quarter_dims(*S[3], k + 3, r4, c4, sh4);
+  CTM_REQUIRE(c1 == r4, CTM_ERR_INVALID, "half-system: quarter tensors do not chain");
+  const int64_t m = r1, n = c4;
+  const int64_t q = std::min({o.chi + o.rsvd_oversampling, m, n});
+  const int64_t cap = std::min(o.chi, q);
+  // ---- quarter tensors as BF16 operands (tensor cores, 3xBF16)
+  const QOps A1 = quarter_mixed(c, *S[0], k);
+  const QOps A4 = quarter_mixed(c, *S[3], k + 3);
+  const TcMode x1 = TcMode::kBf16x1, x3 = TcMode::kBf16x3;
+  // ---- range finder: Y = Q1 (Q4 Omega), niter x [QR; Y = Q1 Q4 Q4^T Q1^T Y]
+  double* Y = c.alloc<double>(size_t(m) * q);
+  {
+    Scope s2(c);
+    const TcOperand om = yt_operand(c, omega, n, q, q, false);     // Omega^T (q x n)
+    const TcOperand t = gemm_to_operand(c, A4.q(false), om, x1, false);  // (Q4 Om)^T
+    gemm_to_f64(c, A1.q(false), t, x1, Y, q, false);
+  }
+  for (int it = 0; it < o.rsvd_niter; ++it) {
+    orthonormalize(c, Y, m, q, nullptr);
+    Scope s2(c);
+    const TcOperand yt = yt_operand(c, Y, m, q, q, false);
+    const TcOperand z1 = gemm_to_operand(c, A1.t(false), yt, x1, false);  // (Q1^T Y)^T
+    const TcOperand z2 = gemm_to_operand(c, A4.t(false), z1, x1, false);  // (Q4^T z1)^T
+    const TcOperand z3 = gemm_to_operand(c, A4.q(false), z2, x1, false);  // (Q4 z2)^T
+    gemm_to_f64(c, A1.q(false), z3, x1, Y, q, false);
+  }
+  orthonormalize(c, Y, m, q, nullptr);
+  // ---- Rayleigh-Ritz: B = (Q^T Q1) Q4 in 3xBF16, SVD in FP64
+  double* Bm = c.alloc<double>(size_t(q) * n);
+  double* Ub = c.alloc<double>(size_t(q) * q);
+  double* s = c.alloc<double>(q);
+  double* V = c.alloc<double>(size_t(n) * q);
+  double* U = c.alloc<double>(size_t(m) * q);
+  {
+    Scope s2(c);
+    const TcOperand qt = yt_operand(c, Y, m, q, q, true);               // Q^T (q x m)
+    const TcOperand w = gemm_to_operand(c, A1.t(true), qt, x3, true);    // W = Q^T Q1 (q x c1)
+    gemm_to_f64(c, A4.t(true), w, x3, Bm, n, true);                     // B (q x n)
+  }
+  svd_thin(c, Bm, q, n, Ub, s, V);
+  einsum(c, "ik,kj->ij", View(Y, {m, q}), View(Ub, {q, q}), View(U, {m, q}));
+  // ---- truncation and projector products (3xBF16)
+  double* f = c.alloc<double>(cap);
+  truncation_factors(c, s, q, o.chi, o.svd_cutoff, f, cap, chi_new);
+  scale_columns(c, U, m, cap, q, f);
+  scale_columns(c, V, n, cap, q, f);
+  double* P1f = c.alloc<double>(size_t(c1) * cap);
+  double* P2f = c.alloc<double>(size_t(r4) * cap);
+  {
+    Scope s2(c);
+    const TcOperand ut = yt_operand(c, U, m, cap, q, true);  // (U f)^T (cap x m)
+    gemm_to_f64(c, A1.t(true), ut, x3, P1f, cap, false);    // Q1^T U f (c1 x cap)
+    const TcOperand vt = yt_operand(c, V, n, cap, q, true);  // (V f)^T (cap x n)
+    gemm_to_f64(c, A4.q(true), vt, x3, P2f, cap, false);    // Q4 V f (r4 x cap)
+  }
+  scale_columns_compact(c, P1f, c1, cap, nullptr, chi_new, P1);
+  scale_columns_compact(c, P2f, r4, cap, nullptr, chi_new, P2);
+}
+
+}  // namespace ctm

@@ -266,28 +266,51 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-// Sums the split-K partials in order and writes the requested outputs.
+// Sums the split-K partials in order and writes every destination.
 struct ReduceParams {
   const float* part;
   int splits, m_pad, n_pad;
   int64_t M, N;
   double alpha;
-  double* f64;
-  int64_t ld_f64;
-  int f64_trans;
-  float* f32;
-  int64_t ld_f32;
-  bf16* hi_t;
-  bf16* lo_t;
-  int64_t ld_t;
+  const double* inv_scale;
+  int nd;
+  TcDest d[4];
 };
 
+__device__ __forceinline__ int64_t lay_off(const TcLayout& l, int64_t m, int64_t n) {
+  int64_t o = 0;
+  for (int j = l.nm - 1; j >= 0; --j) {
+    o += (m % l.me[j]) * l.ms[j];
+    m /= l.me[j];
+  }
+  for (int j = l.nn - 1; j >= 0; --j) {
+    o += (n % l.ne[j]) * l.ns[j];
+    n /= l.ne[j];
+  }
+  return o;
+}
+
+__device__ __forceinline__ void store(const TcDest& d, int64_t off, double v) {
+  switch (d.kind) {
+    case TcKind::kF64: static_cast<double*>(d.p)[off] = v; break;
+    case TcKind::kF32: static_cast<float*>(d.p)[off] = float(v); break;
+    case TcKind::kBf16Hi: static_cast<bf16*>(d.p)[off] = __double2bfloat16(v); break;
+    case TcKind::kBf16Lo: {
+      const bf16 h = __double2bfloat16(v);
+      static_cast<bf16*>(d.p)[off] = __double2bfloat16(v - double(__bfloat162float(h)));
+      break;
+    }
+  }
+}
+
+// 32 x 32 output tile per block (32 x 8 threads).  Destinations whose
+// innermost column stride is 1 are written with the column index fastest,
+// the others with the row index fastest, so warps store contiguously in the
+// common row- and column-major cases.
 __global__ void tc_reduce_kernel(const ReduceParams r) {
-  // 32 x 32 tile through shared memory so both row- and column-major
-  // destinations are written with contiguous warps
   __shared__ double tile[32][33];
   const int64_t m0 = int64_t(blockIdx.x) * 32, n0 = int64_t(blockIdx.y) * 32;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   for (int yy = ty; yy < 32; yy += 8) {
     const int64_t m = m0 + yy, n = n0 + tx;
     double s = 0.0;
@@ -295,21 +318,18 @@ __global__ void tc_reduce_kernel(const ReduceParams r) {
       for (int t = 0; t < r.splits; ++t)
         s += double(r.part[(size_t(t) * r.m_pad + m) * r.n_pad + n]);
       s *= r.alpha;
-      if (r.f64 != nullptr && !r.f64_trans) r.f64[m * r.ld_f64 + n] = s;
-      if (r.f32 != nullptr) r.f32[m * r.ld_f32 + n] = float(s);
+      if (r.inv_scale != nullptr) s = s / r.inv_scale[0];
     }
     tile[yy][tx] = s;
   }
   __syncthreads();
-  for (int yy = ty; yy < 32; yy += 8) {
-    const int64_t n = n0 + yy, m = m0 + tx;
-    if (m >= r.M || n >= r.N) continue;
-    const double s = tile[tx][yy];
-    if (r.f64 != nullptr && r.f64_trans) r.f64[n * r.ld_f64 + m] = s;
-    if (r.hi_t != nullptr) {
-      const bf16 h = __double2bfloat16(s);
-      r.hi_t[n * r.ld_t + m] = h;
-      if (r.lo_t != nullptr) r.lo_t[n * r.ld_t + m] = __double2bfloat16(s - double(__bfloat162float(h)));
+  for (int k = 0; k < r.nd; ++k) {
+    const TcDest& d = r.d[k];
+    const bool n_fast = d.lay.ns[d.lay.nn - 1] == 1;
+    for (int yy = ty; yy < 32; yy += 8) {
+      const int64_t m = m0 + (n_fast ? yy : tx), n = n0 + (n_fast ? tx : yy);
+      if (m >= r.M || n >= r.N) continue;
+      store(d, lay_off(d.lay, m, n), n_fast ? tile[yy][tx] : tile[tx][yy]);
     }
   }
 }
@@ -408,7 +428,78 @@ void split_bf16(Ctx& c, const double* src, int64_t rows, int64_t cols, int64_t l
   CTM_LAUNCH_CHECK();
 }
 
-void tc_gemm(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, const TcOut& out) {
+namespace {
+
+__global__ void gather_split_kernel(const double* src, const Gather g, int64_t rows, int64_t K,
+                                    bf16* hi, bf16* lo, int64_t ld) {
+  const int64_t total = rows * K;
+  for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < total;
+       idx += int64_t(gridDim.x) * blockDim.x) {
+    int64_t r = idx / K, k = idx % K;
+    const int64_t r0 = r, k0 = k;
+    int64_t off = 0;
+    for (int j = g.nr - 1; j >= 0; --j) {
+      off += (r % g.re[j]) * g.rs[j];
+      r /= g.re[j];
+    }
+    for (int j = g.nk - 1; j >= 0; --j) {
+      off += (k % g.ke[j]) * g.ks[j];
+      k /= g.ke[j];
+    }
+    const double x = src[off];
+    const bf16 h = __double2bfloat16(x);
+    hi[r0 * ld + k0] = h;
+    if (lo != nullptr) lo[r0 * ld + k0] = __double2bfloat16(x - double(__bfloat162float(h)));
+  }
+}
+
+// max |x| over the valid M x N block of split-0 partials (single split only)
+__global__ void partial_absmax_kernel(const float* part, int64_t M, int64_t N, int n_pad,
+                                      unsigned long long* out_bits) {
+  float m = 0.f;
+  for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < M * N;
+       idx += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t r = idx / N, q = idx % N;
+    m = fmaxf(m, fabsf(part[r * n_pad + q]));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  // non-negative doubles order like their bit patterns
+  if ((threadIdx.x & 31) == 0) atomicMax(out_bits, (unsigned long long)__double_as_longlong(double(m)));
+}
+
+}  // namespace
+
+__global__ void join_bf16_kernel(const bf16* hi, const bf16* lo, int64_t rows, int64_t cols,
+                                 int64_t ld, double* out) {
+  for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < rows * cols;
+       idx += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t r = idx / cols, q = idx % cols;
+    double v = double(__bfloat162float(hi[r * ld + q]));
+    if (lo != nullptr) v += double(__bfloat162float(lo[r * ld + q]));
+    out[idx] = v;
+  }
+}
+
+void join_bf16(Ctx& c, const bf16* hi, const bf16* lo, int64_t rows, int64_t cols, int64_t ld,
+               double* out) {
+  if (c.sizing() || rows * cols == 0) return;
+  join_bf16_kernel<<<grid_for(rows * cols, 256), 256, 0, c.stream>>>(hi, lo, rows, cols, ld, out);
+  CTM_LAUNCH_CHECK();
+}
+
+void gather_split_bf16(Ctx& c, const double* src, const Gather& g, bf16* hi, bf16* lo, int64_t ld) {
+  int64_t rows = 1, K = 1;
+  for (int j = 0; j < g.nr; ++j) rows *= g.re[j];
+  for (int j = 0; j < g.nk; ++j) K *= g.ke[j];
+  if (c.sizing() || rows * K == 0) return;
+  gather_split_kernel<<<grid_for(rows * K, 256), 256, 0, c.stream>>>(src, g, rows, K, hi, lo, ld);
+  CTM_LAUNCH_CHECK();
+}
+
+namespace {
+
+void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, TcOut out,
+                  double* absmax) {
   CTM_REQUIRE(A.k == B.k && A.k >= 1 && A.rows >= 1 && B.rows >= 1, CTM_ERR_INVALID,
               "tc_gemm: operand shapes");
   const int imode = static_cast<int>(mode);
@@ -425,6 +516,7 @@ void tc_gemm(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, const 
   int splits = static_cast<int>(std::min<int64_t>((sms + base_ctas - 1) / base_ctas,
                                                   std::max(1, kb_total / 4)));
   splits = std::max(splits, 1);
+  if (absmax != nullptr) splits = 1;  // the scale is taken from complete sums
   const int kb_per_split = (kb_total + splits - 1) / splits;
   splits = (kb_total + kb_per_split - 1) / kb_per_split;
   const int m_pad = static_cast<int>(m_tiles * kBM);
@@ -468,6 +560,13 @@ void tc_gemm(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, const 
     tc_gemm_kernel<<<grid, kThreads, smem, c.stream>>>(tA, tAl, tB, tBl, p);
     CTM_LAUNCH_CHECK();
   }
+  if (absmax != nullptr) {
+    CTM_CUDA(cudaMemsetAsync(absmax, 0, sizeof(double), c.stream));
+    partial_absmax_kernel<<<grid_for(M * N, 256, 152 * 8), 256, 0, c.stream>>>(
+        part, M, N, n_pad, reinterpret_cast<unsigned long long*>(absmax));
+    CTM_LAUNCH_CHECK();
+    out.inv_scale = absmax;
+  }
   ReduceParams r{};
   r.part = part;
   r.splits = splits;
@@ -476,18 +575,25 @@ void tc_gemm(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, const 
   r.M = M;
   r.N = N;
   r.alpha = out.alpha;
-  r.f64 = out.f64;
-  r.ld_f64 = out.ld_f64;
-  r.f64_trans = out.f64_trans ? 1 : 0;
-  r.f32 = out.f32;
-  r.ld_f32 = out.ld_f32;
-  r.hi_t = out.hi_t;
-  r.lo_t = out.lo_t;
-  r.ld_t = out.ld_t;
+  r.inv_scale = out.inv_scale;
+  r.nd = out.nd;
+  for (int i = 0; i < out.nd; ++i) r.d[i] = out.d[i];
   dim3 rg(unsigned((M + 31) / 32), unsigned((N + 31) / 32));
   CTM_REQUIRE(rg.y <= 65535, CTM_ERR_UNSUPPORTED, "tc_gemm: output too wide");
   tc_reduce_kernel<<<rg, 256, 0, c.stream>>>(r);
   CTM_LAUNCH_CHECK();
+}
+
+}  // namespace
+
+void tc_gemm(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, const TcOut& out) {
+  tc_gemm_impl(c, A, B, mode, out, nullptr);
+}
+
+void tc_gemm_absmax_normalized(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode,
+                               TcOut out, double* absmax) {
+  CTM_REQUIRE(absmax != nullptr || c.sizing(), CTM_ERR_INVALID, "absmax scalar is NULL");
+  tc_gemm_impl(c, A, B, mode, out, c.sizing() ? reinterpret_cast<double*>(16) : absmax);
 }
 
 }  // namespace ctm

@@ -23,23 +23,71 @@ struct TcOperand {
   int64_t rows = 0, k = 0, ld = 0;
 };
 
-// Destinations of the reduced result (any subset).
+// Output layout: offset(m, n) = sum_j i_j(m) * ms[j] + sum_j i_j(n) * ns[j]
+// where m and n are decoded mixed-radix over (me[0..nm), last fastest).
+struct TcLayout {
+  int nm = 1, nn = 1;
+  int64_t me[4] = {1, 1, 1, 1}, ms[4] = {0, 0, 0, 0};
+  int64_t ne[4] = {1, 1, 1, 1}, ns[4] = {0, 0, 0, 0};
+  static TcLayout rows(int64_t M, int64_t N, int64_t ld) {  // C[m][n] at m*ld + n
+    TcLayout l;
+    l.me[0] = M; l.ms[0] = ld; l.ne[0] = N; l.ns[0] = 1;
+    return l;
+  }
+  static TcLayout cols(int64_t M, int64_t N, int64_t ld) {  // C[m][n] at n*ld + m
+    TcLayout l;
+    l.me[0] = M; l.ms[0] = 1; l.ne[0] = N; l.ns[0] = ld;
+    return l;
+  }
+};
+
+enum class TcKind { kF64 = 0, kF32 = 1, kBf16Hi = 2, kBf16Lo = 3 };
+
+struct TcDest {
+  TcKind kind = TcKind::kF64;
+  void* p = nullptr;
+  TcLayout lay;
+};
+
+// Destinations of the reduced result: alpha * C written to every entry of d.
 struct TcOut {
   double alpha = 1.0;
-  double* f64 = nullptr;       // C (M x N) row-major with ld_f64, or C^T when f64_trans
-  int64_t ld_f64 = 0;
-  bool f64_trans = false;
-  float* f32 = nullptr;        // C (M x N) row-major with ld_f32
-  int64_t ld_f32 = 0;
-  bf16* hi_t = nullptr;        // C^T (N x M) split into BF16 hi (+ lo), ld_t
-  bf16* lo_t = nullptr;
-  int64_t ld_t = 0;
+  const double* inv_scale = nullptr;  // device scalar: results are divided by *inv_scale
+  int nd = 0;
+  TcDest d[4];
+  TcOut& add(TcKind k, void* p, const TcLayout& l) {
+    d[nd].kind = k;
+    d[nd].p = p;
+    d[nd].lay = l;
+    ++nd;
+    return *this;
+  }
 };
 
 // Leading dimension used for BF16 operand arrays of width k.
 inline int64_t tc_ld(int64_t k) { return (k + 63) / 64 * 64; }
 
 void tc_gemm(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, const TcOut& out);
+
+// As tc_gemm, but first reduces max |C| into *absmax (device) and sets
+// out.inv_scale to it: the outputs hold C / max |C|.
+void tc_gemm_absmax_normalized(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode,
+                               TcOut out, double* absmax);
+
+// out (rows x cols FP64, contiguous) = hi + lo (BF16, leading dimension ld).
+void join_bf16(Ctx& c, const bf16* hi, const bf16* lo, int64_t rows, int64_t cols, int64_t ld,
+               double* out);
+
+// Gather-and-split of a strided FP64 tensor into a K-major BF16 operand:
+// dst[r][k] (ld) = src[off(r, k)], off decoded mixed-radix from row modes
+// (re, rs) and column modes (ke, ks), last mode fastest.
+struct Gather {
+  int nr = 1, nk = 1;
+  int64_t re[4] = {1, 1, 1, 1}, rs[4] = {0, 0, 0, 0};
+  int64_t ke[4] = {1, 1, 1, 1}, ks[4] = {0, 0, 0, 0};
+};
+void gather_split_bf16(Ctx& c, const double* src, const Gather& g, bf16* hi, bf16* lo,
+                       int64_t ld);
 
 // src (rows x cols FP64, leading dimension ld_src) -> hi/lo BF16 split; with
 // transpose the destination is (cols x rows).  lo may be null.

@@ -60,7 +60,7 @@ class ProjectorCalculator:
             raise ValueError(f"Invalid ctmrg projector type: {self.projectors} provided.")
 
     @staticmethod
-    def make_quarter_tensor(site_tensor, k):
+    def make_quarter_tensor(site_tensor, k, precision="fp64"):
         """acetn/renormalization/projectors.py:35-60: returns (qk matrix, 6-leg shape)."""
         ref = _abi.SiteRef(site_tensor)
         D, d = ref.D, ref.d
@@ -72,8 +72,9 @@ class ProjectorCalculator:
         rows, cols = e2.shape[1] * D * D, e1.shape[0] * D * D
         Q = torch.empty(rows, cols, dtype=torch.float64, device=ref.device)
         sh = (_abi.c_i64 * 6)()
-        _abi.call("ctm_quarter_tensor", [ref.pointer, D, d, k, _abi.ptr(Q), sh, 0], ref.device,
-                  key=("quarter", ref.shapes(), k))
+        _abi.call("ctm_quarter_tensor", [ref.pointer, D, d, k, _abi.ptr(Q), sh,
+                                          _abi.PREC[precision]], ref.device,
+                  key=("quarter", ref.shapes(), k, precision))
         return Q, tuple(sh)
 
     # ---------------------------------------------------------------- launches

@@ -100,7 +100,9 @@ int ctm_profile_query(int tag, double* total_ms, double* total_work, long long* 
 
 /* Enlarged corner (quarter tensor) of one site in direction k, reshaped to a
  * (rows x cols) matrix, rows = (c, r, R), cols = (e, d, D), divided by its
- * largest |entry|.  qshape receives the six leg sizes.
+ * largest |entry|.  qshape receives the six leg sizes.  CTM_PREC_MIXED
+ * computes it on tensor cores in 3xBF16 and returns the FP64 sum hi + lo of
+ * its split form.
  * Reference: ProjectorCalculator.make_quarter_tensor,
  * acetn/renormalization/projectors.py:35-60. */
 int ctm_quarter_tensor(const ctm_site_f64* site, int64_t D, int64_t d, int32_t k,
