@@ -166,7 +166,8 @@ def call(name, args_before_ws, device, key=None, stream=None):
     check(fn(*args_before_ws, ctypes.c_void_p(ws.data_ptr()), ctypes.byref(sz), stream), name)
 
 
-PROFILE_TAGS = {"gett_f64": 0, "tc_gemm": 1, "quarter_tc": 2, "other": 3}
+PROFILE_TAGS = {"gett_f64": 0, "tc_gemm": 1, "quarter": 2, "range_finder": 3, "orthonormalize": 4,
+                "svd": 5, "projector_products": 6, "renormalize": 7}
 
 
 def profile_begin():

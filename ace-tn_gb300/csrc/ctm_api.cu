@@ -356,8 +356,9 @@ void calculate_projectors(Ctx& c, const Site* S[4], int k, const ctm_ctmrg_opts&
 void renormalize_boundary(Ctx& c, const Site& S, int k, const double* P1i, int64_t x1i,
                           const double* P2j, int64_t x2j, const double* P2i, int64_t x2i,
                           const double* P1j, int64_t x1j, double* Cout1, double* Cout2,
-                          double* Eout) {
+                          double* Eout, int precision) {
   const int64_t D = S.D, d = S.d;
+  KernelTimer span(c.stream, kTagRenorm, 0.0);
   Scope scope(c);
   double* nrm = c.alloc<double>(3);
   {  // renormalize_cj1
@@ -383,6 +384,10 @@ void renormalize_boundary(Ctx& c, const Site& S, int k, const double* P1i, int64
            View(Cout2, {x2j, cc}));
     sumsq(c, Cout2, x2j * cc, nrm + 1);
     divide_by(c, Cout2, x2j * cc, nrm + 1, 1);
+  }
+  if (precision == CTM_PREC_MIXED) {
+    renormalize_ej_mixed(c, S, k, P2i, x2i, P1j, x1j, Eout);
+    return;
   }
   {  // renormalize_ej
     const View ei = S.E(3 + k), ai = S.A(k);
@@ -610,7 +615,7 @@ int ctm_renormalize_boundary(const ctm_site_f64* s1, int64_t D, int64_t d, int32
                   "NULL tensor pointer");
     Site S{s1, D, d};
     renormalize_boundary(c, S, k, P1_i, chi_p1i, P2_j, chi_p2j, P2_i, chi_p2i, P1_j, chi_p1j,
-                         Cout1, Cout2, Eout);
+                         Cout1, Cout2, Eout, precision);
   });
 }
 

@@ -46,8 +46,19 @@ void count_launch();
   } while (0)
 
 // Kernel classes of the live timer (ctm_profile_*).
-enum ProfileTag { kTagGettF64 = 0, kTagTcGemm = 1, kTagQuarterTc = 2, kTagOther = 3 };
-constexpr int kProfileTags = 4;
+// Tags 0-1 bracket single kernels (work = FLOPs); tags 2-7 bracket spans of
+// a projector computation or a renormalization (work = 0).
+enum ProfileTag {
+  kTagGettF64 = 0,
+  kTagTcGemm = 1,
+  kTagQuarter = 2,
+  kTagRangeFinder = 3,
+  kTagOrtho = 4,
+  kTagSvd = 5,
+  kTagProject = 6,
+  kTagRenorm = 7
+};
+constexpr int kProfileTags = 8;
 
 // Brackets one launch with CUDA events while profiling is on; `work` is the
 // algorithmic FLOP (or byte) count of the launch.

@@ -27,6 +27,11 @@ void orthonormalize(Ctx& c, double* Y, int64_t n, int64_t q, double* R);
 // X = U diag(S) V^T, U (m x r), S (r) descending, V (n x r), r = min(m, n).
 void svd_thin(Ctx& c, const double* X, int64_t m, int64_t n, double* U, double* S,
               double* V);
+// Thin SVD of B (q x n, q <= min(n, 1024)) from its FP64 Gram matrix: FP32
+// Jacobi eigenvectors, FP64 Rayleigh quotients; singular values accurate to
+// FP64 relative to s_0^2, vectors to FP32.  Used by the mixed path only.
+void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, double* S,
+                  double* V);
 // Truncation of acetn/renormalization/projectors.py:163-167 on a descending
 // spectrum s (len r): chi_new = min(chi, #{s/s0 > cutoff}); f[i] = 1/sqrt(s_i/s_0)
 // for i < chi_new else 0 (i < cap).
@@ -62,6 +67,9 @@ void quarter_dims(const Site& S, int k, int64_t& rows, int64_t& cols, int64_t sh
 void quarter_tensor(Ctx& c, const Site& S, int k, double* Q, int64_t qshape[6]);
 // make_quarter_tensor on tensor cores (3xBF16), returned as FP64 hi + lo.
 void quarter_tensor_mixed_f64(Ctx& c, const Site& S, int k, double* Q);
+// renormalize_ej on tensor cores (3xBF16), FP64 output normalised in FP64.
+void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64_t Y,
+                          const double* P1j, int64_t X, double* Eout);
 // Half-system rSVD projectors with tensor-core arithmetic (CTM_PREC_MIXED).
 void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg_opts& o,
                                 const double* omega, double* P1, double* P2, int64_t* chi_new);

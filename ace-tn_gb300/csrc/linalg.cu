@@ -537,3 +537,163 @@ void scale_columns_compact(Ctx& c, const double* in, int64_t rows, int64_t cap, 
 }
 
 }  // namespace ctm
+
+// ======================================================================
+// Symmetric eigen-decomposition for the mixed-precision SVD: parallel
+// (round-robin) two-sided Jacobi in FP32 on one CTA, followed by FP64
+// Rayleigh quotients of the FP64 matrix.
+namespace ctm {
+
+namespace {
+
+constexpr int ET = 1024;
+
+// A (q x q, symmetric, FP32 in global scratch) -> eigenvectors in V (q x q,
+// columns), diagonal of the rotated A holds the eigenvalues.  cs holds 2
+// floats per pair, pr 2 ints per pair.
+__global__ void __launch_bounds__(ET) jacobi_eig_f32_kernel(float* A, float* V, int q, int pp,
+                                                            float* cs, int* pr, int max_sweeps,
+                                                            int* flags) {
+  __shared__ int s_rot;
+  for (int idx = threadIdx.x; idx < q * q; idx += ET) V[idx] = (idx / q == idx % q) ? 1.f : 0.f;
+  const int npairs = pp / 2;
+  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    if (threadIdx.x == 0) s_rot = 0;
+    __syncthreads();
+    for (int r = 0; r < pp - 1; ++r) {
+      // rotation angles of the round's disjoint pairs
+      for (int k = threadIdx.x; k < npairs; k += ET) {
+        const int i0 = k == 0 ? 0 : ((k - 1 + r) % (pp - 1)) + 1;
+        const int k2 = pp - 1 - k;
+        const int j0 = k2 == 0 ? 0 : ((k2 - 1 + r) % (pp - 1)) + 1;
+        const int i = min(i0, j0), j = max(i0, j0);
+        float c = 1.f, s = 0.f;
+        if (j < q) {
+          const float aii = A[i * q + i], ajj = A[j * q + j], aij = A[i * q + j];
+          if (fabsf(aij) > 1e-6f * sqrtf(fabsf(aii) * fabsf(ajj)) && aij != 0.f) {
+            const float tau = (ajj - aii) / (2.f * aij);
+            const float t = copysignf(1.f, tau) / (fabsf(tau) + sqrtf(1.f + tau * tau));
+            c = 1.f / sqrtf(1.f + t * t);
+            s = t * c;
+            s_rot = 1;
+          }
+        }
+        cs[2 * k] = c;
+        cs[2 * k + 1] = s;
+        pr[2 * k] = i;
+        pr[2 * k + 1] = j;
+      }
+      __syncthreads();
+      // rows: A <- J^T A
+      for (int idx = threadIdx.x; idx < npairs * q; idx += ET) {
+        const int k = idx / q, col = idx % q;
+        const int i = pr[2 * k], j = pr[2 * k + 1];
+        if (j >= q) continue;
+        const float c = cs[2 * k], s = cs[2 * k + 1];
+        if (s == 0.f) continue;
+        const float ai = A[i * q + col], aj = A[j * q + col];
+        A[i * q + col] = c * ai - s * aj;
+        A[j * q + col] = s * ai + c * aj;
+      }
+      __syncthreads();
+      // columns: A <- A J, V <- V J
+      for (int idx = threadIdx.x; idx < npairs * q; idx += ET) {
+        const int k = idx / q, row = idx % q;
+        const int i = pr[2 * k], j = pr[2 * k + 1];
+        if (j >= q) continue;
+        const float c = cs[2 * k], s = cs[2 * k + 1];
+        if (s == 0.f) continue;
+        const float ai = A[row * q + i], aj = A[row * q + j];
+        A[row * q + i] = c * ai - s * aj;
+        A[row * q + j] = s * ai + c * aj;
+        const float vi = V[row * q + i], vj = V[row * q + j];
+        V[row * q + i] = c * vi - s * vj;
+        V[row * q + j] = s * vi + c * vj;
+      }
+      __syncthreads();
+    }
+    if (s_rot == 0) return;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicOr(flags, 2);
+}
+
+__global__ void f64_to_f32_kernel(const double* x, float* y, int64_t n) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    y[i] = float(x[i]);
+}
+
+__global__ void f32_to_f64_kernel(const float* x, double* y, int64_t n) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    y[i] = double(x[i]);
+}
+
+// lambda_j = (W^T G W)_jj from H = G W: lambda_j = sum_i W_ij H_ij; then
+// order by descending lambda, s = sqrt(max(lambda, 0)), Ub columns permuted.
+__global__ void eig_finish_kernel(const double* W, const double* H, int64_t q, double* Ub,
+                                  double* S, double* inv_s, int* order) {
+  __shared__ double lam[1024];
+  for (int64_t j = threadIdx.x; j < q; j += blockDim.x) {
+    double l = 0.0;
+    for (int64_t i = 0; i < q; ++i) l = fma(W[i * q + j], H[i * q + j], l);
+    lam[j] = l;
+  }
+  __syncthreads();
+  for (int64_t j = threadIdx.x; j < q; j += blockDim.x) {
+    int64_t rank = 0;
+    for (int64_t i = 0; i < q; ++i)
+      if (lam[i] > lam[j] || (lam[i] == lam[j] && i < j)) ++rank;
+    order[rank] = static_cast<int>(j);
+    const double s = sqrt(fmax(lam[j], 0.0));
+    S[rank] = s;
+    inv_s[rank] = s > 0.0 ? 1.0 / s : 0.0;
+  }
+  __syncthreads();
+  for (int64_t idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
+    const int64_t i = idx / q, r = idx % q;
+    Ub[i * q + r] = W[i * q + order[r]];
+  }
+}
+
+}  // namespace
+
+void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, double* S,
+                  double* V) {
+  CTM_REQUIRE(q >= 1 && q <= 1024 && q <= n, CTM_ERR_UNSUPPORTED,
+              "svd_via_gram: needs 1 <= q <= min(n, 1024)");
+  Scope scope(c);
+  double* G = c.alloc<double>(size_t(q) * q);
+  float* Af = c.alloc<float>(size_t(q) * q);
+  float* Vf = c.alloc<float>(size_t(q) * q);
+  double* W = c.alloc<double>(size_t(q) * q);
+  double* H = c.alloc<double>(size_t(q) * q);
+  double* inv_s = c.alloc<double>(q);
+  const int64_t pp = q + (q & 1);
+  float* cs = c.alloc<float>(pp);
+  int* pr = c.alloc<int>(pp);
+  int* order = c.alloc<int>(q);
+  // G = B B^T in FP64
+  einsum(c, "ik,jk->ij", View(B, {q, n}), View(B, {q, n}), View(G, {q, q}));
+  if (!c.sizing()) {
+    f64_to_f32_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(G, Af, q * q);
+    CTM_LAUNCH_CHECK();
+    jacobi_eig_f32_kernel<<<1, ET, 0, c.stream>>>(Af, Vf, int(q), int(pp), cs, pr, 40,
+                                                  status_flags(c));
+    CTM_LAUNCH_CHECK();
+    f32_to_f64_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(Vf, W, q * q);
+    CTM_LAUNCH_CHECK();
+  }
+  // Rayleigh quotients in FP64
+  einsum(c, "ik,kj->ij", View(G, {q, q}), View(W, {q, q}), View(H, {q, q}));
+  if (!c.sizing()) {
+    eig_finish_kernel<<<1, 1024, 0, c.stream>>>(W, H, q, Ub, S, inv_s, order);
+    CTM_LAUNCH_CHECK();
+  }
+  // V = B^T Ub diag(1/s)
+  einsum(c, "ki,kj->ij", View(B, {q, n}), View(Ub, {q, q}), View(V, {n, q}));
+  scale_columns(c, V, n, q, q, inv_s);
+}
+
+}  // namespace ctm

@@ -204,6 +204,157 @@ void gemm_to_f64(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, do
 
 }  // namespace
 
+// renormalize_ej (acetn/renormalization/directional_mover.py:345-366) on
+// tensor cores in 3xBF16: the four einsums become four GEMMs whose epilogues
+// store straight into the next GEMM's K-major operand; the last one writes
+// the FP64 result, normalised in FP64.
+//   G1 t1[(a,l,L)][(u,U,x)]  = sum_b E[a][b][l][L] P1[b][u][U][x]
+//   G2 t2[(a,l,u,x)][(R,D,P)] = sum_(L,U) t1 A*[L][U][R][D][P]
+//   G3 t3[(R,D,a,x)][(r,d)]   = sum_(l,u,p) t2 A[l][u][r][d][p]
+//   G4 E'[y][(x,r,R)]         = sum_(a,d,D) t3 P2[a][d][D][y]
+void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64_t Y,
+                          const double* P1j, int64_t X, double* Eout) {
+  const View ei = S.E(3 + k), ak = S.A(k);
+  const int64_t Aa = ei.shape[0], B = ei.shape[1], D = S.D, d = S.d, D2 = D * D;
+  const TcMode x3 = TcMode::kBf16x3;
+  Scope scope(c);
+  // G1 operands
+  const int64_t ld1 = tc_ld(B);
+  bf16* a1h = c.alloc<bf16>(size_t(Aa) * D2 * ld1);
+  bf16* a1l = c.alloc<bf16>(size_t(Aa) * D2 * ld1);
+  {
+    Gather g;
+    g.nr = 2;
+    g.re[0] = Aa; g.rs[0] = ei.stride[0];
+    g.re[1] = D2; g.rs[1] = 1;
+    g.nk = 1;
+    g.ke[0] = B; g.ks[0] = ei.stride[1];
+    gather_split_bf16(c, ei.p, g, a1h, a1l, ld1);
+  }
+  bf16* b1h = c.alloc<bf16>(size_t(D2) * X * ld1);
+  bf16* b1l = c.alloc<bf16>(size_t(D2) * X * ld1);
+  {
+    Gather g;
+    g.nr = 1;
+    g.re[0] = D2 * X; g.rs[0] = 1;
+    g.nk = 1;
+    g.ke[0] = B; g.ks[0] = D2 * X;
+    gather_split_bf16(c, P1j, g, b1h, b1l, ld1);
+  }
+  // G1 -> T1p[(a,l,u,x)][(L,U)]
+  const int64_t ldk = round8(D2);
+  const int64_t rows2 = Aa * D * D * X;
+  bf16* t1h = c.alloc<bf16>(size_t(rows2) * ldk);
+  bf16* t1l = c.alloc<bf16>(size_t(rows2) * ldk);
+  {
+    TcLayout l;
+    l.nm = 3;
+    l.me[0] = Aa; l.ms[0] = D * D * X * ldk;
+    l.me[1] = D;  l.ms[1] = D * X * ldk;
+    l.me[2] = D;  l.ms[2] = D;
+    l.nn = 3;
+    l.ne[0] = D; l.ns[0] = X * ldk;
+    l.ne[1] = D; l.ns[1] = 1;
+    l.ne[2] = X; l.ns[2] = ldk;
+    TcOut out;
+    out.add(TcKind::kBf16Hi, t1h, l).add(TcKind::kBf16Lo, t1l, l);
+    tc_gemm(c, TcOperand{a1h, a1l, Aa * D2, B, ld1}, TcOperand{b1h, b1l, D2 * X, B, ld1}, x3, out);
+  }
+  // G2: B2[(R,D,P)][(L,U)] = A*[L][U][R][D][P]
+  bf16* b2h = c.alloc<bf16>(size_t(D2) * d * ldk);
+  bf16* b2l = c.alloc<bf16>(size_t(D2) * d * ldk);
+  {
+    Gather g;
+    g.nr = 3;
+    g.re[0] = D; g.rs[0] = ak.stride[2];
+    g.re[1] = D; g.rs[1] = ak.stride[3];
+    g.re[2] = d; g.rs[2] = ak.stride[4];
+    g.nk = 2;
+    g.ke[0] = D; g.ks[0] = ak.stride[0];
+    g.ke[1] = D; g.ks[1] = ak.stride[1];
+    gather_split_bf16(c, ak.p, g, b2h, b2l, ldk);
+  }
+  // G2 -> T2p[(R,D,a,x)][(l,u,p)]
+  const int64_t ldk3 = round8(D2 * d);
+  bf16* t2h = c.alloc<bf16>(size_t(rows2) * ldk3);
+  bf16* t2l = c.alloc<bf16>(size_t(rows2) * ldk3);
+  {
+    TcLayout l;
+    l.nm = 4;
+    l.me[0] = Aa; l.ms[0] = X * ldk3;
+    l.me[1] = D;  l.ms[1] = D * d;
+    l.me[2] = D;  l.ms[2] = d;
+    l.me[3] = X;  l.ms[3] = ldk3;
+    l.nn = 3;
+    l.ne[0] = D; l.ns[0] = D * Aa * X * ldk3;
+    l.ne[1] = D; l.ns[1] = Aa * X * ldk3;
+    l.ne[2] = d; l.ns[2] = 1;
+    TcOut out;
+    out.add(TcKind::kBf16Hi, t2h, l).add(TcKind::kBf16Lo, t2l, l);
+    tc_gemm(c, TcOperand{t1h, t1l, rows2, D2, ldk}, TcOperand{b2h, b2l, D2 * d, D2, ldk}, x3, out);
+  }
+  // G3: B3[(r,d)][(l,u,p)] = A[l][u][r][d][p]
+  bf16* b3h = c.alloc<bf16>(size_t(D2) * ldk3);
+  bf16* b3l = c.alloc<bf16>(size_t(D2) * ldk3);
+  {
+    Gather g;
+    g.nr = 2;
+    g.re[0] = D; g.rs[0] = ak.stride[2];
+    g.re[1] = D; g.rs[1] = ak.stride[3];
+    g.nk = 3;
+    g.ke[0] = D; g.ks[0] = ak.stride[0];
+    g.ke[1] = D; g.ks[1] = ak.stride[1];
+    g.ke[2] = d; g.ks[2] = ak.stride[4];
+    gather_split_bf16(c, ak.p, g, b3h, b3l, ldk3);
+  }
+  // G3 -> T3p[(x,r,R)][(a,d,D)]
+  const int64_t K4 = Aa * D2;
+  const int64_t ldk4 = tc_ld(K4);
+  bf16* t3h = c.alloc<bf16>(size_t(X) * D2 * ldk4);
+  bf16* t3l = c.alloc<bf16>(size_t(X) * D2 * ldk4);
+  {
+    TcLayout l;
+    l.nm = 4;
+    l.me[0] = D;  l.ms[0] = ldk4;
+    l.me[1] = D;  l.ms[1] = 1;
+    l.me[2] = Aa; l.ms[2] = D2;
+    l.me[3] = X;  l.ms[3] = D2 * ldk4;
+    l.nn = 2;
+    l.ne[0] = D; l.ns[0] = D * ldk4;
+    l.ne[1] = D; l.ns[1] = D;
+    TcOut out;
+    out.add(TcKind::kBf16Hi, t3h, l).add(TcKind::kBf16Lo, t3l, l);
+    tc_gemm(c, TcOperand{t2h, t2l, rows2, D2 * d, ldk3}, TcOperand{b3h, b3l, D2, D2 * d, ldk3}, x3,
+            out);
+  }
+  // G4: B4[y][(a,d,D)] = P2[a][d][D][y]
+  bf16* b4h = c.alloc<bf16>(size_t(Y) * ldk4);
+  bf16* b4l = c.alloc<bf16>(size_t(Y) * ldk4);
+  {
+    Gather g;
+    g.nr = 1;
+    g.re[0] = Y; g.rs[0] = 1;
+    g.nk = 1;
+    g.ke[0] = K4; g.ks[0] = Y;
+    gather_split_bf16(c, P2i, g, b4h, b4l, ldk4);
+  }
+  {
+    TcLayout l;  // E'[y][x][r][R]
+    l.nm = 3;
+    l.me[0] = X; l.ms[0] = D2;
+    l.me[1] = D; l.ms[1] = D;
+    l.me[2] = D; l.ms[2] = 1;
+    l.nn = 1;
+    l.ne[0] = Y; l.ns[0] = X * D2;
+    TcOut out;
+    out.add(TcKind::kF64, Eout, l);
+    tc_gemm(c, TcOperand{t3h, t3l, X * D2, K4, ldk4}, TcOperand{b4h, b4l, Y, K4, ldk4}, x3, out);
+  }
+  double* nrm = c.alloc<double>(1);
+  sumsq(c, Eout, Y * X * D2, nrm);
+  divide_by(c, Eout, Y * X * D2, nrm, 1);
+}
+
 void quarter_tensor_mixed_f64(Ctx& c, const Site& S, int k, double* Q) {
   Scope scope(c);
   const QOps o = quarter_mixed(c, S, k);
@@ -223,11 +374,16 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
   const int64_t q = std::min({o.chi + o.rsvd_oversampling, m, n});
   const int64_t cap = std::min(o.chi, q);
   // ---- quarter tensors as BF16 operands (tensor cores, 3xBF16)
-  const QOps A1 = quarter_mixed(c, *S[0], k);
-  const QOps A4 = quarter_mixed(c, *S[3], k + 3);
+  QOps A1, A4;
+  {
+    KernelTimer span(c.stream, kTagQuarter, 0.0);
+    A1 = quarter_mixed(c, *S[0], k);
+    A4 = quarter_mixed(c, *S[3], k + 3);
+  }
   const TcMode x1 = TcMode::kBf16x1, x3 = TcMode::kBf16x3;
   // ---- range finder: Y = Q1 (Q4 Omega), niter x [QR; Y = Q1 Q4 Q4^T Q1^T Y]
   double* Y = c.alloc<double>(size_t(m) * q);
+  KernelTimer* rf_span = new KernelTimer(c.stream, kTagRangeFinder, 0.0);
   {
     Scope s2(c);
     const TcOperand om = yt_operand(c, omega, n, q, q, false);     // Omega^T (q x n)
@@ -235,7 +391,10 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
     gemm_to_f64(c, A1.q(false), t, x1, Y, q, false);
   }
   for (int it = 0; it < o.rsvd_niter; ++it) {
-    orthonormalize(c, Y, m, q, nullptr);
+    {
+      KernelTimer span(c.stream, kTagOrtho, 0.0);
+      orthonormalize(c, Y, m, q, nullptr);
+    }
     Scope s2(c);
     const TcOperand yt = yt_operand(c, Y, m, q, q, false);
     const TcOperand z1 = gemm_to_operand(c, A1.t(false), yt, x1, false);  // (Q1^T Y)^T
@@ -243,22 +402,29 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
     const TcOperand z3 = gemm_to_operand(c, A4.q(false), z2, x1, false);  // (Q4 z2)^T
     gemm_to_f64(c, A1.q(false), z3, x1, Y, q, false);
   }
-  orthonormalize(c, Y, m, q, nullptr);
+  {
+    KernelTimer span(c.stream, kTagOrtho, 0.0);
+    orthonormalize(c, Y, m, q, nullptr);
+  }
+  delete rf_span;
   // ---- Rayleigh-Ritz: B = (Q^T Q1) Q4 in 3xBF16, SVD in FP64
   double* Bm = c.alloc<double>(size_t(q) * n);
   double* Ub = c.alloc<double>(size_t(q) * q);
   double* s = c.alloc<double>(q);
   double* V = c.alloc<double>(size_t(n) * q);
   double* U = c.alloc<double>(size_t(m) * q);
+  KernelTimer* svd_span = new KernelTimer(c.stream, kTagSvd, 0.0);
   {
     Scope s2(c);
     const TcOperand qt = yt_operand(c, Y, m, q, q, true);               // Q^T (q x m)
     const TcOperand w = gemm_to_operand(c, A1.t(true), qt, x3, true);    // W = Q^T Q1 (q x c1)
     gemm_to_f64(c, A4.t(true), w, x3, Bm, n, true);                     // B (q x n)
   }
-  svd_thin(c, Bm, q, n, Ub, s, V);
+  svd_via_gram(c, Bm, q, n, Ub, s, V);
   einsum(c, "ik,kj->ij", View(Y, {m, q}), View(Ub, {q, q}), View(U, {m, q}));
+  delete svd_span;
   // ---- truncation and projector products (3xBF16)
+  KernelTimer proj_span(c.stream, kTagProject, 0.0);
   double* f = c.alloc<double>(cap);
   truncation_factors(c, s, q, o.chi, o.svd_cutoff, f, cap, chi_new);
   scale_columns(c, U, m, cap, q, f);

@@ -323,6 +323,7 @@ def run_gb300(args, rank, world, local_rank):
             "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
             "gpu_launches": int(launches),
+            "breakdown_ms_per_step": {k: v[0] / args.steps for k, v in prof.items() if v[2]},
             "clocks": clk,
         }
         if world == 1 and not args.no_cpu_baseline:

@@ -91,8 +91,10 @@ unsigned long long ctm_kernel_launches(void);
  * ctm_profile_end() the main kernels are bracketed by CUDA events on their
  * stream; ctm_profile_end() waits for them and ctm_profile_query(tag, ...)
  * returns total milliseconds, algorithmic work (FLOPs) and launch count of a
- * kernel class: 0 = FP64 contraction (GETT), 1 = tensor-core GEMM,
- * 2 = tensor-core quarter-tensor kernel, 3 = other.  No counterpart in the
+ * kernel class: 0 = FP64 contraction (GETT), 1 = tensor-core GEMM; or of a
+ * span of stream work: 2 = quarter tensors, 3 = rSVD range finder,
+ * 4 = orthonormalization, 5 = Rayleigh-Ritz SVD, 6 = projector products,
+ * 7 = boundary renormalization.  No counterpart in the
  * reference (its benchmarking decorators time whole Python calls). */
 void ctm_profile_begin(void);
 int ctm_profile_end(void);
