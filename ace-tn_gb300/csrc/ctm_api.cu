@@ -351,6 +351,58 @@ void calculate_projectors(Ctx& c, const Site* S[4], int k, const ctm_ctmrg_opts&
 }
 
 // ------------------------------------------------------------------ renormalization
+namespace {
+
+// renormalize_cj1 / renormalize_cj2 of the mixed path: FP32 contractions,
+// FP64 normalisation.
+void renormalize_corners_f32(Ctx& c, const Site& S, int k, const double* P1i, int64_t x1i,
+                             const double* P2j, int64_t x2j, double* Cout1, double* Cout2) {
+  const int64_t D = S.D;
+  Scope scope(c);
+  double* nrm = c.alloc<double>(2);
+  auto f32 = [&](const double* p, int64_t n) {
+    float* y = c.alloc<float>(size_t(n));
+    to_f32(c, p, y, n);
+    return y;
+  };
+  {  // renormalize_cj1
+    const View ci = S.C(3 + k), ei = S.E(2 + k);
+    const int64_t a = ei.shape[0], b = ei.shape[1], cc = ci.shape[1];
+    CTM_REQUIRE(ci.shape[0] == b, CTM_ERR_INVALID, "cj1: C and E do not chain");
+    Scope s2(c);
+    float* cf = f32(ci.p, ci.numel());
+    float* ef = f32(ei.p, ei.numel());
+    float* pf = f32(P1i, cc * D * D * x1i);
+    float* t = c.alloc<float>(size_t(a) * D * D * cc);
+    float* o = c.alloc<float>(size_t(a) * x1i);
+    einsum(c, "ablL,bc->alLc", ViewF(ef, {a, b, D, D}), ViewF(cf, {b, cc}), ViewF(t, {a, D, D, cc}));
+    einsum(c, "alLc,clLx->ax", ViewF(t, {a, D, D, cc}), ViewF(pf, {cc, D, D, x1i}),
+           ViewF(o, {a, x1i}));
+    to_f64(c, o, Cout1, a * x1i);
+    sumsq(c, Cout1, a * x1i, nrm);
+    divide_by(c, Cout1, a * x1i, nrm, 1);
+  }
+  {  // renormalize_cj2
+    const View ci = S.C(k), ei = S.E(k);
+    const int64_t a = ci.shape[0], b = ci.shape[1], cc = ei.shape[1];
+    CTM_REQUIRE(ei.shape[0] == b, CTM_ERR_INVALID, "cj2: C and E do not chain");
+    Scope s2(c);
+    float* cf = f32(ci.p, ci.numel());
+    float* ef = f32(ei.p, ei.numel());
+    float* pf = f32(P2j, a * D * D * x2j);
+    float* t = c.alloc<float>(size_t(a) * cc * D * D);
+    float* o = c.alloc<float>(size_t(x2j) * cc);
+    einsum(c, "ab,bcrR->acrR", ViewF(cf, {a, b}), ViewF(ef, {b, cc, D, D}), ViewF(t, {a, cc, D, D}));
+    einsum(c, "arRx,acrR->xc", ViewF(pf, {a, D, D, x2j}), ViewF(t, {a, cc, D, D}),
+           ViewF(o, {x2j, cc}));
+    to_f64(c, o, Cout2, x2j * cc);
+    sumsq(c, Cout2, x2j * cc, nrm + 1);
+    divide_by(c, Cout2, x2j * cc, nrm + 1, 1);
+  }
+}
+
+}  // namespace
+
 // DirectionalMover.renormalize_boundary and its three kernels
 // (acetn/renormalization/directional_mover.py:273-366).
 void renormalize_boundary(Ctx& c, const Site& S, int k, const double* P1i, int64_t x1i,
@@ -361,6 +413,11 @@ void renormalize_boundary(Ctx& c, const Site& S, int k, const double* P1i, int64
   KernelTimer span(c.stream, kTagRenorm, 0.0);
   Scope scope(c);
   double* nrm = c.alloc<double>(3);
+  if (precision == CTM_PREC_MIXED) {
+    renormalize_corners_f32(c, S, k, P1i, x1i, P2j, x2j, Cout1, Cout2);
+    renormalize_ej_mixed(c, S, k, P2i, x2i, P1j, x1j, Eout);
+    return;
+  }
   {  // renormalize_cj1
     const View ci = S.C(3 + k), ei = S.E(2 + k);
     const int64_t a = ei.shape[0], b = ei.shape[1], cc = ci.shape[1];
@@ -384,10 +441,6 @@ void renormalize_boundary(Ctx& c, const Site& S, int k, const double* P1i, int64
            View(Cout2, {x2j, cc}));
     sumsq(c, Cout2, x2j * cc, nrm + 1);
     divide_by(c, Cout2, x2j * cc, nrm + 1, 1);
-  }
-  if (precision == CTM_PREC_MIXED) {
-    renormalize_ej_mixed(c, S, k, P2i, x2i, P1j, x1j, Eout);
-    return;
   }
   {  // renormalize_ej
     const View ei = S.E(3 + k), ai = S.A(k);

@@ -56,9 +56,10 @@ enum ProfileTag {
   kTagOrtho = 4,
   kTagSvd = 5,
   kTagProject = 6,
-  kTagRenorm = 7
+  kTagRenorm = 7,
+  kTagGettF32 = 8
 };
-constexpr int kProfileTags = 8;
+constexpr int kProfileTags = 9;
 
 // Brackets one launch with CUDA events while profiling is on; `work` is the
 // algorithmic FLOP (or byte) count of the launch.
@@ -147,15 +148,16 @@ int with_workspace(void* ws, size_t* ws_bytes, cudaStream_t stream, F&& body) {
 // ----------------------------------------------------------------- tensor views
 constexpr int kMaxDims = 8;
 
-struct View {
-  double* p = nullptr;
+template <class T>
+struct ViewT {
+  T* p = nullptr;
   int nd = 0;
   int64_t shape[kMaxDims] = {0};
   int64_t stride[kMaxDims] = {0};
 
-  View() = default;
-  View(const double* ptr, std::initializer_list<int64_t> dims) {
-    p = const_cast<double*>(ptr);
+  ViewT() = default;
+  ViewT(const T* ptr, std::initializer_list<int64_t> dims) {
+    p = const_cast<T*>(ptr);
     nd = static_cast<int>(dims.size());
     int i = 0;
     for (int64_t v : dims) shape[i++] = v;
@@ -171,8 +173,8 @@ struct View {
     return n;
   }
   // Axis permutation without a copy: out.dim[i] = in.dim[perm[i]].
-  View permute(std::initializer_list<int> perm) const {
-    View v = *this;
+  ViewT permute(std::initializer_list<int> perm) const {
+    ViewT v = *this;
     int i = 0;
     for (int a : perm) {
       v.shape[i] = shape[a];
@@ -190,6 +192,9 @@ struct View {
     return true;
   }
 };
+
+using View = ViewT<double>;
+using ViewF = ViewT<float>;
 
 // The site tensor A permuted by bond_permute(k): legs (l,u,r,d,p) rotated by k
 // (acetn/ipeps/site_tensor.py:138-150).

@@ -9,6 +9,9 @@ namespace ctm {
 // outer-only labels).  All views are strided; nothing is copied.
 void einsum(Ctx& c, const char* spec, const View& A, const View& B, const View& C,
             double alpha = 1.0, double beta = 0.0);
+// The same contraction in FP32 (FP32 FMAs, FP32 accumulation).
+void einsum(Ctx& c, const char* spec, const ViewF& A, const ViewF& B, const ViewF& C,
+            double alpha = 1.0, double beta = 0.0);
 
 // Deterministic reductions into a device scalar.
 void absmax(Ctx& c, const double* x, int64_t n, double* out);
@@ -18,11 +21,16 @@ void divide_by(Ctx& c, double* x, int64_t n, const double* scal, int mode);
 // dst (rows x cols, row-major, ld_dst) = src view (2-D strided)
 void copy2d(Ctx& c, const View& src, double* dst, int64_t ld_dst);
 void fill(Ctx& c, double* x, int64_t n, double v);
+// Element-wise precision conversions (n elements, contiguous).
+void to_f32(Ctx& c, const double* x, float* y, int64_t n);
+void to_f64(Ctx& c, const float* x, double* y, int64_t n);
 
 // --- linear algebra (FP64) ---------------------------------------------------
 // Orthonormal basis of the columns of Y (n x q, row-major): Y := Q.
 // If R != nullptr it receives the q x q upper-triangular factor with Y_in = Q R.
 void orthonormalize(Ctx& c, double* Y, int64_t n, int64_t q, double* R);
+// The same in FP32 arithmetic (mixed path).
+void orthonormalize(Ctx& c, float* Y, int64_t n, int64_t q, float* R);
 // Thin SVD of X (m x n, row-major, m >= n is not required):
 // X = U diag(S) V^T, U (m x r), S (r) descending, V (n x r), r = min(m, n).
 void svd_thin(Ctx& c, const double* X, int64_t m, int64_t n, double* U, double* S,
@@ -31,7 +39,7 @@ void svd_thin(Ctx& c, const double* X, int64_t m, int64_t n, double* U, double* 
 // Jacobi eigenvectors, FP64 Rayleigh quotients; singular values accurate to
 // FP64 relative to s_0^2, vectors to FP32.  Used by the mixed path only.
 void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, double* S,
-                  double* V);
+                  float* V);
 // Truncation of acetn/renormalization/projectors.py:163-167 on a descending
 // spectrum s (len r): chi_new = min(chi, #{s/s0 > cutoff}); f[i] = 1/sqrt(s_i/s_0)
 // for i < chi_new else 0 (i < cap).

@@ -29,17 +29,18 @@ struct Group {
   Mode m[kMaxModes];
 };
 
+template <class T>
 struct GettArgs {
-  const double* A;
-  const double* B;
-  double* C;
+  const T* A;
+  const T* B;
+  T* C;
   Group M, N, K;  // M: (A, C) strides, N: (B, C), K: (A, B)
   int64_t Mt, Nt, Kt;
   int64_t bext, bsa, bsb, bsc;
-  double alpha, beta;
+  T alpha, beta;
   int splitk;
   int64_t kchunk;
-  double* part;
+  T* part;
 };
 
 __device__ __forceinline__ void decode(const Group& g, int64_t idx, int64_t& o0, int64_t& o1) {
@@ -62,11 +63,12 @@ constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
 // One 64x64 output tile per CTA, 4x4 outputs per thread, K staged through
 // shared memory 16 at a time.  FP64 FMAs are the bound on this part, so the
 // loaders favour generality (any strides) over vector width.
-__global__ void __launch_bounds__(NT) gett_f64_kernel(const GettArgs p) {
+template <class T>
+__global__ void __launch_bounds__(NT) gett_kernel(const GettArgs<T> p) {
   __shared__ int64_t sAm[BM], sCm[BM], sBn[BN], sCn[BN];
   __shared__ int64_t sAk[BK], sBk[BK];
-  __shared__ double As[BK][BM + 1];
-  __shared__ double Bs[BK][BN + 1];
+  __shared__ T As[BK][BM + 1];
+  __shared__ T Bs[BK][BN + 1];
 
   const int tid = threadIdx.x;
   const int64_t m0 = static_cast<int64_t>(blockIdx.x) * BM;
@@ -74,8 +76,8 @@ __global__ void __launch_bounds__(NT) gett_f64_kernel(const GettArgs p) {
   const int64_t z = blockIdx.z;
   const int64_t batch = z % p.bext;
   const int64_t split = z / p.bext;
-  const double* A = p.A + batch * p.bsa;
-  const double* B = p.B + batch * p.bsb;
+  const T* A = p.A + batch * p.bsa;
+  const T* B = p.B + batch * p.bsb;
 
   if (tid < BM) {
     const int64_t m = m0 + tid;
@@ -90,11 +92,11 @@ __global__ void __launch_bounds__(NT) gett_f64_kernel(const GettArgs p) {
   const int64_t kb = split * p.kchunk;
   const int64_t ke = min(kb + p.kchunk, p.Kt);
 
-  double acc[4][4];
+  T acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
 
   const int tx = tid & 15, ty = tid >> 4;
   for (int64_t k0 = kb; k0 < ke; k0 += BK) {
@@ -110,14 +112,14 @@ __global__ void __launch_bounds__(NT) gett_f64_kernel(const GettArgs p) {
       const int lin = tid + e * NT;
       const int mm = lin % BM, kk = lin / BM;
       const int64_t am = sAm[mm], ak = sAk[kk];
-      As[kk][mm] = (am >= 0 && ak >= 0) ? A[am + ak] : 0.0;
+      As[kk][mm] = (am >= 0 && ak >= 0) ? A[am + ak] : T(0);
       const int64_t bn = sBn[mm], bk = sBk[kk];
-      Bs[kk][mm] = (bn >= 0 && bk >= 0) ? B[bk + bn] : 0.0;
+      Bs[kk][mm] = (bn >= 0 && bk >= 0) ? B[bk + bn] : T(0);
     }
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
-      double a[4], b[4];
+      T a[4], b[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
 #pragma unroll
@@ -142,30 +144,31 @@ __global__ void __launch_bounds__(NT) gett_f64_kernel(const GettArgs p) {
       if (p.splitk > 1) {
         p.part[((split * p.bext + batch) * p.Mt + m) * p.Nt + n] = acc[i][j];
       } else {
-        double* c = p.C + batch * p.bsc + sCm[mi] + sCn[nj];
-        const double v = p.alpha * acc[i][j];
-        *c = (p.beta != 0.0) ? fma(p.beta, *c, v) : v;
+        T* c = p.C + batch * p.bsc + sCm[mi] + sCn[nj];
+        const T v = p.alpha * acc[i][j];
+        *c = (p.beta != T(0)) ? fma(p.beta, *c, v) : v;
       }
     }
   }
 }
 
 // Sums split-K partial tiles in a fixed order (deterministic) into C.
-__global__ void gett_splitk_reduce(const GettArgs p) {
+template <class T>
+__global__ void gett_splitk_reduce(const GettArgs<T> p) {
   const int64_t total = p.bext * p.Mt * p.Nt;
   for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < total;
        idx += int64_t(gridDim.x) * blockDim.x) {
     const int64_t n = idx % p.Nt;
     const int64_t m = (idx / p.Nt) % p.Mt;
     const int64_t b = idx / (p.Nt * p.Mt);
-    double s = 0.0;
+    T s = T(0);
     for (int t = 0; t < p.splitk; ++t) s += p.part[((t * p.bext + b) * p.Mt + m) * p.Nt + n];
     int64_t am, cm, bn, cn;
     decode(p.M, m, am, cm);
     decode(p.N, n, bn, cn);
-    double* c = p.C + b * p.bsc + cm + cn;
-    const double v = p.alpha * s;
-    *c = (p.beta != 0.0) ? fma(p.beta, *c, v) : v;
+    T* c = p.C + b * p.bsc + cm + cn;
+    const T v = p.alpha * s;
+    *c = (p.beta != T(0)) ? fma(p.beta, *c, v) : v;
   }
 }
 
@@ -214,8 +217,9 @@ int64_t group_size(const Group& g) {
 
 }  // namespace
 
-void einsum(Ctx& c, const char* spec, const View& A, const View& B, const View& C, double alpha,
-            double beta) {
+template <class T>
+void einsum_impl(Ctx& c, const char* spec, const ViewT<T>& A, const ViewT<T>& B, const ViewT<T>& C,
+                 double alpha, double beta) {
   std::string s(spec);
   const size_t comma = s.find(','), arrow = s.find("->");
   CTM_REQUIRE(comma != std::string::npos && arrow != std::string::npos, CTM_ERR_INVALID,
@@ -225,7 +229,7 @@ void einsum(Ctx& c, const char* spec, const View& A, const View& B, const View& 
   CTM_REQUIRE(int(la.size()) == A.nd && int(lb.size()) == B.nd && int(lc.size()) == C.nd,
               CTM_ERR_INVALID, "einsum: rank mismatch in " + s);
   std::map<char, Label> labels;
-  auto add = [&](const std::string& l, const View& v, int which) {
+  auto add = [&](const std::string& l, const ViewT<T>& v, int which) {
     for (size_t i = 0; i < l.size(); ++i) {
       Label& L = labels[l[i]];
       if (L.ch == 0) {
@@ -266,7 +270,7 @@ void einsum(Ctx& c, const char* spec, const View& A, const View& B, const View& 
   for (auto& L : ml) mm.push_back({L.ext, L.sa, L.sc});
   for (auto& L : nl) nn.push_back({L.ext, L.sb, L.sc});
   for (auto& L : kl) kk.push_back({L.ext, L.sa, L.sb});
-  GettArgs p{};
+  GettArgs<T> p{};
   p.M = to_group(mm, "row");
   p.N = to_group(nn, "column");
   p.K = to_group(kk, "contracted");
@@ -294,8 +298,8 @@ void einsum(Ctx& c, const char* spec, const View& A, const View& B, const View& 
   p.Nt = group_size(p.N);
   p.Kt = group_size(p.K);
   p.bext = bext; p.bsa = bsa; p.bsb = bsb; p.bsc = bsc;
-  p.alpha = alpha;
-  p.beta = beta;
+  p.alpha = T(alpha);
+  p.beta = T(beta);
   if (p.Mt == 0 || p.Nt == 0) return;
 
   const int64_t tiles = ((p.Mt + BM - 1) / BM) * ((p.Nt + BN - 1) / BN) * bext;
@@ -310,20 +314,31 @@ void einsum(Ctx& c, const char* spec, const View& A, const View& B, const View& 
   splitk = static_cast<int>(std::max<int64_t>(1, (p.Kt + p.kchunk - 1) / p.kchunk));
   p.splitk = splitk;
   Scope scope(c);
-  if (splitk > 1) p.part = c.alloc<double>(size_t(splitk) * bext * p.Mt * p.Nt);
+  if (splitk > 1) p.part = c.alloc<T>(size_t(splitk) * bext * p.Mt * p.Nt);
   if (c.sizing()) return;
   dim3 grid(static_cast<unsigned>((p.Mt + BM - 1) / BM), static_cast<unsigned>((p.Nt + BN - 1) / BN),
             static_cast<unsigned>(bext * splitk));
   CTM_REQUIRE(grid.y <= 65535 && grid.z <= 65535, CTM_ERR_UNSUPPORTED, "einsum: grid too large");
   {
-    KernelTimer timer(c.stream, kTagGettF64, 2.0 * double(p.Mt) * p.Nt * p.Kt * bext);
-    gett_f64_kernel<<<grid, NT, 0, c.stream>>>(p);
+    KernelTimer timer(c.stream, sizeof(T) == 8 ? kTagGettF64 : kTagGettF32,
+                      2.0 * double(p.Mt) * p.Nt * p.Kt * bext);
+    gett_kernel<T><<<grid, NT, 0, c.stream>>>(p);
     CTM_LAUNCH_CHECK();
   }
   if (splitk > 1) {
-    gett_splitk_reduce<<<grid_for(bext * p.Mt * p.Nt, 256), 256, 0, c.stream>>>(p);
+    gett_splitk_reduce<T><<<grid_for(bext * p.Mt * p.Nt, 256), 256, 0, c.stream>>>(p);
     CTM_LAUNCH_CHECK();
   }
+}
+
+void einsum(Ctx& c, const char* spec, const View& A, const View& B, const View& C, double alpha,
+            double beta) {
+  einsum_impl<double>(c, spec, A, B, C, alpha, beta);
+}
+
+void einsum(Ctx& c, const char* spec, const ViewF& A, const ViewF& B, const ViewF& C, double alpha,
+            double beta) {
+  einsum_impl<float>(c, spec, A, B, C, alpha, beta);
 }
 
 // ----------------------------------------------------------------- reductions
@@ -415,6 +430,31 @@ void copy2d(Ctx& c, const View& src, double* dst, int64_t ld_dst) {
   if (c.sizing() || src.numel() == 0) return;
   copy2d_kernel<<<grid_for(src.numel(), 256), 256, 0, c.stream>>>(
       src.p, src.shape[0], src.shape[1], src.stride[0], src.stride[1], dst, ld_dst);
+  CTM_LAUNCH_CHECK();
+}
+
+namespace {
+__global__ void cvt_f32_kernel(const double* x, float* y, int64_t n) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    y[i] = float(x[i]);
+}
+__global__ void cvt_f64_kernel(const float* x, double* y, int64_t n) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    y[i] = double(x[i]);
+}
+}  // namespace
+
+void to_f32(Ctx& c, const double* x, float* y, int64_t n) {
+  if (c.sizing() || n == 0) return;
+  cvt_f32_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(x, y, n);
+  CTM_LAUNCH_CHECK();
+}
+
+void to_f64(Ctx& c, const float* x, double* y, int64_t n) {
+  if (c.sizing() || n == 0) return;
+  cvt_f64_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(x, y, n);
   CTM_LAUNCH_CHECK();
 }
 

@@ -22,20 +22,22 @@ __device__ int g_status_flags;
 
 constexpr int LT = 256;  // threads of one-CTA linear-algebra kernels
 
-__device__ __forceinline__ double warp_sum(double v) {
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
-// Block-wide sum (all threads get the result).  sh must hold LT/32 doubles.
-__device__ double block_sum(double v, double* sh) {
+// Block-wide sum (all threads get the result).  sh must hold LT/32 values.
+template <class T>
+__device__ T block_sum(T v, T* sh) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   v = warp_sum(v);
   __syncthreads();
   if (lane == 0) sh[w] = v;
   __syncthreads();
-  double t = 0.0;
+  T t = T(0);
   for (int i = 0; i < int(blockDim.x >> 5); ++i) t += sh[i];
   return t;
 }
@@ -44,45 +46,46 @@ __device__ double block_sum(double v, double* sh) {
 // One CTA.  Y (n x q, row-major) is overwritten by the explicit Q; R (q x q)
 // receives the triangular factor when non-null.  V (n x q) and beta (q) are
 // scratch.  Runs only when (flags == nullptr) or (*flags & 1) != 0.
-__global__ void __launch_bounds__(LT) householder_qr_kernel(double* Y, int64_t n, int64_t q,
-                                                            double* R, double* V, double* beta,
+template <class T>
+__global__ void __launch_bounds__(LT) householder_qr_kernel(T* Y, int64_t n, int64_t q,
+                                                            T* R, T* V, T* beta,
                                                             const int* flags, int clear_bit) {
   if (flags != nullptr && ((*flags) & clear_bit) == 0) return;
-  __shared__ double sh[LT / 32];
-  __shared__ double s_beta, s_alpha;
+  __shared__ T sh[LT / 32];
+  __shared__ T s_beta, s_alpha;
   for (int64_t j = 0; j < q; ++j) {
     // norm of the column below the diagonal
-    double part = 0.0;
+    T part = T(0);
     for (int64_t i = j + threadIdx.x; i < n; i += LT) {
-      const double x = Y[i * q + j];
+      const T x = Y[i * q + j];
       part = fma(x, x, part);
     }
-    const double nrm2 = block_sum(part, sh);
+    const T nrm2 = block_sum(part, sh);
     if (threadIdx.x == 0) {
-      const double x0 = Y[j * q + j];
-      const double nrm = sqrt(nrm2);
-      if (nrm == 0.0) {
-        s_alpha = 0.0;
-        s_beta = 0.0;
+      const T x0 = Y[j * q + j];
+      const T nrm = sqrt(nrm2);
+      if (nrm == T(0)) {
+        s_alpha = T(0);
+        s_beta = T(0);
       } else {
-        const double alpha = x0 >= 0.0 ? -nrm : nrm;
-        const double v0 = x0 - alpha;
+        const T alpha = x0 >= T(0) ? -nrm : nrm;
+        const T v0 = x0 - alpha;
         // v = x - alpha e1, stored with v0 in place; beta = 2 / (v^T v)
-        const double vtv = nrm2 - x0 * x0 + v0 * v0;
+        const T vtv = nrm2 - x0 * x0 + v0 * v0;
         s_alpha = alpha;
-        s_beta = vtv > 0.0 ? 2.0 / vtv : 0.0;
+        s_beta = vtv > T(0) ? T(2) / vtv : T(0);
         Y[j * q + j] = v0;
       }
     }
     __syncthreads();
-    const double bj = s_beta;
+    const T bj = s_beta;
     for (int64_t i = j + threadIdx.x; i < n; i += LT) V[i * q + j] = Y[i * q + j];
     __syncthreads();
     // trailing update Y[j:, j+1:] -= beta v (v^T Y)
     for (int64_t c = j + 1; c < q; ++c) {
-      double d = 0.0;
+      T d = T(0);
       for (int64_t i = j + threadIdx.x; i < n; i += LT) d = fma(V[i * q + j], Y[i * q + c], d);
-      const double w = block_sum(d, sh) * bj;
+      const T w = block_sum(d, sh) * bj;
       for (int64_t i = j + threadIdx.x; i < n; i += LT) Y[i * q + c] -= w * V[i * q + j];
     }
     __syncthreads();
@@ -95,23 +98,23 @@ __global__ void __launch_bounds__(LT) householder_qr_kernel(double* Y, int64_t n
   if (R != nullptr) {
     for (int64_t idx = threadIdx.x; idx < q * q; idx += LT) {
       const int64_t r = idx / q, c = idx % q;
-      R[idx] = (c >= r) ? Y[r * q + c] : 0.0;
+      R[idx] = (c >= r) ? Y[r * q + c] : T(0);
     }
   }
   __syncthreads();
   // explicit Q = H_0 ... H_{q-1} [I; 0], applied right to left
   for (int64_t idx = threadIdx.x; idx < n * q; idx += LT) {
     const int64_t r = idx / q, c = idx % q;
-    Y[idx] = (r == c) ? 1.0 : 0.0;
+    Y[idx] = (r == c) ? T(1) : T(0);
   }
   __syncthreads();
   for (int64_t j = q - 1; j >= 0; --j) {
-    const double bj = beta[j];
-    if (bj == 0.0) continue;
+    const T bj = beta[j];
+    if (bj == T(0)) continue;
     for (int64_t c = j; c < q; ++c) {
-      double d = 0.0;
+      T d = T(0);
       for (int64_t i = j + threadIdx.x; i < n; i += LT) d = fma(V[i * q + j], Y[i * q + c], d);
-      const double w = block_sum(d, sh) * bj;
+      const T w = block_sum(d, sh) * bj;
       for (int64_t i = j + threadIdx.x; i < n; i += LT) Y[i * q + c] -= w * V[i * q + j];
     }
     __syncthreads();
@@ -122,36 +125,38 @@ __global__ void __launch_bounds__(LT) householder_qr_kernel(double* Y, int64_t n
 // One CTA.  G (q x q) -> Linv (q x q, lower-triangular inverse of the
 // Cholesky factor of G + shift I), Lt (q x q) = L^T (upper).  W is q x q
 // scratch.  shift = 11 (n q + q (q + 1)) u tr(G) when shifted != 0.
-__global__ void __launch_bounds__(LT) cholesky_inverse_kernel(const double* G, int64_t q,
-                                                              int64_t n, int shifted, double* W,
-                                                              double* Linv, double* Lt,
+template <class T>
+__global__ void __launch_bounds__(LT) cholesky_inverse_kernel(const T* G, int64_t q,
+                                                              int64_t n, int shifted, T* W,
+                                                              T* Linv, T* Lt,
                                                               int* flags) {
-  __shared__ double sh[LT / 32];
-  __shared__ double s_shift;
+  __shared__ T sh[LT / 32];
+  __shared__ T s_shift;
   __shared__ int s_fail;
-  double tr = 0.0;
+  T tr = T(0);
   for (int64_t i = threadIdx.x; i < q; i += LT) tr += G[i * q + i];
   tr = block_sum(tr, sh);
   if (threadIdx.x == 0) {
-    const double u = 1.1102230246251565e-16;  // 2^-53
-    s_shift = shifted ? 11.0 * (double(n) * q + double(q) * (q + 1)) * u * tr : 0.0;
+    // unit roundoff of T: 2^-53 (double) or 2^-24 (float)
+    const double u = sizeof(T) == 8 ? 1.1102230246251565e-16 : 5.9604644775390625e-08;
+    s_shift = shifted ? T(11.0 * (double(n) * q + double(q) * (q + 1)) * u * double(tr)) : T(0);
     s_fail = 0;
   }
   __syncthreads();
   for (int64_t idx = threadIdx.x; idx < q * q; idx += LT) {
     const int64_t r = idx / q, c = idx % q;
-    W[idx] = (c <= r) ? G[idx] + ((r == c) ? s_shift : 0.0) : 0.0;
+    W[idx] = (c <= r) ? G[idx] + ((r == c) ? s_shift : T(0)) : T(0);
   }
   __syncthreads();
   // right-looking Cholesky on the lower triangle of W
   for (int64_t j = 0; j < q; ++j) {
     if (threadIdx.x == 0) {
-      const double d = W[j * q + j];
-      if (!(d > 0.0)) s_fail = 1;
-      W[j * q + j] = d > 0.0 ? sqrt(d) : 1.0;
+      const T d = W[j * q + j];
+      if (!(d > T(0))) s_fail = 1;
+      W[j * q + j] = d > T(0) ? sqrt(d) : T(1);
     }
     __syncthreads();
-    const double ljj = W[j * q + j];
+    const T ljj = W[j * q + j];
     for (int64_t i = j + 1 + threadIdx.x; i < q; i += LT) W[i * q + j] /= ljj;
     __syncthreads();
     const int64_t m = q - j - 1;
@@ -165,11 +170,11 @@ __global__ void __launch_bounds__(LT) cholesky_inverse_kernel(const double* G, i
   // Linv: forward substitution, one column per thread
   for (int64_t c = threadIdx.x; c < q; c += LT) {
     for (int64_t i = 0; i < q; ++i) {
-      double v;
+      T v;
       if (i < c) {
-        v = 0.0;
+        v = T(0);
       } else {
-        double s = (i == c) ? 1.0 : 0.0;
+        T s = (i == c) ? T(1) : T(0);
         for (int64_t k = c; k < i; ++k) s -= W[i * q + k] * Linv[k * q + c];
         v = s / W[i * q + i];
       }
@@ -179,19 +184,20 @@ __global__ void __launch_bounds__(LT) cholesky_inverse_kernel(const double* G, i
   if (Lt != nullptr) {
     for (int64_t idx = threadIdx.x; idx < q * q; idx += LT) {
       const int64_t r = idx / q, c = idx % q;
-      Lt[idx] = (c >= r) ? W[c * q + r] : 0.0;
+      Lt[idx] = (c >= r) ? W[c * q + r] : T(0);
     }
   }
 }
 
 // Sets flag bit 1 when max |G - I| exceeds tol (NaN counts as failure).
-__global__ void orthogonality_check_kernel(const double* G, int64_t q, double tol, int* flags) {
+template <class T>
+__global__ void orthogonality_check_kernel(const T* G, int64_t q, double tol, int* flags) {
   __shared__ int bad;
   if (threadIdx.x == 0) bad = 0;
   __syncthreads();
   for (int64_t idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
     const int64_t r = idx / q, c = idx % q;
-    const double e = fabs(G[idx] - (r == c ? 1.0 : 0.0));
+    const double e = fabs(double(G[idx]) - (r == c ? 1.0 : 0.0));
     if (!(e <= tol)) bad = 1;
   }
   __syncthreads();
@@ -376,8 +382,8 @@ __global__ void scale_compact_kernel(const double* in, int64_t rows, int64_t cap
   }
 }
 
-__global__ void restore_if_flagged_kernel(double* Y, const double* saved, int64_t n,
-                                          const int* flags) {
+template <class T>
+__global__ void restore_if_flagged_kernel(T* Y, const T* saved, int64_t n, const int* flags) {
   if (((*flags) & 1) == 0) return;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * blockDim.x)
@@ -393,69 +399,79 @@ int* status_flags(Ctx& c) {
   return p;
 }
 
-void orthonormalize(Ctx& c, double* Y, int64_t n, int64_t q, double* R) {
+template <class T>
+void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R) {
   CTM_REQUIRE(n >= q && q >= 1, CTM_ERR_INVALID, "orthonormalize: needs n >= q >= 1");
   Scope scope(c);
-  double* V = c.alloc<double>(size_t(n) * q);
-  double* beta = c.alloc<double>(q);
+  T* V = c.alloc<T>(size_t(n) * q);
+  T* beta = c.alloc<T>(q);
   const bool small = double(n) * q * q <= 4.0e6;
   if (small) {
     if (c.sizing()) return;
-    householder_qr_kernel<<<1, LT, 0, c.stream>>>(Y, n, q, R, V, beta, nullptr, 1);
+    householder_qr_kernel<T><<<1, LT, 0, c.stream>>>(Y, n, q, R, V, beta, nullptr, 1);
     CTM_LAUNCH_CHECK();
     return;
   }
   // shifted Cholesky-QR3 with a Householder re-run when the check fails
-  double* X2 = c.alloc<double>(size_t(n) * q);
-  double* G = c.alloc<double>(size_t(q) * q);
-  double* Wk = c.alloc<double>(size_t(q) * q);
-  double* Li = c.alloc<double>(size_t(q) * q);
-  double* Lt = c.alloc<double>(size_t(q) * q);
-  double* Rt = c.alloc<double>(size_t(q) * q);
-  double* Rt2 = c.alloc<double>(size_t(q) * q);
+  T* X2 = c.alloc<T>(size_t(n) * q);
+  T* G = c.alloc<T>(size_t(q) * q);
+  T* Wk = c.alloc<T>(size_t(q) * q);
+  T* Li = c.alloc<T>(size_t(q) * q);
+  T* Lt = c.alloc<T>(size_t(q) * q);
+  T* Rt = c.alloc<T>(size_t(q) * q);
+  T* Rt2 = c.alloc<T>(size_t(q) * q);
   int* flags = c.alloc<int>(1);
   // keep the input for the fallback in V
   if (!c.sizing()) {
-    CTM_CUDA(cudaMemcpyAsync(V, Y, sizeof(double) * n * q, cudaMemcpyDeviceToDevice, c.stream));
+    CTM_CUDA(cudaMemcpyAsync(V, Y, sizeof(T) * n * q, cudaMemcpyDeviceToDevice, c.stream));
     CTM_CUDA(cudaMemsetAsync(flags, 0, sizeof(int), c.stream));
   }
-  double* cur = Y;
-  double* nxt = X2;
+  T* cur = Y;
+  T* nxt = X2;
   for (int stage = 0; stage < 3; ++stage) {
-    einsum(c, "ia,ib->ab", View(cur, {n, q}), View(cur, {n, q}), View(G, {q, q}));
+    einsum(c, "ia,ib->ab", ViewT<T>(cur, {n, q}), ViewT<T>(cur, {n, q}), ViewT<T>(G, {q, q}));
     if (!c.sizing()) {
-      cholesky_inverse_kernel<<<1, LT, 0, c.stream>>>(G, q, n, stage == 0 ? 1 : 0, Wk, Li, Lt,
+      cholesky_inverse_kernel<T><<<1, LT, 0, c.stream>>>(G, q, n, stage == 0 ? 1 : 0, Wk, Li, Lt,
                                                       flags);
       CTM_LAUNCH_CHECK();
     }
     // nxt = cur @ Linv^T
-    einsum(c, "ia,ba->ib", View(cur, {n, q}), View(Li, {q, q}), View(nxt, {n, q}));
+    einsum(c, "ia,ba->ib", ViewT<T>(cur, {n, q}), ViewT<T>(Li, {q, q}), ViewT<T>(nxt, {n, q}));
     if (R != nullptr) {
       if (stage == 0) {
         if (!c.sizing())
-          CTM_CUDA(cudaMemcpyAsync(Rt, Lt, sizeof(double) * q * q, cudaMemcpyDeviceToDevice,
+          CTM_CUDA(cudaMemcpyAsync(Rt, Lt, sizeof(T) * q * q, cudaMemcpyDeviceToDevice,
                                    c.stream));
       } else {
-        einsum(c, "ab,bc->ac", View(Lt, {q, q}), View(Rt, {q, q}), View(Rt2, {q, q}));
+        einsum(c, "ab,bc->ac", ViewT<T>(Lt, {q, q}), ViewT<T>(Rt, {q, q}), ViewT<T>(Rt2, {q, q}));
         std::swap(Rt, Rt2);
       }
     }
     std::swap(cur, nxt);
   }
   // cur holds Q after the three stages; check it and fall back when needed
-  einsum(c, "ia,ib->ab", View(cur, {n, q}), View(cur, {n, q}), View(G, {q, q}));
-  double* hv = c.alloc<double>(size_t(n) * q);
+  einsum(c, "ia,ib->ab", ViewT<T>(cur, {n, q}), ViewT<T>(cur, {n, q}), ViewT<T>(G, {q, q}));
+  T* hv = c.alloc<T>(size_t(n) * q);
   if (c.sizing()) return;
-  orthogonality_check_kernel<<<1, LT, 0, c.stream>>>(G, q, 1e-11, flags);
+  orthogonality_check_kernel<T><<<1, LT, 0, c.stream>>>(G, q, sizeof(T) == 8 ? 1e-11 : 2e-4,
+                                                     flags);
   CTM_LAUNCH_CHECK();
   if (cur != Y)
-    CTM_CUDA(cudaMemcpyAsync(Y, cur, sizeof(double) * n * q, cudaMemcpyDeviceToDevice, c.stream));
+    CTM_CUDA(cudaMemcpyAsync(Y, cur, sizeof(T) * n * q, cudaMemcpyDeviceToDevice, c.stream));
   if (R != nullptr)
-    CTM_CUDA(cudaMemcpyAsync(R, Rt, sizeof(double) * q * q, cudaMemcpyDeviceToDevice, c.stream));
-  restore_if_flagged_kernel<<<grid_for(n * q, 256), 256, 0, c.stream>>>(Y, V, n * q, flags);
+    CTM_CUDA(cudaMemcpyAsync(R, Rt, sizeof(T) * q * q, cudaMemcpyDeviceToDevice, c.stream));
+  restore_if_flagged_kernel<T><<<grid_for(n * q, 256), 256, 0, c.stream>>>(Y, V, n * q, flags);
   CTM_LAUNCH_CHECK();
-  householder_qr_kernel<<<1, LT, 0, c.stream>>>(Y, n, q, R, hv, beta, flags, 1);
+  householder_qr_kernel<T><<<1, LT, 0, c.stream>>>(Y, n, q, R, hv, beta, flags, 1);
   CTM_LAUNCH_CHECK();
+}
+
+void orthonormalize(Ctx& c, double* Y, int64_t n, int64_t q, double* R) {
+  orthonormalize_impl<double>(c, Y, n, q, R);
+}
+
+void orthonormalize(Ctx& c, float* Y, int64_t n, int64_t q, float* R) {
+  orthonormalize_impl<float>(c, Y, n, q, R);
 }
 
 void svd_thin(Ctx& c, const double* X, int64_t m, int64_t n, double* U, double* S, double* V) {
@@ -551,11 +567,17 @@ constexpr int ET = 1024;
 // A (q x q, symmetric, FP32 in global scratch) -> eigenvectors in V (q x q,
 // columns), diagonal of the rotated A holds the eigenvalues.  cs holds 2
 // floats per pair, pr 2 ints per pair.
-__global__ void __launch_bounds__(ET) jacobi_eig_f32_kernel(float* A, float* V, int q, int pp,
+__global__ void __launch_bounds__(ET) jacobi_eig_f32_kernel(float* Ag, float* Vg, int q, int pp,
                                                             float* cs, int* pr, int max_sweeps,
-                                                            int* flags) {
+                                                            float tol, int use_smem, int* flags) {
   __shared__ int s_rot;
+  extern __shared__ float jsm[];
+  float* A = use_smem ? jsm : Ag;
+  float* V = use_smem ? jsm + q * q : Vg;
+  if (use_smem)
+    for (int idx = threadIdx.x; idx < q * q; idx += ET) A[idx] = Ag[idx];
   for (int idx = threadIdx.x; idx < q * q; idx += ET) V[idx] = (idx / q == idx % q) ? 1.f : 0.f;
+  __syncthreads();
   const int npairs = pp / 2;
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     if (threadIdx.x == 0) s_rot = 0;
@@ -570,7 +592,7 @@ __global__ void __launch_bounds__(ET) jacobi_eig_f32_kernel(float* A, float* V, 
         float c = 1.f, s = 0.f;
         if (j < q) {
           const float aii = A[i * q + i], ajj = A[j * q + j], aij = A[i * q + j];
-          if (fabsf(aij) > 1e-6f * sqrtf(fabsf(aii) * fabsf(ajj)) && aij != 0.f) {
+          if (fabsf(aij) > tol * sqrtf(fabsf(aii) * fabsf(ajj)) && aij != 0.f) {
             const float tau = (ajj - aii) / (2.f * aij);
             const float t = copysignf(1.f, tau) / (fabsf(tau) + sqrtf(1.f + tau * tau));
             c = 1.f / sqrtf(1.f + t * t);
@@ -612,10 +634,12 @@ __global__ void __launch_bounds__(ET) jacobi_eig_f32_kernel(float* A, float* V, 
       }
       __syncthreads();
     }
-    if (s_rot == 0) return;
+    if (s_rot == 0) break;
     __syncthreads();
   }
-  if (threadIdx.x == 0) atomicOr(flags, 2);
+  __syncthreads();
+  if (use_smem)
+    for (int idx = threadIdx.x; idx < q * q; idx += ET) Vg[idx] = V[idx];
 }
 
 __global__ void f64_to_f32_kernel(const double* x, float* y, int64_t n) {
@@ -657,10 +681,55 @@ __global__ void eig_finish_kernel(const double* W, const double* H, int64_t q, d
   }
 }
 
+// One Ogita-Aishima refinement step of an approximate eigenvector matrix X
+// of the symmetric G (Ogita & Aishima, Japan J. Indust. Appl. Math. 35 (2018)
+// 1007): with R = I - X^T X and S = X^T G X, lambda_i = S_ii / (1 - R_ii);
+// E_ij = (S_ij + lambda_j R_ij) / (lambda_j - lambda_i) for separated pairs,
+// R_ij / 2 otherwise; X <- X + X E.  This kernel forms E from R and S.
+__global__ void oa_correction_kernel(const double* R, const double* Sm, int64_t q, double* E) {
+  __shared__ double lam[1024];
+  __shared__ double sh_delta;
+  for (int64_t i = threadIdx.x; i < q; i += blockDim.x) lam[i] = Sm[i * q + i] / (1.0 - R[i * q + i]);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // delta = 2 (||S - diag(lambda)|| + max|lambda| ||R||), Frobenius norms
+    // bounding the spectral norms of the paper
+    double so = 0.0, rm = 0.0, lm = 0.0;
+    for (int64_t i = 0; i < q; ++i) {
+      lm = fmax(lm, fabs(lam[i]));
+      for (int64_t j = 0; j < q; ++j) {
+        const double sij = (i == j) ? Sm[i * q + j] - lam[i] : Sm[i * q + j];
+        so = fma(sij, sij, so);
+        rm = fma(R[i * q + j], R[i * q + j], rm);
+      }
+    }
+    sh_delta = 2.0 * (sqrt(so) + lm * sqrt(rm));
+  }
+  __syncthreads();
+  const double delta = sh_delta;
+  for (int64_t idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
+    const int64_t i = idx / q, j = idx % q;
+    double e;
+    if (i == j) {
+      e = 0.5 * R[idx];
+    } else {
+      const double gap = lam[j] - lam[i];
+      e = (fabs(gap) > delta) ? (Sm[idx] + lam[j] * R[idx]) / gap : 0.5 * R[idx];
+    }
+    E[idx] = e;
+  }
+}
+
+__global__ void identity_minus_kernel(double* R, int64_t q) {
+  for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < q * q;
+       idx += int64_t(gridDim.x) * blockDim.x)
+    R[idx] = ((idx / q == idx % q) ? 1.0 : 0.0) - R[idx];
+}
+
 }  // namespace
 
 void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, double* S,
-                  double* V) {
+                  float* V) {
   CTM_REQUIRE(q >= 1 && q <= 1024 && q <= n, CTM_ERR_UNSUPPORTED,
               "svd_via_gram: needs 1 <= q <= min(n, 1024)");
   Scope scope(c);
@@ -676,14 +745,39 @@ void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, dou
   int* order = c.alloc<int>(q);
   // G = B B^T in FP64
   einsum(c, "ik,jk->ij", View(B, {q, n}), View(B, {q, n}), View(G, {q, q}));
+  double* Rm = c.alloc<double>(size_t(q) * q);
+  double* Sm = c.alloc<double>(size_t(q) * q);
+  double* Em = c.alloc<double>(size_t(q) * q);
+  double* W2 = c.alloc<double>(size_t(q) * q);
   if (!c.sizing()) {
     f64_to_f32_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(G, Af, q * q);
     CTM_LAUNCH_CHECK();
-    jacobi_eig_f32_kernel<<<1, ET, 0, c.stream>>>(Af, Vf, int(q), int(pp), cs, pr, 40,
-                                                  status_flags(c));
+    const size_t smem = size_t(2) * q * q * sizeof(float);
+    const int use_smem = smem <= 200 * 1024 ? 1 : 0;
+    if (use_smem)
+      CTM_CUDA(cudaFuncSetAttribute(jacobi_eig_f32_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    jacobi_eig_f32_kernel<<<1, ET, use_smem ? smem : 0, c.stream>>>(
+        Af, Vf, int(q), int(pp), cs, pr, 30, 2e-6f, use_smem, status_flags(c));
     CTM_LAUNCH_CHECK();
     f32_to_f64_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(Vf, W, q * q);
     CTM_LAUNCH_CHECK();
+  }
+  // two FP64 refinement steps of the eigenvectors
+  for (int it = 0; it < 2; ++it) {
+    einsum(c, "ki,kj->ij", View(W, {q, q}), View(W, {q, q}), View(Rm, {q, q}));
+    if (!c.sizing()) {
+      identity_minus_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(Rm, q);
+      CTM_LAUNCH_CHECK();
+    }
+    einsum(c, "ik,kj->ij", View(G, {q, q}), View(W, {q, q}), View(H, {q, q}));
+    einsum(c, "ki,kj->ij", View(W, {q, q}), View(H, {q, q}), View(Sm, {q, q}));
+    if (!c.sizing()) {
+      oa_correction_kernel<<<1, 1024, 0, c.stream>>>(Rm, Sm, q, Em);
+      CTM_LAUNCH_CHECK();
+      CTM_CUDA(cudaMemcpyAsync(W2, W, sizeof(double) * q * q, cudaMemcpyDeviceToDevice, c.stream));
+    }
+    einsum(c, "ik,kj->ij", View(W2, {q, q}), View(Em, {q, q}), View(W, {q, q}), 1.0, 1.0);
   }
   // Rayleigh quotients in FP64
   einsum(c, "ik,kj->ij", View(G, {q, q}), View(W, {q, q}), View(H, {q, q}));
@@ -691,9 +785,16 @@ void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, dou
     eig_finish_kernel<<<1, 1024, 0, c.stream>>>(W, H, q, Ub, S, inv_s, order);
     CTM_LAUNCH_CHECK();
   }
-  // V = B^T Ub diag(1/s)
-  einsum(c, "ki,kj->ij", View(B, {q, n}), View(Ub, {q, q}), View(V, {n, q}));
-  scale_columns(c, V, n, q, q, inv_s);
+  // V = B^T Ub diag(1/s), FP32
+  float* bf = c.alloc<float>(size_t(q) * n);
+  float* uf = c.alloc<float>(size_t(q) * q);
+  double* vd = c.alloc<double>(size_t(n) * q);
+  to_f32(c, B, bf, q * n);
+  to_f32(c, Ub, uf, q * q);
+  einsum(c, "ki,kj->ij", ViewF(bf, {q, n}), ViewF(uf, {q, q}), ViewF(V, {n, q}));
+  to_f64(c, V, vd, n * q);
+  scale_columns(c, vd, n, q, q, inv_s);
+  to_f32(c, vd, V, n * q);
 }
 
 }  // namespace ctm

@@ -59,9 +59,17 @@ QOps quarter_mixed(Ctx& c, const Site& S, int k) {
   const TcMode x3 = TcMode::kBf16x3;
   Scope scope(c);
   double* absmax = c.alloc<double>(1);
-  // t1 = C E_k (a x (c,u,U)), FP64
-  double* t1 = c.alloc<double>(size_t(a) * cc * D2);
-  einsum(c, "ab,bcuU->acuU", ck, ek2, View(t1, {a, cc, D, D}));
+  // t1 = C E_k (a x (c,u,U)), FP32
+  float* t1 = c.alloc<float>(size_t(a) * cc * D2);
+  {
+    Scope s2(c);
+    float* cf = c.alloc<float>(size_t(ck.numel()));
+    float* ef = c.alloc<float>(size_t(ek2.numel()));
+    to_f32(c, ck.p, cf, ck.numel());
+    to_f32(c, ek2.p, ef, ek2.numel());
+    einsum(c, "ab,bcuU->acuU", ViewF(cf, {ck.shape[0], ck.shape[1]}),
+           ViewF(ef, {ek2.shape[0], ek2.shape[1], D, D}), ViewF(t1, {a, cc, D, D}));
+  }
   // t2 operands: A2 = t1^T ((c,u,U) x a), B2 = E_{k+3} as ((e,l,L) x a)
   const int64_t ld2 = tc_ld(a);
   bf16* a2h = c.alloc<bf16>(size_t(cc) * D2 * ld2);
@@ -174,6 +182,14 @@ QOps quarter_mixed(Ctx& c, const Site& S, int k) {
 
 // Y^T as a BF16 operand (q x n) from Y (n x q, ld)
 TcOperand yt_operand(Ctx& c, const double* Y, int64_t n, int64_t q, int64_t ldy, bool lo) {
+  const int64_t ld = tc_ld(n);
+  bf16* hi = c.alloc<bf16>(size_t(q) * ld);
+  bf16* lw = lo ? c.alloc<bf16>(size_t(q) * ld) : nullptr;
+  split_bf16(c, Y, n, q, ldy, true, hi, lw, ld);
+  return TcOperand{hi, lw, q, n, ld};
+}
+
+TcOperand yt_operand_f32(Ctx& c, const float* Y, int64_t n, int64_t q, int64_t ldy, bool lo) {
   const int64_t ld = tc_ld(n);
   bf16* hi = c.alloc<bf16>(size_t(q) * ld);
   bf16* lw = lo ? c.alloc<bf16>(size_t(q) * ld) : nullptr;
@@ -373,6 +389,7 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
   const int64_t m = r1, n = c4;
   const int64_t q = std::min({o.chi + o.rsvd_oversampling, m, n});
   const int64_t cap = std::min(o.chi, q);
+  const TcMode x1 = TcMode::kBf16x1, x3 = TcMode::kBf16x3;
   // ---- quarter tensors as BF16 operands (tensor cores, 3xBF16)
   QOps A1, A4;
   {
@@ -380,15 +397,17 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
     A1 = quarter_mixed(c, *S[0], k);
     A4 = quarter_mixed(c, *S[3], k + 3);
   }
-  const TcMode x1 = TcMode::kBf16x1, x3 = TcMode::kBf16x3;
-  // ---- range finder: Y = Q1 (Q4 Omega), niter x [QR; Y = Q1 Q4 Q4^T Q1^T Y]
-  double* Y = c.alloc<double>(size_t(m) * q);
+  // ---- range finder in BF16 with FP32 orthonormalization:
+  //      Y = Q1 (Q4 Omega), niter x [QR; Y = Q1 Q4 Q4^T Q1^T Y]
+  float* Y = c.alloc<float>(size_t(m) * q);
   KernelTimer* rf_span = new KernelTimer(c.stream, kTagRangeFinder, 0.0);
   {
     Scope s2(c);
-    const TcOperand om = yt_operand(c, omega, n, q, q, false);     // Omega^T (q x n)
+    const TcOperand om = yt_operand(c, omega, n, q, q, false);           // Omega^T (q x n)
     const TcOperand t = gemm_to_operand(c, A4.q(false), om, x1, false);  // (Q4 Om)^T
-    gemm_to_f64(c, A1.q(false), t, x1, Y, q, false);
+    TcOut out;
+    out.add(TcKind::kF32, Y, TcLayout::rows(m, q, q));
+    tc_gemm(c, A1.q(false), t, x1, out);
   }
   for (int it = 0; it < o.rsvd_niter; ++it) {
     {
@@ -396,47 +415,60 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
       orthonormalize(c, Y, m, q, nullptr);
     }
     Scope s2(c);
-    const TcOperand yt = yt_operand(c, Y, m, q, q, false);
+    const TcOperand yt = yt_operand_f32(c, Y, m, q, q, false);
     const TcOperand z1 = gemm_to_operand(c, A1.t(false), yt, x1, false);  // (Q1^T Y)^T
     const TcOperand z2 = gemm_to_operand(c, A4.t(false), z1, x1, false);  // (Q4^T z1)^T
     const TcOperand z3 = gemm_to_operand(c, A4.q(false), z2, x1, false);  // (Q4 z2)^T
-    gemm_to_f64(c, A1.q(false), z3, x1, Y, q, false);
+    TcOut out;
+    out.add(TcKind::kF32, Y, TcLayout::rows(m, q, q));
+    tc_gemm(c, A1.q(false), z3, x1, out);
   }
   {
     KernelTimer span(c.stream, kTagOrtho, 0.0);
     orthonormalize(c, Y, m, q, nullptr);
   }
   delete rf_span;
-  // ---- Rayleigh-Ritz: B = (Q^T Q1) Q4 in 3xBF16, SVD in FP64
+  // ---- Rayleigh-Ritz: B = (Q^T Q1) Q4 in 3xBF16, SVD from the FP64 Gram matrix
   double* Bm = c.alloc<double>(size_t(q) * n);
   double* Ub = c.alloc<double>(size_t(q) * q);
   double* s = c.alloc<double>(q);
-  double* V = c.alloc<double>(size_t(n) * q);
-  double* U = c.alloc<double>(size_t(m) * q);
+  float* V = c.alloc<float>(size_t(n) * q);
+  float* U = c.alloc<float>(size_t(m) * q);
   KernelTimer* svd_span = new KernelTimer(c.stream, kTagSvd, 0.0);
   {
     Scope s2(c);
-    const TcOperand qt = yt_operand(c, Y, m, q, q, true);               // Q^T (q x m)
+    const TcOperand qt = yt_operand_f32(c, Y, m, q, q, true);           // Q^T (q x m)
     const TcOperand w = gemm_to_operand(c, A1.t(true), qt, x3, true);    // W = Q^T Q1 (q x c1)
-    gemm_to_f64(c, A4.t(true), w, x3, Bm, n, true);                     // B (q x n)
+    TcOut out;
+    out.add(TcKind::kF64, Bm, TcLayout::cols(A4.cols, q, n));            // B (q x n)
+    tc_gemm(c, A4.t(true), w, x3, out);
   }
   svd_via_gram(c, Bm, q, n, Ub, s, V);
-  einsum(c, "ik,kj->ij", View(Y, {m, q}), View(Ub, {q, q}), View(U, {m, q}));
+  {
+    Scope s2(c);
+    float* ubf = c.alloc<float>(size_t(q) * q);
+    to_f32(c, Ub, ubf, q * q);
+    einsum(c, "ik,kj->ij", ViewF(Y, {m, q}), ViewF(ubf, {q, q}), ViewF(U, {m, q}));
+  }
   delete svd_span;
-  // ---- truncation and projector products (3xBF16)
+  // ---- truncation (FP64 spectrum) and projector products (3xBF16)
   KernelTimer proj_span(c.stream, kTagProject, 0.0);
   double* f = c.alloc<double>(cap);
   truncation_factors(c, s, q, o.chi, o.svd_cutoff, f, cap, chi_new);
-  scale_columns(c, U, m, cap, q, f);
-  scale_columns(c, V, n, cap, q, f);
   double* P1f = c.alloc<double>(size_t(c1) * cap);
   double* P2f = c.alloc<double>(size_t(r4) * cap);
   {
     Scope s2(c);
-    const TcOperand ut = yt_operand(c, U, m, cap, q, true);  // (U f)^T (cap x m)
-    gemm_to_f64(c, A1.t(true), ut, x3, P1f, cap, false);    // Q1^T U f (c1 x cap)
-    const TcOperand vt = yt_operand(c, V, n, cap, q, true);  // (V f)^T (cap x n)
-    gemm_to_f64(c, A4.q(true), vt, x3, P2f, cap, false);    // Q4 V f (r4 x cap)
+    double* Ud = c.alloc<double>(size_t(m) * q);
+    double* Vd = c.alloc<double>(size_t(n) * q);
+    to_f64(c, U, Ud, m * q);
+    to_f64(c, V, Vd, n * q);
+    scale_columns(c, Ud, m, cap, q, f);
+    scale_columns(c, Vd, n, cap, q, f);
+    const TcOperand ut = yt_operand(c, Ud, m, cap, q, true);  // (U f)^T (cap x m)
+    gemm_to_f64(c, A1.t(true), ut, x3, P1f, cap, false);     // Q1^T U f (c1 x cap)
+    const TcOperand vt = yt_operand(c, Vd, n, cap, q, true);  // (V f)^T (cap x n)
+    gemm_to_f64(c, A4.q(true), vt, x3, P2f, cap, false);     // Q4 V f (r4 x cap)
   }
   scale_columns_compact(c, P1f, c1, cap, nullptr, chi_new, P1);
   scale_columns_compact(c, P2f, r4, cap, nullptr, chi_new, P2);

@@ -277,12 +277,17 @@ struct ReduceParams {
   TcDest d[4];
 };
 
-__device__ __forceinline__ int64_t lay_off(const TcLayout& l, int64_t m, int64_t n) {
+__device__ __forceinline__ int64_t lay_row(const TcLayout& l, int64_t m) {
   int64_t o = 0;
   for (int j = l.nm - 1; j >= 0; --j) {
     o += (m % l.me[j]) * l.ms[j];
     m /= l.me[j];
   }
+  return o;
+}
+
+__device__ __forceinline__ int64_t lay_col(const TcLayout& l, int64_t n) {
+  int64_t o = 0;
   for (int j = l.nn - 1; j >= 0; --j) {
     o += (n % l.ne[j]) * l.ns[j];
     n /= l.ne[j];
@@ -303,12 +308,14 @@ __device__ __forceinline__ void store(const TcDest& d, int64_t off, double v) {
   }
 }
 
-// 32 x 32 output tile per block (32 x 8 threads).  Destinations whose
-// innermost column stride is 1 are written with the column index fastest,
-// the others with the row index fastest, so warps store contiguously in the
-// common row- and column-major cases.
+// 32 x 32 output tile per block (32 x 8 threads).  Every layout is separable
+// (offset = row part + column part), so each block decodes its 32 row and 32
+// column offsets once per destination.  Destinations whose innermost column
+// stride is 1 are written with the column index fastest, the others with the
+// row index fastest, so warps store contiguously in the common cases.
 __global__ void tc_reduce_kernel(const ReduceParams r) {
   __shared__ double tile[32][33];
+  __shared__ int64_t ro[32], co[32];
   const int64_t m0 = int64_t(blockIdx.x) * 32, n0 = int64_t(blockIdx.y) * 32;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   for (int yy = ty; yy < 32; yy += 8) {
@@ -322,19 +329,23 @@ __global__ void tc_reduce_kernel(const ReduceParams r) {
     }
     tile[yy][tx] = s;
   }
-  __syncthreads();
   for (int k = 0; k < r.nd; ++k) {
     const TcDest& d = r.d[k];
+    __syncthreads();
+    if (threadIdx.x < 32) ro[threadIdx.x] = lay_row(d.lay, m0 + threadIdx.x);
+    else if (threadIdx.x < 64) co[threadIdx.x - 32] = lay_col(d.lay, n0 + threadIdx.x - 32);
+    __syncthreads();
     const bool n_fast = d.lay.ns[d.lay.nn - 1] == 1;
     for (int yy = ty; yy < 32; yy += 8) {
-      const int64_t m = m0 + (n_fast ? yy : tx), n = n0 + (n_fast ? tx : yy);
-      if (m >= r.M || n >= r.N) continue;
-      store(d, lay_off(d.lay, m, n), n_fast ? tile[yy][tx] : tile[tx][yy]);
+      const int mi = n_fast ? yy : tx, ni = n_fast ? tx : yy;
+      if (m0 + mi >= r.M || n0 + ni >= r.N) continue;
+      store(d, ro[mi] + co[ni], tile[mi][ni]);
     }
   }
 }
 
-__global__ void split_bf16_kernel(const double* src, int64_t rows, int64_t cols, int64_t ld_src,
+template <class S>
+__global__ void split_bf16_kernel(const S* src, int64_t rows, int64_t cols, int64_t ld_src,
                                   int transpose, bf16* hi, bf16* lo, int64_t ld_dst) {
   __shared__ double tile[32][33];
   const int64_t r0 = int64_t(blockIdx.y) * 32, c0 = int64_t(blockIdx.x) * 32;
@@ -343,7 +354,7 @@ __global__ void split_bf16_kernel(const double* src, int64_t rows, int64_t cols,
     for (int yy = ty; yy < 32; yy += 8) {
       const int64_t r = r0 + yy, c = c0 + tx;
       if (r < rows && c < cols) {
-        const double x = src[r * ld_src + c];
+        const double x = double(src[r * ld_src + c]);
         const bf16 h = __double2bfloat16(x);
         hi[r * ld_dst + c] = h;
         if (lo != nullptr) lo[r * ld_dst + c] = __double2bfloat16(x - double(__bfloat162float(h)));
@@ -353,7 +364,7 @@ __global__ void split_bf16_kernel(const double* src, int64_t rows, int64_t cols,
   }
   for (int yy = ty; yy < 32; yy += 8) {
     const int64_t r = r0 + yy, c = c0 + tx;
-    tile[yy][tx] = (r < rows && c < cols) ? src[r * ld_src + c] : 0.0;
+    tile[yy][tx] = (r < rows && c < cols) ? double(src[r * ld_src + c]) : 0.0;
   }
   __syncthreads();
   for (int yy = ty; yy < 32; yy += 8) {
@@ -418,14 +429,25 @@ int sm_count() {
 
 }  // namespace
 
-void split_bf16(Ctx& c, const double* src, int64_t rows, int64_t cols, int64_t ld_src,
-                bool transpose, bf16* hi, bf16* lo, int64_t ld_dst) {
+template <class S>
+void split_bf16_impl(Ctx& c, const S* src, int64_t rows, int64_t cols, int64_t ld_src,
+                     bool transpose, bf16* hi, bf16* lo, int64_t ld_dst) {
   if (c.sizing() || rows * cols == 0) return;
   dim3 grid(unsigned((cols + 31) / 32), unsigned((rows + 31) / 32));
   CTM_REQUIRE(grid.y <= 65535, CTM_ERR_UNSUPPORTED, "split_bf16: too many rows");
-  split_bf16_kernel<<<grid, 256, 0, c.stream>>>(src, rows, cols, ld_src, transpose ? 1 : 0, hi, lo,
-                                                ld_dst);
+  split_bf16_kernel<S><<<grid, 256, 0, c.stream>>>(src, rows, cols, ld_src, transpose ? 1 : 0, hi,
+                                                   lo, ld_dst);
   CTM_LAUNCH_CHECK();
+}
+
+void split_bf16(Ctx& c, const double* src, int64_t rows, int64_t cols, int64_t ld_src,
+                bool transpose, bf16* hi, bf16* lo, int64_t ld_dst) {
+  split_bf16_impl<double>(c, src, rows, cols, ld_src, transpose, hi, lo, ld_dst);
+}
+
+void split_bf16(Ctx& c, const float* src, int64_t rows, int64_t cols, int64_t ld_src,
+                bool transpose, bf16* hi, bf16* lo, int64_t ld_dst) {
+  split_bf16_impl<float>(c, src, rows, cols, ld_src, transpose, hi, lo, ld_dst);
 }
 
 namespace {

@@ -93,5 +93,7 @@ void gather_split_bf16(Ctx& c, const double* src, const Gather& g, bf16* hi, bf1
 // transpose the destination is (cols x rows).  lo may be null.
 void split_bf16(Ctx& c, const double* src, int64_t rows, int64_t cols, int64_t ld_src,
                 bool transpose, bf16* hi, bf16* lo, int64_t ld_dst);
+void split_bf16(Ctx& c, const float* src, int64_t rows, int64_t cols, int64_t ld_src,
+                bool transpose, bf16* hi, bf16* lo, int64_t ld_dst);
 
 }  // namespace ctm
