@@ -33,7 +33,8 @@ class CtmSite(ctypes.Structure):
 class CtmOpts(ctypes.Structure):
     _fields_ = [("chi", c_i64), ("projectors", c_i32), ("svd_type", c_i32),
                 ("svd_cutoff", ctypes.c_double), ("rsvd_niter", c_i32),
-                ("rsvd_oversampling", c_i32), ("precision", c_i32), ("reserved", c_i32)]
+                ("rsvd_oversampling", c_i32), ("precision", c_i32), ("reserved", c_i32),
+                ("mixed_floor", ctypes.c_double)]
 
 
 SITE_P = ctypes.POINTER(CtmSite)
@@ -252,4 +253,5 @@ def opts_struct(config, chi, precision):
     if precision not in PREC:
         raise ValueError(f"Invalid precision: {precision} provided.")
     o.precision = PREC[precision]
+    o.mixed_floor = float(getattr(config, "mixed_svd_floor", 1e-6))
     return o

@@ -7,6 +7,10 @@ documented in docs/source/input_settings.rst:45-54) and adds two fields:
 * ``precision`` -- "fp64": every product in FP64, the drop-in path;
                    "mixed": tensor-core range finder and split-precision
                    products feeding the projectors (half-system rSVD only).
+* ``mixed_svd_floor`` -- mixed precision only: singular values below this
+                   fraction of the largest are dropped in addition to
+                   ``svd_cutoff`` (the 3xBF16 Rayleigh-Ritz product resolves
+                   about 1e-5 of the largest).
 
 Any object with the reference's attribute names works as a config; missing
 attributes take the defaults below.
@@ -27,6 +31,7 @@ class CTMRGConfig:
     disable_progressbar: bool = False
     backend: Literal["gb300"] = "gb300"
     precision: Literal["fp64", "mixed"] = "fp64"
+    mixed_svd_floor: float = 1e-6
 
 
 def resolve(config):

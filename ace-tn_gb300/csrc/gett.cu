@@ -305,8 +305,8 @@ void einsum_impl(Ctx& c, const char* spec, const ViewT<T>& A, const ViewT<T>& B,
   const int64_t tiles = ((p.Mt + BM - 1) / BM) * ((p.Nt + BN - 1) / BN) * bext;
   int splitk = 1;
   const int64_t target = 2 * 152;
-  if (tiles < target && p.Kt >= 4 * BK) {
-    splitk = static_cast<int>(std::min<int64_t>((target + tiles - 1) / tiles, p.Kt / (4 * BK)));
+  if (tiles < target && p.Kt >= 2 * BK) {
+    splitk = static_cast<int>(std::min<int64_t>((target + tiles - 1) / tiles, p.Kt / BK));
     splitk = std::max(splitk, 1);
   }
   p.kchunk = ((p.Kt + splitk - 1) / splitk + BK - 1) / BK * BK;

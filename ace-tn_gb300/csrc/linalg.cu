@@ -137,9 +137,13 @@ __global__ void __launch_bounds__(LT) cholesky_inverse_kernel(const T* G, int64_
   for (int64_t i = threadIdx.x; i < q; i += LT) tr += G[i * q + i];
   tr = block_sum(tr, sh);
   if (threadIdx.x == 0) {
-    // unit roundoff of T: 2^-53 (double) or 2^-24 (float)
+    // FP64: the shift of Fukaya et al., 11 (n q + q (q + 1)) u ||Y||_F^2.  In FP32
+    // that bound exceeds the spectrum itself for n q ~ 1e6; the FP32 variant
+    // (mixed path only) uses 100 u ||Y||_F^2, enough to keep the Cholesky of
+    // the Gram matrix positive and to bring cond(Y R^-1) under ~1e3.
     const double u = sizeof(T) == 8 ? 1.1102230246251565e-16 : 5.9604644775390625e-08;
-    s_shift = shifted ? T(11.0 * (double(n) * q + double(q) * (q + 1)) * u * double(tr)) : T(0);
+    const double factor = sizeof(T) == 8 ? 11.0 * (double(n) * q + double(q) * (q + 1)) : 100.0;
+    s_shift = shifted ? T(factor * u * double(tr)) : T(0);
     s_fail = 0;
   }
   __syncthreads();
@@ -564,79 +568,100 @@ namespace {
 
 constexpr int ET = 1024;
 
-// A (q x q, symmetric, FP32 in global scratch) -> eigenvectors in V (q x q,
-// columns), diagonal of the rotated A holds the eigenvalues.  cs holds 2
-// floats per pair, pr 2 ints per pair.
+// A (q x q, symmetric, FP32) -> eigenvectors in V (q x q, columns); the
+// diagonal of the rotated A holds the eigenvalues.  Parallel cyclic Jacobi:
+// each round rotates q/2 disjoint pairs (round-robin ordering), applying
+// J^T A then A J.  Shared memory holds A, V and the round's rotations when
+// they fit.  A pair is rotated when |a_ij| exceeds tol * max(sqrt|a_ii a_jj|,
+// 1e-7 * max_k |a_kk|): FP32 cannot resolve smaller couplings, which the FP64
+// refinement that follows removes.
 __global__ void __launch_bounds__(ET) jacobi_eig_f32_kernel(float* Ag, float* Vg, int q, int pp,
-                                                            float* cs, int* pr, int max_sweeps,
-                                                            float tol, int use_smem, int* flags) {
+                                                            int max_sweeps, float tol, int use_smem,
+                                                            int* flags) {
   __shared__ int s_rot;
+  __shared__ float s_amax;
+  __shared__ float cs[2 * 512];
+  __shared__ int pr[2 * 512];
   extern __shared__ float jsm[];
   float* A = use_smem ? jsm : Ag;
   float* V = use_smem ? jsm + q * q : Vg;
   if (use_smem)
     for (int idx = threadIdx.x; idx < q * q; idx += ET) A[idx] = Ag[idx];
   for (int idx = threadIdx.x; idx < q * q; idx += ET) V[idx] = (idx / q == idx % q) ? 1.f : 0.f;
-  __syncthreads();
   const int npairs = pp / 2;
-  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
-    if (threadIdx.x == 0) s_rot = 0;
+  // threads per pair in the update phases
+  const int tpp = max(1, min(32, ET / max(npairs, 1)));
+  const int slot = threadIdx.x / tpp, lane = threadIdx.x % tpp;
+  const int slots = ET / tpp;
+  __syncthreads();
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    if (threadIdx.x == 0) {
+      float m = 0.f;
+      for (int i = 0; i < q; ++i) m = fmaxf(m, fabsf(A[i * q + i]));
+      s_amax = m;
+      s_rot = 0;
+    }
     __syncthreads();
+    const float floor_abs = 1e-7f * s_amax;
     for (int r = 0; r < pp - 1; ++r) {
-      // rotation angles of the round's disjoint pairs
       for (int k = threadIdx.x; k < npairs; k += ET) {
         const int i0 = k == 0 ? 0 : ((k - 1 + r) % (pp - 1)) + 1;
         const int k2 = pp - 1 - k;
         const int j0 = k2 == 0 ? 0 : ((k2 - 1 + r) % (pp - 1)) + 1;
         const int i = min(i0, j0), j = max(i0, j0);
-        float c = 1.f, s = 0.f;
+        float c = 1.f, sn = 0.f;
         if (j < q) {
           const float aii = A[i * q + i], ajj = A[j * q + j], aij = A[i * q + j];
-          if (fabsf(aij) > tol * sqrtf(fabsf(aii) * fabsf(ajj)) && aij != 0.f) {
+          const float thr = tol * fmaxf(sqrtf(fabsf(aii) * fabsf(ajj)), floor_abs);
+          if (fabsf(aij) > thr && aij != 0.f) {
             const float tau = (ajj - aii) / (2.f * aij);
             const float t = copysignf(1.f, tau) / (fabsf(tau) + sqrtf(1.f + tau * tau));
             c = 1.f / sqrtf(1.f + t * t);
-            s = t * c;
+            sn = t * c;
             s_rot = 1;
           }
         }
         cs[2 * k] = c;
-        cs[2 * k + 1] = s;
+        cs[2 * k + 1] = sn;
         pr[2 * k] = i;
         pr[2 * k + 1] = j;
       }
       __syncthreads();
       // rows: A <- J^T A
-      for (int idx = threadIdx.x; idx < npairs * q; idx += ET) {
-        const int k = idx / q, col = idx % q;
+      for (int k = slot; k < npairs; k += slots) {
+        const float sn = cs[2 * k + 1];
         const int i = pr[2 * k], j = pr[2 * k + 1];
-        if (j >= q) continue;
-        const float c = cs[2 * k], s = cs[2 * k + 1];
-        if (s == 0.f) continue;
-        const float ai = A[i * q + col], aj = A[j * q + col];
-        A[i * q + col] = c * ai - s * aj;
-        A[j * q + col] = s * ai + c * aj;
+        if (sn == 0.f || j >= q) continue;
+        const float c = cs[2 * k];
+        for (int col = lane; col < q; col += tpp) {
+          const float ai = A[i * q + col], aj = A[j * q + col];
+          A[i * q + col] = c * ai - sn * aj;
+          A[j * q + col] = sn * ai + c * aj;
+        }
       }
       __syncthreads();
       // columns: A <- A J, V <- V J
-      for (int idx = threadIdx.x; idx < npairs * q; idx += ET) {
-        const int k = idx / q, row = idx % q;
+      for (int k = slot; k < npairs; k += slots) {
+        const float sn = cs[2 * k + 1];
         const int i = pr[2 * k], j = pr[2 * k + 1];
-        if (j >= q) continue;
-        const float c = cs[2 * k], s = cs[2 * k + 1];
-        if (s == 0.f) continue;
-        const float ai = A[row * q + i], aj = A[row * q + j];
-        A[row * q + i] = c * ai - s * aj;
-        A[row * q + j] = s * ai + c * aj;
-        const float vi = V[row * q + i], vj = V[row * q + j];
-        V[row * q + i] = c * vi - s * vj;
-        V[row * q + j] = s * vi + c * vj;
+        if (sn == 0.f || j >= q) continue;
+        const float c = cs[2 * k];
+        for (int row = lane; row < q; row += tpp) {
+          const float ai = A[row * q + i], aj = A[row * q + j];
+          A[row * q + i] = c * ai - sn * aj;
+          A[row * q + j] = sn * ai + c * aj;
+          const float vi = V[row * q + i], vj = V[row * q + j];
+          V[row * q + i] = c * vi - sn * vj;
+          V[row * q + j] = sn * vi + c * vj;
+        }
       }
       __syncthreads();
     }
     if (s_rot == 0) break;
     __syncthreads();
   }
+  if (threadIdx.x == 0 && sweep == max_sweeps) atomicOr(flags, 2);
   __syncthreads();
   if (use_smem)
     for (int idx = threadIdx.x; idx < q * q; idx += ET) Vg[idx] = V[idx];
@@ -691,19 +716,36 @@ __global__ void oa_correction_kernel(const double* R, const double* Sm, int64_t 
   __shared__ double sh_delta;
   for (int64_t i = threadIdx.x; i < q; i += blockDim.x) lam[i] = Sm[i * q + i] / (1.0 - R[i * q + i]);
   __syncthreads();
+  // delta = 2 (||S - diag(lambda)|| + max|lambda| ||R||), Frobenius norms
+  // bounding the spectral norms of the paper
+  __shared__ double red[3][32];
+  double so = 0.0, rm = 0.0, lm = 0.0;
+  for (int64_t idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
+    const int64_t i = idx / q, j = idx % q;
+    const double sij = (i == j) ? Sm[idx] - lam[i] : Sm[idx];
+    so = fma(sij, sij, so);
+    rm = fma(R[idx], R[idx], rm);
+    if (i == j) lm = fmax(lm, fabs(lam[i]));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    so += __shfl_xor_sync(0xffffffffu, so, o);
+    rm += __shfl_xor_sync(0xffffffffu, rm, o);
+    lm = fmax(lm, __shfl_xor_sync(0xffffffffu, lm, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = so;
+    red[1][threadIdx.x >> 5] = rm;
+    red[2][threadIdx.x >> 5] = lm;
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
-    // delta = 2 (||S - diag(lambda)|| + max|lambda| ||R||), Frobenius norms
-    // bounding the spectral norms of the paper
-    double so = 0.0, rm = 0.0, lm = 0.0;
-    for (int64_t i = 0; i < q; ++i) {
-      lm = fmax(lm, fabs(lam[i]));
-      for (int64_t j = 0; j < q; ++j) {
-        const double sij = (i == j) ? Sm[i * q + j] - lam[i] : Sm[i * q + j];
-        so = fma(sij, sij, so);
-        rm = fma(R[i * q + j], R[i * q + j], rm);
-      }
+    double a = 0.0, b = 0.0, l = 0.0;
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) {
+      a += red[0][w];
+      b += red[1][w];
+      l = fmax(l, red[2][w]);
     }
-    sh_delta = 2.0 * (sqrt(so) + lm * sqrt(rm));
+    sh_delta = 2.0 * (sqrt(a) + l * sqrt(b));
   }
   __syncthreads();
   const double delta = sh_delta;
@@ -740,8 +782,6 @@ void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, dou
   double* H = c.alloc<double>(size_t(q) * q);
   double* inv_s = c.alloc<double>(q);
   const int64_t pp = q + (q & 1);
-  float* cs = c.alloc<float>(pp);
-  int* pr = c.alloc<int>(pp);
   int* order = c.alloc<int>(q);
   // G = B B^T in FP64
   einsum(c, "ik,jk->ij", View(B, {q, n}), View(B, {q, n}), View(G, {q, q}));
@@ -758,7 +798,7 @@ void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, dou
       CTM_CUDA(cudaFuncSetAttribute(jacobi_eig_f32_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     jacobi_eig_f32_kernel<<<1, ET, use_smem ? smem : 0, c.stream>>>(
-        Af, Vf, int(q), int(pp), cs, pr, 30, 2e-6f, use_smem, status_flags(c));
+        Af, Vf, int(q), int(pp), 30, 1e-6f, use_smem, status_flags(c));
     CTM_LAUNCH_CHECK();
     f32_to_f64_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(Vf, W, q * q);
     CTM_LAUNCH_CHECK();

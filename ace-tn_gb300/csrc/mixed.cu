@@ -454,7 +454,7 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
   // ---- truncation (FP64 spectrum) and projector products (3xBF16)
   KernelTimer proj_span(c.stream, kTagProject, 0.0);
   double* f = c.alloc<double>(cap);
-  truncation_factors(c, s, q, o.chi, o.svd_cutoff, f, cap, chi_new);
+  truncation_factors(c, s, q, o.chi, std::max(o.svd_cutoff, o.mixed_floor), f, cap, chi_new);
   double* P1f = c.alloc<double>(size_t(c1) * cap);
   double* P2f = c.alloc<double>(size_t(r4) * cap);
   {

@@ -71,6 +71,10 @@ typedef struct ctm_ctmrg_opts {
   int32_t rsvd_oversampling; /* q = chi + oversampling (2)              */
   int32_t precision;    /* CTM_PREC_FP64 | CTM_PREC_MIXED               */
   int32_t reserved;
+  double mixed_floor;   /* CTM_PREC_MIXED only: singular values below
+                           mixed_floor * s_0 are dropped as well (they are
+                           below the resolution of the 3xBF16 products);
+                           0 keeps svd_cutoff alone                        */
 } ctm_ctmrg_opts;
 
 /* Library version string and message of the last failure on this thread. */

@@ -1,0 +1,97 @@
+"""Mixed-precision path (CTM_PREC_MIXED) against the FP64 path and the
+oracle.  The error budget: 3xBF16 products carry ~1e-5 relative error; the
+BF16 range finder changes the rSVD subspace by about as much as drawing a
+different random test matrix does (the algorithm's own noise), so projector
+pairs are compared loosely and energies after one move tightly."""
+
+import numpy as np
+import pytest
+import torch
+
+import acetn_gb300 as gb
+from _golden import gpu_state, load
+from oracle import ctm_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+CFG = dict(projectors="half-system", svd_type="rsvd", rsvd_niter=2, disable_progressbar=True)
+
+
+def omega_from(seed):
+    s = orc.OmegaStream(seed)
+    return lambda n, q, dev: torch.from_numpy(s(n, q)).to(dev)
+
+
+def clone(st):
+    g = gb.IpepsState(st.nx, st.ny, st.dims, st.device)
+    for s in st.site_list:
+        v = st[s]
+        g[s] = {"A": v["A"].clone(), "C": [c.clone() for c in v["C"]],
+                "E": [e.clone() for e in v["E"]]}
+    return g
+
+
+@pytest.fixture(scope="module")
+def grown_d4():
+    st = gb.random_state(4, 32, 1234, device="cuda")
+    gb.ctmrg(st, gb.CTMRGConfig(**CFG, rsvd_oversampling=4, steps=2), omega_source=omega_from(1))
+    return st
+
+
+def test_mixed_quarter_tensor_matches_fp64(grown_d4):
+    z = load("move_d3_chi9.npz")
+    for st in (gpu_state(z, 9), grown_d4):
+        for k in range(4):
+            q64, sh = gb.ProjectorCalculator.make_quarter_tensor(st[(0, 0)], k)
+            qmx, sh2 = gb.ProjectorCalculator.make_quarter_tensor(st[(0, 0)], k, precision="mixed")
+            assert sh == sh2
+            err = float((q64 - qmx).abs().max() / q64.abs().max())
+            assert err < 2e-5, (k, err)
+
+
+def test_mixed_move_energy_close_to_fp64(grown_d4):
+    es = {}
+    for prec in ("fp64", "mixed"):
+        st = clone(grown_d4)
+        mv = gb.DirectionalMover(gb.CTMRGConfig(**CFG, rsvd_oversampling=4, precision=prec),
+                                 omega_source=omega_from(9))
+        for k in range(4):
+            mv.move(st, k, 0)
+        es[prec] = float(gb.measure(st, gb.HeisenbergModel(1.0), verbose=False)["Energy"])
+    assert abs(es["mixed"] - es["fp64"]) <= 1e-4 * abs(es["fp64"]), es
+
+
+def test_mixed_shapes_match_fp64_shapes(grown_d4):
+    sites = [(0, 0), (1, 0), (1, 1), (0, 1)]
+    out = {}
+    for prec in ("fp64", "mixed"):
+        pc = gb.ProjectorCalculator(gb.CTMRGConfig(**CFG, rsvd_oversampling=4, precision=prec),
+                                    omega_source=omega_from(7))
+        out[prec] = pc.calculate(grown_d4, sites, 0)
+    for a, b in zip(out["fp64"], out["mixed"]):
+        assert a.shape == b.shape
+
+
+@pytest.mark.parametrize("case", ["ising_dims_2_20_dtau_001_hx_295",
+                                  "heisenberg_dims_3_16_dtau_001"])
+def test_mixed_ctmrg_keeps_ground_state_energy(case):
+    z = load(f"gs_{case}.npz")
+    chi = z["in_00_C0"].shape[0]
+    model = gb.IsingModel(1.0, 2.95) if case.startswith("ising") else gb.HeisenbergModel(1.0)
+    st = gpu_state(z, chi)
+    gb.ctmrg(st, gb.CTMRGConfig(steps=5, precision="mixed", disable_progressbar=True),
+             omega_source=omega_from(31))
+    e = float(gb.measure(st, model, verbose=False)["Energy"])
+    e_pub = float(z["published_energy"])
+    assert abs(e - e_pub) <= 1e-6 * abs(e_pub), (e, e_pub)
+
+
+def test_mixed_rejects_unsupported_configurations(grown_d4):
+    pc = gb.ProjectorCalculator(gb.CTMRGConfig(**{**CFG, "projectors": "full-system"},
+                                               precision="mixed"))
+    with pytest.raises(RuntimeError):
+        pc.calculate(grown_d4, [(0, 0), (1, 0), (1, 1), (0, 1)], 0)
+
+
+def test_mixed_no_device_flags():
+    assert gb._abi.device_status() == 0
