@@ -139,10 +139,11 @@ __global__ void __launch_bounds__(LT) cholesky_inverse_kernel(const T* G, int64_
   if (threadIdx.x == 0) {
     // FP64: the shift of Fukaya et al., 11 (n q + q (q + 1)) u ||Y||_F^2.  In FP32
     // that bound exceeds the spectrum itself for n q ~ 1e6; the FP32 variant
-    // (mixed path only) uses 100 u ||Y||_F^2, enough to keep the Cholesky of
-    // the Gram matrix positive and to bring cond(Y R^-1) under ~1e3.
+    // (mixed path only) uses 1000 u ||Y||_F^2 (6e-5 ||Y||_F^2): above the
+    // rounding noise of the FP32 Gram matrix and of its factorization, so the
+    // Cholesky stays positive, while cond(Y R^-1) stays below ~1e2.
     const double u = sizeof(T) == 8 ? 1.1102230246251565e-16 : 5.9604644775390625e-08;
-    const double factor = sizeof(T) == 8 ? 11.0 * (double(n) * q + double(q) * (q + 1)) : 100.0;
+    const double factor = sizeof(T) == 8 ? 11.0 * (double(n) * q + double(q) * (q + 1)) : 1000.0;
     s_shift = shifted ? T(factor * u * double(tr)) : T(0);
     s_fail = 0;
   }
@@ -572,8 +573,8 @@ constexpr int ET = 1024;
 // diagonal of the rotated A holds the eigenvalues.  Parallel cyclic Jacobi:
 // each round rotates q/2 disjoint pairs (round-robin ordering), applying
 // J^T A then A J.  Shared memory holds A, V and the round's rotations when
-// they fit.  A pair is rotated when |a_ij| exceeds tol * max(sqrt|a_ii a_jj|,
-// 1e-7 * max_k |a_kk|): FP32 cannot resolve smaller couplings, which the FP64
+// they fit.  A pair is rotated when |a_ij| exceeds max(tol sqrt|a_ii a_jj|,
+// 1e-6 max_k |a_kk|): FP32 cannot resolve smaller couplings, which the FP64
 // refinement that follows removes.
 __global__ void __launch_bounds__(ET) jacobi_eig_f32_kernel(float* Ag, float* Vg, int q, int pp,
                                                             int max_sweeps, float tol, int use_smem,
@@ -603,7 +604,7 @@ __global__ void __launch_bounds__(ET) jacobi_eig_f32_kernel(float* Ag, float* Vg
       s_rot = 0;
     }
     __syncthreads();
-    const float floor_abs = 1e-7f * s_amax;
+    const float floor_abs = 1e-6f * s_amax;
     for (int r = 0; r < pp - 1; ++r) {
       for (int k = threadIdx.x; k < npairs; k += ET) {
         const int i0 = k == 0 ? 0 : ((k - 1 + r) % (pp - 1)) + 1;
@@ -613,7 +614,7 @@ __global__ void __launch_bounds__(ET) jacobi_eig_f32_kernel(float* Ag, float* Vg
         float c = 1.f, sn = 0.f;
         if (j < q) {
           const float aii = A[i * q + i], ajj = A[j * q + j], aij = A[i * q + j];
-          const float thr = tol * fmaxf(sqrtf(fabsf(aii) * fabsf(ajj)), floor_abs);
+          const float thr = fmaxf(tol * sqrtf(fabsf(aii) * fabsf(ajj)), floor_abs);
           if (fabsf(aij) > thr && aij != 0.f) {
             const float tau = (ajj - aii) / (2.f * aij);
             const float t = copysignf(1.f, tau) / (fabsf(tau) + sqrtf(1.f + tau * tau));
