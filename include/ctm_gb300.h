@@ -199,6 +199,22 @@ int ctm_matmul(const double* A, const double* B, double* C, int64_t M, int64_t N
                int64_t K, int32_t precision, void* ws, size_t* ws_bytes,
                ctm_stream_t stream);
 
+/* C = A @ B (FP64 in and out, 3xBF16 tensor-core arithmetic as ctm_matmul
+ * with CTM_PREC_MIXED) for callers that cannot allocate device memory: a
+ * host that hands a plugin only its input and output buffers, or code that
+ * runs while a global-mode stream capture forbids cudaMalloc.  No workspace:
+ * the scratch (BF16 operand copies, split-K partial sums) lives in a 32 MiB
+ * file-scope device array that every GPU loading the library keeps until the
+ * process exits; products needing more scratch (about M = N = K > 1000)
+ * return CTM_ERR_WORKSPACE.  The first call on a device looks up that
+ * device's address of the array (cudaGetSymbolAddress): make it before any
+ * stream capture.  All calls share the array and it keeps the last call's
+ * contents, so calls that overlap on the GPU (different streams, or threads
+ * without ordering) race; serialise them.  Allocates nothing: no cudaMalloc,
+ * cudaFree or allocating library call.  No counterpart in the reference. */
+int ctm_matmul_mixed_noalloc(const double* A, const double* B, double* C, int64_t M,
+                             int64_t N, int64_t K, ctm_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
