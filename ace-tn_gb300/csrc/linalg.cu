@@ -123,28 +123,30 @@ __global__ void __launch_bounds__(LT) householder_qr_kernel(T* Y, int64_t n, int
 
 // ------------------------------------------------------------- Cholesky
 // One CTA.  G (q x q) -> Linv (q x q, lower-triangular inverse of the
-// Cholesky factor of G + shift I), Lt (q x q) = L^T (upper).  W is q x q
-// scratch.  shift = 11 (n q + q (q + 1)) u tr(G) when shifted != 0.
+// Cholesky factor of G + shift I) and Lt = L^T (upper).  W is q x q global
+// scratch used when the working matrices do not fit in shared memory.
+// shift_mode 0: none; 1: 11 (n q + q (q + 1)) u tr(G) (Fukaya et al.);
+// 2: 1000 u tr(G) (FP32 stages of the mixed path).
 template <class T>
 __global__ void __launch_bounds__(LT) cholesky_inverse_kernel(const T* G, int64_t q,
-                                                              int64_t n, int shifted, T* W,
-                                                              T* Linv, T* Lt,
-                                                              int* flags) {
+                                                              int64_t n, int shift_mode, T* Wg,
+                                                              T* Linv, T* Lt, int* flags,
+                                                              int use_smem) {
   __shared__ T sh[LT / 32];
   __shared__ T s_shift;
   __shared__ int s_fail;
+  extern __shared__ unsigned char chol_smem[];
+  T* W = use_smem ? reinterpret_cast<T*>(chol_smem) : Wg;
+  T* X = (use_smem == 2) ? W + q * q : Linv;  // inverse built in shared memory too
   T tr = T(0);
   for (int64_t i = threadIdx.x; i < q; i += LT) tr += G[i * q + i];
   tr = block_sum(tr, sh);
   if (threadIdx.x == 0) {
-    // FP64: the shift of Fukaya et al., 11 (n q + q (q + 1)) u ||Y||_F^2.  In FP32
-    // that bound exceeds the spectrum itself for n q ~ 1e6; the FP32 variant
-    // (mixed path only) uses 1000 u ||Y||_F^2 (6e-5 ||Y||_F^2): above the
-    // rounding noise of the FP32 Gram matrix and of its factorization, so the
-    // Cholesky stays positive, while cond(Y R^-1) stays below ~1e2.
     const double u = sizeof(T) == 8 ? 1.1102230246251565e-16 : 5.9604644775390625e-08;
-    const double factor = sizeof(T) == 8 ? 11.0 * (double(n) * q + double(q) * (q + 1)) : 1000.0;
-    s_shift = shifted ? T(factor * u * double(tr)) : T(0);
+    double factor = 0.0;
+    if (shift_mode == 1) factor = 11.0 * (double(n) * q + double(q) * (q + 1));
+    if (shift_mode == 2) factor = 1000.0;
+    s_shift = T(factor * u * double(tr));
     s_fail = 0;
   }
   __syncthreads();
@@ -172,20 +174,23 @@ __global__ void __launch_bounds__(LT) cholesky_inverse_kernel(const T* G, int64_
     __syncthreads();
   }
   if (threadIdx.x == 0 && s_fail) atomicOr(flags, 1);
-  // Linv: forward substitution, one column per thread
-  for (int64_t c = threadIdx.x; c < q; c += LT) {
-    for (int64_t i = 0; i < q; ++i) {
-      T v;
-      if (i < c) {
-        v = T(0);
-      } else {
+  // X = L^-1 row by row: X[i][:] = (e_i - sum_{k<i} L[i][k] X[k][:]) / L[i][i],
+  // columns in parallel
+  for (int64_t i = 0; i < q; ++i) {
+    const T lii = W[i * q + i];
+    for (int64_t c = threadIdx.x; c < q; c += LT) {
+      T v = T(0);
+      if (c <= i) {
         T s = (i == c) ? T(1) : T(0);
-        for (int64_t k = c; k < i; ++k) s -= W[i * q + k] * Linv[k * q + c];
-        v = s / W[i * q + i];
+        for (int64_t k = c; k < i; ++k) s -= W[i * q + k] * X[k * q + c];
+        v = s / lii;
       }
-      Linv[i * q + c] = v;
+      X[i * q + c] = v;
     }
+    __syncthreads();
   }
+  if (X != Linv)
+    for (int64_t idx = threadIdx.x; idx < q * q; idx += LT) Linv[idx] = X[idx];
   if (Lt != nullptr) {
     for (int64_t idx = threadIdx.x; idx < q * q; idx += LT) {
       const int64_t r = idx / q, c = idx % q;
@@ -433,11 +438,24 @@ void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R) {
   }
   T* cur = Y;
   T* nxt = X2;
-  for (int stage = 0; stage < 3; ++stage) {
+  // FP64: shifted Cholesky-QR3.  FP32: four shifted stages (each divides the
+  // condition number by ~1e2, down from cond(Y) up to ~1e8) and two plain
+  // ones, so the power-iteration bases of the mixed range finder come out
+  // orthonormal without the one-CTA Householder fallback.
+  const int stages = sizeof(T) == 8 ? 3 : 6;
+  const int shifted_stages = sizeof(T) == 8 ? 1 : 4;
+  const size_t wbytes = size_t(q) * q * sizeof(T);
+  const int use_smem = (2 * wbytes <= 200 * 1024) ? 2 : (wbytes <= 200 * 1024 ? 1 : 0);
+  const size_t smem = use_smem == 2 ? 2 * wbytes : (use_smem == 1 ? wbytes : 0);
+  if (!c.sizing() && smem > 0)
+    CTM_CUDA(cudaFuncSetAttribute(cholesky_inverse_kernel<T>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  for (int stage = 0; stage < stages; ++stage) {
     einsum(c, "ia,ib->ab", ViewT<T>(cur, {n, q}), ViewT<T>(cur, {n, q}), ViewT<T>(G, {q, q}));
     if (!c.sizing()) {
-      cholesky_inverse_kernel<T><<<1, LT, 0, c.stream>>>(G, q, n, stage == 0 ? 1 : 0, Wk, Li, Lt,
-                                                      flags);
+      const int mode = stage < shifted_stages ? (sizeof(T) == 8 ? 1 : 2) : 0;
+      cholesky_inverse_kernel<T><<<1, LT, smem, c.stream>>>(G, q, n, mode, Wk, Li, Lt, flags,
+                                                            use_smem);
       CTM_LAUNCH_CHECK();
     }
     // nxt = cur @ Linv^T
@@ -454,7 +472,7 @@ void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R) {
     }
     std::swap(cur, nxt);
   }
-  // cur holds Q after the three stages; check it and fall back when needed
+  // cur holds Q after the stages; check it and fall back when needed
   einsum(c, "ia,ib->ab", ViewT<T>(cur, {n, q}), ViewT<T>(cur, {n, q}), ViewT<T>(G, {q, q}));
   T* hv = c.alloc<T>(size_t(n) * q);
   if (c.sizing()) return;

@@ -50,17 +50,20 @@ def test_mixed_quarter_tensor_matches_fp64(grown_d4):
 
 
 @pytest.mark.parametrize("k", range(4))
-def test_mixed_move_energy_close_to_fp64(grown_d4, k):
-    # one move from the same state with the same test matrices (successive
-    # rSVD moves amplify any difference, see the parity tests)
-    es = {}
-    for prec in ("fp64", "mixed"):
+def test_mixed_move_energy_within_rsvd_noise(grown_d4, k):
+    """One move from the same state with the same test matrices.  The BF16
+    range finder perturbs the rSVD basis; its effect on the energy must stay
+    within the spread that the FP64 algorithm itself shows between two draws
+    of the test matrix (the rSVD's own noise), plus 1e-5 relative."""
+    def energy(prec, seed):
         st = clone(grown_d4)
         mv = gb.DirectionalMover(gb.CTMRGConfig(**CFG, rsvd_oversampling=4, precision=prec),
-                                 omega_source=omega_from(9))
+                                 omega_source=omega_from(seed))
         mv.move(st, k, 0)
-        es[prec] = float(gb.measure(st, gb.HeisenbergModel(1.0), verbose=False)["Energy"])
-    assert abs(es["mixed"] - es["fp64"]) <= 1e-4 * abs(es["fp64"]), es
+        return float(gb.measure(st, gb.HeisenbergModel(1.0), verbose=False)["Energy"])
+    e64, e64b, emx = energy("fp64", 9), energy("fp64", 10), energy("mixed", 9)
+    band = 3.0 * abs(e64 - e64b) + 1e-5 * abs(e64)
+    assert abs(emx - e64) <= band, (emx, e64, e64b)
 
 
 def test_mixed_shapes_match_fp64_shapes(grown_d4):
