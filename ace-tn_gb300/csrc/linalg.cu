@@ -155,46 +155,45 @@ __global__ void __launch_bounds__(LT) cholesky_inverse_kernel(const T* G, int64_
     W[idx] = (c <= r) ? G[idx] + ((r == c) ? s_shift : T(0)) : T(0);
   }
   __syncthreads();
-  // right-looking Cholesky on the lower triangle of W
-  for (int64_t j = 0; j < q; ++j) {
+  // right-looking Cholesky on the lower triangle of W (32-bit indices: q <= 1024)
+  const int qi = static_cast<int>(q);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int j = 0; j < qi; ++j) {
     if (threadIdx.x == 0) {
-      const T d = W[j * q + j];
+      const T d = W[j * qi + j];
       if (!(d > T(0))) s_fail = 1;
-      W[j * q + j] = d > T(0) ? sqrt(d) : T(1);
+      W[j * qi + j] = d > T(0) ? sqrt(d) : T(1);
     }
     __syncthreads();
-    const T ljj = W[j * q + j];
-    for (int64_t i = j + 1 + threadIdx.x; i < q; i += LT) W[i * q + j] /= ljj;
+    const T inv = T(1) / W[j * qi + j];
+    for (int i = j + 1 + threadIdx.x; i < qi; i += LT) W[i * qi + j] *= inv;
     __syncthreads();
-    const int64_t m = q - j - 1;
-    for (int64_t idx = threadIdx.x; idx < m * m; idx += LT) {
-      const int64_t i = j + 1 + idx / m, k = j + 1 + idx % m;
-      if (k <= i) W[i * q + k] -= W[i * q + j] * W[k * q + j];
+    // trailing update: one warp per row i, lanes over k in (j, i]
+    for (int i = j + 1 + warp; i < qi; i += LT / 32) {
+      const T lij = W[i * qi + j];
+      for (int k = j + 1 + lane; k <= i; k += 32) W[i * qi + k] -= lij * W[k * qi + j];
     }
     __syncthreads();
   }
   if (threadIdx.x == 0 && s_fail) atomicOr(flags, 1);
-  // X = L^-1 row by row: X[i][:] = (e_i - sum_{k<i} L[i][k] X[k][:]) / L[i][i],
-  // columns in parallel
-  for (int64_t i = 0; i < q; ++i) {
-    const T lii = W[i * q + i];
-    for (int64_t c = threadIdx.x; c < q; c += LT) {
-      T v = T(0);
-      if (c <= i) {
-        T s = (i == c) ? T(1) : T(0);
-        for (int64_t k = c; k < i; ++k) s -= W[i * q + k] * X[k * q + c];
-        v = s / lii;
-      }
-      X[i * q + c] = v;
+  // X = L^-1 by columns: each thread runs the forward substitution of its
+  // own columns, x_i = (delta_ic - sum_{c<=k<i} L_ik x_k) / L_ii
+  for (int cc = threadIdx.x; cc < qi; cc += LT) {
+    for (int i = 0; i < cc; ++i) X[i * qi + cc] = T(0);
+    for (int i = cc; i < qi; ++i) {
+      T s = (i == cc) ? T(1) : T(0);
+      const T* Lrow = W + i * qi;
+      for (int k = cc; k < i; ++k) s -= Lrow[k] * X[k * qi + cc];
+      X[i * qi + cc] = s / Lrow[i];
     }
-    __syncthreads();
   }
+  __syncthreads();
   if (X != Linv)
-    for (int64_t idx = threadIdx.x; idx < q * q; idx += LT) Linv[idx] = X[idx];
+    for (int idx = threadIdx.x; idx < qi * qi; idx += LT) Linv[idx] = X[idx];
   if (Lt != nullptr) {
-    for (int64_t idx = threadIdx.x; idx < q * q; idx += LT) {
-      const int64_t r = idx / q, c = idx % q;
-      Lt[idx] = (c >= r) ? W[c * q + r] : T(0);
+    for (int idx = threadIdx.x; idx < qi * qi; idx += LT) {
+      const int r = idx / qi, c = idx % qi;
+      Lt[idx] = (c >= r) ? W[c * qi + r] : T(0);
     }
   }
 }

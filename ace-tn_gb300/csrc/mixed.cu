@@ -398,7 +398,11 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
     A4 = quarter_mixed(c, *S[3], k + 3);
   }
   // ---- range finder in BF16 with FP32 orthonormalization:
-  //      Y = Q1 (Q4 Omega), niter x [QR; Y = Q1 Q4 Q4^T Q1^T Y]
+  //      Y = Q1 (Q4 Omega), niter x [QR; Z = Q4^T Q1^T Y; QR; Y = Q1 Q4 Z].
+  //      The reference orthonormalises once per power iteration; the extra
+  //      QR of the half step spans the same space in exact arithmetic and
+  //      keeps the matrices that FP32 has to orthonormalise at the condition
+  //      number of Q1 Q4 instead of its square.
   float* Y = c.alloc<float>(size_t(m) * q);
   KernelTimer* rf_span = new KernelTimer(c.stream, kTagRangeFinder, 0.0);
   {
@@ -415,10 +419,21 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
       orthonormalize(c, Y, m, q, nullptr);
     }
     Scope s2(c);
-    const TcOperand yt = yt_operand_f32(c, Y, m, q, q, false);
-    const TcOperand z1 = gemm_to_operand(c, A1.t(false), yt, x1, false);  // (Q1^T Y)^T
-    const TcOperand z2 = gemm_to_operand(c, A4.t(false), z1, x1, false);  // (Q4^T z1)^T
-    const TcOperand z3 = gemm_to_operand(c, A4.q(false), z2, x1, false);  // (Q4 z2)^T
+    float* Z = c.alloc<float>(size_t(n) * q);
+    {
+      Scope s3(c);
+      const TcOperand yt = yt_operand_f32(c, Y, m, q, q, false);
+      const TcOperand z1 = gemm_to_operand(c, A1.t(false), yt, x1, false);  // (Q1^T Y)^T
+      TcOut out;
+      out.add(TcKind::kF32, Z, TcLayout::rows(n, q, q));
+      tc_gemm(c, A4.t(false), z1, x1, out);                                   // Z = Q4^T Q1^T Y
+    }
+    {
+      KernelTimer span(c.stream, kTagOrtho, 0.0);
+      orthonormalize(c, Z, n, q, nullptr);
+    }
+    const TcOperand zt = yt_operand_f32(c, Z, n, q, q, false);
+    const TcOperand z3 = gemm_to_operand(c, A4.q(false), zt, x1, false);  // (Q4 Z)^T
     TcOut out;
     out.add(TcKind::kF32, Y, TcLayout::rows(m, q, q));
     tc_gemm(c, A1.q(false), z3, x1, out);

@@ -123,15 +123,52 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ int64_t lay_row(const TcLayout& l, int64_t m) {
+  int64_t o = 0;
+  for (int j = l.nm - 1; j >= 0; --j) {
+    o += (m % l.me[j]) * l.ms[j];
+    m /= l.me[j];
+  }
+  return o;
+}
+
+__device__ __forceinline__ int64_t lay_col(const TcLayout& l, int64_t n) {
+  int64_t o = 0;
+  for (int j = l.nn - 1; j >= 0; --j) {
+    o += (n % l.ne[j]) * l.ns[j];
+    n /= l.ne[j];
+  }
+  return o;
+}
+
+__device__ __forceinline__ void store(const TcDest& d, int64_t off, double v) {
+  switch (d.kind) {
+    case TcKind::kF64: static_cast<double*>(d.p)[off] = v; break;
+    case TcKind::kF32: static_cast<float*>(d.p)[off] = float(v); break;
+    case TcKind::kBf16Hi: static_cast<bf16*>(d.p)[off] = __double2bfloat16(v); break;
+    case TcKind::kBf16Lo: {
+      const bf16 h = __double2bfloat16(v);
+      static_cast<bf16*>(d.p)[off] = __double2bfloat16(v - double(__bfloat162float(h)));
+      break;
+    }
+  }
+}
+
 struct GemmParams {
   int ntile;         // MMA N (multiple of 16, <= 256)
   int kb_total;      // 64-wide K blocks
   int kb_per_split;
   int stages;
   int mode;          // 1 or 3
-  float* part;       // [split][m_pad][n_pad]
+  float* part;       // [split][m_pad][n_pad] (unfused epilogue)
   int m_pad, n_pad;
   int* status;
+  // fused epilogue (single K split): the tile goes straight to the destinations
+  int fused;
+  int nd;
+  double alpha;
+  int64_t M, N;
+  TcDest d[4];
 };
 
 __global__ void __launch_bounds__(kThreads, 1)
@@ -236,8 +273,44 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncwarp();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const int row = m0 + warp * 32 + lane;
+  if (p.fused) {
+    // stage the 128 x ntile tile in the (now idle) pipeline buffers, then
+    // store every destination with a warp-contiguous mapping
+    const int ldt = p.ntile + 4;
+    float* tile = reinterpret_cast<float*>(base);
+    int64_t* ro = reinterpret_cast<int64_t*>(tile + size_t(kBM) * ldt);
+    int64_t* co = ro + kBM;
+    if (ok) {
+      for (int c = 0; c < p.ntile; c += 16) {
+        float v[16];
+        tmem_ld16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c), v);
+        float* dst = tile + size_t(warp * 32 + lane) * ldt + c;
+#pragma unroll
+        for (int j = 0; j < 16; j += 4)
+          *reinterpret_cast<float4*>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+      }
+    }
+    __syncthreads();
+    if (ok && !s_fail) {
+      for (int k = 0; k < p.nd; ++k) {
+        const TcDest& d = p.d[k];
+        ro[threadIdx.x] = lay_row(d.lay, m0 + threadIdx.x);
+        for (int c = threadIdx.x; c < p.ntile; c += kThreads) co[c] = lay_col(d.lay, n0 + c);
+        __syncthreads();
+        const bool n_fast = d.lay.ns[d.lay.nn - 1] == 1;
+        const int total = kBM * p.ntile;
+        for (int idx = threadIdx.x; idx < total; idx += kThreads) {
+          const int mi = n_fast ? idx / p.ntile : idx % kBM;
+          const int ni = n_fast ? idx % p.ntile : idx / kBM;
+          if (m0 + mi >= p.M || n0 + ni >= p.N) continue;
+          store(d, ro[mi] + co[ni], p.alpha * double(tile[size_t(mi) * ldt + ni]));
+        }
+        __syncthreads();
+      }
+    }
+  }
   float* out = p.part + (size_t(blockIdx.z) * p.m_pad + row) * p.n_pad + n0;
-  if (ok) {
+  if (ok && !p.fused) {
     for (int c = 0; c < p.ntile; c += 16) {
       float v[16];
       tmem_ld16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c), v);
@@ -276,37 +349,6 @@ struct ReduceParams {
   int nd;
   TcDest d[4];
 };
-
-__device__ __forceinline__ int64_t lay_row(const TcLayout& l, int64_t m) {
-  int64_t o = 0;
-  for (int j = l.nm - 1; j >= 0; --j) {
-    o += (m % l.me[j]) * l.ms[j];
-    m /= l.me[j];
-  }
-  return o;
-}
-
-__device__ __forceinline__ int64_t lay_col(const TcLayout& l, int64_t n) {
-  int64_t o = 0;
-  for (int j = l.nn - 1; j >= 0; --j) {
-    o += (n % l.ne[j]) * l.ns[j];
-    n /= l.ne[j];
-  }
-  return o;
-}
-
-__device__ __forceinline__ void store(const TcDest& d, int64_t off, double v) {
-  switch (d.kind) {
-    case TcKind::kF64: static_cast<double*>(d.p)[off] = v; break;
-    case TcKind::kF32: static_cast<float*>(d.p)[off] = float(v); break;
-    case TcKind::kBf16Hi: static_cast<bf16*>(d.p)[off] = __double2bfloat16(v); break;
-    case TcKind::kBf16Lo: {
-      const bf16 h = __double2bfloat16(v);
-      static_cast<bf16*>(d.p)[off] = __double2bfloat16(v - double(__bfloat162float(h)));
-      break;
-    }
-  }
-}
 
 // 32 x 32 output tile per block (32 x 8 threads).  Every layout is separable
 // (offset = row part + column part), so each block decodes its 32 row and 32
@@ -541,13 +583,16 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   if (absmax != nullptr) splits = 1;  // the scale is taken from complete sums
   const int kb_per_split = (kb_total + splits - 1) / splits;
   splits = (kb_total + kb_per_split - 1) / kb_per_split;
+  const bool fused = splits == 1 && absmax == nullptr;
   const int m_pad = static_cast<int>(m_tiles * kBM);
   const int n_pad = static_cast<int>(n_tiles * ntile);
   const uint32_t stage_bytes = uint32_t(kBM * kBK * 2 + ntile * kBK * 2) * (imode == 3 ? 2 : 1);
   const int stages = std::max(2, std::min(6, int((200 * 1024) / stage_bytes)));
-  const size_t smem = size_t(stages) * stage_bytes + 1024 + 256;
+  const size_t tile_bytes = size_t(kBM) * (ntile + 4) * 4 + size_t(kBM + ntile) * 8;
+  const size_t smem =
+      std::max(size_t(stages) * stage_bytes + 256, fused ? tile_bytes : size_t(0)) + 1024;
   Scope scope(c);
-  float* part = c.alloc<float>(size_t(splits) * m_pad * n_pad);
+  float* part = fused ? nullptr : c.alloc<float>(size_t(splits) * m_pad * n_pad);
   if (c.sizing()) return;
   CTM_REQUIRE(imode == 1 || (A.lo != nullptr && B.lo != nullptr), CTM_ERR_INVALID,
               "tc_gemm: 3xBF16 needs lo parts");
@@ -573,6 +618,12 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   p.m_pad = m_pad;
   p.n_pad = n_pad;
   p.status = status_flags(c);
+  p.fused = fused ? 1 : 0;
+  p.nd = out.nd;
+  p.alpha = out.alpha;
+  p.M = M;
+  p.N = N;
+  for (int i = 0; i < out.nd; ++i) p.d[i] = out.d[i];
   CTM_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(smem)));
   const dim3 grid(static_cast<unsigned>(m_tiles), static_cast<unsigned>(n_tiles),
@@ -582,6 +633,7 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
     tc_gemm_kernel<<<grid, kThreads, smem, c.stream>>>(tA, tAl, tB, tBl, p);
     CTM_LAUNCH_CHECK();
   }
+  if (fused) return;
   if (absmax != nullptr) {
     CTM_CUDA(cudaMemsetAsync(absmax, 0, sizeof(double), c.stream));
     partial_absmax_kernel<<<grid_for(M * N, 256, 152 * 8), 256, 0, c.stream>>>(

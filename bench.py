@@ -239,12 +239,7 @@ def run_gb300(args, rank, world, local_rank):
     clk = clocks.stop()
     ms = [a.elapsed_time(b) for a, b in ev]
     total_s = sum(ms) / 1e3
-    t = torch.tensor([total_s], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dist.barrier()
-    total_max = float(t.item())
-    value = world * args.steps / total_max
+    total_max, value = aggregate(total_s, args.steps, world, dev)
 
     # ---- e2e: host buffers through the public API, copies inside the timed region
     host = {s: {"A": st[s]["A"].cpu().pin_memory(),
@@ -339,6 +334,20 @@ def run_gb300(args, rank, world, local_rank):
                                               f"saturated chi={CHI} state",
                                     "cpu_model": cpu_model()}
     return line
+
+
+def aggregate(total_s, steps, world, device="cpu"):
+    """Whole-job throughput of `world` independent replicas: every rank ran
+    `steps` moves in `total_s` seconds; the job's time is the slowest rank's.
+    Returns (max seconds over ranks, moves/s of the whole job)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([total_s], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    total_max = float(t.item())
+    return total_max, world * steps / total_max
 
 
 _FP64_PEAK = {}
