@@ -35,9 +35,10 @@ void orthonormalize(Ctx& c, float* Y, int64_t n, int64_t q, float* R);
 // X = U diag(S) V^T, U (m x r), S (r) descending, V (n x r), r = min(m, n).
 void svd_thin(Ctx& c, const double* X, int64_t m, int64_t n, double* U, double* S,
               double* V);
-// Thin SVD of B (q x n, q <= min(n, 1024)) from its FP64 Gram matrix: FP32
-// Jacobi eigenvectors, FP64 Rayleigh quotients; singular values accurate to
-// FP64 relative to s_0^2, vectors to FP32.  Used by the mixed path only.
+// Thin SVD of B (q x n, q <= min(n, 1024)): FP32 Jacobi eigenvectors W of
+// the FP64 Gram matrix B B^T precondition FP64 one-sided Jacobi sweeps on
+// B^T W, which give singular values and vectors with FP64 relative accuracy.
+// V is returned in FP32.  Used by the mixed path.
 void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, double* S,
                   float* V);
 // Truncation of acetn/renormalization/projectors.py:163-167 on a descending

@@ -697,95 +697,6 @@ __global__ void f32_to_f64_kernel(const float* x, double* y, int64_t n) {
     y[i] = double(x[i]);
 }
 
-// lambda_j = (W^T G W)_jj from H = G W: lambda_j = sum_i W_ij H_ij; then
-// order by descending lambda, s = sqrt(max(lambda, 0)), Ub columns permuted.
-__global__ void eig_finish_kernel(const double* W, const double* H, int64_t q, double* Ub,
-                                  double* S, double* inv_s, int* order) {
-  __shared__ double lam[1024];
-  for (int64_t j = threadIdx.x; j < q; j += blockDim.x) {
-    double l = 0.0;
-    for (int64_t i = 0; i < q; ++i) l = fma(W[i * q + j], H[i * q + j], l);
-    lam[j] = l;
-  }
-  __syncthreads();
-  for (int64_t j = threadIdx.x; j < q; j += blockDim.x) {
-    int64_t rank = 0;
-    for (int64_t i = 0; i < q; ++i)
-      if (lam[i] > lam[j] || (lam[i] == lam[j] && i < j)) ++rank;
-    order[rank] = static_cast<int>(j);
-    const double s = sqrt(fmax(lam[j], 0.0));
-    S[rank] = s;
-    inv_s[rank] = s > 0.0 ? 1.0 / s : 0.0;
-  }
-  __syncthreads();
-  for (int64_t idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
-    const int64_t i = idx / q, r = idx % q;
-    Ub[i * q + r] = W[i * q + order[r]];
-  }
-}
-
-// One Ogita-Aishima refinement step of an approximate eigenvector matrix X
-// of the symmetric G (Ogita & Aishima, Japan J. Indust. Appl. Math. 35 (2018)
-// 1007): with R = I - X^T X and S = X^T G X, lambda_i = S_ii / (1 - R_ii);
-// E_ij = (S_ij + lambda_j R_ij) / (lambda_j - lambda_i) for separated pairs,
-// R_ij / 2 otherwise; X <- X + X E.  This kernel forms E from R and S.
-__global__ void oa_correction_kernel(const double* R, const double* Sm, int64_t q, double* E) {
-  __shared__ double lam[1024];
-  __shared__ double sh_delta;
-  for (int64_t i = threadIdx.x; i < q; i += blockDim.x) lam[i] = Sm[i * q + i] / (1.0 - R[i * q + i]);
-  __syncthreads();
-  // delta = 2 (||S - diag(lambda)|| + max|lambda| ||R||), Frobenius norms
-  // bounding the spectral norms of the paper
-  __shared__ double red[3][32];
-  double so = 0.0, rm = 0.0, lm = 0.0;
-  for (int64_t idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
-    const int64_t i = idx / q, j = idx % q;
-    const double sij = (i == j) ? Sm[idx] - lam[i] : Sm[idx];
-    so = fma(sij, sij, so);
-    rm = fma(R[idx], R[idx], rm);
-    if (i == j) lm = fmax(lm, fabs(lam[i]));
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    so += __shfl_xor_sync(0xffffffffu, so, o);
-    rm += __shfl_xor_sync(0xffffffffu, rm, o);
-    lm = fmax(lm, __shfl_xor_sync(0xffffffffu, lm, o));
-  }
-  if ((threadIdx.x & 31) == 0) {
-    red[0][threadIdx.x >> 5] = so;
-    red[1][threadIdx.x >> 5] = rm;
-    red[2][threadIdx.x >> 5] = lm;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double a = 0.0, b = 0.0, l = 0.0;
-    for (int w = 0; w < int(blockDim.x >> 5); ++w) {
-      a += red[0][w];
-      b += red[1][w];
-      l = fmax(l, red[2][w]);
-    }
-    sh_delta = 2.0 * (sqrt(a) + l * sqrt(b));
-  }
-  __syncthreads();
-  const double delta = sh_delta;
-  for (int64_t idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
-    const int64_t i = idx / q, j = idx % q;
-    double e;
-    if (i == j) {
-      e = 0.5 * R[idx];
-    } else {
-      const double gap = lam[j] - lam[i];
-      e = (fabs(gap) > delta) ? (Sm[idx] + lam[j] * R[idx]) / gap : 0.5 * R[idx];
-    }
-    E[idx] = e;
-  }
-}
-
-__global__ void identity_minus_kernel(double* R, int64_t q) {
-  for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < q * q;
-       idx += int64_t(gridDim.x) * blockDim.x)
-    R[idx] = ((idx / q == idx % q) ? 1.0 : 0.0) - R[idx];
-}
-
 }  // namespace
 
 void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, double* S,
@@ -797,16 +708,9 @@ void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, dou
   float* Af = c.alloc<float>(size_t(q) * q);
   float* Vf = c.alloc<float>(size_t(q) * q);
   double* W = c.alloc<double>(size_t(q) * q);
-  double* H = c.alloc<double>(size_t(q) * q);
-  double* inv_s = c.alloc<double>(q);
   const int64_t pp = q + (q & 1);
-  int* order = c.alloc<int>(q);
   // G = B B^T in FP64
   einsum(c, "ik,jk->ij", View(B, {q, n}), View(B, {q, n}), View(G, {q, q}));
-  double* Rm = c.alloc<double>(size_t(q) * q);
-  double* Sm = c.alloc<double>(size_t(q) * q);
-  double* Em = c.alloc<double>(size_t(q) * q);
-  double* W2 = c.alloc<double>(size_t(q) * q);
   if (!c.sizing()) {
     f64_to_f32_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(G, Af, q * q);
     CTM_LAUNCH_CHECK();
@@ -821,38 +725,19 @@ void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, dou
     f32_to_f64_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(Vf, W, q * q);
     CTM_LAUNCH_CHECK();
   }
-  // two FP64 refinement steps of the eigenvectors
-  for (int it = 0; it < 2; ++it) {
-    einsum(c, "ki,kj->ij", View(W, {q, q}), View(W, {q, q}), View(Rm, {q, q}));
-    if (!c.sizing()) {
-      identity_minus_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(Rm, q);
-      CTM_LAUNCH_CHECK();
-    }
-    einsum(c, "ik,kj->ij", View(G, {q, q}), View(W, {q, q}), View(H, {q, q}));
-    einsum(c, "ki,kj->ij", View(W, {q, q}), View(H, {q, q}), View(Sm, {q, q}));
-    if (!c.sizing()) {
-      oa_correction_kernel<<<1, 1024, 0, c.stream>>>(Rm, Sm, q, Em);
-      CTM_LAUNCH_CHECK();
-      CTM_CUDA(cudaMemcpyAsync(W2, W, sizeof(double) * q * q, cudaMemcpyDeviceToDevice, c.stream));
-    }
-    einsum(c, "ik,kj->ij", View(W2, {q, q}), View(Em, {q, q}), View(W, {q, q}), 1.0, 1.0);
-  }
-  // Rayleigh quotients in FP64
-  einsum(c, "ik,kj->ij", View(G, {q, q}), View(W, {q, q}), View(H, {q, q}));
-  if (!c.sizing()) {
-    eig_finish_kernel<<<1, 1024, 0, c.stream>>>(W, H, q, Ub, S, inv_s, order);
-    CTM_LAUNCH_CHECK();
-  }
-  // V = B^T Ub diag(1/s), FP32
-  float* bf = c.alloc<float>(size_t(q) * n);
-  float* uf = c.alloc<float>(size_t(q) * q);
-  double* vd = c.alloc<double>(size_t(n) * q);
-  to_f32(c, B, bf, q * n);
-  to_f32(c, Ub, uf, q * q);
-  einsum(c, "ki,kj->ij", ViewF(bf, {q, n}), ViewF(uf, {q, q}), ViewF(V, {n, q}));
-  to_f64(c, V, vd, n * q);
-  scale_columns(c, vd, n, q, q, inv_s);
-  to_f32(c, vd, V, n * q);
+  // W: FP32 eigenvectors of the Gram matrix.  They are accurate for the
+  // large eigenvalues only (FP32 resolves lambda >= ~1e-6 lambda_max), so they
+  // serve as a preconditioner: X = B^T W has nearly orthogonal columns and a
+  // few FP64 one-sided Jacobi sweeps on X (high relative accuracy, no
+  // squaring of the spectrum) give the singular triplets: X J = V_B S,
+  // B = (W J) S V_B^T.
+  double* X = c.alloc<double>(size_t(n) * q);
+  double* Vx = c.alloc<double>(size_t(n) * q);
+  double* J = c.alloc<double>(size_t(q) * q);
+  einsum(c, "ki,kj->ij", View(B, {q, n}), View(W, {q, q}), View(X, {n, q}));
+  svd_thin(c, X, n, q, Vx, S, J);
+  einsum(c, "ik,kj->ij", View(W, {q, q}), View(J, {q, q}), View(Ub, {q, q}));
+  to_f32(c, Vx, V, n * q);
 }
 
 }  // namespace ctm

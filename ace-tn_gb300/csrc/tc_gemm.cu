@@ -583,7 +583,12 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   if (absmax != nullptr) splits = 1;  // the scale is taken from complete sums
   const int kb_per_split = (kb_total + splits - 1) / splits;
   splits = (kb_total + kb_per_split - 1) / kb_per_split;
-  const bool fused = splits == 1 && absmax == nullptr;
+  // The fused epilogue (tile staged in shared memory, stored by the CTA's 128
+  // threads) measured slower than the separate reduce kernel for the permuted
+  // layouts of the contraction chains, whose stores are scattered; it stays
+  // available for row-major single-destination outputs.
+  bool fused = splits == 1 && absmax == nullptr && out.nd == 1 &&
+               out.d[0].lay.nm == 1 && out.d[0].lay.nn == 1 && out.d[0].lay.ns[0] == 1;
   const int m_pad = static_cast<int>(m_tiles * kBM);
   const int n_pad = static_cast<int>(n_tiles * ntile);
   const uint32_t stage_bytes = uint32_t(kBM * kBK * 2 + ntile * kBK * 2) * (imode == 3 ? 2 : 1);
