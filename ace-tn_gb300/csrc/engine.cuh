@@ -35,10 +35,10 @@ void orthonormalize(Ctx& c, float* Y, int64_t n, int64_t q, float* R);
 // X = U diag(S) V^T, U (m x r), S (r) descending, V (n x r), r = min(m, n).
 void svd_thin(Ctx& c, const double* X, int64_t m, int64_t n, double* U, double* S,
               double* V);
-// Thin SVD of B (q x n, q <= min(n, 1024)): FP32 Jacobi eigenvectors W of
-// the FP64 Gram matrix B B^T precondition FP64 one-sided Jacobi sweeps on
-// B^T W, which give singular values and vectors with FP64 relative accuracy.
-// V is returned in FP32.  Used by the mixed path.
+// Thin SVD of B (q x n, q <= min(n, 168)) for the mixed path: Cholesky
+// factor L of the FP64 Gram matrix B B^T, FP32 one-sided Jacobi on L^T
+// (relative accuracy for every singular value above the FP64 Gram's
+// resolution, ~1e-7 s_0), V = B^T U diag(1/s) in FP32.
 void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, double* S,
                   float* V);
 // Truncation of acetn/renormalization/projectors.py:163-167 on a descending

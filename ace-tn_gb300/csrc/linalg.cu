@@ -176,6 +176,14 @@ __global__ void __launch_bounds__(LT) cholesky_inverse_kernel(const T* G, int64_
     __syncthreads();
   }
   if (threadIdx.x == 0 && s_fail) atomicOr(flags, 1);
+  if (Linv == nullptr) {
+    // factor only: L (lower, zeros above the diagonal) into Lt's place
+    for (int idx = threadIdx.x; idx < qi * qi; idx += LT) {
+      const int r = idx / qi, c = idx % qi;
+      Lt[idx] = (c <= r) ? W[idx] : T(0);
+    }
+    return;
+  }
   // X = L^-1 by columns: each thread runs the forward substitution of its
   // own columns, x_i = (delta_ic - sum_{c<=k<i} L_ik x_k) / L_ii
   for (int cc = threadIdx.x; cc < qi; cc += LT) {
@@ -195,6 +203,126 @@ __global__ void __launch_bounds__(LT) cholesky_inverse_kernel(const T* G, int64_
       const int r = idx / qi, c = idx % qi;
       Lt[idx] = (c >= r) ? W[c * qi + r] : T(0);
     }
+  }
+}
+
+// X (n x q) = Y L^-T for a lower-triangular L (q x q): each row solves
+// x L^T = y by forward substitution, one warp per row, L in shared memory.
+// Lanes own the columns k = lane (mod 32) of the row.
+template <class T>
+__global__ void __launch_bounds__(256) trsm_rows_kernel(const T* Y, const T* L, T* X, int64_t n,
+                                                        int q) {
+  extern __shared__ unsigned char trsm_smem[];
+  T* Ls = reinterpret_cast<T*>(trsm_smem);
+  for (int idx = threadIdx.x; idx < q * q; idx += blockDim.x) Ls[idx] = L[idx];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = int64_t(gridDim.x) * (blockDim.x >> 5);
+  constexpr int kMaxPerLane = 32;  // q <= 1024
+  for (int64_t row = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); row < n;
+       row += warps) {
+    T xs[kMaxPerLane];
+    const T* y = Y + row * q;
+    for (int j = 0; j < q; ++j) {
+      // partial sum over this lane's solved columns k < j
+      T part = T(0);
+      for (int t = 0; t * 32 + lane < j; ++t) part += xs[t] * Ls[j * q + t * 32 + lane];
+      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+      const T xj = (y[j] - part) / Ls[j * q + j];
+      if ((j & 31) == lane) xs[j >> 5] = xj;
+    }
+    for (int t = 0; t * 32 + lane < q; ++t) X[row * q + t * 32 + lane] = xs[t];
+  }
+}
+
+// One-sided (Hestenes) Jacobi in FP32 on one CTA, everything in shared
+// memory: the q columns of M (stored as rows of Mc, length q) are
+// orthogonalised by rotations J, accumulated as rows of Jc.  Singular values
+// are the final column norms; with M = L^T, L = J Sigma U^T, so the left
+// singular vectors of L are the columns of J.  8 threads per pair.
+__global__ void __launch_bounds__(1024) jacobi_onesided_f32_kernel(const float* Mc_g, int q, int pp,
+                                                                   float* Jc_g, float* norms,
+                                                                   int max_sweeps, float tol,
+                                                                   int* flags) {
+  extern __shared__ float osm[];
+  float* Mc = osm;
+  float* Jc = osm + q * q;
+  __shared__ int s_rot;
+  for (int idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
+    Mc[idx] = Mc_g[idx];
+    Jc[idx] = (idx / q == idx % q) ? 1.f : 0.f;
+  }
+  const int npairs = pp / 2;
+  const int g = threadIdx.x >> 3, sub = threadIdx.x & 7;  // 128 groups of 8
+  __syncthreads();
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    if (threadIdx.x == 0) s_rot = 0;
+    __syncthreads();
+    for (int r = 0; r < pp - 1; ++r) {
+      for (int k = g; k < npairs; k += 128) {
+        const int i0 = k == 0 ? 0 : ((k - 1 + r) % (pp - 1)) + 1;
+        const int k2 = pp - 1 - k;
+        const int j0 = k2 == 0 ? 0 : ((k2 - 1 + r) % (pp - 1)) + 1;
+        const int i = min(i0, j0), j = max(i0, j0);
+        if (j >= q) continue;
+        float* a = Mc + i * q;
+        float* b = Mc + j * q;
+        float al = 0.f, be = 0.f, ga = 0.f;
+        for (int t = sub; t < q; t += 8) {
+          al = fmaf(a[t], a[t], al);
+          be = fmaf(b[t], b[t], be);
+          ga = fmaf(a[t], b[t], ga);
+        }
+        for (int o = 4; o > 0; o >>= 1) {
+          al += __shfl_xor_sync(0xffffffffu, al, o);
+          be += __shfl_xor_sync(0xffffffffu, be, o);
+          ga += __shfl_xor_sync(0xffffffffu, ga, o);
+        }
+        if (al == 0.f || be == 0.f || !(fabsf(ga) > tol * sqrtf(al) * sqrtf(be))) continue;
+        const float zeta = (be - al) / (2.f * ga);
+        const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+        const float cs = 1.f / sqrtf(1.f + t * t), sn = cs * t;
+        for (int u = sub; u < q; u += 8) {
+          const float x = a[u], y = b[u];
+          a[u] = cs * x - sn * y;
+          b[u] = sn * x + cs * y;
+        }
+        float* ja = Jc + i * q;
+        float* jb = Jc + j * q;
+        for (int u = sub; u < q; u += 8) {
+          const float x = ja[u], y = jb[u];
+          ja[u] = cs * x - sn * y;
+          jb[u] = sn * x + cs * y;
+        }
+        if (sub == 0) s_rot = 1;
+      }
+      __syncthreads();
+    }
+    if (s_rot == 0) break;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && sweep == max_sweeps) atomicOr(flags, 2);
+  for (int j = threadIdx.x; j < q; j += blockDim.x) {
+    float nn = 0.f;
+    for (int t = 0; t < q; ++t) nn = fmaf(Mc[j * q + t], Mc[j * q + t], nn);
+    norms[j] = sqrtf(nn);
+  }
+  for (int idx = threadIdx.x; idx < q * q; idx += blockDim.x) Jc_g[idx] = Jc[idx];
+}
+
+// Ub[:, r] = J[:, order[r]] (J columns stored as rows of Jc), S[r] = norm,
+// inv_s[r] = 1 / S[r] (0 for a zero norm); order by descending norm.
+__global__ void sort_singular_kernel(const float* Jc, const float* norms, int q, double* Ub,
+                                     double* S, double* inv_s) {
+  for (int j = threadIdx.x; j < q; j += blockDim.x) {
+    int rank = 0;
+    const float nj = norms[j];
+    for (int i = 0; i < q; ++i)
+      if (norms[i] > nj || (norms[i] == nj && i < j)) ++rank;
+    S[rank] = double(nj);
+    inv_s[rank] = nj > 0.f ? 1.0 / double(nj) : 0.0;
+    for (int t = 0; t < q; ++t) Ub[t * q + rank] = double(Jc[j * q + t]);
   }
 }
 
@@ -401,6 +529,16 @@ __global__ void restore_if_flagged_kernel(T* Y, const T* saved, int64_t n, const
 
 }  // namespace
 
+int sm_count_linalg() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    return 152;
+  }
+  return n;
+}
+
 int* status_flags(Ctx& c) {
   (void)c;
   int* p = nullptr;
@@ -441,8 +579,8 @@ void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R) {
   // condition number by ~1e2, down from cond(Y) up to ~1e8) and two plain
   // ones, so the power-iteration bases of the mixed range finder come out
   // orthonormal without the one-CTA Householder fallback.
-  const int stages = sizeof(T) == 8 ? 3 : 6;
-  const int shifted_stages = sizeof(T) == 8 ? 1 : 4;
+  const int stages = sizeof(T) == 8 ? 3 : 4;
+  const int shifted_stages = sizeof(T) == 8 ? 1 : 2;
   const size_t wbytes = size_t(q) * q * sizeof(T);
   const int use_smem = (2 * wbytes <= 200 * 1024) ? 2 : (wbytes <= 200 * 1024 ? 1 : 0);
   const size_t smem = use_smem == 2 ? 2 * wbytes : (use_smem == 1 ? wbytes : 0);
@@ -451,15 +589,28 @@ void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R) {
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   for (int stage = 0; stage < stages; ++stage) {
     einsum(c, "ia,ib->ab", ViewT<T>(cur, {n, q}), ViewT<T>(cur, {n, q}), ViewT<T>(G, {q, q}));
-    if (!c.sizing()) {
-      const int mode = stage < shifted_stages ? (sizeof(T) == 8 ? 1 : 2) : 0;
-      cholesky_inverse_kernel<T><<<1, LT, smem, c.stream>>>(G, q, n, mode, Wk, Li, Lt, flags,
-                                                            use_smem);
+    const int mode = stage < shifted_stages ? (sizeof(T) == 8 ? 1 : 2) : 0;
+    if (sizeof(T) == 8) {
+      if (!c.sizing()) {
+        cholesky_inverse_kernel<T><<<1, LT, smem, c.stream>>>(G, q, n, mode, Wk, Li, Lt, flags,
+                                                              use_smem);
+        CTM_LAUNCH_CHECK();
+      }
+      // nxt = cur @ Linv^T
+      einsum(c, "ia,ba->ib", ViewT<T>(cur, {n, q}), ViewT<T>(Li, {q, q}), ViewT<T>(nxt, {n, q}));
+    } else if (!c.sizing()) {
+      // FP32: factor only, then a row-parallel triangular solve nxt = cur L^-T
+      cholesky_inverse_kernel<T><<<1, LT, smem, c.stream>>>(G, q, n, mode, Wk, nullptr, Li,
+                                                            flags, use_smem == 2 ? 1 : use_smem);
+      CTM_LAUNCH_CHECK();
+      const size_t tsm = wbytes;
+      CTM_CUDA(cudaFuncSetAttribute(trsm_rows_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    int(tsm)));
+      const int64_t blocks = std::min<int64_t>((n + 7) / 8, int64_t(sm_count_linalg()) * 4);
+      trsm_rows_kernel<T><<<unsigned(blocks), 256, tsm, c.stream>>>(cur, Li, nxt, n, int(q));
       CTM_LAUNCH_CHECK();
     }
-    // nxt = cur @ Linv^T
-    einsum(c, "ia,ba->ib", ViewT<T>(cur, {n, q}), ViewT<T>(Li, {q, q}), ViewT<T>(nxt, {n, q}));
-    if (R != nullptr) {
+    if (R != nullptr && sizeof(T) == 8) {
       if (stage == 0) {
         if (!c.sizing())
           CTM_CUDA(cudaMemcpyAsync(Rt, Lt, sizeof(T) * q * q, cudaMemcpyDeviceToDevice,
@@ -577,113 +728,12 @@ void scale_columns_compact(Ctx& c, const double* in, int64_t rows, int64_t cap, 
 }  // namespace ctm
 
 // ======================================================================
-// Symmetric eigen-decomposition for the mixed-precision SVD: parallel
-// (round-robin) two-sided Jacobi in FP32 on one CTA, followed by FP64
-// Rayleigh quotients of the FP64 matrix.
+// Mixed-precision SVD of the Rayleigh-Ritz matrix.
 namespace ctm {
 
 namespace {
 
 constexpr int ET = 1024;
-
-// A (q x q, symmetric, FP32) -> eigenvectors in V (q x q, columns); the
-// diagonal of the rotated A holds the eigenvalues.  Parallel cyclic Jacobi:
-// each round rotates q/2 disjoint pairs (round-robin ordering), applying
-// J^T A then A J.  Shared memory holds A, V and the round's rotations when
-// they fit.  A pair is rotated when |a_ij| exceeds max(tol sqrt|a_ii a_jj|,
-// 1e-6 max_k |a_kk|): FP32 cannot resolve smaller couplings, which the FP64
-// refinement that follows removes.
-__global__ void __launch_bounds__(ET) jacobi_eig_f32_kernel(float* Ag, float* Vg, int q, int pp,
-                                                            int max_sweeps, float tol, int use_smem,
-                                                            int* flags) {
-  __shared__ int s_rot;
-  __shared__ float s_amax;
-  __shared__ float cs[2 * 512];
-  __shared__ int pr[2 * 512];
-  extern __shared__ float jsm[];
-  float* A = use_smem ? jsm : Ag;
-  float* V = use_smem ? jsm + q * q : Vg;
-  if (use_smem)
-    for (int idx = threadIdx.x; idx < q * q; idx += ET) A[idx] = Ag[idx];
-  for (int idx = threadIdx.x; idx < q * q; idx += ET) V[idx] = (idx / q == idx % q) ? 1.f : 0.f;
-  const int npairs = pp / 2;
-  // threads per pair in the update phases
-  const int tpp = max(1, min(32, ET / max(npairs, 1)));
-  const int slot = threadIdx.x / tpp, lane = threadIdx.x % tpp;
-  const int slots = ET / tpp;
-  __syncthreads();
-  int sweep = 0;
-  for (; sweep < max_sweeps; ++sweep) {
-    if (threadIdx.x == 0) {
-      float m = 0.f;
-      for (int i = 0; i < q; ++i) m = fmaxf(m, fabsf(A[i * q + i]));
-      s_amax = m;
-      s_rot = 0;
-    }
-    __syncthreads();
-    const float floor_abs = 1e-6f * s_amax;
-    for (int r = 0; r < pp - 1; ++r) {
-      for (int k = threadIdx.x; k < npairs; k += ET) {
-        const int i0 = k == 0 ? 0 : ((k - 1 + r) % (pp - 1)) + 1;
-        const int k2 = pp - 1 - k;
-        const int j0 = k2 == 0 ? 0 : ((k2 - 1 + r) % (pp - 1)) + 1;
-        const int i = min(i0, j0), j = max(i0, j0);
-        float c = 1.f, sn = 0.f;
-        if (j < q) {
-          const float aii = A[i * q + i], ajj = A[j * q + j], aij = A[i * q + j];
-          const float thr = fmaxf(tol * sqrtf(fabsf(aii) * fabsf(ajj)), floor_abs);
-          if (fabsf(aij) > thr && aij != 0.f) {
-            const float tau = (ajj - aii) / (2.f * aij);
-            const float t = copysignf(1.f, tau) / (fabsf(tau) + sqrtf(1.f + tau * tau));
-            c = 1.f / sqrtf(1.f + t * t);
-            sn = t * c;
-            s_rot = 1;
-          }
-        }
-        cs[2 * k] = c;
-        cs[2 * k + 1] = sn;
-        pr[2 * k] = i;
-        pr[2 * k + 1] = j;
-      }
-      __syncthreads();
-      // rows: A <- J^T A
-      for (int k = slot; k < npairs; k += slots) {
-        const float sn = cs[2 * k + 1];
-        const int i = pr[2 * k], j = pr[2 * k + 1];
-        if (sn == 0.f || j >= q) continue;
-        const float c = cs[2 * k];
-        for (int col = lane; col < q; col += tpp) {
-          const float ai = A[i * q + col], aj = A[j * q + col];
-          A[i * q + col] = c * ai - sn * aj;
-          A[j * q + col] = sn * ai + c * aj;
-        }
-      }
-      __syncthreads();
-      // columns: A <- A J, V <- V J
-      for (int k = slot; k < npairs; k += slots) {
-        const float sn = cs[2 * k + 1];
-        const int i = pr[2 * k], j = pr[2 * k + 1];
-        if (sn == 0.f || j >= q) continue;
-        const float c = cs[2 * k];
-        for (int row = lane; row < q; row += tpp) {
-          const float ai = A[row * q + i], aj = A[row * q + j];
-          A[row * q + i] = c * ai - sn * aj;
-          A[row * q + j] = sn * ai + c * aj;
-          const float vi = V[row * q + i], vj = V[row * q + j];
-          V[row * q + i] = c * vi - sn * vj;
-          V[row * q + j] = sn * vi + c * vj;
-        }
-      }
-      __syncthreads();
-    }
-    if (s_rot == 0) break;
-    __syncthreads();
-  }
-  if (threadIdx.x == 0 && sweep == max_sweeps) atomicOr(flags, 2);
-  __syncthreads();
-  if (use_smem)
-    for (int idx = threadIdx.x; idx < q * q; idx += ET) Vg[idx] = V[idx];
-}
 
 __global__ void f64_to_f32_kernel(const double* x, float* y, int64_t n) {
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
@@ -691,53 +741,60 @@ __global__ void f64_to_f32_kernel(const double* x, float* y, int64_t n) {
     y[i] = float(x[i]);
 }
 
-__global__ void f32_to_f64_kernel(const float* x, double* y, int64_t n) {
-  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
-       i += int64_t(gridDim.x) * blockDim.x)
-    y[i] = double(x[i]);
-}
 
 }  // namespace
 
 void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, double* S,
                   float* V) {
-  CTM_REQUIRE(q >= 1 && q <= 1024 && q <= n, CTM_ERR_UNSUPPORTED,
-              "svd_via_gram: needs 1 <= q <= min(n, 1024)");
+  // the one-sided Jacobi keeps two q x q FP32 matrices in shared memory
+  CTM_REQUIRE(q >= 1 && q <= 168 && q <= n, CTM_ERR_UNSUPPORTED,
+              "mixed SVD: needs 1 <= q <= min(n, 168) (chi + oversampling)");
   Scope scope(c);
   double* G = c.alloc<double>(size_t(q) * q);
-  float* Af = c.alloc<float>(size_t(q) * q);
-  float* Vf = c.alloc<float>(size_t(q) * q);
-  double* W = c.alloc<double>(size_t(q) * q);
+  double* Wk = c.alloc<double>(size_t(q) * q);
+  double* L = c.alloc<double>(size_t(q) * q);
+  float* Mc = c.alloc<float>(size_t(q) * q);
+  float* Jc = c.alloc<float>(size_t(q) * q);
+  float* norms = c.alloc<float>(q);
+  double* inv_s = c.alloc<double>(q);
+  int* flags = c.alloc<int>(1);
   const int64_t pp = q + (q & 1);
-  // G = B B^T in FP64
+  // G = B B^T = L L^T in FP64 (B = L Qb^T with orthonormal Qb); the spectrum of
+  // B is that of L, whose singular values FP32 one-sided Jacobi resolves with
+  // relative accuracy (no squaring): L^T J = U Sigma, so B = J Sigma (Qb U)^T.
   einsum(c, "ik,jk->ij", View(B, {q, n}), View(B, {q, n}), View(G, {q, q}));
   if (!c.sizing()) {
-    f64_to_f32_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(G, Af, q * q);
-    CTM_LAUNCH_CHECK();
-    const size_t smem = size_t(2) * q * q * sizeof(float);
-    const int use_smem = smem <= 200 * 1024 ? 1 : 0;
+    CTM_CUDA(cudaMemsetAsync(flags, 0, sizeof(int), c.stream));
+    const size_t wsm = size_t(q) * q * sizeof(double);
+    const int use_smem = wsm <= 200 * 1024 ? 1 : 0;
     if (use_smem)
-      CTM_CUDA(cudaFuncSetAttribute(jacobi_eig_f32_kernel,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    jacobi_eig_f32_kernel<<<1, ET, use_smem ? smem : 0, c.stream>>>(
-        Af, Vf, int(q), int(pp), 30, 1e-6f, use_smem, status_flags(c));
+      CTM_CUDA(cudaFuncSetAttribute(cholesky_inverse_kernel<double>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, int(wsm)));
+    cholesky_inverse_kernel<double><<<1, LT, use_smem ? wsm : 0, c.stream>>>(
+        G, q, n, 0, Wk, nullptr, L, flags, use_smem);
     CTM_LAUNCH_CHECK();
-    f32_to_f64_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(Vf, W, q * q);
+    // Mc rows = columns of L^T = rows of L (FP32)
+    f64_to_f32_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(L, Mc, q * q);
+    CTM_LAUNCH_CHECK();
+    const size_t osm = size_t(2) * q * q * sizeof(float);
+    CTM_CUDA(cudaFuncSetAttribute(jacobi_onesided_f32_kernel,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(osm)));
+    jacobi_onesided_f32_kernel<<<1, 1024, osm, c.stream>>>(Mc, int(q), int(pp), Jc, norms, 40,
+                                                           2e-7f, status_flags(c));
+    CTM_LAUNCH_CHECK();
+    sort_singular_kernel<<<1, 256, 0, c.stream>>>(Jc, norms, int(q), Ub, S, inv_s);
     CTM_LAUNCH_CHECK();
   }
-  // W: FP32 eigenvectors of the Gram matrix.  They are accurate for the
-  // large eigenvalues only (FP32 resolves lambda >= ~1e-6 lambda_max), so they
-  // serve as a preconditioner: X = B^T W has nearly orthogonal columns and a
-  // few FP64 one-sided Jacobi sweeps on X (high relative accuracy, no
-  // squaring of the spectrum) give the singular triplets: X J = V_B S,
-  // B = (W J) S V_B^T.
-  double* X = c.alloc<double>(size_t(n) * q);
-  double* Vx = c.alloc<double>(size_t(n) * q);
-  double* J = c.alloc<double>(size_t(q) * q);
-  einsum(c, "ki,kj->ij", View(B, {q, n}), View(W, {q, q}), View(X, {n, q}));
-  svd_thin(c, X, n, q, Vx, S, J);
-  einsum(c, "ik,kj->ij", View(W, {q, q}), View(J, {q, q}), View(Ub, {q, q}));
-  to_f32(c, Vx, V, n * q);
+  // V = B^T Ub diag(1/s), FP32
+  float* bf = c.alloc<float>(size_t(q) * n);
+  float* uf = c.alloc<float>(size_t(q) * q);
+  double* vd = c.alloc<double>(size_t(n) * q);
+  to_f32(c, B, bf, q * n);
+  to_f32(c, Ub, uf, q * q);
+  einsum(c, "ki,kj->ij", ViewF(bf, {q, n}), ViewF(uf, {q, q}), ViewF(V, {n, q}));
+  to_f64(c, V, vd, n * q);
+  scale_columns(c, vd, n, q, q, inv_s);
+  to_f32(c, vd, V, n * q);
 }
 
 }  // namespace ctm

@@ -459,12 +459,15 @@ void make_map(CUtensorMap* map, const bf16* ptr, int64_t rows, int64_t k, int64_
               "cuTensorMapEncodeTiled failed with code " + std::to_string(int(res)));
 }
 
+// SM count of the current device (152 on GB300), used by both the sizing
+// pass and the launch so that they choose the same split-K; 152 when no
+// device is visible (workspace queries on a machine without a GPU).
 int sm_count() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    CTM_CUDA(cudaGetDevice(&dev));
-    CTM_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    return 152;
   }
   return n;
 }
@@ -574,10 +577,11 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   ntile = std::max(ntile, 16);
   const int64_t m_tiles = (M + kBM - 1) / kBM;
   const int kb_total = static_cast<int>((K + kBK - 1) / kBK);
-  // split K so that the grid covers the SMs at least once
   const int64_t base_ctas = m_tiles * n_tiles;
-  const int sms = c.sizing() ? 152 : sm_count();
-  int splits = static_cast<int>(std::min<int64_t>((sms + base_ctas - 1) / base_ctas,
+  const int sms = sm_count();
+  // split K so that the grid fills the SMs in one wave: a partial second wave
+  // costs as much time as a full one
+  int splits = static_cast<int>(std::min<int64_t>(std::max<int64_t>(1, sms / base_ctas),
                                                   std::max(1, kb_total / 4)));
   splits = std::max(splits, 1);
   if (absmax != nullptr) splits = 1;  // the scale is taken from complete sums
@@ -592,7 +596,7 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   const int m_pad = static_cast<int>(m_tiles * kBM);
   const int n_pad = static_cast<int>(n_tiles * ntile);
   const uint32_t stage_bytes = uint32_t(kBM * kBK * 2 + ntile * kBK * 2) * (imode == 3 ? 2 : 1);
-  const int stages = std::max(2, std::min(6, int((200 * 1024) / stage_bytes)));
+  const int stages = std::max(2, std::min(6, int((220 * 1024) / stage_bytes)));
   const size_t tile_bytes = size_t(kBM) * (ntile + 4) * 4 + size_t(kBM + ntile) * 8;
   const size_t smem =
       std::max(size_t(stages) * stage_bytes + 256, fused ? tile_bytes : size_t(0)) + 1024;
