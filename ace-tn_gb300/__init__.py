@@ -22,6 +22,7 @@ from ._build import build
 from .config import CTMRGConfig
 from .ctmrg import ctmrg, sweep_order
 from .directional_mover import DirectionalMover
+from .graph import CTMRGGraph
 from .linalg import (fused_3matmul_svd_lowrank, fused_matmul_svd_lowrank, matmul, svd,
                      svd_lowrank)
 from .measure import measure
@@ -31,6 +32,6 @@ from .rdm import RDM
 from .state import Bond, IpepsState, random_state
 
 __all__ = ["build", "CTMRGConfig", "ctmrg", "sweep_order", "DirectionalMover",
-           "ProjectorCalculator", "RDM", "measure", "svd_lowrank", "fused_matmul_svd_lowrank",
+           "ProjectorCalculator", "CTMRGGraph", "RDM", "measure", "svd_lowrank", "fused_matmul_svd_lowrank",
            "fused_3matmul_svd_lowrank", "svd", "matmul", "HeisenbergModel", "IsingModel",
            "Bond", "IpepsState", "random_state"]

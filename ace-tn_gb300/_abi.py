@@ -33,7 +33,7 @@ class CtmSite(ctypes.Structure):
 class CtmOpts(ctypes.Structure):
     _fields_ = [("chi", c_i64), ("projectors", c_i32), ("svd_type", c_i32),
                 ("svd_cutoff", ctypes.c_double), ("rsvd_niter", c_i32),
-                ("rsvd_oversampling", c_i32), ("precision", c_i32), ("reserved", c_i32),
+                ("rsvd_oversampling", c_i32), ("precision", c_i32), ("fixed_width", c_i32),
                 ("mixed_floor", ctypes.c_double)]
 
 
@@ -45,6 +45,7 @@ _SIGNATURES = {
     "ctm_last_error": ([], ctypes.c_char_p),
     "ctm_device_status": ([ctypes.POINTER(ctypes.c_int), c_vp], ctypes.c_int),
     "ctm_kernel_launches": ([], ctypes.c_ulonglong),
+    "ctm_qr_fallbacks": ([ctypes.POINTER(ctypes.c_ulonglong), c_vp], ctypes.c_int),
     "ctm_profile_begin": ([], None),
     "ctm_profile_end": ([], ctypes.c_int),
     "ctm_profile_query": ([ctypes.c_int, ctypes.POINTER(ctypes.c_double),
@@ -189,6 +190,12 @@ def profile_end():
     return out
 
 
+def qr_fallbacks(device=None):
+    n = ctypes.c_ulonglong(0)
+    check(load().ctm_qr_fallbacks(ctypes.byref(n), stream_handle(device)), "ctm_qr_fallbacks")
+    return int(n.value)
+
+
 def kernel_launches():
     return int(load().ctm_kernel_launches())
 
@@ -236,7 +243,7 @@ class SiteRef:
         return ctypes.pointer(self.s)
 
 
-def opts_struct(config, chi, precision):
+def opts_struct(config, chi, precision, fixed_width=False):
     o = CtmOpts()
     o.chi = int(chi)
     proj = getattr(config, "projectors", "half-system")
@@ -255,4 +262,5 @@ def opts_struct(config, chi, precision):
         raise ValueError(f"Invalid precision: {precision} provided.")
     o.precision = PREC[precision]
     o.mixed_floor = float(getattr(config, "mixed_svd_floor", 1e-6))
+    o.fixed_width = 1 if fixed_width else 0
     return o

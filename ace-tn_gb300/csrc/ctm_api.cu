@@ -216,8 +216,17 @@ void truncate_and_project(Ctx& c, double* U, double* V, int64_t m, int64_t n, in
   } else {
     einsum(c, "ik,kz->iz", mat(right1.p, right1.rows, right1.cols), Vv, mat(P2f, p2rows, cap));
   }
-  scale_columns_compact(c, P1f, p1rows, cap, nullptr, chi_new, P1);
-  scale_columns_compact(c, P2f, p2rows, cap, nullptr, chi_new, P2);
+  if (o.fixed_width) {
+    if (!c.sizing()) {
+      CTM_CUDA(cudaMemcpyAsync(P1, P1f, sizeof(double) * p1rows * cap, cudaMemcpyDeviceToDevice,
+                               c.stream));
+      CTM_CUDA(cudaMemcpyAsync(P2, P2f, sizeof(double) * p2rows * cap, cudaMemcpyDeviceToDevice,
+                               c.stream));
+    }
+  } else {
+    scale_columns_compact(c, P1f, p1rows, cap, nullptr, chi_new, P1);
+    scale_columns_compact(c, P2f, p2rows, cap, nullptr, chi_new, P2);
+  }
 }
 
 }  // namespace
@@ -571,6 +580,16 @@ const char* ctm_version(void) { return "ctm_gb300 0.1 (sm_103a)"; }
 const char* ctm_last_error(void) { return ctm::g_last_error_cstr(); }
 
 unsigned long long ctm_kernel_launches(void) { return g_launches.load(); }
+
+int ctm_qr_fallbacks(unsigned long long* count, ctm_stream_t stream) {
+  return guarded([&] {
+    CTM_REQUIRE(count != nullptr, CTM_ERR_INVALID, "count is NULL");
+    unsigned long long* d = qr_fallback_counter();
+    CTM_CUDA(cudaMemcpyAsync(count, d, sizeof(*count), cudaMemcpyDeviceToHost, as_stream(stream)));
+    CTM_CUDA(cudaStreamSynchronize(as_stream(stream)));
+    CTM_CUDA(cudaMemsetAsync(d, 0, sizeof(*count), as_stream(stream)));
+  });
+}
 
 int ctm_device_status(int* flags_out, ctm_stream_t stream) {
   return guarded([&] {

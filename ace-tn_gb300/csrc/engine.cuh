@@ -86,5 +86,8 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
 // Device-side failure flags (bit set by kernels: 1 = factorization failed,
 // 2 = iteration limit reached); read and cleared by ctm_device_status().
 int* status_flags(Ctx& c);
+// Device counter of Cholesky-QR results rejected by the orthogonality check
+// (the Householder fallback ran), read by ctm_qr_fallbacks().
+unsigned long long* qr_fallback_counter();
 
 }  // namespace ctm

@@ -485,8 +485,17 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
     const TcOperand vt = yt_operand(c, Vd, n, cap, q, true);  // (V f)^T (cap x n)
     gemm_to_f64(c, A4.q(true), vt, x3, P2f, cap, false);     // Q4 V f (r4 x cap)
   }
-  scale_columns_compact(c, P1f, c1, cap, nullptr, chi_new, P1);
-  scale_columns_compact(c, P2f, r4, cap, nullptr, chi_new, P2);
+  if (o.fixed_width) {
+    if (!c.sizing()) {
+      CTM_CUDA(cudaMemcpyAsync(P1, P1f, sizeof(double) * c1 * cap, cudaMemcpyDeviceToDevice,
+                               c.stream));
+      CTM_CUDA(cudaMemcpyAsync(P2, P2f, sizeof(double) * r4 * cap, cudaMemcpyDeviceToDevice,
+                               c.stream));
+    }
+  } else {
+    scale_columns_compact(c, P1f, c1, cap, nullptr, chi_new, P1);
+    scale_columns_compact(c, P2f, r4, cap, nullptr, chi_new, P2);
+  }
 }
 
 }  // namespace ctm

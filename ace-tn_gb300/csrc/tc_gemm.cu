@@ -271,6 +271,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   bool ok = mbar_wait(tfull, 0);
   if (!ok) atomicOr(&s_fail, 1);
   __syncwarp();
+  // tcgen05.ld is warp-collective: decide per warp, never per lane
+  ok = __all_sync(0xffffffffu, ok);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const int row = m0 + warp * 32 + lane;
   if (p.fused) {

@@ -21,6 +21,10 @@ class DirectionalMover:
         self.projector_calculator = ProjectorCalculator(self.config, omega_source)
         self.calculate_projectors = self.projector_calculator.calculate
         self.precision = self.config.precision
+        # graph mode: no host synchronisation, projectors of fixed width chi_cap;
+        # the truncation counts of the last move stay on the device
+        self.graph_mode = False
+        self.last_counts = None
 
     # ---------------------------------------------------------------- sites
     @staticmethod
@@ -67,8 +71,15 @@ class DirectionalMover:
     def _projectors_all(self, ipeps, site_lists, k):
         device = ipeps[site_lists[0][0]]["A"].device
         slots = torch.zeros(len(site_lists), dtype=torch.int64, device=device)
-        pend = [self.projector_calculator.launch(ipeps, sites, k, slots[n:n + 1])
+        pend = [self.projector_calculator.launch(ipeps, sites, k, slots[n:n + 1],
+                                                 fixed_width=self.graph_mode)
                 for n, sites in enumerate(site_lists)]
+        if self.graph_mode:
+            self.last_counts = slots
+            proj1, proj2 = {}, {}
+            for n, p in enumerate(pend):
+                proj1[n], proj2[n] = p.finish(p.cap)
+            return proj1, proj2
         chis = slots.tolist()  # the move's one device-to-host read
         proj1, proj2 = {}, {}
         for n, (p, c) in enumerate(zip(pend, chis)):

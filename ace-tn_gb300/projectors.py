@@ -82,13 +82,15 @@ class ProjectorCalculator:
     def _site_refs(self, ipeps, sites):
         return [_abi.SiteRef(ipeps[s]) for s in sites]
 
-    def launch(self, ipeps, sites, k, chi_slot, precision=None):
-        """Enqueues one projector pair; its width lands in ``chi_slot``."""
+    def launch(self, ipeps, sites, k, chi_slot, precision=None, fixed_width=False):
+        """Enqueues one projector pair; its width lands in ``chi_slot``.  With
+        ``fixed_width`` the projectors keep chi_cap columns (zero beyond the
+        truncation count) so that shapes do not depend on device data."""
         refs = self._site_refs(ipeps, sites)
         D, d = refs[0].D, refs[0].d
         device = refs[0].device
         chi = ipeps.dims["chi"]
-        opts = _abi.opts_struct(self, chi, precision or self.precision)
+        opts = _abi.opts_struct(self, chi, precision or self.precision, fixed_width)
         arr = (_abi.SITE_P * 4)(*[r.pointer for r in refs])
         p1r, p2r, nr, q, cap = (_abi.c_i64() for _ in range(5))
         _abi.check(_abi.load().ctm_projector_dims(arr, D, k, ctypes.byref(opts), ctypes.byref(p1r),
@@ -114,6 +116,7 @@ class ProjectorCalculator:
         qD4 = (c4, D, D)
         pend = PendingProjectors(p1buf, p2buf, p1r.value, p2r.value, qD1, qD4, chi_slot)
         pend.keep = (refs, om)
+        pend.cap = cap.value
         return pend
 
     def _calculate(self, ipeps, sites, k):

@@ -236,10 +236,35 @@ def run_gb300(args, rank, world, local_rank):
     torch.cuda.synchronize(dev)
     prof = gb._abi.profile_end()
     launches = gb._abi.kernel_launches() - launches0
+    qr_fallbacks = gb._abi.qr_fallbacks(dev)
     clk = clocks.stop()
     ms = [a.elapsed_time(b) for a, b in ev]
     total_s = sum(ms) / 1e3
-    total_max, value = aggregate(total_s, args.steps, world, dev)
+    eager = None
+    if args.graph:
+        # one CTMRG iteration (8 moves) captured as a CUDA graph and replayed;
+        # the rSVD test matrices come from torch's default CUDA generator
+        eager_total, eager_value = aggregate(total_s, args.steps, world, dev)
+        eager = {"value": eager_value, "ms_per_step": 1e3 * eager_total / args.steps}
+        graph = gb.CTMRGGraph(st, cfg).capture(warmup=1)
+        graph.replay(1)
+        replays = max(1, -(-args.steps // len(order)))
+        gev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(replays)]
+        clocks = ClockSampler(local_rank)
+        clocks.start()
+        torch.cuda.synchronize(dev)
+        for i in range(replays):
+            flush.zero_()
+            gev[i][0].record(stream)
+            graph.replay(1)
+            gev[i][1].record(stream)
+        torch.cuda.synchronize(dev)
+        clk = clocks.stop()
+        total_s = sum(a.elapsed_time(b) for a, b in gev) / 1e3
+        graph_truncated = graph.truncated()
+        args.steps_timed = replays * len(order)
+    total_max, value = aggregate(total_s, getattr(args, "steps_timed", args.steps), world, dev)
 
     # ---- e2e: host buffers through the public API, copies inside the timed region
     host = {s: {"A": st[s]["A"].cpu().pin_memory(),
@@ -275,6 +300,10 @@ def run_gb300(args, rank, world, local_rank):
     e2e_s = time.perf_counter() - t0
     e2e_value = world * e2e_steps / e2e_s
 
+    compare = None
+    if rank == 0 and not args.no_compare:
+        compare = compare_paths(gb, st, cfg, dev, args.precision)
+
     gett_ms, gett_flops, gett_n = prof["gett_f64"]
     tc_ms, tc_flops, tc_n = prof["tc_gemm"]
     if tc_ms > gett_ms:
@@ -301,7 +330,8 @@ def run_gb300(args, rank, world, local_rank):
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "moves/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_max / args.steps,
+            "steps": getattr(args, "steps_timed", args.steps), "warmup": args.warmup,
+            "ms_per_step": 1e3 * total_max / getattr(args, "steps_timed", args.steps),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if args.precision == "fp64" else "bf16/3xbf16+f64",
             "data": "synthetic",
@@ -310,14 +340,21 @@ def run_gb300(args, rank, world, local_rank):
                        "svd_type": "rsvd", "precision": args.precision, "seed": SEED,
                        "l2": "256 MiB flush between timed moves; quarter tensors 215 MB each",
                        "parallelism": f"replicas x{world}"},
-            "tflops": move_flops(D, CHI, q) / (total_max / args.steps) / 1e12,
+            "tflops": move_flops(D, CHI, q) / (total_max / getattr(args, "steps_timed", args.steps))
+                      / 1e12,
             "roofline": {"bound": bound, "kernel": dom, "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
                          "traffic": None, "launches": dom_n, "peak_source": peak_src,
                          "share_of_step": dom_ms / (1e3 * total_s) if total_s else None},
             "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
-            "gpu_launches": int(launches),
+            # graph replays run the captured launches of the eager moves
+            "gpu_launches": int(launches) if not args.graph else
+            int(round(launches / args.steps * args.steps_timed)),
+            "execution": ("cuda_graph" if args.graph else "eager"),
+            "qr_fallbacks_in_timed_moves": qr_fallbacks,
+            "eager": eager,
+            "comparison": compare,
             "breakdown_ms_per_step": {k: v[0] / args.steps for k, v in prof.items() if v[2]},
             "clocks": clk,
         }
@@ -334,6 +371,60 @@ def run_gb300(args, rank, world, local_rank):
                                               f"saturated chi={CHI} state",
                                     "cpu_model": cpu_model()}
     return line
+
+
+def clone_state(gb, st):
+    c = gb.IpepsState(st.nx, st.ny, st.dims, st.device)
+    for s in st.site_list:
+        v = st[s]
+        c[s] = {"A": v["A"].clone(), "C": [t.clone() for t in v["C"]],
+                "E": [t.clone() for t in v["E"]]}
+    return c
+
+
+def compare_paths(gb, st, cfg, dev, precision):
+    """From the benchmark's saturated state: moves/s of this library's plain
+    FP64 path (the drop-in), and the energy after one move in each precision
+    with the same rSVD test matrices, next to the FP64 path's own spread
+    between two draws of the test matrices (the rSVD's noise)."""
+    import dataclasses
+    import torch
+    order = gb.sweep_order(2, 2)
+    cfg64 = dataclasses.replace(cfg, precision="fp64")
+
+    def seeded(seed):
+        g = torch.Generator(device=dev)
+        g.manual_seed(seed)
+        return lambda n, q, device: torch.randn(n, q, dtype=torch.float64, device=device,
+                                               generator=g)
+
+    # FP64 path timing: two moves (one warm), CUDA events
+    s64 = clone_state(gb, st)
+    mover = gb.DirectionalMover(cfg64, omega_source=seeded(1))
+    mover.move(s64, *order[0])
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    a.record()
+    for k, idx in order[1:3]:
+        mover.move(s64, k, idx)
+    b.record()
+    torch.cuda.synchronize(dev)
+    fp64_ms = a.elapsed_time(b) / 2
+    del s64
+    # one-move energies
+    model = gb.HeisenbergModel(1.0, device=dev)
+    energies = {}
+    for tag, c, seed in (("fp64", cfg64, 7), ("fp64_other_draw", cfg64, 8),
+                         (precision, cfg, 7)):
+        s1 = clone_state(gb, st)
+        gb.DirectionalMover(c, omega_source=seeded(seed)).move(s1, *order[0])
+        energies[tag] = float(gb.measure(s1, model, verbose=False)["Energy"])
+        del s1
+    e64 = energies["fp64"]
+    return {"fp64_path": {"moves_per_s": 1e3 / fp64_ms, "ms_per_step": fp64_ms},
+            "one_move_energy": energies,
+            "rel_err_vs_fp64": abs(energies[precision] - e64) / abs(e64),
+            "fp64_rsvd_draw_spread": abs(energies["fp64_other_draw"] - e64) / abs(e64)}
 
 
 def aggregate(total_s, steps, world, device="cpu"):
@@ -381,7 +472,11 @@ def main():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
+    ap.add_argument("--graph", action="store_true",
+                    help="time replays of one CUDA-graph-captured CTMRG iteration (8 moves)")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the FP64-path timing and the one-move accuracy check")
     ap.add_argument("--cpu-moves", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

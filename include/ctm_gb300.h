@@ -70,7 +70,10 @@ typedef struct ctm_ctmrg_opts {
   int32_t rsvd_niter;   /* power iterations (2)                         */
   int32_t rsvd_oversampling; /* q = chi + oversampling (2)              */
   int32_t precision;    /* CTM_PREC_FP64 | CTM_PREC_MIXED               */
-  int32_t reserved;
+  int32_t fixed_width;  /* 1: write P1/P2 with exactly chi_cap columns, zero
+                           beyond the truncation count (shape-stable output
+                           for CUDA-graph capture); chi_new still receives
+                           the count.  0: compact chi_new columns        */
   double mixed_floor;   /* CTM_PREC_MIXED only: singular values below
                            mixed_floor * s_0 are dropped as well (they are
                            below the resolution of the 3xBF16 products);
@@ -90,6 +93,12 @@ int ctm_device_status(int* flags, ctm_stream_t stream);
 /* Number of CUDA kernels this library has launched in the process (for
  * launch accounting in benchmarks).  No counterpart in the reference. */
 unsigned long long ctm_kernel_launches(void);
+
+/* Synchronizes `stream`, stores and clears the device counter of Cholesky-QR
+ * factorizations whose orthogonality check failed so that the one-CTA
+ * Householder QR ran instead (a performance diagnostic).  No counterpart in
+ * the reference. */
+int ctm_qr_fallbacks(unsigned long long* count, ctm_stream_t stream);
 
 /* Live kernel timing for benchmarks.  Between ctm_profile_begin() and
  * ctm_profile_end() the main kernels are bracketed by CUDA events on their
