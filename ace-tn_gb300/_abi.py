@@ -132,13 +132,14 @@ def stream_handle(device=None):
 
 
 class _Workspace:
-    """Per-device scratch buffer, grown on demand and reused stream-ordered."""
+    """Scratch buffer per (device, stream), grown on demand and reused
+    stream-ordered; calls on different streams never share one."""
 
     def __init__(self):
         self.buf = {}
 
     def get(self, nbytes, device):
-        key = torch.device(device).index
+        key = (torch.device(device).index, torch.cuda.current_stream(device).cuda_stream)
         b = self.buf.get(key)
         if b is None or b.numel() < nbytes:
             size = max(int(nbytes * 1.25), 1 << 20)

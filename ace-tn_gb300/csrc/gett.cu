@@ -41,6 +41,7 @@ struct GettArgs {
   int splitk;
   int64_t kchunk;
   T* part;
+  int kfa, kfb;  // tile loaders walk K fastest (K is the unit-stride mode of A / B)
 };
 
 __device__ __forceinline__ void decode(const Group& g, int64_t idx, int64_t& o0, int64_t& o1) {
@@ -61,14 +62,17 @@ __device__ __forceinline__ void decode(const Group& g, int64_t idx, int64_t& o0,
 constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
 
 // One 64x64 output tile per CTA, 4x4 outputs per thread, K staged through
-// shared memory 16 at a time.  FP64 FMAs are the bound on this part, so the
-// loaders favour generality (any strides) over vector width.
+// shared memory 16 at a time with a register prefetch of the next step (its
+// global loads are in flight while the current step computes).  Each tile
+// loader walks whichever of its two index groups has unit stride, so warps
+// read contiguous memory for either operand orientation.
 template <class T>
 __global__ void __launch_bounds__(NT) gett_kernel(const GettArgs<T> p) {
   __shared__ int64_t sAm[BM], sCm[BM], sBn[BN], sCn[BN];
-  __shared__ int64_t sAk[BK], sBk[BK];
+  __shared__ int64_t sAk[2][BK], sBk[2][BK];
   __shared__ T As[BK][BM + 1];
   __shared__ T Bs[BK][BN + 1];
+  constexpr int E = (BM * BK) / NT;
 
   const int tid = threadIdx.x;
   const int64_t m0 = static_cast<int64_t>(blockIdx.x) * BM;
@@ -91,6 +95,37 @@ __global__ void __launch_bounds__(NT) gett_kernel(const GettArgs<T> p) {
   }
   const int64_t kb = split * p.kchunk;
   const int64_t ke = min(kb + p.kchunk, p.Kt);
+  const int nsteps = ke > kb ? int((ke - kb + BK - 1) / BK) : 0;
+  auto decode_k = [&](int step, int buf) {
+    if (tid < BK) {
+      const int64_t k = kb + int64_t(step) * BK + tid;
+      if (step < nsteps && k < ke) decode(p.K, k, sAk[buf][tid], sBk[buf][tid]);
+      else { sAk[buf][tid] = -1; sBk[buf][tid] = -1; }
+    }
+  };
+  // element e of this thread: (row, k) of the A tile and (column, k) of the B tile
+  auto a_idx = [&](int e, int& mm, int& kk) {
+    const int lin = tid + e * NT;
+    if (p.kfa) { mm = lin / BK; kk = lin % BK; } else { mm = lin % BM; kk = lin / BM; }
+  };
+  auto b_idx = [&](int e, int& nn, int& kk) {
+    const int lin = tid + e * NT;
+    if (p.kfb) { nn = lin / BK; kk = lin % BK; } else { nn = lin % BN; kk = lin / BN; }
+  };
+  T ra[E], rb[E];
+  auto load = [&](int buf) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      int mm, kk;
+      a_idx(e, mm, kk);
+      const int64_t am = sAm[mm], ak = sAk[buf][kk];
+      ra[e] = (am >= 0 && ak >= 0) ? A[am + ak] : T(0);
+      int nn, kb2;
+      b_idx(e, nn, kb2);
+      const int64_t bn = sBn[nn], bk = sBk[buf][kb2];
+      rb[e] = (bn >= 0 && bk >= 0) ? B[bk + bn] : T(0);
+    }
+  };
 
   T acc[4][4];
 #pragma unroll
@@ -99,24 +134,24 @@ __global__ void __launch_bounds__(NT) gett_kernel(const GettArgs<T> p) {
     for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
 
   const int tx = tid & 15, ty = tid >> 4;
-  for (int64_t k0 = kb; k0 < ke; k0 += BK) {
-    __syncthreads();
-    if (tid < BK) {
-      const int64_t k = k0 + tid;
-      if (k < ke) decode(p.K, k, sAk[tid], sBk[tid]);
-      else { sAk[tid] = -1; sBk[tid] = -1; }
-    }
-    __syncthreads();
+  decode_k(0, 0);
+  __syncthreads();
+  if (nsteps > 0) load(0);
+  decode_k(1, 1);
+  for (int st = 0; st < nsteps; ++st) {
+    __syncthreads();  // the previous step's reads of As/Bs are done
 #pragma unroll
-    for (int e = 0; e < (BM * BK) / NT; ++e) {
-      const int lin = tid + e * NT;
-      const int mm = lin % BM, kk = lin / BM;
-      const int64_t am = sAm[mm], ak = sAk[kk];
-      As[kk][mm] = (am >= 0 && ak >= 0) ? A[am + ak] : T(0);
-      const int64_t bn = sBn[mm], bk = sBk[kk];
-      Bs[kk][mm] = (bn >= 0 && bk >= 0) ? B[bk + bn] : T(0);
+    for (int e = 0; e < E; ++e) {
+      int mm, kk;
+      a_idx(e, mm, kk);
+      As[kk][mm] = ra[e];
+      int nn, kb2;
+      b_idx(e, nn, kb2);
+      Bs[kb2][nn] = rb[e];
     }
     __syncthreads();
+    if (st + 1 < nsteps) load((st + 1) & 1);
+    decode_k(st + 2, st & 1);  // buffer st & 1 was last read by load(st)
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
       T a[4], b[4];
@@ -301,6 +336,11 @@ void einsum_impl(Ctx& c, const char* spec, const ViewT<T>& A, const ViewT<T>& B,
   p.alpha = T(alpha);
   p.beta = T(beta);
   if (p.Mt == 0 || p.Nt == 0) return;
+  // loaders walk K fastest when K, not the row / column group, is unit-stride
+  p.kfa = (p.K.n > 0 && p.K.m[p.K.n - 1].s0 == 1 &&
+           !(p.M.n > 0 && p.M.m[p.M.n - 1].s0 == 1)) ? 1 : 0;
+  p.kfb = (p.K.n > 0 && p.K.m[p.K.n - 1].s1 == 1 &&
+           !(p.N.n > 0 && p.N.m[p.N.n - 1].s0 == 1)) ? 1 : 0;
 
   const int64_t tiles = ((p.Mt + BM - 1) / BM) * ((p.Nt + BN - 1) / BN) * bext;
   int splitk = 1;

@@ -124,135 +124,216 @@ __global__ void __launch_bounds__(LT) householder_qr_kernel(T* Y, int64_t n, int
 }
 
 // ------------------------------------------------------------- Cholesky
-// One CTA.  G (q x q) -> Linv (q x q, lower-triangular inverse of the
-// Cholesky factor of G + shift I) and Lt = L^T (upper).  W is q x q global
-// scratch used when the working matrices do not fit in shared memory.
+// One CTA of kCholThreads threads factorises G + shift I = L L^T (q x q).
+// Right-looking elimination on the upper triangle with the pivot division
+// deferred: step j subtracts (W[j][i] / W[j][j]) * row j from every row
+// i > j, so row j ends as d_j * (row j of L_unit^T) with d_j = W[j][j], and
+// L^T[j][c] = W[j][c] / sqrt(d_j).  Both operands of the update are read
+// along rows (lanes over contiguous columns); rows are padded to q + 1
+// elements so the transposed read of the epilogue is conflict-free as well.
+// When Linv is requested the same row operations run on an identity block
+// E, which ends as L_unit^-1, and L^-1 = diag(d)^-1/2 E.
+// A pivot that is not positive (numerically semidefinite G) contributes a
+// zero column to L and a zero row to L^-1, and sets bit 1 of *flags.
 // shift_mode 0: none; 1: 11 (n q + q (q + 1)) u tr(G) (Fukaya et al.);
 // 2: 1000 u tr(G) (FP32 stages of the mixed path).
+// Outputs (each may be null): Lout = L (lower, row-major), Linv = L^-1
+// (lower), Lt = L^T (upper).  Wg / Eg are q x (q + 1) global scratch used
+// for W / E when they are not kept in shared memory (smem_w / smem_e == 0).
+constexpr int kCholThreads = 1024;
+constexpr size_t kSmemOptin = 227 * 1024;
+
 template <class T>
-__global__ void __launch_bounds__(LT) cholesky_inverse_kernel(const T* G, int64_t q,
-                                                              int64_t n, int shift_mode, T* Wg,
-                                                              T* Linv, T* Lt, int* flags,
-                                                              int use_smem) {
-  __shared__ T sh[LT / 32];
-  __shared__ T s_shift;
-  __shared__ int s_fail;
+__global__ void __launch_bounds__(kCholThreads) cholesky_kernel(
+    const T* G, int q, int64_t n, int shift_mode, T* Wg, T* Eg, T* Lout, T* Linv, T* Lt,
+    int* flags, int smem_w, int smem_e) {
   extern __shared__ unsigned char chol_smem[];
-  T* W = use_smem ? reinterpret_cast<T*>(chol_smem) : Wg;
-  T* X = (use_smem == 2) ? W + q * q : Linv;  // inverse built in shared memory too
+  __shared__ T sh[32];
+  const int ld = q + 1;
+  T* dg = reinterpret_cast<T*>(chol_smem);
+  T* W = smem_w ? dg + q : Wg;
+  T* E = smem_e ? (smem_w ? W + size_t(q) * ld : dg + q) : Eg;
+  const bool want_inv = Linv != nullptr;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nwarps = blockDim.x >> 5;
+  // trace -> shift (every thread ends with the same value)
   T tr = T(0);
-  for (int64_t i = threadIdx.x; i < q; i += LT) tr += G[i * q + i];
-  tr = block_sum(tr, sh);
-  if (threadIdx.x == 0) {
-    const double u = sizeof(T) == 8 ? 1.1102230246251565e-16 : 5.9604644775390625e-08;
-    double factor = 0.0;
-    if (shift_mode == 1) factor = 11.0 * (double(n) * q + double(q) * (q + 1));
-    if (shift_mode == 2) factor = 1000.0;
-    s_shift = T(factor * u * double(tr));
-    s_fail = 0;
+  for (int i = tid; i < q; i += blockDim.x) tr += G[size_t(i) * q + i];
+  tr = warp_sum(tr);
+  if (lane == 0) sh[warp] = tr;
+  __syncthreads();
+  tr = T(0);
+  for (int w = 0; w < nwarps; ++w) tr += sh[w];
+  const double u = sizeof(T) == 8 ? 1.1102230246251565e-16 : 5.9604644775390625e-08;
+  double factor = 0.0;
+  if (shift_mode == 1) factor = 11.0 * (double(n) * q + double(q) * (q + 1));
+  if (shift_mode == 2) factor = 1000.0;
+  const T shift = T(factor * u * double(tr));
+  for (int idx = tid; idx < q * q; idx += blockDim.x) {
+    const int r = idx / q, c = idx - r * q;
+    if (c >= r) W[r * ld + c] = G[idx] + (r == c ? shift : T(0));
+    if (want_inv) E[r * ld + c] = (r == c) ? T(1) : T(0);
   }
   __syncthreads();
-  for (int64_t idx = threadIdx.x; idx < q * q; idx += LT) {
-    const int64_t r = idx / q, c = idx % q;
-    W[idx] = (c <= r) ? G[idx] + ((r == c) ? s_shift : T(0)) : T(0);
+  bool failed = false;
+  for (int j = 0; j < q; ++j) {
+    const T dj = W[j * ld + j];
+    if (dj > T(0)) {
+      const T rinv = T(1) / dj;
+      const T* Wj = W + j * ld;
+      const T* Ej = E + j * ld;
+      for (int i = j + 1 + warp; i < q; i += nwarps) {
+        const T a = Wj[i] * rinv;
+        T* Wi = W + i * ld;
+#pragma unroll 4
+        for (int k = i + lane; k < q; k += 32) Wi[k] -= a * Wj[k];
+        if (want_inv) {
+          T* Ei = E + i * ld;
+#pragma unroll 4
+          for (int c = lane; c <= j; c += 32) Ei[c] -= a * Ej[c];
+        }
+      }
+    } else {
+      failed = true;
+    }
+    __syncthreads();
+  }
+  if (tid == 0 && failed) atomicOr(flags, 1);
+  for (int j = tid; j < q; j += blockDim.x) {
+    const T dj = W[j * ld + j];
+    dg[j] = dj > T(0) ? sqrt(dj) : T(0);
   }
   __syncthreads();
-  // right-looking Cholesky on the lower triangle of W (32-bit indices: q <= 1024)
-  const int qi = static_cast<int>(q);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int j = 0; j < qi; ++j) {
-    if (threadIdx.x == 0) {
-      const T d = W[j * qi + j];
-      if (!(d > T(0))) s_fail = 1;
-      W[j * qi + j] = d > T(0) ? sqrt(d) : T(1);
+  for (int idx = tid; idx < q * q; idx += blockDim.x) {
+    const int r = idx / q, c = idx - r * q;
+    if (Lout != nullptr) {
+      const T dc = dg[c];
+      Lout[idx] = c < r ? (dc > T(0) ? W[c * ld + r] / dc : T(0)) : (c == r ? dc : T(0));
     }
-    __syncthreads();
-    const T inv = T(1) / W[j * qi + j];
-    for (int i = j + 1 + threadIdx.x; i < qi; i += LT) W[i * qi + j] *= inv;
-    __syncthreads();
-    // trailing update: one warp per row i, lanes over k in (j, i]
-    for (int i = j + 1 + warp; i < qi; i += LT / 32) {
-      const T lij = W[i * qi + j];
-      for (int k = j + 1 + lane; k <= i; k += 32) W[i * qi + k] -= lij * W[k * qi + j];
+    if (Lt != nullptr) {
+      const T dr = dg[r];
+      Lt[idx] = c > r ? (dr > T(0) ? W[r * ld + c] / dr : T(0)) : (c == r ? dr : T(0));
     }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0 && s_fail) atomicOr(flags, 1);
-  if (Linv == nullptr) {
-    // factor only: L (lower, zeros above the diagonal) into Lt's place
-    for (int idx = threadIdx.x; idx < qi * qi; idx += LT) {
-      const int r = idx / qi, c = idx % qi;
-      Lt[idx] = (c <= r) ? W[idx] : T(0);
-    }
-    return;
-  }
-  // X = L^-1 by columns: each thread runs the forward substitution of its
-  // own columns, x_i = (delta_ic - sum_{c<=k<i} L_ik x_k) / L_ii
-  for (int cc = threadIdx.x; cc < qi; cc += LT) {
-    for (int i = 0; i < cc; ++i) X[i * qi + cc] = T(0);
-    for (int i = cc; i < qi; ++i) {
-      T s = (i == cc) ? T(1) : T(0);
-      const T* Lrow = W + i * qi;
-      for (int k = cc; k < i; ++k) s -= Lrow[k] * X[k * qi + cc];
-      X[i * qi + cc] = s / Lrow[i];
-    }
-  }
-  __syncthreads();
-  if (X != Linv)
-    for (int idx = threadIdx.x; idx < qi * qi; idx += LT) Linv[idx] = X[idx];
-  if (Lt != nullptr) {
-    for (int idx = threadIdx.x; idx < qi * qi; idx += LT) {
-      const int r = idx / qi, c = idx % qi;
-      Lt[idx] = (c >= r) ? W[c * qi + r] : T(0);
+    if (want_inv) {
+      const T dr = dg[r];
+      Linv[idx] = (c <= r && dr > T(0)) ? E[r * ld + c] / dr : T(0);
     }
   }
 }
 
-// X (n x q) = Y L^-T for a lower-triangular L (q x q): each row solves
-// x L^T = y by forward substitution, one warp per row, L in shared memory.
-// Lanes own the columns k = lane (mod 32) of the row.
+// Launches cholesky_kernel with W (and E when Linv is wanted) in shared
+// memory whenever they fit.  Wg / Eg: q x (q + 1) scratch, used otherwise.
 template <class T>
-__global__ void __launch_bounds__(256) trsm_rows_kernel(const T* Y, const T* L, T* X, int64_t n,
-                                                        int q) {
-  extern __shared__ unsigned char trsm_smem[];
-  T* Ls = reinterpret_cast<T*>(trsm_smem);
-  for (int idx = threadIdx.x; idx < q * q; idx += blockDim.x) Ls[idx] = L[idx];
-  __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const int64_t warps = int64_t(gridDim.x) * (blockDim.x >> 5);
-  constexpr int kMaxPerLane = 32;  // q <= 1024
-  for (int64_t row = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); row < n;
-       row += warps) {
-    T xs[kMaxPerLane];
-    const T* y = Y + row * q;
-    for (int j = 0; j < q; ++j) {
-      // partial sum over this lane's solved columns k < j
-      T part = T(0);
-      for (int t = 0; t * 32 + lane < j; ++t) part += xs[t] * Ls[j * q + t * 32 + lane];
-      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-      const T xj = (y[j] - part) / Ls[j * q + j];
-      if ((j & 31) == lane) xs[j >> 5] = xj;
-    }
-    for (int t = 0; t * 32 + lane < q; ++t) X[row * q + t * 32 + lane] = xs[t];
+void cholesky(cudaStream_t st, const T* G, int64_t q, int64_t n, int shift_mode, T* Wg, T* Eg,
+              T* Lout, T* Linv, T* Lt, int* flags) {
+  const size_t mat = size_t(q) * (q + 1) * sizeof(T);
+  const size_t dgb = size_t(q) * sizeof(T);
+  int smem_w = 0, smem_e = 0;
+  if (dgb + mat <= kSmemOptin) smem_w = 1;
+  if (Linv != nullptr && dgb + 2 * mat <= kSmemOptin) smem_e = 1;
+  const size_t smem = dgb + (smem_w ? mat : 0) + (smem_e ? mat : 0);
+  CTM_CUDA(cudaFuncSetAttribute(cholesky_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(smem)));
+  cholesky_kernel<T><<<1, kCholThreads, smem, st>>>(G, int(q), n, shift_mode, Wg, Eg, Lout,
+                                                     Linv, Lt, flags, smem_w, smem_e);
+  CTM_LAUNCH_CHECK();
+}
+
+// One CTA.  Pivoted Cholesky of a symmetric positive semidefinite G (FP64,
+// q x q): G = sum_j l_j l_j^T, the pivot of step j being the largest diagonal
+// entry of the remaining Schur complement (kept in full, both triangles, in
+// shared memory).  Row j of Lc (FP32, q x q) is l_j in G's own row order;
+// the rows after the numerical rank (no positive pivot left) are zero.
+// With pivoting the columns of L come out graded and close to orthogonal,
+// which is what makes the one-sided Jacobi below converge in a few sweeps.
+// Wg: q x (q + 1) global scratch for the Schur complement when it does not
+// fit in shared memory (null otherwise).
+__global__ void __launch_bounds__(1024) pivoted_cholesky_kernel(const double* G, int q,
+                                                                float* Lc, double* Wg) {
+  extern __shared__ unsigned char pc_smem[];
+  const int ld = q + 1;
+  int* used = reinterpret_cast<int*>(pc_smem);
+  double* W = Wg != nullptr ? Wg
+                            : reinterpret_cast<double*>(pc_smem + ((size_t(q) * 4 + 15) / 16) * 16);
+  __shared__ int s_piv;
+  __shared__ double s_dp;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  for (int idx = tid; idx < q * q; idx += blockDim.x) {
+    const int r = idx / q, c = idx - r * q;
+    W[r * ld + c] = G[idx];
   }
+  for (int i = tid; i < q; i += blockDim.x) used[i] = 0;
+  __syncthreads();
+  int j = 0;
+  for (; j < q; ++j) {
+    if (warp == 0) {
+      double best = -1.0;
+      int bi = -1;
+      for (int i = lane; i < q; i += 32) {
+        const double v = W[i * ld + i];
+        if (!used[i] && v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi >= 0 && (bi < 0 || oi < bi))) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      if (lane == 0) {
+        s_piv = bi;
+        s_dp = best;
+      }
+    }
+    __syncthreads();
+    const int p = s_piv;
+    const double dp = s_dp;
+    if (p < 0 || !(dp > 0.0)) break;  // block-uniform
+    const double* Wp = W + size_t(p) * ld;  // row p = column p (symmetric)
+    const double rs = 1.0 / sqrt(dp);
+    for (int i = tid; i < q; i += blockDim.x)
+      Lc[size_t(j) * q + i] = (used[i] && i != p) ? 0.f : float(Wp[i] * rs);
+    const double rinv = 1.0 / dp;
+    for (int i = warp; i < q; i += nwarps) {
+      if (used[i] || i == p) continue;
+      const double a = Wp[i] * rinv;
+      double* Wi = W + size_t(i) * ld;
+      for (int k = lane; k < q; k += 32)
+        if (!used[k] && k != p) Wi[k] -= a * Wp[k];
+    }
+    __syncthreads();
+    if (tid == 0) used[p] = 1;
+    __syncthreads();
+  }
+  for (size_t idx = size_t(j) * q + tid; idx < size_t(q) * q; idx += blockDim.x) Lc[idx] = 0.f;
 }
 
 // One-sided (Hestenes) Jacobi in FP32 on one CTA, everything in shared
-// memory: the q columns of M (stored as rows of Mc, length q) are
-// orthogonalised by rotations J, accumulated as rows of Jc.  Singular values
-// are the final column norms; with M = L^T, L = J Sigma U^T, so the left
-// singular vectors of L are the columns of J.  8 threads per pair.
+// memory: the q rows of Mc (the columns x_j of X, length q) are made mutually
+// orthogonal by plane rotations, X V = W.  The singular values are the final
+// row norms and the left singular vectors the normalised final rows; the
+// rotations themselves are not accumulated.  8 threads per pair.
+// Rows are ld = jacobi_ld(q) floats apart with ld = 8 (mod 32): the four
+// 8-thread groups of a warp work on consecutive pair indices, whose rows then
+// start in different bank octets.
+__host__ __device__ inline int jacobi_ld(int q) { return q + ((8 - q % 32) + 32) % 32; }
+
+// With in_smem == 0 the rows live in Wc_g itself (leading dimension q).
 __global__ void __launch_bounds__(1024) jacobi_onesided_f32_kernel(const float* Mc_g, int q, int pp,
-                                                                   float* Jc_g, float* norms,
+                                                                   float* Wc_g, float* norms,
                                                                    int max_sweeps, float tol,
-                                                                   int* flags) {
+                                                                   int* flags, int in_smem) {
   extern __shared__ float osm[];
-  float* Mc = osm;
-  float* Jc = osm + q * q;
+  const int ld = in_smem ? jacobi_ld(q) : q;
+  float* Mc = in_smem ? osm : Wc_g;
   __shared__ int s_rot;
   for (int idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
-    Mc[idx] = Mc_g[idx];
-    Jc[idx] = (idx / q == idx % q) ? 1.f : 0.f;
+    const int r = idx / q, c = idx - r * q;
+    Mc[r * ld + c] = Mc_g[idx];
   }
   const int npairs = pp / 2;
   const int g = threadIdx.x >> 3, sub = threadIdx.x & 7;  // 128 groups of 8
@@ -276,8 +357,8 @@ __global__ void __launch_bounds__(1024) jacobi_onesided_f32_kernel(const float* 
           j = max(i0, j0);
         }
         const bool active = j < q;
-        float* a = Mc + i * q;
-        float* b = Mc + (active ? j : i) * q;
+        float* a = Mc + i * ld;
+        float* b = Mc + (active ? j : i) * ld;
         float al = 0.f, be = 0.f, ga = 0.f;
         if (active) {
           for (int t = sub; t < q; t += 8) {
@@ -301,13 +382,6 @@ __global__ void __launch_bounds__(1024) jacobi_onesided_f32_kernel(const float* 
           a[u] = cs * x - sn * y;
           b[u] = sn * x + cs * y;
         }
-        float* ja = Jc + i * q;
-        float* jb = Jc + j * q;
-        for (int u = sub; u < q; u += 8) {
-          const float x = ja[u], y = jb[u];
-          ja[u] = cs * x - sn * y;
-          jb[u] = sn * x + cs * y;
-        }
         if (sub == 0) s_rot = 1;
       }
       __syncthreads();
@@ -318,15 +392,21 @@ __global__ void __launch_bounds__(1024) jacobi_onesided_f32_kernel(const float* 
   if (threadIdx.x == 0 && sweep == max_sweeps) atomicOr(flags, 2);
   for (int j = threadIdx.x; j < q; j += blockDim.x) {
     float nn = 0.f;
-    for (int t = 0; t < q; ++t) nn = fmaf(Mc[j * q + t], Mc[j * q + t], nn);
+    for (int t = 0; t < q; ++t) nn = fmaf(Mc[j * ld + t], Mc[j * ld + t], nn);
     norms[j] = sqrtf(nn);
   }
-  for (int idx = threadIdx.x; idx < q * q; idx += blockDim.x) Jc_g[idx] = Jc[idx];
+  if (in_smem) {
+    for (int idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
+      const int r = idx / q, c = idx - r * q;
+      Wc_g[idx] = Mc[r * ld + c];
+    }
+  }
 }
 
-// Ub[:, r] = J[:, order[r]] (J columns stored as rows of Jc), S[r] = norm,
-// inv_s[r] = 1 / S[r] (0 for a zero norm); order by descending norm.
-__global__ void sort_singular_kernel(const float* Jc, const float* norms, int q, double* Ub,
+// Ub[:, r] = w_j / |w_j| for the final Jacobi rows w_j ordered by descending
+// norm, S[r] = |w_j|, inv_s[r] = 1 / S[r] (0 for a zero norm, whose column
+// of Ub is left zero).
+__global__ void sort_singular_kernel(const float* Wc, const float* norms, int q, double* Ub,
                                      double* S, double* inv_s) {
   for (int j = threadIdx.x; j < q; j += blockDim.x) {
     int rank = 0;
@@ -334,8 +414,9 @@ __global__ void sort_singular_kernel(const float* Jc, const float* norms, int q,
     for (int i = 0; i < q; ++i)
       if (norms[i] > nj || (norms[i] == nj && i < j)) ++rank;
     S[rank] = double(nj);
-    inv_s[rank] = nj > 0.f ? 1.0 / double(nj) : 0.0;
-    for (int t = 0; t < q; ++t) Ub[t * q + rank] = double(Jc[j * q + t]);
+    const double inv = nj > 0.f ? 1.0 / double(nj) : 0.0;
+    inv_s[rank] = inv;
+    for (int t = 0; t < q; ++t) Ub[t * q + rank] = double(Wc[j * q + t]) * inv;
   }
 }
 
@@ -581,7 +662,8 @@ void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R) {
   // shifted Cholesky-QR3 with a Householder re-run when the check fails
   T* X2 = c.alloc<T>(size_t(n) * q);
   T* G = c.alloc<T>(size_t(q) * q);
-  T* Wk = c.alloc<T>(size_t(q) * q);
+  T* Wk = c.alloc<T>(size_t(q) * (q + 1));
+  T* Ek = c.alloc<T>(size_t(q) * (q + 1));
   T* Li = c.alloc<T>(size_t(q) * q);
   T* Lt = c.alloc<T>(size_t(q) * q);
   T* Rt = c.alloc<T>(size_t(q) * q);
@@ -594,41 +676,20 @@ void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R) {
   }
   T* cur = Y;
   T* nxt = X2;
-  // FP64: shifted Cholesky-QR3.  FP32: four shifted stages (each divides the
+  // FP64: shifted Cholesky-QR3.  FP32: two shifted stages (each divides the
   // condition number by ~1e2, down from cond(Y) up to ~1e8) and two plain
   // ones, so the power-iteration bases of the mixed range finder come out
   // orthonormal without the one-CTA Householder fallback.
   const int stages = sizeof(T) == 8 ? 3 : 4;
   const int shifted_stages = sizeof(T) == 8 ? 1 : 2;
-  const size_t wbytes = size_t(q) * q * sizeof(T);
-  const int use_smem = (2 * wbytes <= 200 * 1024) ? 2 : (wbytes <= 200 * 1024 ? 1 : 0);
-  const size_t smem = use_smem == 2 ? 2 * wbytes : (use_smem == 1 ? wbytes : 0);
-  if (!c.sizing() && smem > 0)
-    CTM_CUDA(cudaFuncSetAttribute(cholesky_inverse_kernel<T>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   for (int stage = 0; stage < stages; ++stage) {
     einsum(c, "ia,ib->ab", ViewT<T>(cur, {n, q}), ViewT<T>(cur, {n, q}), ViewT<T>(G, {q, q}));
     const int mode = stage < shifted_stages ? (sizeof(T) == 8 ? 1 : 2) : 0;
-    if (sizeof(T) == 8) {
-      if (!c.sizing()) {
-        cholesky_inverse_kernel<T><<<1, LT, smem, c.stream>>>(G, q, n, mode, Wk, Li, Lt, flags,
-                                                              use_smem);
-        CTM_LAUNCH_CHECK();
-      }
-      // nxt = cur @ Linv^T
-      einsum(c, "ia,ba->ib", ViewT<T>(cur, {n, q}), ViewT<T>(Li, {q, q}), ViewT<T>(nxt, {n, q}));
-    } else if (!c.sizing()) {
-      // FP32: factor only, then a row-parallel triangular solve nxt = cur L^-T
-      cholesky_inverse_kernel<T><<<1, LT, smem, c.stream>>>(G, q, n, mode, Wk, nullptr, Li,
-                                                            flags, use_smem == 2 ? 1 : use_smem);
-      CTM_LAUNCH_CHECK();
-      const size_t tsm = wbytes;
-      CTM_CUDA(cudaFuncSetAttribute(trsm_rows_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    int(tsm)));
-      const int64_t blocks = std::min<int64_t>((n + 7) / 8, int64_t(sm_count_linalg()) * 4);
-      trsm_rows_kernel<T><<<unsigned(blocks), 256, tsm, c.stream>>>(cur, Li, nxt, n, int(q));
-      CTM_LAUNCH_CHECK();
-    }
+    if (!c.sizing())
+      cholesky<T>(c.stream, G, q, n, mode, Wk, Ek, nullptr, Li, R != nullptr ? Lt : nullptr,
+                  flags);
+    // nxt = cur @ Linv^T
+    einsum(c, "ia,ba->ib", ViewT<T>(cur, {n, q}), ViewT<T>(Li, {q, q}), ViewT<T>(nxt, {n, q}));
     if (R != nullptr && sizeof(T) == 8) {
       if (stage == 0) {
         if (!c.sizing())
@@ -750,59 +811,46 @@ void scale_columns_compact(Ctx& c, const double* in, int64_t rows, int64_t cap, 
 // Mixed-precision SVD of the Rayleigh-Ritz matrix.
 namespace ctm {
 
-namespace {
-
-
-__global__ void f64_to_f32_kernel(const double* x, float* y, int64_t n) {
-  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
-       i += int64_t(gridDim.x) * blockDim.x)
-    y[i] = float(x[i]);
-}
-
-
-}  // namespace
-
 void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, double* S,
                   float* V) {
-  // the one-sided Jacobi keeps two q x q FP32 matrices in shared memory
-  CTM_REQUIRE(q >= 1 && q <= 168 && q <= n, CTM_ERR_UNSUPPORTED,
-              "mixed SVD: needs 1 <= q <= min(n, 168) (chi + oversampling)");
+  CTM_REQUIRE(q >= 1 && q <= 1024 && q <= n, CTM_ERR_UNSUPPORTED,
+              "mixed SVD: needs 1 <= q <= min(n, 1024) (chi + oversampling)");
   Scope scope(c);
   double* G = c.alloc<double>(size_t(q) * q);
-  double* Wk = c.alloc<double>(size_t(q) * q);
-  double* L = c.alloc<double>(size_t(q) * q);
-  float* Mc = c.alloc<float>(size_t(q) * q);
-  float* Jc = c.alloc<float>(size_t(q) * q);
+  // working matrices in shared memory up to q = 168, in global memory (L2)
+  // beyond
+  const size_t used_b = (size_t(q) * 4 + 15) / 16 * 16;
+  const size_t wchol = size_t(q) * (q + 1) * sizeof(double);
+  const bool chol_smem = used_b + wchol <= 227 * 1024;
+  double* Wg = chol_smem ? nullptr : c.alloc<double>(size_t(q) * (q + 1));
+  const size_t wjac = size_t(q) * jacobi_ld(int(q)) * sizeof(float);
+  const bool jac_smem = wjac <= 227 * 1024;
+  float* Lc = c.alloc<float>(size_t(q) * q);
+  float* Wc = c.alloc<float>(size_t(q) * q);
   float* norms = c.alloc<float>(q);
   double* inv_s = c.alloc<double>(q);
-  int* flags = c.alloc<int>(1);
   const int64_t pp = q + (q & 1);
-  // G = B B^T = L L^T in FP64 (B = L Qb^T with orthonormal Qb); the spectrum of
-  // B is that of L, whose singular values FP32 one-sided Jacobi resolves with
-  // relative accuracy (no squaring): L^T J = U Sigma, so B = J Sigma (Qb U)^T.
+  // G = B B^T = L L^T in FP64 (pivoted Cholesky, B = L Qb^T with orthonormal
+  // Qb); the spectrum of B is that of L, whose singular values FP32 one-sided
+  // Jacobi on the columns of L resolves with relative accuracy (no squaring):
+  // L V = W = U Sigma, so B = U Sigma (Qb V)^T and Ub = U.
   einsum(c, "ik,jk->ij", View(B, {q, n}), View(B, {q, n}), View(G, {q, q}));
   if (!c.sizing()) {
-    CTM_CUDA(cudaMemsetAsync(flags, 0, sizeof(int), c.stream));
-    const size_t wsm = size_t(q) * q * sizeof(double);
-    const int use_smem = wsm <= 200 * 1024 ? 1 : 0;
-    if (use_smem)
-      CTM_CUDA(cudaFuncSetAttribute(cholesky_inverse_kernel<double>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, int(wsm)));
-    cholesky_inverse_kernel<double><<<1, LT, use_smem ? wsm : 0, c.stream>>>(
-        G, q, n, 0, Wk, nullptr, L, flags, use_smem);
+    const size_t csm = used_b + (chol_smem ? wchol : 0);
+    CTM_CUDA(cudaFuncSetAttribute(pivoted_cholesky_kernel,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(csm)));
+    pivoted_cholesky_kernel<<<1, 1024, csm, c.stream>>>(G, int(q), Lc, Wg);
     CTM_LAUNCH_CHECK();
-    // Mc rows = columns of L^T = rows of L (FP32)
-    f64_to_f32_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(L, Mc, q * q);
-    CTM_LAUNCH_CHECK();
-    const size_t osm = size_t(2) * q * q * sizeof(float);
+    const size_t osm = jac_smem ? wjac : 0;
     CTM_CUDA(cudaFuncSetAttribute(jacobi_onesided_f32_kernel,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, int(osm)));
     // FP32 dot products of length q carry ~sqrt(q) u relative error: 4e-6
     // is the smallest coupling the sweeps can drive below
-    jacobi_onesided_f32_kernel<<<1, 1024, osm, c.stream>>>(Mc, int(q), int(pp), Jc, norms, 40,
-                                                           4e-6f, status_flags(c));
+    jacobi_onesided_f32_kernel<<<1, 1024, osm, c.stream>>>(Lc, int(q), int(pp), Wc, norms, 40,
+                                                           4e-6f, status_flags(c),
+                                                           jac_smem ? 1 : 0);
     CTM_LAUNCH_CHECK();
-    sort_singular_kernel<<<1, 256, 0, c.stream>>>(Jc, norms, int(q), Ub, S, inv_s);
+    sort_singular_kernel<<<1, 256, 0, c.stream>>>(Wc, norms, int(q), Ub, S, inv_s);
     CTM_LAUNCH_CHECK();
   }
   // V = B^T Ub diag(1/s), FP32

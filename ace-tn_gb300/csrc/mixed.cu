@@ -18,8 +18,12 @@ namespace {
 
 // BF16 operands of one quarter matrix Q (rows x cols): Q itself (K = cols)
 // and its transpose (K = rows), hi and lo parts.
+// The stored values are Q * max|Q| relative to the normalised quarter tensor
+// of the reference: *scale (device) holds max|Q|, and every product that
+// leaves the range finder divides by it.
 struct QOps {
   bf16 *q_hi = nullptr, *q_lo = nullptr, *t_hi = nullptr, *t_lo = nullptr;
+  double* scale = nullptr;
   int64_t rows = 0, cols = 0, ld = 0, ldt = 0;
   TcOperand q(bool lo) const { return TcOperand{q_hi, lo ? q_lo : nullptr, rows, cols, ld}; }
   TcOperand t(bool lo) const { return TcOperand{t_hi, lo ? t_lo : nullptr, cols, rows, ldt}; }
@@ -35,21 +39,68 @@ QOps alloc_ops(Ctx& c, int64_t rows, int64_t cols) {
   o.q_lo = c.alloc<bf16>(size_t(rows) * o.ld);
   o.t_hi = c.alloc<bf16>(size_t(cols) * o.ldt);
   o.t_lo = c.alloc<bf16>(size_t(cols) * o.ldt);
+  o.scale = c.alloc<double>(1);
   return o;
 }
 
-int64_t round8(int64_t x) { return (x + 7) / 8 * 8; }
+// Double-layer site matrix of A = S.A(k) (dims l, u, r, d, p):
+//   DL[(r,R,d,D)][(l,L,u,U)] = sum_p A[l][u][r][d][p] A*[L][U][R][D][p]
+// as a K-major BF16 hi/lo operand (K = (l,L,u,U)), leading dimension ld.
+// Contracting a ket-bra pair of environment legs against it replaces the two
+// one-layer contractions of make_quarter_tensor / renormalize_ej, whose
+// K = D^2 and D^2 d are too short to keep the tensor cores busy.
+__global__ void double_layer_kernel(const double* A, int64_t s0, int64_t s1, int64_t s2,
+                                    int64_t s3, int64_t s4, int D, int d, bf16* hi, bf16* lo,
+                                    int64_t ld) {
+  const int64_t D4 = int64_t(D) * D * D * D;
+  for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < D4 * D4;
+       idx += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t n = idx / D4, k = idx - n * D4;
+    const int DD = int(n % D), dd = int((n / D) % D), R = int((n / (D * D)) % D),
+              r = int(n / (D * D * D));
+    const int U = int(k % D), u = int((k / D) % D), L = int((k / (D * D)) % D),
+              l = int(k / (D * D * D));
+    const double* ket = A + l * s0 + u * s1 + r * s2 + dd * s3;
+    const double* bra = A + L * s0 + U * s1 + R * s2 + DD * s3;
+    double v = 0.0;
+    for (int p = 0; p < d; ++p) v = fma(ket[p * s4], bra[p * s4], v);
+    const bf16 h = __double2bfloat16(v);
+    hi[n * ld + k] = h;
+    lo[n * ld + k] = __double2bfloat16(v - double(__bfloat162float(h)));
+  }
+}
+
+struct DLOp {
+  bf16 *hi = nullptr, *lo = nullptr;
+  int64_t n = 0, ld = 0;
+  TcOperand op() const { return TcOperand{hi, lo, n, n, ld}; }
+};
+
+DLOp double_layer(Ctx& c, const View& ak, int64_t D, int64_t d) {
+  DLOp o;
+  o.n = D * D * D * D;
+  o.ld = tc_ld(o.n);
+  o.hi = c.alloc<bf16>(size_t(o.n) * o.ld);
+  o.lo = c.alloc<bf16>(size_t(o.n) * o.ld);
+  if (!c.sizing()) {
+    double_layer_kernel<<<grid_for(o.n * o.n, 256), 256, 0, c.stream>>>(
+        ak.p, ak.stride[0], ak.stride[1], ak.stride[2], ak.stride[3], ak.stride[4], int(D),
+        int(d), o.hi, o.lo, o.ld);
+    CTM_LAUNCH_CHECK();
+  }
+  return o;
+}
 
 // make_quarter_tensor (acetn/renormalization/projectors.py:35-60) on tensor
 // cores, 3xBF16 throughout.  The four einsums become
-//   t1 = C E_k (FP64, the small chi^3 D^2 step),
-//   t2[(c,u,U)][(e,l,L)] = sum_a t1[a][(c,u,U)] E_{k+3}[e][a][l][L],
-//   t3[(c,u,e,l)][(R,D,P)] = sum_(U,L) t2 A*[L][U][R][D][P],
-//   Q[(c,R,e,D)][(r,d)] = sum_(l,u,p) t3 A[l][u][r][d][p],
-// each GEMM's epilogue storing its result directly in the K-major layout of
-// the next GEMM's operand (the permutes of the reference's einsums folded
-// into the store addresses), and the last one writing Q / max|Q| and its
-// transpose as BF16 hi/lo operands.
+//   t1 = C E_k (FP32, the small chi^3 D^2 step),
+//   X[(c,e)][(l,L,u,U)] = sum_a t1[a][(c,u,U)] E_{k+3}[e][a][l][L]      (K = chi),
+//   Q[(c,r,R)][(e,d,D)] = sum_(l,L,u,U) DL[(r,R,d,D)][(l,L,u,U)] X    (K = D^4),
+// with the double-layer matrix DL of the site tensor (the two A / A* steps
+// of the reference in one GEMM with a long K).  Each epilogue stores into the
+// layout the next step reads, with the GEMM rows (one per epilogue lane) on
+// the index that is contiguous in that layout; Q^T comes from a tiled
+// transpose, and max|Q| from the last epilogue.
 QOps quarter_mixed(Ctx& c, const Site& S, int k) {
   int64_t sh[6], rows, cols;
   quarter_dims(S, k, rows, cols, sh);
@@ -58,7 +109,6 @@ QOps quarter_mixed(Ctx& c, const Site& S, int k) {
   const int64_t a = ck.shape[0], cc = sh[0], E = sh[3], D = S.D, d = S.d, D2 = D * D;
   const TcMode x3 = TcMode::kBf16x3;
   Scope scope(c);
-  double* absmax = c.alloc<double>(1);
   // t1 = C E_k (a x (c,u,U)), FP32
   float* t1 = c.alloc<float>(size_t(a) * cc * D2);
   {
@@ -70,13 +120,10 @@ QOps quarter_mixed(Ctx& c, const Site& S, int k) {
     einsum(c, "ab,bcuU->acuU", ViewF(cf, {ck.shape[0], ck.shape[1]}),
            ViewF(ef, {ek2.shape[0], ek2.shape[1], D, D}), ViewF(t1, {a, cc, D, D}));
   }
-  // t2 operands: A2 = t1^T ((c,u,U) x a), B2 = E_{k+3} as ((e,l,L) x a)
+  // GEMM 1 operands: E_{k+3} as ((e,l,L) x a) and t1^T as ((c,u,U) x a)
   const int64_t ld2 = tc_ld(a);
-  bf16* a2h = c.alloc<bf16>(size_t(cc) * D2 * ld2);
-  bf16* a2l = c.alloc<bf16>(size_t(cc) * D2 * ld2);
-  split_bf16(c, t1, a, cc * D2, cc * D2, true, a2h, a2l, ld2);
-  bf16* b2h = c.alloc<bf16>(size_t(E) * D2 * ld2);
-  bf16* b2l = c.alloc<bf16>(size_t(E) * D2 * ld2);
+  bf16* eh = c.alloc<bf16>(size_t(E) * D2 * ld2);
+  bf16* el = c.alloc<bf16>(size_t(E) * D2 * ld2);
   {
     Gather g;
     g.nr = 2;
@@ -84,99 +131,48 @@ QOps quarter_mixed(Ctx& c, const Site& S, int k) {
     g.re[1] = D2; g.rs[1] = 1;
     g.nk = 1;
     g.ke[0] = a; g.ks[0] = ek1.stride[1];
-    gather_split_bf16(c, ek1.p, g, b2h, b2l, ld2);
+    gather_split_bf16(c, ek1.p, g, eh, el, ld2);
   }
-  // t2 -> T2p[(c,u,e,l)][(U,L)], ld3
-  const int64_t ld3 = round8(D2);
-  const int64_t rows3 = cc * D * E * D;
-  bf16* t2h = c.alloc<bf16>(size_t(rows3) * ld3);
-  bf16* t2l = c.alloc<bf16>(size_t(rows3) * ld3);
+  bf16* th = c.alloc<bf16>(size_t(cc) * D2 * ld2);
+  bf16* tl = c.alloc<bf16>(size_t(cc) * D2 * ld2);
+  split_bf16(c, t1, a, cc * D2, cc * D2, true, th, tl, ld2);
+  // X[(c,e)][(l,L,u,U)]: rows of GEMM 1 are (c,u,U), columns (e,l,L); the
+  // epilogue's lanes (rows) then store contiguous (u,U) runs
+  const int64_t K2 = D2 * D2, ldx = tc_ld(K2);
+  bf16* xh = c.alloc<bf16>(size_t(cc) * E * ldx);
+  bf16* xl = c.alloc<bf16>(size_t(cc) * E * ldx);
   {
     TcLayout l;
     l.nm = 3;
-    l.me[0] = cc; l.ms[0] = D * E * D * ld3;
-    l.me[1] = D;  l.ms[1] = E * D * ld3;
-    l.me[2] = D;  l.ms[2] = D;
+    l.me[0] = cc; l.ms[0] = E * ldx;
+    l.me[1] = D;  l.ms[1] = D;
+    l.me[2] = D;  l.ms[2] = 1;
     l.nn = 3;
-    l.ne[0] = E; l.ns[0] = D * ld3;
-    l.ne[1] = D; l.ns[1] = ld3;
-    l.ne[2] = D; l.ns[2] = 1;
+    l.ne[0] = E; l.ns[0] = ldx;
+    l.ne[1] = D; l.ns[1] = D * D2;
+    l.ne[2] = D; l.ns[2] = D2;
     TcOut out;
-    out.add(TcKind::kBf16Hi, t2h, l).add(TcKind::kBf16Lo, t2l, l);
-    tc_gemm(c, TcOperand{a2h, a2l, cc * D2, a, ld2}, TcOperand{b2h, b2l, E * D2, a, ld2}, x3, out);
+    out.add(TcKind::kBf16Hi, xh, l).add(TcKind::kBf16Lo, xl, l);
+    tc_gemm(c, TcOperand{th, tl, cc * D2, a, ld2}, TcOperand{eh, el, E * D2, a, ld2}, x3, out);
   }
-  // t3: B3[(R,D,P)][(U,L)] = A*[L][U][R][D][P]
-  bf16* b3h = c.alloc<bf16>(size_t(D2) * d * ld3);
-  bf16* b3l = c.alloc<bf16>(size_t(D2) * d * ld3);
+  // GEMM 2 against the double-layer matrix -> Q[(c,r,R)][(e,d,D)] and max|Q|;
+  // rows (r,R,d,D) from DL, columns (c,e) from X
+  const DLOp dl = double_layer(c, ak, D, d);
   {
-    Gather g;
-    g.nr = 3;
-    g.re[0] = D; g.rs[0] = ak.stride[2];
-    g.re[1] = D; g.rs[1] = ak.stride[3];
-    g.re[2] = d; g.rs[2] = ak.stride[4];
-    g.nk = 2;
-    g.ke[0] = D; g.ks[0] = ak.stride[1];
-    g.ke[1] = D; g.ks[1] = ak.stride[0];
-    gather_split_bf16(c, ak.p, g, b3h, b3l, ld3);
-  }
-  // t3 -> T3p[(c,R,e,D)][(l,u,p)], ld4
-  const int64_t ld4 = round8(D2 * d);
-  bf16* t3h = c.alloc<bf16>(size_t(rows3) * ld4);
-  bf16* t3l = c.alloc<bf16>(size_t(rows3) * ld4);
-  {
-    TcLayout l;
-    l.nm = 4;
-    l.me[0] = cc; l.ms[0] = D * E * D * ld4;
-    l.me[1] = D;  l.ms[1] = d;
-    l.me[2] = E;  l.ms[2] = D * ld4;
-    l.me[3] = D;  l.ms[3] = D * d;
-    l.nn = 3;
-    l.ne[0] = D; l.ns[0] = E * D * ld4;
-    l.ne[1] = D; l.ns[1] = ld4;
-    l.ne[2] = d; l.ns[2] = 1;
-    TcOut out;
-    out.add(TcKind::kBf16Hi, t3h, l).add(TcKind::kBf16Lo, t3l, l);
-    tc_gemm(c, TcOperand{t2h, t2l, rows3, D2, ld3}, TcOperand{b3h, b3l, D2 * d, D2, ld3}, x3, out);
-  }
-  // Q: B4[(r,d)][(l,u,p)] = A[l][u][r][d][p]
-  bf16* b4h = c.alloc<bf16>(size_t(D2) * ld4);
-  bf16* b4l = c.alloc<bf16>(size_t(D2) * ld4);
-  {
-    Gather g;
-    g.nr = 2;
-    g.re[0] = D; g.rs[0] = ak.stride[2];
-    g.re[1] = D; g.rs[1] = ak.stride[3];
-    g.nk = 3;
-    g.ke[0] = D; g.ks[0] = ak.stride[0];
-    g.ke[1] = D; g.ks[1] = ak.stride[1];
-    g.ke[2] = d; g.ks[2] = ak.stride[4];
-    gather_split_bf16(c, ak.p, g, b4h, b4l, ld4);
-  }
-  {
-    TcLayout lq;  // Q[(c,r,R)][(e,d,D)] row-major, ld
+    TcLayout lq;
     lq.nm = 4;
-    lq.me[0] = cc; lq.ms[0] = D * D * o.ld;
-    lq.me[1] = D;  lq.ms[1] = o.ld;
-    lq.me[2] = E;  lq.ms[2] = D * D;
-    lq.me[3] = D;  lq.ms[3] = 1;
+    lq.me[0] = D; lq.ms[0] = D * o.ld;
+    lq.me[1] = D; lq.ms[1] = o.ld;
+    lq.me[2] = D; lq.ms[2] = D;
+    lq.me[3] = D; lq.ms[3] = 1;
     lq.nn = 2;
-    lq.ne[0] = D; lq.ns[0] = D * o.ld;
-    lq.ne[1] = D; lq.ns[1] = D;
-    TcLayout lt;  // Q^T, ldt
-    lt.nm = 4;
-    lt.me[0] = cc; lt.ms[0] = D * D;
-    lt.me[1] = D;  lt.ms[1] = 1;
-    lt.me[2] = E;  lt.ms[2] = D * D * o.ldt;
-    lt.me[3] = D;  lt.ms[3] = o.ldt;
-    lt.nn = 2;
-    lt.ne[0] = D; lt.ns[0] = D;
-    lt.ne[1] = D; lt.ns[1] = D * o.ldt;
+    lq.ne[0] = cc; lq.ns[0] = D2 * o.ld;
+    lq.ne[1] = E;  lq.ns[1] = D2;
     TcOut out;
     out.add(TcKind::kBf16Hi, o.q_hi, lq).add(TcKind::kBf16Lo, o.q_lo, lq);
-    out.add(TcKind::kBf16Hi, o.t_hi, lt).add(TcKind::kBf16Lo, o.t_lo, lt);
-    tc_gemm_absmax_normalized(c, TcOperand{t3h, t3l, rows3, D2 * d, ld4},
-                              TcOperand{b4h, b4l, D2, D2 * d, ld4}, x3, out, absmax);
+    tc_gemm_absmax(c, dl.op(), TcOperand{xh, xl, cc * E, K2, ldx}, x3, out, o.scale);
   }
+  transpose_bf16(c, o.q_hi, o.q_lo, rows, cols, o.ld, o.t_hi, o.t_lo, o.ldt);
   return o;
 }
 
@@ -211,30 +207,31 @@ TcOperand gemm_to_operand(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode
 }
 
 void gemm_to_f64(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, double* C,
-                 int64_t ldc, bool transposed) {
+                 int64_t ldc, bool transposed, const double* inv_scale) {
   TcOut out;
   out.add(TcKind::kF64, C,
           transposed ? TcLayout::cols(A.rows, B.rows, ldc) : TcLayout::rows(A.rows, B.rows, ldc));
+  out.inv_scale = inv_scale;
   tc_gemm(c, A, B, mode, out);
 }
 
 }  // namespace
 
 // renormalize_ej (acetn/renormalization/directional_mover.py:345-366) on
-// tensor cores in 3xBF16: the four einsums become four GEMMs whose epilogues
-// store straight into the next GEMM's K-major operand; the last one writes
-// the FP64 result, normalised in FP64.
-//   G1 t1[(a,l,L)][(u,U,x)]  = sum_b E[a][b][l][L] P1[b][u][U][x]
-//   G2 t2[(a,l,u,x)][(R,D,P)] = sum_(L,U) t1 A*[L][U][R][D][P]
-//   G3 t3[(R,D,a,x)][(r,d)]   = sum_(l,u,p) t2 A[l][u][r][d][p]
-//   G4 E'[y][(x,r,R)]         = sum_(a,d,D) t3 P2[a][d][D][y]
+// tensor cores in 3xBF16.  The four einsums become three GEMMs, the two
+// site-tensor steps merged into one against the double-layer matrix DL:
+//   G1 X[(a,x)][(l,L,u,U)]   = sum_b P1[b][u][U][x] E[a][b][l][L]     (K = chi)
+//   G2 T[(x,r,R)][(a,d,D)]   = sum_(l,L,u,U) DL[(r,R,d,D)][(l,L,u,U)] X
+//   G3 E'[y][(x,r,R)]        = sum_(a,d,D) T P2[a][d][D][y]             (K = chi D^2)
+// each epilogue storing the next GEMM's K-major operand; the last writes the
+// FP64 result, normalised in FP64.
 void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64_t Y,
                           const double* P1j, int64_t X, double* Eout) {
   const View ei = S.E(3 + k), ak = S.A(k);
   const int64_t Aa = ei.shape[0], B = ei.shape[1], D = S.D, d = S.d, D2 = D * D;
   const TcMode x3 = TcMode::kBf16x3;
   Scope scope(c);
-  // G1 operands
+  // G1 operands: E as ((a,l,L) x b), P1 as ((x,u,U) x b)
   const int64_t ld1 = tc_ld(B);
   bf16* a1h = c.alloc<bf16>(size_t(Aa) * D2 * ld1);
   bf16* a1l = c.alloc<bf16>(size_t(Aa) * D2 * ld1);
@@ -247,112 +244,64 @@ void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64
     g.ke[0] = B; g.ks[0] = ei.stride[1];
     gather_split_bf16(c, ei.p, g, a1h, a1l, ld1);
   }
-  bf16* b1h = c.alloc<bf16>(size_t(D2) * X * ld1);
-  bf16* b1l = c.alloc<bf16>(size_t(D2) * X * ld1);
+  bf16* b1h = c.alloc<bf16>(size_t(X) * D2 * ld1);
+  bf16* b1l = c.alloc<bf16>(size_t(X) * D2 * ld1);
   {
-    Gather g;
-    g.nr = 1;
-    g.re[0] = D2 * X; g.rs[0] = 1;
+    Gather g;  // P1j is (b,u,U) x X row-major
+    g.nr = 2;
+    g.re[0] = X;  g.rs[0] = 1;
+    g.re[1] = D2; g.rs[1] = X;
     g.nk = 1;
     g.ke[0] = B; g.ks[0] = D2 * X;
     gather_split_bf16(c, P1j, g, b1h, b1l, ld1);
   }
-  // G1 -> T1p[(a,l,u,x)][(L,U)]
-  const int64_t ldk = round8(D2);
-  const int64_t rows2 = Aa * D * D * X;
-  bf16* t1h = c.alloc<bf16>(size_t(rows2) * ldk);
-  bf16* t1l = c.alloc<bf16>(size_t(rows2) * ldk);
+  // G1 -> X[(a,x)][(l,L,u,U)]; rows (x,u,U) from P1, columns (a,l,L) from E
+  const int64_t K2 = D2 * D2, ldx = tc_ld(K2);
+  bf16* xh = c.alloc<bf16>(size_t(Aa) * X * ldx);
+  bf16* xl = c.alloc<bf16>(size_t(Aa) * X * ldx);
   {
     TcLayout l;
-    l.nm = 3;
-    l.me[0] = Aa; l.ms[0] = D * D * X * ldk;
-    l.me[1] = D;  l.ms[1] = D * X * ldk;
-    l.me[2] = D;  l.ms[2] = D;
+    l.nm = 2;
+    l.me[0] = X;  l.ms[0] = ldx;
+    l.me[1] = D2; l.ms[1] = 1;
     l.nn = 3;
-    l.ne[0] = D; l.ns[0] = X * ldk;
-    l.ne[1] = D; l.ns[1] = 1;
-    l.ne[2] = X; l.ns[2] = ldk;
+    l.ne[0] = Aa; l.ns[0] = X * ldx;
+    l.ne[1] = D;  l.ns[1] = D * D2;
+    l.ne[2] = D;  l.ns[2] = D2;
     TcOut out;
-    out.add(TcKind::kBf16Hi, t1h, l).add(TcKind::kBf16Lo, t1l, l);
-    tc_gemm(c, TcOperand{a1h, a1l, Aa * D2, B, ld1}, TcOperand{b1h, b1l, D2 * X, B, ld1}, x3, out);
+    out.add(TcKind::kBf16Hi, xh, l).add(TcKind::kBf16Lo, xl, l);
+    tc_gemm(c, TcOperand{b1h, b1l, X * D2, B, ld1}, TcOperand{a1h, a1l, Aa * D2, B, ld1}, x3, out);
   }
-  // G2: B2[(R,D,P)][(L,U)] = A*[L][U][R][D][P]
-  bf16* b2h = c.alloc<bf16>(size_t(D2) * d * ldk);
-  bf16* b2l = c.alloc<bf16>(size_t(D2) * d * ldk);
-  {
-    Gather g;
-    g.nr = 3;
-    g.re[0] = D; g.rs[0] = ak.stride[2];
-    g.re[1] = D; g.rs[1] = ak.stride[3];
-    g.re[2] = d; g.rs[2] = ak.stride[4];
-    g.nk = 2;
-    g.ke[0] = D; g.ks[0] = ak.stride[0];
-    g.ke[1] = D; g.ks[1] = ak.stride[1];
-    gather_split_bf16(c, ak.p, g, b2h, b2l, ldk);
-  }
-  // G2 -> T2p[(R,D,a,x)][(l,u,p)]
-  const int64_t ldk3 = round8(D2 * d);
-  bf16* t2h = c.alloc<bf16>(size_t(rows2) * ldk3);
-  bf16* t2l = c.alloc<bf16>(size_t(rows2) * ldk3);
-  {
-    TcLayout l;
-    l.nm = 4;
-    l.me[0] = Aa; l.ms[0] = X * ldk3;
-    l.me[1] = D;  l.ms[1] = D * d;
-    l.me[2] = D;  l.ms[2] = d;
-    l.me[3] = X;  l.ms[3] = ldk3;
-    l.nn = 3;
-    l.ne[0] = D; l.ns[0] = D * Aa * X * ldk3;
-    l.ne[1] = D; l.ns[1] = Aa * X * ldk3;
-    l.ne[2] = d; l.ns[2] = 1;
-    TcOut out;
-    out.add(TcKind::kBf16Hi, t2h, l).add(TcKind::kBf16Lo, t2l, l);
-    tc_gemm(c, TcOperand{t1h, t1l, rows2, D2, ldk}, TcOperand{b2h, b2l, D2 * d, D2, ldk}, x3, out);
-  }
-  // G3: B3[(r,d)][(l,u,p)] = A[l][u][r][d][p]
-  bf16* b3h = c.alloc<bf16>(size_t(D2) * ldk3);
-  bf16* b3l = c.alloc<bf16>(size_t(D2) * ldk3);
-  {
-    Gather g;
-    g.nr = 2;
-    g.re[0] = D; g.rs[0] = ak.stride[2];
-    g.re[1] = D; g.rs[1] = ak.stride[3];
-    g.nk = 3;
-    g.ke[0] = D; g.ks[0] = ak.stride[0];
-    g.ke[1] = D; g.ks[1] = ak.stride[1];
-    g.ke[2] = d; g.ks[2] = ak.stride[4];
-    gather_split_bf16(c, ak.p, g, b3h, b3l, ldk3);
-  }
-  // G3 -> T3p[(x,r,R)][(a,d,D)]
+  // G2 -> T[(x,r,R)][(a,d,D)]
+  const DLOp dl = double_layer(c, ak, D, d);
   const int64_t K4 = Aa * D2;
-  const int64_t ldk4 = tc_ld(K4);
-  bf16* t3h = c.alloc<bf16>(size_t(X) * D2 * ldk4);
-  bf16* t3l = c.alloc<bf16>(size_t(X) * D2 * ldk4);
+  const int64_t ld4 = tc_ld(K4);
+  bf16* t3h = c.alloc<bf16>(size_t(X) * D2 * ld4);
+  bf16* t3l = c.alloc<bf16>(size_t(X) * D2 * ld4);
   {
-    TcLayout l;
+    TcLayout l;  // rows (r,R,d,D) from DL, columns (a,x) from X
     l.nm = 4;
-    l.me[0] = D;  l.ms[0] = ldk4;
-    l.me[1] = D;  l.ms[1] = 1;
-    l.me[2] = Aa; l.ms[2] = D2;
-    l.me[3] = X;  l.ms[3] = D2 * ldk4;
+    l.me[0] = D; l.ms[0] = D * ld4;
+    l.me[1] = D; l.ms[1] = ld4;
+    l.me[2] = D; l.ms[2] = D;
+    l.me[3] = D; l.ms[3] = 1;
     l.nn = 2;
-    l.ne[0] = D; l.ns[0] = D * ldk4;
-    l.ne[1] = D; l.ns[1] = D;
+    l.ne[0] = Aa; l.ns[0] = D2;
+    l.ne[1] = X;  l.ns[1] = D2 * ld4;
     TcOut out;
     out.add(TcKind::kBf16Hi, t3h, l).add(TcKind::kBf16Lo, t3l, l);
-    tc_gemm(c, TcOperand{t2h, t2l, rows2, D2 * d, ldk3}, TcOperand{b3h, b3l, D2, D2 * d, ldk3}, x3,
-            out);
+    tc_gemm(c, dl.op(), TcOperand{xh, xl, Aa * X, K2, ldx}, x3, out);
   }
-  // G4: B4[y][(a,d,D)] = P2[a][d][D][y]
-  bf16* b4h = c.alloc<bf16>(size_t(Y) * ldk4);
-  bf16* b4l = c.alloc<bf16>(size_t(Y) * ldk4);
+  // G3: B4[y][(a,d,D)] = P2[a][d][D][y]
+  bf16* b4h = c.alloc<bf16>(size_t(Y) * ld4);
+  bf16* b4l = c.alloc<bf16>(size_t(Y) * ld4);
   {
     Gather g;
     g.nr = 1;
     g.re[0] = Y; g.rs[0] = 1;
     g.nk = 1;
     g.ke[0] = K4; g.ks[0] = Y;
-    gather_split_bf16(c, P2i, g, b4h, b4l, ldk4);
+    gather_split_bf16(c, P2i, g, b4h, b4l, ld4);
   }
   {
     TcLayout l;  // E'[y][x][r][R]
@@ -364,7 +313,7 @@ void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64
     l.ne[0] = Y; l.ns[0] = X * D2;
     TcOut out;
     out.add(TcKind::kF64, Eout, l);
-    tc_gemm(c, TcOperand{t3h, t3l, X * D2, K4, ldk4}, TcOperand{b4h, b4l, Y, K4, ldk4}, x3, out);
+    tc_gemm(c, TcOperand{t3h, t3l, X * D2, K4, ld4}, TcOperand{b4h, b4l, Y, K4, ld4}, x3, out);
   }
   double* nrm = c.alloc<double>(1);
   sumsq(c, Eout, Y * X * D2, nrm);
@@ -375,6 +324,7 @@ void quarter_tensor_mixed_f64(Ctx& c, const Site& S, int k, double* Q) {
   Scope scope(c);
   const QOps o = quarter_mixed(c, S, k);
   join_bf16(c, o.q_hi, o.q_lo, o.rows, o.cols, o.ld, Q);
+  divide_by(c, Q, o.rows * o.cols, o.scale, 0);
 }
 
 void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg_opts& o,
@@ -397,7 +347,8 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
     A1 = quarter_mixed(c, *S[0], k);
     A4 = quarter_mixed(c, *S[3], k + 3);
   }
-  // ---- range finder in BF16 with FP32 orthonormalization:
+  // ---- range finder in BF16 with FP32 orthonormalization (on the unscaled
+  //      quarter tensors: every product is orthonormalised before use):
   //      Y = Q1 (Q4 Omega), niter x [QR; Z = Q4^T Q1^T Y; QR; Y = Q1 Q4 Z].
   //      The reference orthonormalises once per power iteration; the extra
   //      QR of the half step spans the same space in exact arithmetic and
@@ -456,6 +407,8 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
     const TcOperand w = gemm_to_operand(c, A1.t(true), qt, x3, true);    // W = Q^T Q1 (q x c1)
     TcOut out;
     out.add(TcKind::kF64, Bm, TcLayout::cols(A4.cols, q, n));            // B (q x n)
+    out.inv_scale = A1.scale;  // normalised quarter tensors
+    out.inv_scale2 = A4.scale;
     tc_gemm(c, A4.t(true), w, x3, out);
   }
   svd_via_gram(c, Bm, q, n, Ub, s, V);
@@ -481,9 +434,9 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
     scale_columns(c, Ud, m, cap, q, f);
     scale_columns(c, Vd, n, cap, q, f);
     const TcOperand ut = yt_operand(c, Ud, m, cap, q, true);  // (U f)^T (cap x m)
-    gemm_to_f64(c, A1.t(true), ut, x3, P1f, cap, false);     // Q1^T U f (c1 x cap)
+    gemm_to_f64(c, A1.t(true), ut, x3, P1f, cap, false, A1.scale);  // Q1^T U f (c1 x cap)
     const TcOperand vt = yt_operand(c, Vd, n, cap, q, true);  // (V f)^T (cap x n)
-    gemm_to_f64(c, A4.q(true), vt, x3, P2f, cap, false);     // Q4 V f (r4 x cap)
+    gemm_to_f64(c, A4.q(true), vt, x3, P2f, cap, false, A4.scale);  // Q4 V f (r4 x cap)
   }
   if (o.fixed_width) {
     if (!c.sizing()) {

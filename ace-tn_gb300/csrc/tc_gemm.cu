@@ -1,9 +1,11 @@
 // tcgen05 GEMM for sm_103a: TMA loads (128-byte swizzle) into a multi-stage
 // shared-memory ring, one thread issuing tcgen05.mma into a TMEM accumulator
-// (M = 128 rows per CTA, N up to 256 columns), split-K over the grid's z
-// dimension, and an epilogue reading TMEM with tcgen05.ld into FP32 partial
-// tiles that a second kernel reduces (fixed order) into the requested
-// output formats.
+// (M = 128 rows per CTA, N up to 256 columns).  Without a K split the
+// epilogue reads TMEM with tcgen05.ld and stores every destination directly
+// (each thread owns one output row; groups of four consecutive columns that
+// are contiguous in a destination go out as one vector store).  With a K
+// split over the grid's z dimension the epilogue writes FP32 partial tiles
+// that a second kernel reduces in a fixed order.
 //
 // Every mbarrier wait is bounded: on expiry the kernel records bit 2 in the
 // status word, stops issuing work, waits (bounded) for its own outstanding
@@ -141,14 +143,45 @@ __device__ __forceinline__ int64_t lay_col(const TcLayout& l, int64_t n) {
   return o;
 }
 
-__device__ __forceinline__ void store(const TcDest& d, int64_t off, double v) {
+// One value / four consecutive values (destination offset a multiple of 4)
+// of an FP32 accumulator tile, scaled by sc, in the destination's format.
+// FP32 arithmetic throughout (FP64 units are scarce on this part); an FP64
+// destination receives the FP32 product widened.
+__device__ __forceinline__ void store1(const TcDest& d, int64_t off, float v, float sc) {
+  const float x = v * sc;
   switch (d.kind) {
-    case TcKind::kF64: static_cast<double*>(d.p)[off] = v; break;
-    case TcKind::kF32: static_cast<float*>(d.p)[off] = float(v); break;
-    case TcKind::kBf16Hi: static_cast<bf16*>(d.p)[off] = __double2bfloat16(v); break;
+    case TcKind::kF64: static_cast<double*>(d.p)[off] = double(x); break;
+    case TcKind::kF32: static_cast<float*>(d.p)[off] = x; break;
+    case TcKind::kBf16Hi: static_cast<bf16*>(d.p)[off] = __float2bfloat16(x); break;
+    case TcKind::kBf16Lo:
+      static_cast<bf16*>(d.p)[off] = __float2bfloat16(x - __bfloat162float(__float2bfloat16(x)));
+      break;
+  }
+}
+
+__device__ __forceinline__ void store4(const TcDest& d, int64_t off, const float* v, float sc) {
+  const float x0 = v[0] * sc, x1 = v[1] * sc, x2 = v[2] * sc, x3 = v[3] * sc;
+  switch (d.kind) {
+    case TcKind::kF64: {
+      double2* q = reinterpret_cast<double2*>(static_cast<double*>(d.p) + off);
+      q[0] = make_double2(double(x0), double(x1));
+      q[1] = make_double2(double(x2), double(x3));
+      break;
+    }
+    case TcKind::kF32:
+      *reinterpret_cast<float4*>(static_cast<float*>(d.p) + off) = make_float4(x0, x1, x2, x3);
+      break;
+    case TcKind::kBf16Hi:
     case TcKind::kBf16Lo: {
-      const bf16 h = __double2bfloat16(v);
-      static_cast<bf16*>(d.p)[off] = __double2bfloat16(v - double(__bfloat162float(h)));
+      float y[4] = {x0, x1, x2, x3};
+      if (d.kind == TcKind::kBf16Lo) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) y[i] -= __bfloat162float(__float2bfloat16(y[i]));
+      }
+      const __nv_bfloat162 o0 = __halves2bfloat162(__float2bfloat16(y[0]), __float2bfloat16(y[1]));
+      const __nv_bfloat162 o1 = __halves2bfloat162(__float2bfloat16(y[2]), __float2bfloat16(y[3]));
+      *reinterpret_cast<uint2*>(static_cast<bf16*>(d.p) + off) =
+          make_uint2(*reinterpret_cast<const uint32_t*>(&o0), *reinterpret_cast<const uint32_t*>(&o1));
       break;
     }
   }
@@ -163,10 +196,14 @@ struct GemmParams {
   float* part;       // [split][m_pad][n_pad] (unfused epilogue)
   int m_pad, n_pad;
   int* status;
-  // fused epilogue (single K split): the tile goes straight to the destinations
-  int fused;
+  // direct epilogue (single K split): the tile goes straight to the destinations
+  int direct;
+  int n_fast;        // grid x runs over N tiles (CTAs sharing an A tile run together)
   int nd;
   double alpha;
+  const double* scale1;  // outputs divided by *scale1 and *scale2 when non-null
+  const double* scale2;
+  unsigned long long* absmax;  // max |output| accumulated as ordered bits when non-null
   int64_t M, N;
   TcDest d[4];
 };
@@ -187,6 +224,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t* tfull = empty + p.stages;
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(tfull + 1);
   __shared__ int s_fail;
+  __shared__ int64_t s_co[4][256];
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -214,8 +252,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int kb0 = blockIdx.z * p.kb_per_split;
   const int kb1 = min(kb0 + p.kb_per_split, p.kb_total);
   const int nkb = kb1 - kb0;
-  const int m0 = blockIdx.x * kBM;
-  const int n0 = blockIdx.y * p.ntile;
+  const int m0 = (p.n_fast ? blockIdx.y : blockIdx.x) * kBM;
+  const int n0 = (p.n_fast ? blockIdx.x : blockIdx.y) * p.ntile;
   int issued_loads = 0;  // producer: stages handed to TMA
 
   if (threadIdx.x == 0) {
@@ -275,44 +313,68 @@ __global__ void __launch_bounds__(kThreads, 1)
   ok = __all_sync(0xffffffffu, ok);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const int row = m0 + warp * 32 + lane;
-  if (p.fused) {
-    // stage the 128 x ntile tile in the (now idle) pipeline buffers, then
-    // store every destination with a warp-contiguous mapping
-    const int ldt = p.ntile + 4;
-    float* tile = reinterpret_cast<float*>(base);
-    int64_t* ro = reinterpret_cast<int64_t*>(tile + size_t(kBM) * ldt);
-    int64_t* co = ro + kBM;
+  if (p.direct) {
+    // column offsets of this tile in every destination (-1 beyond N)
+    for (int k = 0; k < p.nd; ++k)
+      for (int cc = threadIdx.x; cc < p.ntile; cc += kThreads) {
+        const int64_t n = int64_t(n0) + cc;
+        s_co[k][cc] = n < p.N ? lay_col(p.d[k].lay, n) : int64_t(-1);
+      }
+    __syncthreads();
+    const bool mvalid = row < p.M;
+    int64_t ro[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (k < p.nd && mvalid) ro[k] = lay_row(p.d[k].lay, row);
+    double scd = p.alpha;
+    if (p.scale1 != nullptr) scd /= p.scale1[0];
+    if (p.scale2 != nullptr) scd /= p.scale2[0];
+    const float sc = float(scd);
+    float amax = 0.f;
     if (ok) {
       for (int c = 0; c < p.ntile; c += 16) {
         float v[16];
+        __syncwarp();
         tmem_ld16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c), v);
-        float* dst = tile + size_t(warp * 32 + lane) * ldt + c;
+        if (mvalid) {
 #pragma unroll
-        for (int j = 0; j < 16; j += 4)
-          *reinterpret_cast<float4*>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+          for (int k = 0; k < 4; ++k) {
+            if (k >= p.nd) break;
+            const TcDest& d = p.d[k];
+#pragma unroll
+            for (int g = 0; g < 4; ++g) {
+              const int cb = c + 4 * g;
+              const int64_t c0 = s_co[k][cb];
+              const bool vec = c0 >= 0 && ((ro[k] + c0) & 3) == 0 && s_co[k][cb + 1] == c0 + 1 &&
+                               s_co[k][cb + 2] == c0 + 2 && s_co[k][cb + 3] == c0 + 3;
+              if (vec) {
+                store4(d, ro[k] + c0, v + 4 * g, sc);
+              } else {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                  const int64_t ci = s_co[k][cb + i];
+                  if (ci >= 0) store1(d, ro[k] + ci, v[4 * g + i], sc);
+                }
+              }
+            }
+          }
+          if (p.absmax != nullptr) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+              if (s_co[0][c + i] >= 0) amax = fmaxf(amax, fabsf(v[i] * sc));
+          }
+        }
       }
     }
-    __syncthreads();
-    if (ok && !s_fail) {
-      for (int k = 0; k < p.nd; ++k) {
-        const TcDest& d = p.d[k];
-        ro[threadIdx.x] = lay_row(d.lay, m0 + threadIdx.x);
-        for (int c = threadIdx.x; c < p.ntile; c += kThreads) co[c] = lay_col(d.lay, n0 + c);
-        __syncthreads();
-        const bool n_fast = d.lay.ns[d.lay.nn - 1] == 1;
-        const int total = kBM * p.ntile;
-        for (int idx = threadIdx.x; idx < total; idx += kThreads) {
-          const int mi = n_fast ? idx / p.ntile : idx % kBM;
-          const int ni = n_fast ? idx % p.ntile : idx / kBM;
-          if (m0 + mi >= p.M || n0 + ni >= p.N) continue;
-          store(d, ro[mi] + co[ni], p.alpha * double(tile[size_t(mi) * ldt + ni]));
-        }
-        __syncthreads();
-      }
+    if (p.absmax != nullptr) {
+      for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+      // non-negative doubles order like their bit patterns
+      if (lane == 0 && amax > 0.f)
+        atomicMax(p.absmax, (unsigned long long)__double_as_longlong(double(amax)));
     }
   }
   float* out = p.part + (size_t(blockIdx.z) * p.m_pad + row) * p.n_pad + n0;
-  if (ok && !p.fused) {
+  if (ok && !p.direct) {
     for (int c = 0; c < p.ntile; c += 16) {
       float v[16];
       tmem_ld16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c), v);
@@ -348,6 +410,7 @@ struct ReduceParams {
   int64_t M, N;
   double alpha;
   const double* inv_scale;
+  const double* inv_scale2;
   int nd;
   TcDest d[4];
 };
@@ -358,18 +421,19 @@ struct ReduceParams {
 // stride is 1 are written with the column index fastest, the others with the
 // row index fastest, so warps store contiguously in the common cases.
 __global__ void tc_reduce_kernel(const ReduceParams r) {
-  __shared__ double tile[32][33];
+  __shared__ float tile[32][33];
   __shared__ int64_t ro[32], co[32];
   const int64_t m0 = int64_t(blockIdx.x) * 32, n0 = int64_t(blockIdx.y) * 32;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  double scd = r.alpha;
+  if (r.inv_scale != nullptr) scd /= r.inv_scale[0];
+  if (r.inv_scale2 != nullptr) scd /= r.inv_scale2[0];
+  const float sc = float(scd);
   for (int yy = ty; yy < 32; yy += 8) {
     const int64_t m = m0 + yy, n = n0 + tx;
-    double s = 0.0;
+    float s = 0.f;
     if (m < r.M && n < r.N) {
-      for (int t = 0; t < r.splits; ++t)
-        s += double(r.part[(size_t(t) * r.m_pad + m) * r.n_pad + n]);
-      s *= r.alpha;
-      if (r.inv_scale != nullptr) s = s / r.inv_scale[0];
+      for (int t = 0; t < r.splits; ++t) s += r.part[(size_t(t) * r.m_pad + m) * r.n_pad + n];
     }
     tile[yy][tx] = s;
   }
@@ -383,7 +447,7 @@ __global__ void tc_reduce_kernel(const ReduceParams r) {
     for (int yy = ty; yy < 32; yy += 8) {
       const int mi = n_fast ? yy : tx, ni = n_fast ? tx : yy;
       if (m0 + mi >= r.M || n0 + ni >= r.N) continue;
-      store(d, ro[mi] + co[ni], tile[mi][ni]);
+      store1(d, ro[mi] + co[ni], tile[mi][ni], sc);
     }
   }
 }
@@ -522,20 +586,6 @@ __global__ void gather_split_kernel(const double* src, const Gather g, int64_t r
   }
 }
 
-// max |x| over the valid M x N block of split-0 partials (single split only)
-__global__ void partial_absmax_kernel(const float* part, int64_t M, int64_t N, int n_pad,
-                                      unsigned long long* out_bits) {
-  float m = 0.f;
-  for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < M * N;
-       idx += int64_t(gridDim.x) * blockDim.x) {
-    const int64_t r = idx / N, q = idx % N;
-    m = fmaxf(m, fabsf(part[r * n_pad + q]));
-  }
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  // non-negative doubles order like their bit patterns
-  if ((threadIdx.x & 31) == 0) atomicMax(out_bits, (unsigned long long)__double_as_longlong(double(m)));
-}
-
 }  // namespace
 
 __global__ void join_bf16_kernel(const bf16* hi, const bf16* lo, int64_t rows, int64_t cols,
@@ -547,6 +597,46 @@ __global__ void join_bf16_kernel(const bf16* hi, const bf16* lo, int64_t rows, i
     if (lo != nullptr) v += double(__bfloat162float(lo[r * ld + q]));
     out[idx] = v;
   }
+}
+
+namespace {
+
+// 64 x 64 tiles through shared memory; blockIdx.z selects the hi or lo array.
+__global__ void transpose_bf16_kernel(const bf16* src_hi, const bf16* src_lo, int64_t rows,
+                                      int64_t cols, int64_t ld_src, bf16* dst_hi, bf16* dst_lo,
+                                      int64_t ld_dst) {
+  __shared__ bf16 tile[64][66];
+  const bf16* src = blockIdx.z ? src_lo : src_hi;
+  bf16* dst = blockIdx.z ? dst_lo : dst_hi;
+  const int64_t r0 = int64_t(blockIdx.y) * 64, c0 = int64_t(blockIdx.x) * 64;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int yy = ty; yy < 64; yy += 8) {
+    const int64_t r = r0 + yy, cc = c0 + 2 * tx;
+    const bf16 z = __float2bfloat16(0.f);
+    tile[yy][2 * tx] = (r < rows && cc < cols) ? src[r * ld_src + cc] : z;
+    tile[yy][2 * tx + 1] = (r < rows && cc + 1 < cols) ? src[r * ld_src + cc + 1] : z;
+  }
+  __syncthreads();
+  for (int yy = ty; yy < 64; yy += 8) {
+    const int64_t dr = c0 + yy, dc = r0 + 2 * tx;  // destination row = source column
+    if (dr >= cols) continue;
+    if (dc < rows) dst[dr * ld_dst + dc] = tile[2 * tx][yy];
+    if (dc + 1 < rows) dst[dr * ld_dst + dc + 1] = tile[2 * tx + 1][yy];
+  }
+}
+
+}  // namespace
+
+void transpose_bf16(Ctx& c, const bf16* src_hi, const bf16* src_lo, int64_t rows, int64_t cols,
+                    int64_t ld_src, bf16* dst_hi, bf16* dst_lo, int64_t ld_dst) {
+  if (c.sizing() || rows * cols == 0) return;
+  CTM_REQUIRE((src_lo == nullptr) == (dst_lo == nullptr), CTM_ERR_INVALID,
+              "transpose_bf16: lo arrays must be given on both sides or neither");
+  const dim3 grid(unsigned((cols + 63) / 64), unsigned((rows + 63) / 64), src_lo ? 2u : 1u);
+  CTM_REQUIRE(grid.y <= 65535, CTM_ERR_UNSUPPORTED, "transpose_bf16: too many rows");
+  transpose_bf16_kernel<<<grid, 256, 0, c.stream>>>(src_hi, src_lo, rows, cols, ld_src, dst_hi,
+                                                    dst_lo, ld_dst);
+  CTM_LAUNCH_CHECK();
 }
 
 void join_bf16(Ctx& c, const bf16* hi, const bf16* lo, int64_t rows, int64_t cols, int64_t ld,
@@ -586,24 +676,21 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   int splits = static_cast<int>(std::min<int64_t>(std::max<int64_t>(1, sms / base_ctas),
                                                   std::max(1, kb_total / 4)));
   splits = std::max(splits, 1);
-  if (absmax != nullptr) splits = 1;  // the scale is taken from complete sums
+  if (absmax != nullptr) splits = 1;  // the maximum is taken over complete sums
   const int kb_per_split = (kb_total + splits - 1) / splits;
   splits = (kb_total + kb_per_split - 1) / kb_per_split;
-  // The fused epilogue (tile staged in shared memory, stored by the CTA's 128
-  // threads) measured slower than the separate reduce kernel for the permuted
-  // layouts of the contraction chains, whose stores are scattered; it stays
-  // available for row-major single-destination outputs.
-  bool fused = splits == 1 && absmax == nullptr && out.nd == 1 &&
-               out.d[0].lay.nm == 1 && out.d[0].lay.nn == 1 && out.d[0].lay.ns[0] == 1;
+  const bool direct = splits == 1;
   const int m_pad = static_cast<int>(m_tiles * kBM);
   const int n_pad = static_cast<int>(n_tiles * ntile);
   const uint32_t stage_bytes = uint32_t(kBM * kBK * 2 + ntile * kBK * 2) * (imode == 3 ? 2 : 1);
-  const int stages = std::max(2, std::min(6, int((220 * 1024) / stage_bytes)));
-  const size_t tile_bytes = size_t(kBM) * (ntile + 4) * 4 + size_t(kBM + ntile) * 8;
-  const size_t smem =
-      std::max(size_t(stages) * stage_bytes + 256, fused ? tile_bytes : size_t(0)) + 1024;
+  // dynamic shared memory: the stage ring (the kernel's static arrays take ~8 KB)
+  const int stages = std::max(2, std::min(6, int((210 * 1024) / stage_bytes)));
+  const size_t smem = size_t(stages) * stage_bytes + 256 + 1024;
+  // grid x over N tiles when A is the larger operand: the CTAs that share an
+  // A tile are then resident together and A streams from DRAM once
+  const bool n_fast = n_tiles > 1 && m_tiles > n_tiles && m_tiles <= 65535;
   Scope scope(c);
-  float* part = fused ? nullptr : c.alloc<float>(size_t(splits) * m_pad * n_pad);
+  float* part = direct ? nullptr : c.alloc<float>(size_t(splits) * m_pad * n_pad);
   if (c.sizing()) return;
   CTM_REQUIRE(imode == 1 || (A.lo != nullptr && B.lo != nullptr), CTM_ERR_INVALID,
               "tc_gemm: 3xBF16 needs lo parts");
@@ -629,29 +716,27 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   p.m_pad = m_pad;
   p.n_pad = n_pad;
   p.status = status_flags(c);
-  p.fused = fused ? 1 : 0;
+  p.direct = direct ? 1 : 0;
+  p.n_fast = n_fast ? 1 : 0;
   p.nd = out.nd;
   p.alpha = out.alpha;
+  p.scale1 = out.inv_scale;
+  p.scale2 = out.inv_scale2;
+  p.absmax = reinterpret_cast<unsigned long long*>(absmax);
   p.M = M;
   p.N = N;
   for (int i = 0; i < out.nd; ++i) p.d[i] = out.d[i];
+  if (absmax != nullptr) CTM_CUDA(cudaMemsetAsync(absmax, 0, sizeof(double), c.stream));
   CTM_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(smem)));
-  const dim3 grid(static_cast<unsigned>(m_tiles), static_cast<unsigned>(n_tiles),
-                  static_cast<unsigned>(splits));
+  const dim3 grid(static_cast<unsigned>(n_fast ? n_tiles : m_tiles),
+                  static_cast<unsigned>(n_fast ? m_tiles : n_tiles), static_cast<unsigned>(splits));
   {
     KernelTimer timer(c.stream, kTagTcGemm, 2.0 * double(M) * N * K * imode);
     tc_gemm_kernel<<<grid, kThreads, smem, c.stream>>>(tA, tAl, tB, tBl, p);
     CTM_LAUNCH_CHECK();
   }
-  if (fused) return;
-  if (absmax != nullptr) {
-    CTM_CUDA(cudaMemsetAsync(absmax, 0, sizeof(double), c.stream));
-    partial_absmax_kernel<<<grid_for(M * N, 256, 152 * 8), 256, 0, c.stream>>>(
-        part, M, N, n_pad, reinterpret_cast<unsigned long long*>(absmax));
-    CTM_LAUNCH_CHECK();
-    out.inv_scale = absmax;
-  }
+  if (direct) return;
   ReduceParams r{};
   r.part = part;
   r.splits = splits;
@@ -661,6 +746,7 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   r.N = N;
   r.alpha = out.alpha;
   r.inv_scale = out.inv_scale;
+  r.inv_scale2 = out.inv_scale2;
   r.nd = out.nd;
   for (int i = 0; i < out.nd; ++i) r.d[i] = out.d[i];
   dim3 rg(unsigned((M + 31) / 32), unsigned((N + 31) / 32));
@@ -675,8 +761,8 @@ void tc_gemm(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, const 
   tc_gemm_impl(c, A, B, mode, out, nullptr);
 }
 
-void tc_gemm_absmax_normalized(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode,
-                               TcOut out, double* absmax) {
+void tc_gemm_absmax(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode,
+                    const TcOut& out, double* absmax) {
   CTM_REQUIRE(absmax != nullptr || c.sizing(), CTM_ERR_INVALID, "absmax scalar is NULL");
   tc_gemm_impl(c, A, B, mode, out, c.sizing() ? reinterpret_cast<double*>(16) : absmax);
 }

@@ -52,7 +52,8 @@ struct TcDest {
 // Destinations of the reduced result: alpha * C written to every entry of d.
 struct TcOut {
   double alpha = 1.0;
-  const double* inv_scale = nullptr;  // device scalar: results are divided by *inv_scale
+  const double* inv_scale = nullptr;   // device scalars: results are divided by *inv_scale
+  const double* inv_scale2 = nullptr;  // and by *inv_scale2 when non-null
   int nd = 0;
   TcDest d[4];
   TcOut& add(TcKind k, void* p, const TcLayout& l) {
@@ -69,10 +70,15 @@ inline int64_t tc_ld(int64_t k) { return (k + 63) / 64 * 64; }
 
 void tc_gemm(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, const TcOut& out);
 
-// As tc_gemm, but first reduces max |C| into *absmax (device) and sets
-// out.inv_scale to it: the outputs hold C / max |C|.
-void tc_gemm_absmax_normalized(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode,
-                               TcOut out, double* absmax);
+// As tc_gemm without a K split, and also writes max |output| to *absmax
+// (device scalar, FP32-accumulated values).
+void tc_gemm_absmax(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode,
+                    const TcOut& out, double* absmax);
+
+// dst (cols x rows, leading dimension ld_dst) = src^T for BF16 hi and lo
+// arrays (src rows x cols, leading dimension ld_src); lo pointers may be null.
+void transpose_bf16(Ctx& c, const bf16* src_hi, const bf16* src_lo, int64_t rows, int64_t cols,
+                    int64_t ld_src, bf16* dst_hi, bf16* dst_lo, int64_t ld_dst);
 
 // out (rows x cols FP64, contiguous) = hi + lo (BF16, leading dimension ld).
 void join_bf16(Ctx& c, const bf16* hi, const bf16* lo, int64_t rows, int64_t cols, int64_t ld,

@@ -4,7 +4,9 @@ Mirror of ``DirectionalMover`` (acetn/renormalization/directional_mover.py:5-366
 for the non-distributed moves.  One move enqueues the projector pairs of all
 rows (columns) of the move, reads their truncated widths with a single
 device-to-host copy, then enqueues the boundary renormalization of every row
-(column).  New tensors are written back by list-item assignment, as in
+(column).  The rows of a move are independent (each renormalization reads
+one site and writes another), so with ``concurrent`` (the default) they run
+on side streams forked from and joined back into the caller's stream.  New tensors are written back by list-item assignment, as in
 ``renormalize_boundary`` of the reference.
 """
 
@@ -25,6 +27,33 @@ class DirectionalMover:
         # the truncation counts of the last move stay on the device
         self.graph_mode = False
         self.last_counts = None
+        self.concurrent = True
+        self._streams = {}
+
+    # ---------------------------------------------------------------- streams
+    def _fork(self, device, n):
+        """Side streams for n concurrent rows, each ordered after the caller's
+        stream; None when the rows run in order on the caller's stream."""
+        if not self.concurrent or n < 2:
+            return None
+        key = torch.device(device).index
+        pool = self._streams.setdefault(key, [])
+        while len(pool) < n:
+            pool.append(torch.cuda.Stream(device))
+        main = torch.cuda.current_stream(device)
+        for s in pool[:n]:
+            s.wait_stream(main)
+        return pool[:n]
+
+    @staticmethod
+    def _join(device, streams, tensors):
+        if streams is None:
+            return
+        main = torch.cuda.current_stream(device)
+        for t in tensors:
+            t.record_stream(main)
+        for s in streams:
+            main.wait_stream(s)
 
     # ---------------------------------------------------------------- sites
     @staticmethod
@@ -71,9 +100,17 @@ class DirectionalMover:
     def _projectors_all(self, ipeps, site_lists, k):
         device = ipeps[site_lists[0][0]]["A"].device
         slots = torch.zeros(len(site_lists), dtype=torch.int64, device=device)
-        pend = [self.projector_calculator.launch(ipeps, sites, k, slots[n:n + 1],
-                                                 fixed_width=self.graph_mode)
-                for n, sites in enumerate(site_lists)]
+        streams = self._fork(device, len(site_lists))
+        pend = []
+        for n, sites in enumerate(site_lists):
+            if streams is None:
+                pend.append(self.projector_calculator.launch(ipeps, sites, k, slots[n:n + 1],
+                                                             fixed_width=self.graph_mode))
+                continue
+            with torch.cuda.stream(streams[n]):
+                pend.append(self.projector_calculator.launch(ipeps, sites, k, slots[n:n + 1],
+                                                             fixed_width=self.graph_mode))
+        self._join(device, streams, [t for p in pend for t in (p.p1buf, p.p2buf)])
         if self.graph_mode:
             self.last_counts = slots
             proj1, proj2 = {}, {}
@@ -93,41 +130,56 @@ class DirectionalMover:
         ny, nx = ipeps.ny, ipeps.nx
         proj1, proj2 = self._projectors_all(
             ipeps, [self.left_sites(ipeps, xi, yi) for yi in range(ny)], 0)
-        for yi in range(ny):
-            xj, yj = (xi + 1) % nx, (yi + 1) % ny
-            self.renormalize_boundary(ipeps, proj1, proj2, (xi, yi), (xj, yi), yi, yj, k=0)
+        self._renormalize_all(ipeps, proj1, proj2,
+                              [((xi, yi), ((xi + 1) % nx, yi), yi, (yi + 1) % ny)
+                               for yi in range(ny)], 0)
 
     def up_move(self, ipeps, yi):
         """directional_mover.py:42-59."""
         nx, ny = ipeps.nx, ipeps.ny
         proj1, proj2 = self._projectors_all(
             ipeps, [self.up_sites(ipeps, xi, yi) for xi in range(nx)], 1)
-        for xi in range(nx):
-            xj, yj = (xi + 1) % nx, (yi - 1 + ny) % ny
-            self.renormalize_boundary(ipeps, proj1, proj2, (xi, yi), (xi, yj), xi, xj, k=1)
+        self._renormalize_all(ipeps, proj1, proj2,
+                              [((xi, yi), (xi, (yi - 1 + ny) % ny), xi, (xi + 1) % nx)
+                               for xi in range(nx)], 1)
 
     def right_move(self, ipeps, xi):
         """directional_mover.py:61-78."""
         ny, nx = ipeps.ny, ipeps.nx
         proj1, proj2 = self._projectors_all(
             ipeps, [self.right_sites(ipeps, xi, yi) for yi in range(ny)], 2)
-        for yi in range(ny):
-            xj, yj = (xi - 1 + nx) % nx, (yi - 1 + ny) % ny
-            self.renormalize_boundary(ipeps, proj1, proj2, (xi, yi), (xj, yi), yi, yj, k=2)
+        self._renormalize_all(ipeps, proj1, proj2,
+                              [((xi, yi), ((xi - 1 + nx) % nx, yi), yi, (yi - 1 + ny) % ny)
+                               for yi in range(ny)], 2)
 
     def down_move(self, ipeps, yi):
         """directional_mover.py:80-97."""
         nx, ny = ipeps.nx, ipeps.ny
         proj1, proj2 = self._projectors_all(
             ipeps, [self.down_sites(ipeps, xi, yi) for xi in range(nx)], 3)
-        for xi in range(nx):
-            xj, yj = (xi - 1 + nx) % nx, (yi + 1) % ny
-            self.renormalize_boundary(ipeps, proj1, proj2, (xi, yi), (xi, yj), xi, xj, k=3)
+        self._renormalize_all(ipeps, proj1, proj2,
+                              [((xi, yi), (xi, (yi + 1) % ny), xi, (xi - 1 + nx) % nx)
+                               for xi in range(nx)], 3)
 
     def move(self, ipeps, k, idx):
         return (self.left_move, self.up_move, self.right_move, self.down_move)[k](ipeps, idx)
 
     # ---------------------------------------------------------------- renormalization
+    def _renormalize_all(self, ipeps, proj1, proj2, jobs, k):
+        """renormalize_boundary for every (s1, s2, i, j) of a move: each reads
+        site s1 and writes site s2, and no s2 of a move is an s1 of it."""
+        device = ipeps[jobs[0][0]]["A"].device
+        streams = self._fork(device, len(jobs))
+        outs = []
+        for n, (s1, s2, i, j) in enumerate(jobs):
+            if streams is None:
+                self.renormalize_boundary(ipeps, proj1, proj2, s1, s2, i, j, k)
+                continue
+            with torch.cuda.stream(streams[n]):
+                self.renormalize_boundary(ipeps, proj1, proj2, s1, s2, i, j, k)
+            outs += [ipeps[s2]["C"][(3 + k) % 4], ipeps[s2]["C"][k], ipeps[s2]["E"][(3 + k) % 4]]
+        self._join(device, streams, outs)
+
     def renormalize_boundary(self, ipeps, proj1, proj2, s1, s2, i, j, k):
         """directional_mover.py:273-303: writes C[(3+k)%4], C[k], E[(3+k)%4] of s2."""
         site = ipeps[s1]
