@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(LT) householder_qr_kernel(T* Y, int64_t n, int
 // Right-looking elimination on the upper triangle with the pivot division
 // deferred: step j subtracts (W[j][i] / W[j][j]) * row j from every row
 // i > j, so row j ends as d_j * (row j of L_unit^T) with d_j = W[j][j], and
-// L^T[j][c] = W[j][c] / sqrt(d_j).  Both operands of the update are read
+// L^T[j][c] = W[j][c] / sqrt(d_j).  The steps run in blocks of four pivots.  Both operands of the update are read
 // along rows (lanes over contiguous columns); rows are padded to q + 1
 // elements so the transposed read of the epilogue is conflict-free as well.
 // When Linv is requested the same row operations run on an identity block
@@ -175,26 +175,93 @@ __global__ void __launch_bounds__(kCholThreads) cholesky_kernel(
     if (want_inv) E[r * ld + c] = (r == c) ? T(1) : T(0);
   }
   __syncthreads();
+  // Blocks of kNb pivots: every thread first redoes the elimination inside
+  // the kNb x kNb diagonal block (pivots and multipliers in registers), then
+  // eliminates the block's pivot rows at its own columns of W and E; after a
+  // barrier the rows below take the block's kNb updates at once.  Two
+  // barriers per kNb pivots instead of one per pivot, and kNb FMAs per
+  // read-modify-write of the trailing rows.
+  constexpr int kNb = 4;
   bool failed = false;
-  for (int j = 0; j < q; ++j) {
-    const T dj = W[j * ld + j];
-    if (dj > T(0)) {
-      const T rinv = T(1) / dj;
-      const T* Wj = W + j * ld;
-      const T* Ej = E + j * ld;
-      for (int i = j + 1 + warp; i < q; i += nwarps) {
-        const T a = Wj[i] * rinv;
-        T* Wi = W + i * ld;
-#pragma unroll 4
-        for (int k = i + lane; k < q; k += 32) Wi[k] -= a * Wj[k];
-        if (want_inv) {
-          T* Ei = E + i * ld;
-#pragma unroll 4
-          for (int c = lane; c <= j; c += 32) Ei[c] -= a * Ej[c];
+  for (int J = 0; J < q; J += kNb) {
+    const int jb = min(kNb, q - J);
+    T dpiv[kNb], mul[kNb][kNb];
+    {
+      T blk[kNb][kNb];
+#pragma unroll
+      for (int t = 0; t < kNb; ++t)
+#pragma unroll
+        for (int u = 0; u < kNb; ++u)
+          blk[t][u] = (t < jb && u < jb && u >= t) ? W[(J + t) * ld + J + u] : T(0);
+#pragma unroll
+      for (int t = 0; t < kNb; ++t) {
+        dpiv[t] = blk[t][t];
+        const T rinv = (t < jb && dpiv[t] > T(0)) ? T(1) / dpiv[t] : T(0);
+#pragma unroll
+        for (int u = 0; u < kNb; ++u) mul[t][u] = u > t ? blk[t][u] * rinv : T(0);
+#pragma unroll
+        for (int sr = t + 1; sr < kNb; ++sr)
+#pragma unroll
+          for (int u = sr; u < kNb; ++u) blk[sr][u] -= mul[t][sr] * blk[t][u];
+      }
+    }
+    if (tid == 0)
+      for (int t = 0; t < jb; ++t)
+        if (!(dpiv[t] > T(0))) failed = true;
+    __syncthreads();  // the diagonal block has been read by every thread
+    for (int k = J + tid; k < q; k += blockDim.x) {
+      T v[kNb];
+#pragma unroll
+      for (int t = 0; t < kNb; ++t) v[t] = (t < jb && J + t <= k) ? W[(J + t) * ld + k] : T(0);
+#pragma unroll
+      for (int t = 0; t < kNb; ++t)
+#pragma unroll
+        for (int sr = t + 1; sr < kNb; ++sr) v[sr] -= mul[t][sr] * v[t];
+#pragma unroll
+      for (int t = 0; t < kNb; ++t)
+        if (t < jb && J + t <= k) W[(J + t) * ld + k] = v[t];
+    }
+    if (want_inv) {
+      for (int c = tid; c < J + jb; c += blockDim.x) {
+        T v[kNb];
+#pragma unroll
+        for (int t = 0; t < kNb; ++t) v[t] = t < jb ? E[(J + t) * ld + c] : T(0);
+#pragma unroll
+        for (int t = 0; t < kNb; ++t)
+#pragma unroll
+          for (int sr = t + 1; sr < kNb; ++sr) v[sr] -= mul[t][sr] * v[t];
+#pragma unroll
+        for (int t = 0; t < kNb; ++t)
+          if (t < jb) E[(J + t) * ld + c] = v[t];
+      }
+    }
+    __syncthreads();
+    // trailing rows i >= J + jb: row_i -= sum_t (W[J+t][i] / d_t) row_(J+t)
+    const T* P0 = W + J * ld;
+    const T* Q0 = E + J * ld;
+    for (int i = J + jb + warp; i < q; i += nwarps) {
+      T a[kNb];
+#pragma unroll
+      for (int t = 0; t < kNb; ++t)
+        a[t] = (t < jb && dpiv[t] > T(0)) ? P0[t * ld + i] / dpiv[t] : T(0);
+      T* Wi = W + i * ld;
+      for (int k = i + lane; k < q; k += 32) {
+        T acc = Wi[k];
+#pragma unroll
+        for (int t = 0; t < kNb; ++t)
+          if (t < jb) acc -= a[t] * P0[t * ld + k];
+        Wi[k] = acc;
+      }
+      if (want_inv) {
+        T* Ei = E + i * ld;
+        for (int c = lane; c < J + jb; c += 32) {
+          T acc = Ei[c];
+#pragma unroll
+          for (int t = 0; t < kNb; ++t)
+            if (t < jb) acc -= a[t] * Q0[t * ld + c];
+          Ei[c] = acc;
         }
       }
-    } else {
-      failed = true;
     }
     __syncthreads();
   }
@@ -239,101 +306,33 @@ void cholesky(cudaStream_t st, const T* G, int64_t q, int64_t n, int shift_mode,
   CTM_LAUNCH_CHECK();
 }
 
-// One CTA.  Pivoted Cholesky of a symmetric positive semidefinite G (FP64,
-// q x q): G = sum_j l_j l_j^T, the pivot of step j being the largest diagonal
-// entry of the remaining Schur complement (kept in full, both triangles, in
-// shared memory).  Row j of Lc (FP32, q x q) is l_j in G's own row order;
-// the rows after the numerical rank (no positive pivot left) are zero.
-// With pivoting the columns of L come out graded and close to orthogonal,
-// which is what makes the one-sided Jacobi below converge in a few sweeps.
-// Wg: q x (q + 1) global scratch for the Schur complement when it does not
-// fit in shared memory (null otherwise).
-__global__ void __launch_bounds__(1024) pivoted_cholesky_kernel(const double* G, int q,
-                                                                float* Lc, double* Wg) {
-  extern __shared__ unsigned char pc_smem[];
-  const int ld = q + 1;
-  int* used = reinterpret_cast<int*>(pc_smem);
-  double* W = Wg != nullptr ? Wg
-                            : reinterpret_cast<double*>(pc_smem + ((size_t(q) * 4 + 15) / 16) * 16);
-  __shared__ int s_piv;
-  __shared__ double s_dp;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
-  for (int idx = tid; idx < q * q; idx += blockDim.x) {
-    const int r = idx / q, c = idx - r * q;
-    W[r * ld + c] = G[idx];
-  }
-  for (int i = tid; i < q; i += blockDim.x) used[i] = 0;
-  __syncthreads();
-  int j = 0;
-  for (; j < q; ++j) {
-    if (warp == 0) {
-      double best = -1.0;
-      int bi = -1;
-      for (int i = lane; i < q; i += 32) {
-        const double v = W[i * ld + i];
-        if (!used[i] && v > best) {
-          best = v;
-          bi = i;
-        }
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ob > best || (ob == best && oi >= 0 && (bi < 0 || oi < bi))) {
-          best = ob;
-          bi = oi;
-        }
-      }
-      if (lane == 0) {
-        s_piv = bi;
-        s_dp = best;
-      }
-    }
-    __syncthreads();
-    const int p = s_piv;
-    const double dp = s_dp;
-    if (p < 0 || !(dp > 0.0)) break;  // block-uniform
-    const double* Wp = W + size_t(p) * ld;  // row p = column p (symmetric)
-    const double rs = 1.0 / sqrt(dp);
-    for (int i = tid; i < q; i += blockDim.x)
-      Lc[size_t(j) * q + i] = (used[i] && i != p) ? 0.f : float(Wp[i] * rs);
-    const double rinv = 1.0 / dp;
-    for (int i = warp; i < q; i += nwarps) {
-      if (used[i] || i == p) continue;
-      const double a = Wp[i] * rinv;
-      double* Wi = W + size_t(i) * ld;
-      for (int k = lane; k < q; k += 32)
-        if (!used[k] && k != p) Wi[k] -= a * Wp[k];
-    }
-    __syncthreads();
-    if (tid == 0) used[p] = 1;
-    __syncthreads();
-  }
-  for (size_t idx = size_t(j) * q + tid; idx < size_t(q) * q; idx += blockDim.x) Lc[idx] = 0.f;
-}
-
-// One-sided (Hestenes) Jacobi in FP32 on one CTA, everything in shared
-// memory: the q rows of Mc (the columns x_j of X, length q) are made mutually
-// orthogonal by plane rotations, X V = W.  The singular values are the final
-// row norms and the left singular vectors the normalised final rows; the
-// rotations themselves are not accumulated.  8 threads per pair.
-// Rows are ld = jacobi_ld(q) floats apart with ld = 8 (mod 32): the four
-// 8-thread groups of a warp work on consecutive pair indices, whose rows then
-// start in different bank octets.
+// One-sided (Hestenes) Jacobi in FP32 on one CTA: the q rows of Mc (the
+// columns of M = L^T, length q) are made mutually orthogonal by plane
+// rotations, which are accumulated as rows of Jc.  Singular values are the
+// final row norms; with M = L^T, L = J Sigma W^T, so the left singular
+// vectors of L are the columns of J, orthogonal to working precision (the
+// rotations are), which keeps V = B^T U / s accurate for small s as well.
+// 8 threads per pair.  In shared memory (in_smem != 0) the rows are
+// ld = jacobi_ld(q) floats apart with ld = 8 (mod 32): the four 8-thread
+// groups of a warp work on consecutive pair indices, whose rows then start in
+// different bank octets.  Otherwise Mc and Jc live in the global scratch
+// Wg (2 q x q floats, leading dimension q).
 __host__ __device__ inline int jacobi_ld(int q) { return q + ((8 - q % 32) + 32) % 32; }
 
-// With in_smem == 0 the rows live in Wc_g itself (leading dimension q).
 __global__ void __launch_bounds__(1024) jacobi_onesided_f32_kernel(const float* Mc_g, int q, int pp,
-                                                                   float* Wc_g, float* norms,
+                                                                   float* Jc_g, float* norms,
                                                                    int max_sweeps, float tol,
-                                                                   int* flags, int in_smem) {
+                                                                   int* flags, float* Wg) {
   extern __shared__ float osm[];
+  const bool in_smem = Wg == nullptr;
   const int ld = in_smem ? jacobi_ld(q) : q;
-  float* Mc = in_smem ? osm : Wc_g;
+  float* Mc = in_smem ? osm : Wg;
+  float* Jc = Mc + size_t(q) * ld;
   __shared__ int s_rot;
   for (int idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
     const int r = idx / q, c = idx - r * q;
     Mc[r * ld + c] = Mc_g[idx];
+    Jc[r * ld + c] = (r == c) ? 1.f : 0.f;
   }
   const int npairs = pp / 2;
   const int g = threadIdx.x >> 3, sub = threadIdx.x & 7;  // 128 groups of 8
@@ -382,6 +381,13 @@ __global__ void __launch_bounds__(1024) jacobi_onesided_f32_kernel(const float* 
           a[u] = cs * x - sn * y;
           b[u] = sn * x + cs * y;
         }
+        float* ja = Jc + i * ld;
+        float* jb = Jc + j * ld;
+        for (int u = sub; u < q; u += 8) {
+          const float x = ja[u], y = jb[u];
+          ja[u] = cs * x - sn * y;
+          jb[u] = sn * x + cs * y;
+        }
         if (sub == 0) s_rot = 1;
       }
       __syncthreads();
@@ -395,18 +401,15 @@ __global__ void __launch_bounds__(1024) jacobi_onesided_f32_kernel(const float* 
     for (int t = 0; t < q; ++t) nn = fmaf(Mc[j * ld + t], Mc[j * ld + t], nn);
     norms[j] = sqrtf(nn);
   }
-  if (in_smem) {
-    for (int idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
-      const int r = idx / q, c = idx - r * q;
-      Wc_g[idx] = Mc[r * ld + c];
-    }
+  for (int idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
+    const int r = idx / q, c = idx - r * q;
+    Jc_g[idx] = Jc[r * ld + c];
   }
 }
 
-// Ub[:, r] = w_j / |w_j| for the final Jacobi rows w_j ordered by descending
-// norm, S[r] = |w_j|, inv_s[r] = 1 / S[r] (0 for a zero norm, whose column
-// of Ub is left zero).
-__global__ void sort_singular_kernel(const float* Wc, const float* norms, int q, double* Ub,
+// Ub[:, r] = J[:, order[r]] (J columns stored as rows of Jc), S[r] = norm,
+// inv_s[r] = 1 / S[r] (0 for a zero norm); order by descending norm.
+__global__ void sort_singular_kernel(const float* Jc, const float* norms, int q, double* Ub,
                                      double* S, double* inv_s) {
   for (int j = threadIdx.x; j < q; j += blockDim.x) {
     int rank = 0;
@@ -414,10 +417,15 @@ __global__ void sort_singular_kernel(const float* Wc, const float* norms, int q,
     for (int i = 0; i < q; ++i)
       if (norms[i] > nj || (norms[i] == nj && i < j)) ++rank;
     S[rank] = double(nj);
-    const double inv = nj > 0.f ? 1.0 / double(nj) : 0.0;
-    inv_s[rank] = inv;
-    for (int t = 0; t < q; ++t) Ub[t * q + rank] = double(Wc[j * q + t]) * inv;
+    inv_s[rank] = nj > 0.f ? 1.0 / double(nj) : 0.0;
+    for (int t = 0; t < q; ++t) Ub[t * q + rank] = double(Jc[j * q + t]);
   }
+}
+
+__global__ void f64_to_f32_kernel(const double* x, float* y, int64_t n) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    y[i] = float(x[i]);
 }
 
 // Sets flag bit 1 when max |G - I| exceeds tol (NaN counts as failure).
@@ -817,40 +825,38 @@ void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, dou
               "mixed SVD: needs 1 <= q <= min(n, 1024) (chi + oversampling)");
   Scope scope(c);
   double* G = c.alloc<double>(size_t(q) * q);
-  // working matrices in shared memory up to q = 168, in global memory (L2)
-  // beyond
-  const size_t used_b = (size_t(q) * 4 + 15) / 16 * 16;
-  const size_t wchol = size_t(q) * (q + 1) * sizeof(double);
-  const bool chol_smem = used_b + wchol <= 227 * 1024;
-  double* Wg = chol_smem ? nullptr : c.alloc<double>(size_t(q) * (q + 1));
-  const size_t wjac = size_t(q) * jacobi_ld(int(q)) * sizeof(float);
-  const bool jac_smem = wjac <= 227 * 1024;
-  float* Lc = c.alloc<float>(size_t(q) * q);
-  float* Wc = c.alloc<float>(size_t(q) * q);
+  double* Wk = c.alloc<double>(size_t(q) * (q + 1));
+  double* L = c.alloc<double>(size_t(q) * q);
+  float* Mc = c.alloc<float>(size_t(q) * q);
+  float* Jc = c.alloc<float>(size_t(q) * q);
   float* norms = c.alloc<float>(q);
   double* inv_s = c.alloc<double>(q);
+  int* flags = c.alloc<int>(1);
+  // the Jacobi matrices stay in shared memory up to q = 168, in global
+  // memory (L2) beyond
+  const size_t wjac = size_t(2) * q * jacobi_ld(int(q)) * sizeof(float);
+  const bool jac_smem = wjac <= 227 * 1024;
+  float* Wg = jac_smem ? nullptr : c.alloc<float>(size_t(2) * q * q);
   const int64_t pp = q + (q & 1);
-  // G = B B^T = L L^T in FP64 (pivoted Cholesky, B = L Qb^T with orthonormal
-  // Qb); the spectrum of B is that of L, whose singular values FP32 one-sided
-  // Jacobi on the columns of L resolves with relative accuracy (no squaring):
-  // L V = W = U Sigma, so B = U Sigma (Qb V)^T and Ub = U.
+  // G = B B^T = L L^T in FP64 (B = L Qb^T with orthonormal Qb); the spectrum of
+  // B is that of L, whose singular values FP32 one-sided Jacobi resolves with
+  // relative accuracy (no squaring): L^T J = W Sigma, so B = J Sigma (Qb W)^T.
   einsum(c, "ik,jk->ij", View(B, {q, n}), View(B, {q, n}), View(G, {q, q}));
   if (!c.sizing()) {
-    const size_t csm = used_b + (chol_smem ? wchol : 0);
-    CTM_CUDA(cudaFuncSetAttribute(pivoted_cholesky_kernel,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(csm)));
-    pivoted_cholesky_kernel<<<1, 1024, csm, c.stream>>>(G, int(q), Lc, Wg);
+    CTM_CUDA(cudaMemsetAsync(flags, 0, sizeof(int), c.stream));
+    cholesky<double>(c.stream, G, q, n, 0, Wk, nullptr, L, nullptr, nullptr, flags);
+    // Mc rows = columns of L^T = rows of L (FP32)
+    f64_to_f32_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(L, Mc, q * q);
     CTM_LAUNCH_CHECK();
     const size_t osm = jac_smem ? wjac : 0;
     CTM_CUDA(cudaFuncSetAttribute(jacobi_onesided_f32_kernel,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, int(osm)));
     // FP32 dot products of length q carry ~sqrt(q) u relative error: 4e-6
     // is the smallest coupling the sweeps can drive below
-    jacobi_onesided_f32_kernel<<<1, 1024, osm, c.stream>>>(Lc, int(q), int(pp), Wc, norms, 40,
-                                                           4e-6f, status_flags(c),
-                                                           jac_smem ? 1 : 0);
+    jacobi_onesided_f32_kernel<<<1, 1024, osm, c.stream>>>(Mc, int(q), int(pp), Jc, norms, 40,
+                                                           4e-6f, status_flags(c), Wg);
     CTM_LAUNCH_CHECK();
-    sort_singular_kernel<<<1, 256, 0, c.stream>>>(Wc, norms, int(q), Ub, S, inv_s);
+    sort_singular_kernel<<<1, 256, 0, c.stream>>>(Jc, norms, int(q), Ub, S, inv_s);
     CTM_LAUNCH_CHECK();
   }
   // V = B^T Ub diag(1/s), FP32
