@@ -171,7 +171,8 @@ def call(name, args_before_ws, device, key=None, stream=None):
 
 
 PROFILE_TAGS = {"gett_f64": 0, "tc_gemm": 1, "quarter": 2, "range_finder": 3, "orthonormalize": 4,
-                "svd": 5, "projector_products": 6, "renormalize": 7}
+                "svd": 5, "projector_products": 6, "renormalize": 7, "gett_f32": 8,
+                "tc_gemm_double_layer": 9}
 
 
 def profile_begin():

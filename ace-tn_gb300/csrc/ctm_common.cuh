@@ -57,9 +57,10 @@ enum ProfileTag {
   kTagSvd = 5,
   kTagProject = 6,
   kTagRenorm = 7,
-  kTagGettF32 = 8
+  kTagGettF32 = 8,
+  kTagTcDoubleLayer = 9
 };
-constexpr int kProfileTags = 9;
+constexpr int kProfileTags = 10;
 
 // Brackets one launch with CUDA events while profiling is on; `work` is the
 // algorithmic FLOP (or byte) count of the launch.

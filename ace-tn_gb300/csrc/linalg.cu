@@ -128,39 +128,76 @@ __global__ void __launch_bounds__(LT) householder_qr_kernel(T* Y, int64_t n, int
 // Right-looking elimination on the upper triangle with the pivot division
 // deferred: step j subtracts (W[j][i] / W[j][j]) * row j from every row
 // i > j, so row j ends as d_j * (row j of L_unit^T) with d_j = W[j][j], and
-// L^T[j][c] = W[j][c] / sqrt(d_j).  The steps run in blocks of four pivots.  Both operands of the update are read
-// along rows (lanes over contiguous columns); rows are padded to q + 1
-// elements so the transposed read of the epilogue is conflict-free as well.
-// When Linv is requested the same row operations run on an identity block
-// E, which ends as L_unit^-1, and L^-1 = diag(d)^-1/2 E.
+// L^T[j][c] = W[j][c] / sqrt(d_j).  When Linv is requested the same row
+// operations run on an identity block E, which ends as L_unit^-1, and
+// L^-1 = diag(d)^-1/2 E.
+//
+// The pivots go in blocks of kCholNb: (a) one thread eliminates inside the
+// kCholNb x kCholNb diagonal block and publishes pivots and multipliers;
+// (b) one thread per column applies them to the block's pivot rows (of W and
+// of E) and stores the scaled multipliers S[t][i] = W[J+t][i] / d_t of the
+// rows below; (c) every thread takes 4 x 4 tiles of the trailing rows and
+// subtracts sum_t S[t][i] row_(J+t) with 128-bit shared-memory accesses.
+// W and E are q4 x ld (q4 = q rounded up to kCholNb, ld = q4 + 4) with zero
+// padding, so the pivot rows of the last block and every 4 x 4 tile are in
+// bounds.
+//
 // A pivot that is not positive (numerically semidefinite G) contributes a
 // zero column to L and a zero row to L^-1, and sets bit 1 of *flags.
 // shift_mode 0: none; 1: 11 (n q + q (q + 1)) u tr(G) (Fukaya et al.);
 // 2: 1000 u tr(G) (FP32 stages of the mixed path).
 // Outputs (each may be null): Lout = L (lower, row-major), Linv = L^-1
-// (lower), Lt = L^T (upper).  Wg / Eg are q x (q + 1) global scratch used
-// for W / E when they are not kept in shared memory (smem_w / smem_e == 0).
+// (lower), Lt = L^T (upper).  Wg / Eg are cholesky_scratch(q) elements of
+// global scratch used for W / E when they are not in shared memory.
 constexpr int kCholThreads = 1024;
+constexpr int kCholNb = 8;
 constexpr size_t kSmemOptin = 227 * 1024;
 
+__host__ __device__ inline int chol_q4(int q) { return (q + kCholNb - 1) / kCholNb * kCholNb; }
+__host__ __device__ inline int chol_ld(int q) { return chol_q4(q) + 4; }
+inline size_t cholesky_scratch(int64_t q) { return size_t(chol_q4(int(q))) * chol_ld(int(q)); }
+
 template <class T>
-__global__ void __launch_bounds__(kCholThreads) cholesky_kernel(
+struct Vec4;
+template <>
+struct Vec4<float> {
+  using type = float4;
+};
+template <>
+struct Vec4<double> {
+  using type = double4_32a;
+};
+
+// kPlace: 0 = W and E in global scratch, 1 = W in shared memory, 2 = both
+// in shared memory (a compile-time choice, so shared accesses stay LDS/STS).
+// FP64 tiles need twice the registers: 512 threads for T = double.
+template <class T>
+constexpr int chol_threads() { return sizeof(T) == 8 ? 512 : kCholThreads; }
+
+template <class T, int kPlace>
+__global__ void __launch_bounds__(chol_threads<T>()) cholesky_kernel(
     const T* G, int q, int64_t n, int shift_mode, T* Wg, T* Eg, T* Lout, T* Linv, T* Lt,
-    int* flags, int smem_w, int smem_e) {
-  extern __shared__ unsigned char chol_smem[];
+    int* flags) {
+  using V4 = typename Vec4<T>::type;
+  extern __shared__ __align__(32) unsigned char chol_smem[];
   __shared__ T sh[32];
-  const int ld = q + 1;
-  T* dg = reinterpret_cast<T*>(chol_smem);
-  T* W = smem_w ? dg + q : Wg;
-  T* E = smem_e ? (smem_w ? W + size_t(q) * ld : dg + q) : Eg;
+  __shared__ T s_d[kCholNb];
+  __shared__ T s_mul[kCholNb][kCholNb];
+  __shared__ int s_fail;
+  const int q4 = chol_q4(q), ld = chol_ld(q);
+  T* dg = reinterpret_cast<T*>(chol_smem);              // q4
+  T* S = dg + q4;                                        // kCholNb x ld
+  T* W = kPlace >= 1 ? S + kCholNb * ld : Wg;            // q4 x ld
+  T* E = kPlace == 2 ? W + size_t(q4) * ld : Eg;         // q4 x ld
   const bool want_inv = Linv != nullptr;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int nwarps = blockDim.x >> 5;
+  const int nwarps = blockDim.x >> 5, nth = blockDim.x;
   // trace -> shift (every thread ends with the same value)
   T tr = T(0);
-  for (int i = tid; i < q; i += blockDim.x) tr += G[size_t(i) * q + i];
+  for (int i = tid; i < q; i += nth) tr += G[size_t(i) * q + i];
   tr = warp_sum(tr);
   if (lane == 0) sh[warp] = tr;
+  if (tid == 0) s_fail = 0;
   __syncthreads();
   tr = T(0);
   for (int w = 0; w < nwarps; ++w) tr += sh[w];
@@ -169,109 +206,136 @@ __global__ void __launch_bounds__(kCholThreads) cholesky_kernel(
   if (shift_mode == 1) factor = 11.0 * (double(n) * q + double(q) * (q + 1));
   if (shift_mode == 2) factor = 1000.0;
   const T shift = T(factor * u * double(tr));
-  for (int idx = tid; idx < q * q; idx += blockDim.x) {
-    const int r = idx / q, c = idx - r * q;
-    if (c >= r) W[r * ld + c] = G[idx] + (r == c ? shift : T(0));
-    if (want_inv) E[r * ld + c] = (r == c) ? T(1) : T(0);
+  for (int idx = tid; idx < q4 * ld; idx += nth) {
+    const int r = idx / ld, c = idx - r * ld;
+    W[idx] = (r < q && c < q && c >= r) ? G[size_t(r) * q + c] + (r == c ? shift : T(0)) : T(0);
+    if (want_inv) E[idx] = (r == c) ? T(1) : T(0);
   }
   __syncthreads();
-  // Blocks of kNb pivots: every thread first redoes the elimination inside
-  // the kNb x kNb diagonal block (pivots and multipliers in registers), then
-  // eliminates the block's pivot rows at its own columns of W and E; after a
-  // barrier the rows below take the block's kNb updates at once.  Two
-  // barriers per kNb pivots instead of one per pivot, and kNb FMAs per
-  // read-modify-write of the trailing rows.
-  constexpr int kNb = 4;
-  bool failed = false;
-  for (int J = 0; J < q; J += kNb) {
-    const int jb = min(kNb, q - J);
-    T dpiv[kNb], mul[kNb][kNb];
-    {
-      T blk[kNb][kNb];
+  for (int J = 0; J < q; J += kCholNb) {
+    const int jb = min(kCholNb, q - J);
+    // (a) diagonal block, by one thread with the block in registers (fully
+    //     unrolled: every index is a compile-time constant)
+    if (tid == 0) {
+      T blk[kCholNb][kCholNb];
 #pragma unroll
-      for (int t = 0; t < kNb; ++t)
+      for (int t = 0; t < kCholNb; ++t)
 #pragma unroll
-        for (int u = 0; u < kNb; ++u)
-          blk[t][u] = (t < jb && u < jb && u >= t) ? W[(J + t) * ld + J + u] : T(0);
+        for (int v = 0; v < kCholNb; ++v)
+          blk[t][v] = (v >= t && t < jb && v < jb) ? W[(J + t) * ld + J + v] : T(0);
+      bool fail = false;
 #pragma unroll
-      for (int t = 0; t < kNb; ++t) {
-        dpiv[t] = blk[t][t];
-        const T rinv = (t < jb && dpiv[t] > T(0)) ? T(1) / dpiv[t] : T(0);
+      for (int t = 0; t < kCholNb; ++t) {
+        const T dt = blk[t][t];
+        const bool ok = t < jb && dt > T(0);
+        fail = fail || (t < jb && !ok);
+        s_d[t] = ok ? dt : T(0);
+        const T rinv = ok ? T(1) / dt : T(0);
+        T m[kCholNb];
 #pragma unroll
-        for (int u = 0; u < kNb; ++u) mul[t][u] = u > t ? blk[t][u] * rinv : T(0);
+        for (int v = 0; v < kCholNb; ++v) {
+          m[v] = v > t ? blk[t][v] * rinv : T(0);
+          s_mul[t][v] = m[v];
+        }
 #pragma unroll
-        for (int sr = t + 1; sr < kNb; ++sr)
+        for (int r = t + 1; r < kCholNb; ++r)
 #pragma unroll
-          for (int u = sr; u < kNb; ++u) blk[sr][u] -= mul[t][sr] * blk[t][u];
+          for (int v = r; v < kCholNb; ++v) blk[r][v] -= m[r] * blk[t][v];
+      }
+      if (fail) s_fail = 1;
+    }
+    __syncthreads();
+    // (b) pivot rows at every column, and the scaled multipliers (s_mul is
+    //     read from shared memory: a broadcast, and it keeps registers free)
+    for (int k = J + tid; k < q4; k += nth) {
+      T x[kCholNb];
+#pragma unroll
+      for (int t = 0; t < kCholNb; ++t) x[t] = (J + t <= k) ? W[(J + t) * ld + k] : T(0);
+#pragma unroll
+      for (int t = 0; t < kCholNb; ++t)
+#pragma unroll
+        for (int r = t + 1; r < kCholNb; ++r) x[r] -= s_mul[t][r] * x[t];
+#pragma unroll
+      for (int t = 0; t < kCholNb; ++t) {
+        if (J + t <= k) W[(J + t) * ld + k] = x[t];
+        const T dt = s_d[t];
+        S[t * ld + k] = (k >= J + kCholNb && dt > T(0)) ? x[t] / dt : T(0);
       }
     }
-    if (tid == 0)
-      for (int t = 0; t < jb; ++t)
-        if (!(dpiv[t] > T(0))) failed = true;
-    __syncthreads();  // the diagonal block has been read by every thread
-    for (int k = J + tid; k < q; k += blockDim.x) {
-      T v[kNb];
-#pragma unroll
-      for (int t = 0; t < kNb; ++t) v[t] = (t < jb && J + t <= k) ? W[(J + t) * ld + k] : T(0);
-#pragma unroll
-      for (int t = 0; t < kNb; ++t)
-#pragma unroll
-        for (int sr = t + 1; sr < kNb; ++sr) v[sr] -= mul[t][sr] * v[t];
-#pragma unroll
-      for (int t = 0; t < kNb; ++t)
-        if (t < jb && J + t <= k) W[(J + t) * ld + k] = v[t];
-    }
     if (want_inv) {
-      for (int c = tid; c < J + jb; c += blockDim.x) {
-        T v[kNb];
+      for (int c = tid; c < J + kCholNb && c < q4; c += nth) {
+        T x[kCholNb];
 #pragma unroll
-        for (int t = 0; t < kNb; ++t) v[t] = t < jb ? E[(J + t) * ld + c] : T(0);
+        for (int t = 0; t < kCholNb; ++t) x[t] = E[(J + t) * ld + c];
 #pragma unroll
-        for (int t = 0; t < kNb; ++t)
+        for (int t = 0; t < kCholNb; ++t)
 #pragma unroll
-          for (int sr = t + 1; sr < kNb; ++sr) v[sr] -= mul[t][sr] * v[t];
+          for (int r = t + 1; r < kCholNb; ++r) x[r] -= s_mul[t][r] * x[t];
 #pragma unroll
-        for (int t = 0; t < kNb; ++t)
-          if (t < jb) E[(J + t) * ld + c] = v[t];
+        for (int t = 0; t < kCholNb; ++t) E[(J + t) * ld + c] = x[t];
       }
     }
     __syncthreads();
-    // trailing rows i >= J + jb: row_i -= sum_t (W[J+t][i] / d_t) row_(J+t)
-    const T* P0 = W + J * ld;
-    const T* Q0 = E + J * ld;
-    for (int i = J + jb + warp; i < q; i += nwarps) {
-      T a[kNb];
-#pragma unroll
-      for (int t = 0; t < kNb; ++t)
-        a[t] = (t < jb && dpiv[t] > T(0)) ? P0[t * ld + i] / dpiv[t] : T(0);
-      T* Wi = W + i * ld;
-      for (int k = i + lane; k < q; k += 32) {
-        T acc = Wi[k];
-#pragma unroll
-        for (int t = 0; t < kNb; ++t)
-          if (t < jb) acc -= a[t] * P0[t * ld + k];
-        Wi[k] = acc;
+    // (c) trailing rows i >= J + kCholNb in 4 x 4 tiles:
+    //     W[i][k] -= sum_t S[t][i] W[J+t][k] (k >= i), E[i][c] likewise (c < J + kCholNb)
+    const int i0 = J + kCholNb;
+    const int nbr = i0 < q4 ? (q4 - i0) / 4 : 0;  // tile rows (and columns) of W
+    const int nbc = want_inv ? min(J + kCholNb, q4) / 4 : 0;
+    const int tiles_w = nbr * nbr, tiles = tiles_w + nbr * nbc;
+    for (int tI = tid; tI < tiles; tI += nth) {
+      int bi, col0;
+      T* Dst;
+      const T* Piv;
+      if (tI < tiles_w) {
+        bi = tI / nbr;
+        const int bk = tI - bi * nbr;
+        if (bk < bi) continue;
+        col0 = i0 + 4 * bk;
+        Dst = W;
+        Piv = W + J * ld;
+      } else {
+        const int e = tI - tiles_w;
+        bi = e / nbc;
+        col0 = 4 * (e - bi * nbc);
+        Dst = E;
+        Piv = E + J * ld;
       }
-      if (want_inv) {
-        T* Ei = E + i * ld;
-        for (int c = lane; c < J + jb; c += 32) {
-          T acc = Ei[c];
+      const int row0 = i0 + 4 * bi;
+      T acc[4][4];
 #pragma unroll
-          for (int t = 0; t < kNb; ++t)
-            if (t < jb) acc -= a[t] * Q0[t * ld + c];
-          Ei[c] = acc;
-        }
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = T(0);
+#pragma unroll
+      for (int t = 0; t < kCholNb; ++t) {
+        const V4 a = *reinterpret_cast<const V4*>(S + t * ld + row0);
+        const V4 pv = *reinterpret_cast<const V4*>(Piv + t * ld + col0);
+        const T av[4] = {a.x, a.y, a.z, a.w}, pw[4] = {pv.x, pv.y, pv.z, pv.w};
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) acc[r][c] = fma(av[r], pw[c], acc[r][c]);
+      }
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        V4* d4 = reinterpret_cast<V4*>(Dst + (row0 + r) * ld + col0);
+        V4 w = *d4;
+        w.x -= acc[r][0];
+        w.y -= acc[r][1];
+        w.z -= acc[r][2];
+        w.w -= acc[r][3];
+        *d4 = w;
       }
     }
     __syncthreads();
   }
-  if (tid == 0 && failed) atomicOr(flags, 1);
-  for (int j = tid; j < q; j += blockDim.x) {
+  if (tid == 0 && s_fail) atomicOr(flags, 1);
+  for (int j = tid; j < q; j += nth) {
     const T dj = W[j * ld + j];
     dg[j] = dj > T(0) ? sqrt(dj) : T(0);
   }
   __syncthreads();
-  for (int idx = tid; idx < q * q; idx += blockDim.x) {
+  for (int idx = tid; idx < q * q; idx += nth) {
     const int r = idx / q, c = idx - r * q;
     if (Lout != nullptr) {
       const T dc = dg[c];
@@ -289,20 +353,23 @@ __global__ void __launch_bounds__(kCholThreads) cholesky_kernel(
 }
 
 // Launches cholesky_kernel with W (and E when Linv is wanted) in shared
-// memory whenever they fit.  Wg / Eg: q x (q + 1) scratch, used otherwise.
+// memory whenever they fit.  Wg / Eg: cholesky_scratch(q) elements each,
+// used otherwise.
 template <class T>
 void cholesky(cudaStream_t st, const T* G, int64_t q, int64_t n, int shift_mode, T* Wg, T* Eg,
               T* Lout, T* Linv, T* Lt, int* flags) {
-  const size_t mat = size_t(q) * (q + 1) * sizeof(T);
-  const size_t dgb = size_t(q) * sizeof(T);
-  int smem_w = 0, smem_e = 0;
-  if (dgb + mat <= kSmemOptin) smem_w = 1;
-  if (Linv != nullptr && dgb + 2 * mat <= kSmemOptin) smem_e = 1;
-  const size_t smem = dgb + (smem_w ? mat : 0) + (smem_e ? mat : 0);
-  CTM_CUDA(cudaFuncSetAttribute(cholesky_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(smem)));
-  cholesky_kernel<T><<<1, kCholThreads, smem, st>>>(G, int(q), n, shift_mode, Wg, Eg, Lout,
-                                                     Linv, Lt, flags, smem_w, smem_e);
+  const size_t mat = cholesky_scratch(q) * sizeof(T);
+  const size_t head = (size_t(chol_q4(int(q))) + size_t(kCholNb) * chol_ld(int(q))) * sizeof(T);
+  const int place = (head + 2 * mat <= kSmemOptin) ? 2 : (head + mat <= kSmemOptin ? 1 : 0);
+  const size_t smem = head + (place >= 1 ? mat : 0) + (place == 2 ? mat : 0);
+  auto launch = [&](auto kern) {
+    CTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    kern<<<1, chol_threads<T>(), smem, st>>>(G, int(q), n, shift_mode, Wg, Eg, Lout, Linv, Lt,
+                                             flags);
+  };
+  if (place == 2) launch(cholesky_kernel<T, 2>);
+  else if (place == 1) launch(cholesky_kernel<T, 1>);
+  else launch(cholesky_kernel<T, 0>);
   CTM_LAUNCH_CHECK();
 }
 
@@ -312,30 +379,31 @@ void cholesky(cudaStream_t st, const T* G, int64_t q, int64_t n, int shift_mode,
 // final row norms; with M = L^T, L = J Sigma W^T, so the left singular
 // vectors of L are the columns of J, orthogonal to working precision (the
 // rotations are), which keeps V = B^T U / s accurate for small s as well.
-// 8 threads per pair.  In shared memory (in_smem != 0) the rows are
-// ld = jacobi_ld(q) floats apart with ld = 8 (mod 32): the four 8-thread
-// groups of a warp work on consecutive pair indices, whose rows then start in
-// different bank octets.  Otherwise Mc and Jc live in the global scratch
-// Wg (2 q x q floats, leading dimension q).
-__host__ __device__ inline int jacobi_ld(int q) { return q + ((8 - q % 32) + 32) % 32; }
+// 8 threads per pair, each owning float4 chunks of the two rows: rows are
+// padded with zeros to ld = jacobi_ld(q) (a multiple of 32 floats), so a
+// warp's four groups read four 128-byte row segments per access phase.
+// Mc and Jc live in shared memory (kSmem) or in the global scratch Wg
+// (2 q ld floats).
+__host__ __device__ inline int jacobi_ld(int q) { return (q + 31) / 32 * 32; }
 
+template <bool kSmem>
 __global__ void __launch_bounds__(1024) jacobi_onesided_f32_kernel(const float* Mc_g, int q, int pp,
                                                                    float* Jc_g, float* norms,
                                                                    int max_sweeps, float tol,
                                                                    int* flags, float* Wg) {
-  extern __shared__ float osm[];
-  const bool in_smem = Wg == nullptr;
-  const int ld = in_smem ? jacobi_ld(q) : q;
-  float* Mc = in_smem ? osm : Wg;
+  extern __shared__ __align__(16) float osm[];
+  const int ld = jacobi_ld(q);
+  float* Mc = kSmem ? osm : Wg;  // resolved at compile time: shared loads stay LDS
   float* Jc = Mc + size_t(q) * ld;
   __shared__ int s_rot;
-  for (int idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
-    const int r = idx / q, c = idx - r * q;
-    Mc[r * ld + c] = Mc_g[idx];
-    Jc[r * ld + c] = (r == c) ? 1.f : 0.f;
+  for (int idx = threadIdx.x; idx < q * ld; idx += blockDim.x) {
+    const int r = idx / ld, c = idx - r * ld;
+    Mc[idx] = c < q ? Mc_g[r * q + c] : 0.f;
+    Jc[idx] = (r == c) ? 1.f : 0.f;
   }
   const int npairs = pp / 2;
   const int g = threadIdx.x >> 3, sub = threadIdx.x & 7;  // 128 groups of 8
+  const int nchunk = ld / 32;                               // float4 chunks per thread
   __syncthreads();
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
@@ -356,14 +424,15 @@ __global__ void __launch_bounds__(1024) jacobi_onesided_f32_kernel(const float* 
           j = max(i0, j0);
         }
         const bool active = j < q;
-        float* a = Mc + i * ld;
-        float* b = Mc + (active ? j : i) * ld;
+        float4* a = reinterpret_cast<float4*>(Mc + size_t(i) * ld) + sub;
+        float4* b = reinterpret_cast<float4*>(Mc + size_t(active ? j : i) * ld) + sub;
         float al = 0.f, be = 0.f, ga = 0.f;
         if (active) {
-          for (int t = sub; t < q; t += 8) {
-            al = fmaf(a[t], a[t], al);
-            be = fmaf(b[t], b[t], be);
-            ga = fmaf(a[t], b[t], ga);
+          for (int m = 0; m < nchunk; ++m) {
+            const float4 x = a[8 * m], y = b[8 * m];
+            al = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, al))));
+            be = fmaf(y.x, y.x, fmaf(y.y, y.y, fmaf(y.z, y.z, fmaf(y.w, y.w, be))));
+            ga = fmaf(x.x, y.x, fmaf(x.y, y.y, fmaf(x.z, y.z, fmaf(x.w, y.w, ga))));
           }
         }
         for (int o = 4; o > 0; o >>= 1) {
@@ -376,17 +445,19 @@ __global__ void __launch_bounds__(1024) jacobi_onesided_f32_kernel(const float* 
         const float zeta = (be - al) / (2.f * ga);
         const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
         const float cs = 1.f / sqrtf(1.f + t * t), sn = cs * t;
-        for (int u = sub; u < q; u += 8) {
-          const float x = a[u], y = b[u];
-          a[u] = cs * x - sn * y;
-          b[u] = sn * x + cs * y;
-        }
-        float* ja = Jc + i * ld;
-        float* jb = Jc + j * ld;
-        for (int u = sub; u < q; u += 8) {
-          const float x = ja[u], y = jb[u];
-          ja[u] = cs * x - sn * y;
-          jb[u] = sn * x + cs * y;
+        float4* ja = reinterpret_cast<float4*>(Jc + size_t(i) * ld) + sub;
+        float4* jb = reinterpret_cast<float4*>(Jc + size_t(j) * ld) + sub;
+        for (int m = 0; m < nchunk; ++m) {
+          const float4 x = a[8 * m], y = b[8 * m];
+          a[8 * m] = make_float4(cs * x.x - sn * y.x, cs * x.y - sn * y.y, cs * x.z - sn * y.z,
+                                 cs * x.w - sn * y.w);
+          b[8 * m] = make_float4(sn * x.x + cs * y.x, sn * x.y + cs * y.y, sn * x.z + cs * y.z,
+                                 sn * x.w + cs * y.w);
+          const float4 u = ja[8 * m], v = jb[8 * m];
+          ja[8 * m] = make_float4(cs * u.x - sn * v.x, cs * u.y - sn * v.y, cs * u.z - sn * v.z,
+                                  cs * u.w - sn * v.w);
+          jb[8 * m] = make_float4(sn * u.x + cs * v.x, sn * u.y + cs * v.y, sn * u.z + cs * v.z,
+                                  sn * u.w + cs * v.w);
         }
         if (sub == 0) s_rot = 1;
       }
@@ -670,8 +741,8 @@ void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R) {
   // shifted Cholesky-QR3 with a Householder re-run when the check fails
   T* X2 = c.alloc<T>(size_t(n) * q);
   T* G = c.alloc<T>(size_t(q) * q);
-  T* Wk = c.alloc<T>(size_t(q) * (q + 1));
-  T* Ek = c.alloc<T>(size_t(q) * (q + 1));
+  T* Wk = c.alloc<T>(cholesky_scratch(q));
+  T* Ek = c.alloc<T>(cholesky_scratch(q));
   T* Li = c.alloc<T>(size_t(q) * q);
   T* Lt = c.alloc<T>(size_t(q) * q);
   T* Rt = c.alloc<T>(size_t(q) * q);
@@ -825,7 +896,7 @@ void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, dou
               "mixed SVD: needs 1 <= q <= min(n, 1024) (chi + oversampling)");
   Scope scope(c);
   double* G = c.alloc<double>(size_t(q) * q);
-  double* Wk = c.alloc<double>(size_t(q) * (q + 1));
+  double* Wk = c.alloc<double>(cholesky_scratch(q));
   double* L = c.alloc<double>(size_t(q) * q);
   float* Mc = c.alloc<float>(size_t(q) * q);
   float* Jc = c.alloc<float>(size_t(q) * q);
@@ -836,7 +907,7 @@ void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, dou
   // memory (L2) beyond
   const size_t wjac = size_t(2) * q * jacobi_ld(int(q)) * sizeof(float);
   const bool jac_smem = wjac <= 227 * 1024;
-  float* Wg = jac_smem ? nullptr : c.alloc<float>(size_t(2) * q * q);
+  float* Wg = jac_smem ? nullptr : c.alloc<float>(size_t(2) * q * jacobi_ld(int(q)));
   const int64_t pp = q + (q & 1);
   // G = B B^T = L L^T in FP64 (B = L Qb^T with orthonormal Qb); the spectrum of
   // B is that of L, whose singular values FP32 one-sided Jacobi resolves with
@@ -848,13 +919,17 @@ void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, dou
     // Mc rows = columns of L^T = rows of L (FP32)
     f64_to_f32_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(L, Mc, q * q);
     CTM_LAUNCH_CHECK();
-    const size_t osm = jac_smem ? wjac : 0;
-    CTM_CUDA(cudaFuncSetAttribute(jacobi_onesided_f32_kernel,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(osm)));
     // FP32 dot products of length q carry ~sqrt(q) u relative error: 4e-6
     // is the smallest coupling the sweeps can drive below
-    jacobi_onesided_f32_kernel<<<1, 1024, osm, c.stream>>>(Mc, int(q), int(pp), Jc, norms, 40,
-                                                           4e-6f, status_flags(c), Wg);
+    if (jac_smem) {
+      CTM_CUDA(cudaFuncSetAttribute(jacobi_onesided_f32_kernel<true>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, int(wjac)));
+      jacobi_onesided_f32_kernel<true><<<1, 1024, wjac, c.stream>>>(
+          Mc, int(q), int(pp), Jc, norms, 40, 4e-6f, status_flags(c), nullptr);
+    } else {
+      jacobi_onesided_f32_kernel<false><<<1, 1024, 0, c.stream>>>(
+          Mc, int(q), int(pp), Jc, norms, 40, 4e-6f, status_flags(c), Wg);
+    }
     CTM_LAUNCH_CHECK();
     sort_singular_kernel<<<1, 256, 0, c.stream>>>(Jc, norms, int(q), Ub, S, inv_s);
     CTM_LAUNCH_CHECK();

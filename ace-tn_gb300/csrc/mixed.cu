@@ -170,6 +170,7 @@ QOps quarter_mixed(Ctx& c, const Site& S, int k) {
     lq.ne[1] = E;  lq.ns[1] = D2;
     TcOut out;
     out.add(TcKind::kBf16Hi, o.q_hi, lq).add(TcKind::kBf16Lo, o.q_lo, lq);
+    out.extra_tag = kTagTcDoubleLayer;
     tc_gemm_absmax(c, dl.op(), TcOperand{xh, xl, cc * E, K2, ldx}, x3, out, o.scale);
   }
   transpose_bf16(c, o.q_hi, o.q_lo, rows, cols, o.ld, o.t_hi, o.t_lo, o.ldt);
@@ -290,6 +291,7 @@ void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64
     l.ne[1] = X;  l.ns[1] = D2 * ld4;
     TcOut out;
     out.add(TcKind::kBf16Hi, t3h, l).add(TcKind::kBf16Lo, t3l, l);
+    out.extra_tag = kTagTcDoubleLayer;
     tc_gemm(c, dl.op(), TcOperand{xh, xl, Aa * X, K2, ldx}, x3, out);
   }
   // G3: B4[y][(a,d,D)] = P2[a][d][D][y]

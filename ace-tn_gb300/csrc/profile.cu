@@ -39,7 +39,7 @@ cudaEvent_t take_event() {
 
 KernelTimer::KernelTimer(cudaStream_t s, int tag, double work) : stream_(s) {
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_on) return;
+  if (!g_on || work < 0.0) return;  // negative work: a disabled timer
   active_ = true;
   idx_ = g_records.size();
   Record r{take_event(), take_event(), tag, work};

@@ -24,7 +24,8 @@ namespace {
 
 constexpr int kBM = 128;         // rows of A per CTA (MMA M)
 constexpr int kBK = 64;          // K per stage: 64 BF16 = 128 bytes = one swizzle row
-constexpr int kThreads = 128;    // 4 warps: TMEM lanes 0-127 in the epilogue
+constexpr int kThreads = 256;    // 8 warps: in the epilogue warp w reads TMEM lanes
+                                 // 32 (w % 4) .. +31 for half (w / 4) of the columns
 constexpr uint32_t kTmemCols = 256;
 constexpr int64_t kSpinLimit = 4LL * 1000 * 1000;
 
@@ -57,11 +58,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return done != 0;
 }
 
-// Bounded wait on an mbarrier phase; false when the limit expired.
+// Bounded wait on an mbarrier phase; false when the limit expired.  Polls
+// without sleeping for the first few thousand tries (a pipeline stage turns
+// over in about a microsecond), then backs off.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   for (int64_t i = 0; i < kSpinLimit; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
-    if (i > 32) __nanosleep(64);
+    if (i > 4096) __nanosleep(64);
   }
   return false;
 }
@@ -312,7 +315,14 @@ __global__ void __launch_bounds__(kThreads, 1)
   // tcgen05.ld is warp-collective: decide per warp, never per lane
   ok = __all_sync(0xffffffffu, ok);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const int row = m0 + warp * 32 + lane;
+  const int lane_base = (warp & 3) * 32;
+  const int row = m0 + lane_base + lane;
+  const uint32_t trow = uint32_t(lane_base) << 16;
+  // column slice of this warp: [c_begin, c_end), 16-aligned
+  constexpr int kSlices = kThreads / 128;
+  const int slice_w = ((p.ntile + kSlices - 1) / kSlices + 15) / 16 * 16;
+  const int c_begin = min(p.ntile, (warp >> 2) * slice_w);
+  const int c_end = min(p.ntile, c_begin + slice_w);
   if (p.direct) {
     // column offsets of this tile in every destination (-1 beyond N)
     for (int k = 0; k < p.nd; ++k)
@@ -332,10 +342,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     const float sc = float(scd);
     float amax = 0.f;
     if (ok) {
-      for (int c = 0; c < p.ntile; c += 16) {
+      for (int c = c_begin; c < c_end; c += 16) {
         float v[16];
         __syncwarp();
-        tmem_ld16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c), v);
+        tmem_ld16(tmem + trow + uint32_t(c), v);
         if (mvalid) {
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
@@ -375,9 +385,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   float* out = p.part + (size_t(blockIdx.z) * p.m_pad + row) * p.n_pad + n0;
   if (ok && !p.direct) {
-    for (int c = 0; c < p.ntile; c += 16) {
+    for (int c = c_begin; c < c_end; c += 16) {
       float v[16];
-      tmem_ld16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c), v);
+      __syncwarp();
+      tmem_ld16(tmem + trow + uint32_t(c), v);
       if (row < p.m_pad) {
 #pragma unroll
         for (int j = 0; j < 16; j += 4)
@@ -732,7 +743,10 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   const dim3 grid(static_cast<unsigned>(n_fast ? n_tiles : m_tiles),
                   static_cast<unsigned>(n_fast ? m_tiles : n_tiles), static_cast<unsigned>(splits));
   {
-    KernelTimer timer(c.stream, kTagTcGemm, 2.0 * double(M) * N * K * imode);
+    const double work = 2.0 * double(M) * N * K * imode;
+    KernelTimer timer(c.stream, kTagTcGemm, work);
+    KernelTimer timer2(c.stream, out.extra_tag >= 0 ? out.extra_tag : kTagTcGemm,
+                       out.extra_tag >= 0 ? work : -1.0);
     tc_gemm_kernel<<<grid, kThreads, smem, c.stream>>>(tA, tAl, tB, tBl, p);
     CTM_LAUNCH_CHECK();
   }

@@ -54,6 +54,7 @@ struct TcOut {
   double alpha = 1.0;
   const double* inv_scale = nullptr;   // device scalars: results are divided by *inv_scale
   const double* inv_scale2 = nullptr;  // and by *inv_scale2 when non-null
+  int extra_tag = -1;                  // profiling class timed besides "tensor-core GEMM"
   int nd = 0;
   TcDest d[4];
   TcOut& add(TcKind k, void* p, const TcLayout& l) {

@@ -29,6 +29,10 @@ sys.path.insert(0, ROOT)
 D, CHI, PHYS, OVERSAMPLING, NITER, SEED = 6, 144, 2, 16, 2, 20250
 N_Q = CHI * D * D
 METRIC = "CTMRG moves/s at D=6, chi=144 (Heisenberg, 2x2, half-system rSVD os=16 niter=2)"
+# DRAM bytes (read + write) of one launch of the double-layer contraction GEMM
+# at this workload (M = D^4 = 1296, N = chi^2 = 20736, K = 1296, 3xBF16),
+# from the ncu capture summarised in profiles/tc_gemm_double_layer_d6_chi144.md
+DL_GEMM_TRAFFIC = 118.601472e6 + 70.477312e6
 
 
 def move_flops(D, chi, q, d=2, ny=2, niter=2):
@@ -222,7 +226,6 @@ def run_gb300(args, rank, world, local_rank):
     clocks = ClockSampler(local_rank)
     clocks.start()
     launches0 = gb._abi.kernel_launches()
-    gb._abi.profile_begin()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
     torch.cuda.synchronize(dev)
@@ -234,10 +237,28 @@ def run_gb300(args, rank, world, local_rank):
         ev[i][1].record(stream)
         pos += 1
     torch.cuda.synchronize(dev)
-    prof = gb._abi.profile_end()
     launches = gb._abi.kernel_launches() - launches0
     qr_fallbacks = gb._abi.qr_fallbacks(dev)
     clk = clocks.stop()
+    # per-kernel-class timing (CUDA events inside the library) on a separate,
+    # untimed pass with the rows of each move run one after the other, so
+    # that no two kernels of the pass share the GPU
+    prof_moves = max(1, min(args.steps, 4))
+    mover.concurrent = False
+    pev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(prof_moves)]
+    gb._abi.profile_begin()
+    for i in range(prof_moves):
+        flush.zero_()
+        k, idx = order[pos % len(order)]
+        pev[i][0].record(stream)
+        mover.move(st, k, idx)
+        pev[i][1].record(stream)
+        pos += 1
+    torch.cuda.synchronize(dev)
+    prof = gb._abi.profile_end()
+    prof_move_ms = sum(a.elapsed_time(b) for a, b in pev) / prof_moves
+    mover.concurrent = True
     ms = [a.elapsed_time(b) for a, b in ev]
     total_s = sum(ms) / 1e3
     eager = None
@@ -304,26 +325,30 @@ def run_gb300(args, rank, world, local_rank):
     if rank == 0 and not args.no_compare:
         compare = compare_paths(gb, st, cfg, dev, args.precision)
 
-    gett_ms, gett_flops, gett_n = prof["gett_f64"]
-    tc_ms, tc_flops, tc_n = prof["tc_gemm"]
-    if tc_ms > gett_ms:
-        dom, dom_ms, dom_work, dom_n = "tc_gemm", tc_ms, tc_flops, tc_n
-    else:
-        dom, dom_ms, dom_work, dom_n = "gett_f64", gett_ms, gett_flops, gett_n
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
             peaks = json.load(fh)
     except OSError:
         pass
-    if dom == "tc_gemm":
+    if args.precision == "mixed":
+        # the double-layer contraction GEMMs (enlarged corners and edge
+        # renormalization, 3xBF16 on tcgen05) are the largest kernel class
+        dom_ms, dom_work, dom_n = prof["tc_gemm_double_layer"]
+        dom = "tc_gemm_kernel (double-layer contraction, 3xBF16)"
         peak = peaks.get("bf16_tflops_sustained") or 1700.0
-        peak_src = "MEASURED_PEAKS.json bf16_tflops_sustained" if peaks else "fallback 1.7 PF/s"
+        peak_src = ("MEASURED_PEAKS.json bf16_tflops_sustained" if peaks
+                    else "fallback 1.7 PF/s")
         bound = "tensor"
+        traffic = DL_GEMM_TRAFFIC
     else:
+        dom_ms, dom_work, dom_n = prof["gett_f64"]
+        dom = "gett_kernel<double>"
         peak = fp64_peak_tflops(dev)
-        peak_src = "cuBLAS DGEMM 8192^3 measured by bench.py on this GPU (no FP64 entry in MEASURED_PEAKS.json)"
+        peak_src = ("cuBLAS DGEMM 8192^3 measured by bench.py on this GPU "
+                    "(no FP64 entry in MEASURED_PEAKS.json)")
         bound = "fp64"
+        traffic = None
     achieved = (dom_work / (dom_ms / 1e3)) / 1e12 if dom_ms > 0 else None
     q = CHI + OVERSAMPLING
     line = None
@@ -344,8 +369,15 @@ def run_gb300(args, rank, world, local_rank):
                       / 1e12,
             "roofline": {"bound": bound, "kernel": dom, "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
-                         "traffic": None, "launches": dom_n, "peak_source": peak_src,
-                         "share_of_step": dom_ms / (1e3 * total_s) if total_s else None},
+                         "traffic": traffic, "launches": dom_n, "peak_source": peak_src,
+                         "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                                            "one launch, profiles/tc_gemm_double_layer_d6_chi144.md"
+                                            if traffic else None),
+                         "work_per_launch": dom_work / dom_n if dom_n else None,
+                         "share_of_step": (dom_ms / prof_moves) / prof_move_ms,
+                         "timing": f"CUDA events around each launch, {prof_moves} moves with "
+                                   "the rows run serially (ms_per_step there: "
+                                   f"{prof_move_ms:.2f})"},
             "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
             # graph replays run the captured launches of the eager moves
@@ -355,7 +387,7 @@ def run_gb300(args, rank, world, local_rank):
             "qr_fallbacks_in_timed_moves": qr_fallbacks,
             "eager": eager,
             "comparison": compare,
-            "breakdown_ms_per_step": {k: v[0] / args.steps for k, v in prof.items() if v[2]},
+            "breakdown_ms_per_step": {k: v[0] / prof_moves for k, v in prof.items() if v[2]},
             "clocks": clk,
         }
         if world == 1 and not args.no_cpu_baseline:

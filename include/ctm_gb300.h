@@ -107,7 +107,8 @@ int ctm_qr_fallbacks(unsigned long long* count, ctm_stream_t stream);
  * kernel class: 0 = FP64 contraction (GETT), 1 = tensor-core GEMM; or of a
  * span of stream work: 2 = quarter tensors, 3 = rSVD range finder,
  * 4 = orthonormalization, 5 = Rayleigh-Ritz SVD, 6 = projector products,
- * 7 = boundary renormalization.  No counterpart in the
+ * 7 = boundary renormalization; 9 = the double-layer tensor-core GEMMs of the
+ * mixed enlarged corner and edge renormalization (a subset of 1).  No counterpart in the
  * reference (its benchmarking decorators time whole Python calls). */
 void ctm_profile_begin(void);
 int ctm_profile_end(void);
