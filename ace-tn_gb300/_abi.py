@@ -116,11 +116,15 @@ def check(status, what=""):
     raise RuntimeError(f"[ctm status {status}] {text}")
 
 
-def require_cuda(t, name="tensor"):
+def require_cuda(t, name="tensor", storage=False):
+    """CUDA float64 tensors; site tensors (``storage``) may also be stored in
+    float32, which the library widens on entry (every contraction stays
+    FP64 or mixed as configured) and the caller narrows on write-back."""
     if not isinstance(t, torch.Tensor) or not t.is_cuda:
         raise ValueError(f"{name} must be a CUDA tensor (the gb300 backend has no CPU path)")
-    if t.dtype != torch.float64:
-        raise ValueError(f"{name} must be float64, got {t.dtype}")
+    ok = (torch.float64, torch.float32) if storage else (torch.float64,)
+    if t.dtype not in ok:
+        raise ValueError(f"{name} must be float64{' or float32' if storage else ''}, got {t.dtype}")
 
 
 def ptr(t):
@@ -215,8 +219,9 @@ class SiteRef:
         A = site_tensor["A"]
         C = site_tensor["C"]
         E = site_tensor["E"]
-        require_cuda(A, "A")
-        self.keep = [A.contiguous()]
+        require_cuda(A, "A", storage=True)
+        self.dtype = A.dtype  # storage type of the site (float64 or float32)
+        self.keep = [A.to(torch.float64).contiguous()]
         self.D = A.shape[0]
         self.d = A.shape[4]
         s = CtmSite()
@@ -224,10 +229,10 @@ class SiteRef:
         for k in range(4):
             ck = C[k]
             ek = E[k]
-            require_cuda(ck, f"C[{k}]")
-            require_cuda(ek, f"E[{k}]")
-            ck = ck.contiguous()
-            ek = ek.contiguous()
+            require_cuda(ck, f"C[{k}]", storage=True)
+            require_cuda(ek, f"E[{k}]", storage=True)
+            ck = ck.to(torch.float64).contiguous()
+            ek = ek.to(torch.float64).contiguous()
             self.keep += [ck, ek]
             s.C[k] = ck.data_ptr()
             s.E[k] = ek.data_ptr()

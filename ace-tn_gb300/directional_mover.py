@@ -206,6 +206,7 @@ class DirectionalMover:
                   [ref.pointer, D, d, k, _abi.ptr(p1i), x1i, _abi.ptr(p2j), x2j, _abi.ptr(p2i),
                    x2i, _abi.ptr(p1j), x1j, _abi.ptr(c1), _abi.ptr(c2), _abi.ptr(e3),
                    _abi.PREC[self.precision]], device, key=key)
-        ipeps[s2]["C"][(3 + k) % 4] = c1
-        ipeps[s2]["C"][k] = c2
-        ipeps[s2]["E"][(3 + k) % 4] = e3
+        dt = ipeps[s2]["A"].dtype  # float32 storage keeps its type
+        ipeps[s2]["C"][(3 + k) % 4] = c1.to(dt)
+        ipeps[s2]["C"][k] = c2.to(dt)
+        ipeps[s2]["E"][(3 + k) % 4] = e3.to(dt)

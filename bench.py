@@ -32,7 +32,7 @@ METRIC = "CTMRG moves/s at D=6, chi=144 (Heisenberg, 2x2, half-system rSVD os=16
 # DRAM bytes (read + write) of one launch of the double-layer contraction GEMM
 # at this workload (M = D^4 = 1296, N = chi^2 = 20736, K = 1296, 3xBF16),
 # from the ncu capture summarised in profiles/tc_gemm_double_layer_d6_chi144.md
-DL_GEMM_TRAFFIC = 118.601472e6 + 70.477312e6
+DL_GEMM_TRAFFIC = 118.574848e6 + 70.035968e6
 
 
 def move_flops(D, chi, q, d=2, ny=2, niter=2):
@@ -498,6 +498,44 @@ def fp64_peak_tflops(dev):
     return _FP64_PEAK[dev]
 
 
+def run_profile_case(args):
+    """The small case for kernel captures: a synthetic saturated environment
+    (C, E at chi with seeded normal entries, unit Frobenius norm) and one
+    left move (both projector pairs and both boundary triples), repeated
+    ``--steps`` times, with a few hundred launches in total.  No growth
+    iterations: the spectra are those of random tensors, not of a converged
+    environment (the Jacobi sweep count depends on them)."""
+    import torch
+
+    gb = package()
+    gb.build()
+    dev = torch.device("cuda", 0)
+    g = torch.Generator().manual_seed(SEED)
+    st = gb.IpepsState(2, 2, {"phys": PHYS, "bond": D, "chi": CHI}, dev)
+    ref = gb.random_state(D, CHI, SEED, d=PHYS, device=dev)
+
+    def rnd(*shape):
+        t = torch.randn(*shape, generator=g, dtype=torch.float64)
+        return (t / t.norm()).to(dev)
+
+    for s in ref.site_list:
+        st[s] = {"A": ref[s]["A"], "C": [rnd(CHI, CHI) for _ in range(4)],
+                 "E": [rnd(CHI, CHI, D, D) for _ in range(4)]}
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(SEED)
+    cfg = gb.CTMRGConfig(projectors="half-system", svd_type="rsvd",
+                         rsvd_oversampling=OVERSAMPLING, rsvd_niter=NITER, svd_cutoff=1e-12,
+                         precision=args.precision, disable_progressbar=True)
+    mover = gb.DirectionalMover(cfg, omega_source=lambda n, q, device: torch.randn(
+        n, q, dtype=torch.float64, device=device, generator=gen))
+    mover.concurrent = False
+    for _ in range(args.steps):
+        mover.move(st, 0, 0)
+    torch.cuda.synchronize(dev)
+    return {"profile_case": "left move on a synthetic chi-saturated state", "moves": args.steps,
+            "device_status": gb._abi.device_status()}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -511,7 +549,13 @@ def main():
                     help="skip the FP64-path timing and the one-move accuracy check")
     ap.add_argument("--cpu-moves", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run --steps moves on a synthetic saturated state and exit "
+                         "(the small case for ncu kernel captures; prints no bench line)")
     args = ap.parse_args()
+    if args.profile_case:
+        print(json.dumps(run_profile_case(args)), flush=True)
+        return
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     world = int(os.environ.get("WORLD_SIZE", "1"))
