@@ -402,18 +402,18 @@ __global__ void __launch_bounds__(1024) jacobi_onesided_f32_kernel(const float* 
     Jc[idx] = (r == c) ? 1.f : 0.f;
   }
   const int npairs = pp / 2;
-  const int g = threadIdx.x >> 3, sub = threadIdx.x & 7;  // 128 groups of 8
+  const int g = threadIdx.x >> 3, sub = threadIdx.x & 7;  // groups of 8 threads
+  const int ngroups = blockDim.x >> 3;
   const int nchunk = ld / 32;                               // float4 chunks per thread
   __syncthreads();
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
     if (threadIdx.x == 0) s_rot = 0;
-    __syncthreads();
     for (int r = 0; r < pp - 1; ++r) {
       // every warp runs the same number of trips (groups of 8 threads whose
       // pair index is out of range compute zeros), so the full-mask shuffles
       // below always see all 32 lanes
-      for (int kb = 0; kb < npairs; kb += 128) {
+      for (int kb = 0; kb < npairs; kb += ngroups) {
         const int k = kb + g;
         int i = 0, j = q;
         if (k < npairs) {
@@ -501,15 +501,18 @@ __global__ void f64_to_f32_kernel(const double* x, float* y, int64_t n) {
 
 // Sets flag bit 1 when max |G - I| exceeds tol (NaN counts as failure).
 template <class T>
-__global__ void orthogonality_check_kernel(const T* G, int64_t q, double tol, int* flags) {
+__global__ void __launch_bounds__(1024) orthogonality_check_kernel(const T* G, int q, T tol,
+                                                                   int* flags) {
   __shared__ int bad;
   if (threadIdx.x == 0) bad = 0;
   __syncthreads();
-  for (int64_t idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
-    const int64_t r = idx / q, c = idx % q;
-    const double e = fabs(double(G[idx]) - (r == c ? 1.0 : 0.0));
-    if (!(e <= tol)) bad = 1;
+  bool local = false;
+  for (int idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
+    const int r = idx / q, c = idx - r * q;
+    const T e = fabs(G[idx] - (r == c ? T(1) : T(0)));
+    local = local || !(e <= tol);
   }
+  if (local) bad = 1;
   __syncthreads();
   if (threadIdx.x == 0 && bad) atomicOr(flags, 1);
 }
@@ -755,12 +758,14 @@ void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R) {
   }
   T* cur = Y;
   T* nxt = X2;
-  // FP64: shifted Cholesky-QR3.  FP32: two shifted stages (each divides the
-  // condition number by ~1e2, down from cond(Y) up to ~1e8) and two plain
-  // ones, so the power-iteration bases of the mixed range finder come out
-  // orthonormal without the one-CTA Householder fallback.
-  const int stages = sizeof(T) == 8 ? 3 : 4;
-  const int shifted_stages = sizeof(T) == 8 ? 1 : 2;
+  // Shifted Cholesky-QR3 in both precisions: one shifted stage (FP32 shift
+  // 1000 u tr(G): the result has cond <= ~1e2 whenever cond(Y) < 1/u) and two
+  // plain ones.  The mixed range finder orthonormalises after every half
+  // step, so its bases have the condition number of Q1 Q4 restricted to the
+  // subspace (<= ~1e5 at D=6 chi=144), well inside that range; the check
+  // below catches anything else.
+  const int stages = 3;
+  const int shifted_stages = 1;
   for (int stage = 0; stage < stages; ++stage) {
     einsum(c, "ia,ib->ab", ViewT<T>(cur, {n, q}), ViewT<T>(cur, {n, q}), ViewT<T>(G, {q, q}));
     const int mode = stage < shifted_stages ? (sizeof(T) == 8 ? 1 : 2) : 0;
@@ -785,8 +790,8 @@ void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R) {
   einsum(c, "ia,ib->ab", ViewT<T>(cur, {n, q}), ViewT<T>(cur, {n, q}), ViewT<T>(G, {q, q}));
   T* hv = c.alloc<T>(size_t(n) * q);
   if (c.sizing()) return;
-  orthogonality_check_kernel<T><<<1, LT, 0, c.stream>>>(G, q, sizeof(T) == 8 ? 1e-11 : 2e-4,
-                                                     flags);
+  orthogonality_check_kernel<T><<<1, 1024, 0, c.stream>>>(G, int(q), T(sizeof(T) == 8 ? 1e-11 : 2e-4),
+                                                       flags);
   CTM_LAUNCH_CHECK();
   if (cur != Y)
     CTM_CUDA(cudaMemcpyAsync(Y, cur, sizeof(T) * n * q, cudaMemcpyDeviceToDevice, c.stream));
@@ -906,7 +911,7 @@ void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, dou
   // the Jacobi matrices stay in shared memory up to q = 168, in global
   // memory (L2) beyond
   const size_t wjac = size_t(2) * q * jacobi_ld(int(q)) * sizeof(float);
-  const bool jac_smem = wjac <= 227 * 1024;
+  const bool jac_smem = wjac <= (227 - 1) * 1024;
   float* Wg = jac_smem ? nullptr : c.alloc<float>(size_t(2) * q * jacobi_ld(int(q)));
   const int64_t pp = q + (q & 1);
   // G = B B^T = L L^T in FP64 (B = L Qb^T with orthonormal Qb); the spectrum of
@@ -920,14 +925,17 @@ void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, dou
     f64_to_f32_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(L, Mc, q * q);
     CTM_LAUNCH_CHECK();
     // FP32 dot products of length q carry ~sqrt(q) u relative error: 4e-6
-    // is the smallest coupling the sweeps can drive below
+    // is the smallest coupling the sweeps can drive below.  One group of 8
+    // threads per pair of a round (no idle warps at the round barriers).
+    const unsigned jthreads =
+        unsigned(std::min<int64_t>(1024, ((pp / 2) * 8 + 31) / 32 * 32));
     if (jac_smem) {
       CTM_CUDA(cudaFuncSetAttribute(jacobi_onesided_f32_kernel<true>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, int(wjac)));
-      jacobi_onesided_f32_kernel<true><<<1, 1024, wjac, c.stream>>>(
+      jacobi_onesided_f32_kernel<true><<<1, jthreads, wjac, c.stream>>>(
           Mc, int(q), int(pp), Jc, norms, 40, 4e-6f, status_flags(c), nullptr);
     } else {
-      jacobi_onesided_f32_kernel<false><<<1, 1024, 0, c.stream>>>(
+      jacobi_onesided_f32_kernel<false><<<1, jthreads, 0, c.stream>>>(
           Mc, int(q), int(pp), Jc, norms, 40, 4e-6f, status_flags(c), Wg);
     }
     CTM_LAUNCH_CHECK();

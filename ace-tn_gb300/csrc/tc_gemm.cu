@@ -23,7 +23,8 @@ namespace ctm {
 namespace {
 
 constexpr int kBM = 128;         // rows of A per CTA (MMA M)
-constexpr int kBK = 64;          // K per stage: 64 BF16 = 128 bytes = one swizzle row
+// K per stage: 64 BF16 (128-byte rows, 128-byte swizzle); the kernel and the
+// tensor maps also take 32 (64-byte rows, 64-byte swizzle).
 constexpr int kThreads = 256;    // 8 warps: in the epilogue warp w reads TMEM lanes
                                  // 32 (w % 4) .. +31 for half (w / 4) of the columns
 constexpr uint32_t kTmemCols = 256;
@@ -78,15 +79,16 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle,
-// 8-row core-matrix groups 1024 bytes apart.
-__device__ __forceinline__ uint64_t smem_desc(const void* p) {
+// Shared-memory matrix descriptor: K-major operand with rows of bk BF16
+// (bk = 64: 128-byte swizzle; bk = 32: 64-byte swizzle), 8-row core-matrix
+// groups 8 * 2 * bk bytes apart.
+__device__ __forceinline__ uint64_t smem_desc(const void* p, int bk) {
   const uint64_t addr = smem_u32(p);
-  uint64_t d = (addr >> 4) & 0x3FFFull;  // start address
-  d |= uint64_t(1) << 16;                // leading byte offset (unused with 128B swizzle)
-  d |= uint64_t(1024 >> 4) << 32;        // stride byte offset
-  d |= uint64_t(1) << 46;                // descriptor version (tcgen05)
-  d |= uint64_t(2) << 61;                // SWIZZLE_128B
+  uint64_t d = (addr >> 4) & 0x3FFFull;              // start address
+  d |= uint64_t(1) << 16;                            // leading byte offset (unused when swizzled)
+  d |= uint64_t((16 * bk) >> 4) << 32;               // stride byte offset
+  d |= uint64_t(1) << 46;                            // descriptor version (tcgen05)
+  d |= uint64_t(bk == 64 ? 2 : 4) << 61;             // SWIZZLE_128B / SWIZZLE_64B
   return d;
 }
 
@@ -192,6 +194,7 @@ __device__ __forceinline__ void store4(const TcDest& d, int64_t off, const float
 
 struct GemmParams {
   int ntile;         // MMA N (multiple of 16, <= 256)
+  int bk;            // K per stage (64 or 32)
   int kb_total;      // 64-wide K blocks
   int kb_per_split;
   int stages;
@@ -218,8 +221,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   extern __shared__ uint8_t dyn_smem[];
   uint8_t* base = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(dyn_smem) + 1023) & ~uintptr_t(1023));
-  const uint32_t a_bytes = kBM * kBK * 2;
-  const uint32_t b_bytes = uint32_t(p.ntile) * kBK * 2;
+  const int bk = p.bk;
+  const uint32_t a_bytes = kBM * bk * 2;
+  const uint32_t b_bytes = uint32_t(p.ntile) * bk * 2;
   const uint32_t half_bytes = a_bytes + b_bytes;
   const uint32_t stage_bytes = half_bytes * (p.mode == 3 ? 2 : 1);
   uint64_t* full = reinterpret_cast<uint64_t*>(base + size_t(p.stages) * stage_bytes);
@@ -270,7 +274,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       uint8_t* st = base + size_t(s) * stage_bytes;
       mbar_expect_tx(&full[s], stage_bytes);
-      const int x = (kb0 + i) * kBK;
+      const int x = (kb0 + i) * bk;
       tma_load_2d(st, &tA, x, m0, &full[s]);
       tma_load_2d(st + a_bytes, &tB, x, n0, &full[s]);
       if (p.mode == 3) {
@@ -292,13 +296,13 @@ __global__ void __launch_bounds__(kThreads, 1)
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       uint8_t* st = base + size_t(s) * stage_bytes;
 #pragma unroll
-      for (int kk = 0; kk < kBK / 16; ++kk) {
-        const uint64_t ah = smem_desc(st + kk * 32);
-        const uint64_t bh = smem_desc(st + a_bytes + kk * 32);
+      for (int kk = 0; kk < bk / 16; ++kk) {
+        const uint64_t ah = smem_desc(st + kk * 32, bk);
+        const uint64_t bh = smem_desc(st + a_bytes + kk * 32, bk);
         mma_bf16(tmem, ah, bh, idesc, (i > 0 || kk > 0) ? 1u : 0u);
         if (p.mode == 3) {
-          const uint64_t al = smem_desc(st + half_bytes + kk * 32);
-          const uint64_t bl = smem_desc(st + half_bytes + a_bytes + kk * 32);
+          const uint64_t al = smem_desc(st + half_bytes + kk * 32, bk);
+          const uint64_t bl = smem_desc(st + half_bytes + a_bytes + kk * 32, bk);
           mma_bf16(tmem, ah, bl, idesc, 1u);
           mma_bf16(tmem, al, bh, idesc, 1u);
         }
@@ -519,19 +523,20 @@ EncodeTiledFn encode_tiled() {
 }
 
 void make_map(CUtensorMap* map, const bf16* ptr, int64_t rows, int64_t k, int64_t ld,
-              uint32_t box_rows) {
+              uint32_t box_rows, int bk) {
   CTM_REQUIRE(ptr != nullptr, CTM_ERR_INVALID, "tc_gemm: operand pointer is NULL");
   CTM_REQUIRE((reinterpret_cast<uintptr_t>(ptr) & 15) == 0, CTM_ERR_INVALID,
               "tc_gemm: operand must be 16-byte aligned");
   CTM_REQUIRE(ld % 8 == 0 && ld >= k, CTM_ERR_INVALID, "tc_gemm: leading dimension");
   const cuuint64_t dims[2] = {cuuint64_t(k), cuuint64_t(rows)};
   const cuuint64_t strides[1] = {cuuint64_t(ld) * 2};
-  const cuuint32_t box[2] = {uint32_t(kBK), box_rows};
+  const cuuint32_t box[2] = {uint32_t(bk), box_rows};
   const cuuint32_t estr[2] = {1, 1};
   const CUresult res = encode_tiled()(
       map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(ptr), dims, strides, box, estr,
-      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      CU_TENSOR_MAP_INTERLEAVE_NONE,
+      bk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   CTM_REQUIRE(res == CUDA_SUCCESS, CTM_ERR_CUDA,
               "cuTensorMapEncodeTiled failed with code " + std::to_string(int(res)));
 }
@@ -679,7 +684,11 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   int ntile = static_cast<int>(((N + n_tiles - 1) / n_tiles + 15) / 16 * 16);
   ntile = std::max(ntile, 16);
   const int64_t m_tiles = (M + kBM - 1) / kBM;
-  const int kb_total = static_cast<int>((K + kBK - 1) / kBK);
+  // 64-wide K steps: measured faster than 32-wide ones with a deeper ring
+  // (64-byte swizzle) even where only two 3xBF16 stages fit (the double-layer
+  // GEMM at D=6: 373 us against 469 us)
+  const int bk = 64;
+  const int kb_total = static_cast<int>((K + bk - 1) / bk);
   const int64_t base_ctas = m_tiles * n_tiles;
   const int sms = sm_count();
   // split K so that the grid fills the SMs in one wave: a partial second wave
@@ -693,7 +702,7 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   const bool direct = splits == 1;
   const int m_pad = static_cast<int>(m_tiles * kBM);
   const int n_pad = static_cast<int>(n_tiles * ntile);
-  const uint32_t stage_bytes = uint32_t(kBM * kBK * 2 + ntile * kBK * 2) * (imode == 3 ? 2 : 1);
+  const uint32_t stage_bytes = uint32_t(kBM * bk * 2 + ntile * bk * 2) * (imode == 3 ? 2 : 1);
   // dynamic shared memory: the stage ring (the kernel's static arrays take ~8 KB)
   const int stages = std::max(2, std::min(6, int((210 * 1024) / stage_bytes)));
   const size_t smem = size_t(stages) * stage_bytes + 256 + 1024;
@@ -708,17 +717,18 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   CTM_REQUIRE(m_tiles <= 0x7fffffff && n_tiles <= 65535 && splits <= 65535, CTM_ERR_UNSUPPORTED,
               "tc_gemm: grid too large");
   CUtensorMap tA, tAl, tB, tBl;
-  make_map(&tA, A.hi, A.rows, K, A.ld, kBM);
-  make_map(&tB, B.hi, B.rows, K, B.ld, uint32_t(ntile));
+  make_map(&tA, A.hi, A.rows, K, A.ld, kBM, bk);
+  make_map(&tB, B.hi, B.rows, K, B.ld, uint32_t(ntile), bk);
   if (imode == 3) {
-    make_map(&tAl, A.lo, A.rows, K, A.ld, kBM);
-    make_map(&tBl, B.lo, B.rows, K, B.ld, uint32_t(ntile));
+    make_map(&tAl, A.lo, A.rows, K, A.ld, kBM, bk);
+    make_map(&tBl, B.lo, B.rows, K, B.ld, uint32_t(ntile), bk);
   } else {
     tAl = tA;
     tBl = tB;
   }
   GemmParams p{};
   p.ntile = ntile;
+  p.bk = bk;
   p.kb_total = kb_total;
   p.kb_per_split = kb_per_split;
   p.stages = stages;
