@@ -386,8 +386,12 @@ void cholesky(cudaStream_t st, const T* G, int64_t q, int64_t n, int shift_mode,
 // (2 q ld floats).
 __host__ __device__ inline int jacobi_ld(int q) { return (q + 31) / 32 * 32; }
 
-template <bool kSmem>
-__global__ void __launch_bounds__(1024) jacobi_onesided_f32_kernel(const float* Mc_g, int q, int pp,
+// kCh > 0: rows of kCh float4 chunks per thread (ld = 32 kCh), held in
+// registers between the dot products and the rotation; kCh = 0: any ld,
+// rows re-read from memory.
+// (q <= 32 kCh gives at most 16 kCh pairs: 128 kCh threads.)
+template <bool kSmem, int kCh>
+__global__ void __launch_bounds__(kCh > 0 ? 128 * kCh : 1024) jacobi_onesided_f32_kernel(const float* Mc_g, int q, int pp,
                                                                    float* Jc_g, float* norms,
                                                                    int max_sweeps, float tol,
                                                                    int* flags, float* Wg) {
@@ -404,11 +408,12 @@ __global__ void __launch_bounds__(1024) jacobi_onesided_f32_kernel(const float* 
   const int npairs = pp / 2;
   const int g = threadIdx.x >> 3, sub = threadIdx.x & 7;  // groups of 8 threads
   const int ngroups = blockDim.x >> 3;
-  const int nchunk = ld / 32;                               // float4 chunks per thread
+  const int nchunk = kCh > 0 ? kCh : ld / 32;               // float4 chunks per thread
   __syncthreads();
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
     if (threadIdx.x == 0) s_rot = 0;
+    __syncthreads();
     for (int r = 0; r < pp - 1; ++r) {
       // every warp runs the same number of trips (groups of 8 threads whose
       // pair index is out of range compute zeros), so the full-mask shuffles
@@ -426,13 +431,30 @@ __global__ void __launch_bounds__(1024) jacobi_onesided_f32_kernel(const float* 
         const bool active = j < q;
         float4* a = reinterpret_cast<float4*>(Mc + size_t(i) * ld) + sub;
         float4* b = reinterpret_cast<float4*>(Mc + size_t(active ? j : i) * ld) + sub;
+        constexpr int kR = kCh > 0 ? kCh : 1;
+        float4 xa[kR], xb[kR];
         float al = 0.f, be = 0.f, ga = 0.f;
         if (active) {
-          for (int m = 0; m < nchunk; ++m) {
-            const float4 x = a[8 * m], y = b[8 * m];
-            al = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, al))));
-            be = fmaf(y.x, y.x, fmaf(y.y, y.y, fmaf(y.z, y.z, fmaf(y.w, y.w, be))));
-            ga = fmaf(x.x, y.x, fmaf(x.y, y.y, fmaf(x.z, y.z, fmaf(x.w, y.w, ga))));
+          if (kCh > 0) {
+#pragma unroll
+            for (int m = 0; m < kR; ++m) {
+              xa[m] = a[8 * m];
+              xb[m] = b[8 * m];
+            }
+#pragma unroll
+            for (int m = 0; m < kR; ++m) {
+              const float4 x = xa[m], y = xb[m];
+              al = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, al))));
+              be = fmaf(y.x, y.x, fmaf(y.y, y.y, fmaf(y.z, y.z, fmaf(y.w, y.w, be))));
+              ga = fmaf(x.x, y.x, fmaf(x.y, y.y, fmaf(x.z, y.z, fmaf(x.w, y.w, ga))));
+            }
+          } else {
+            for (int m = 0; m < nchunk; ++m) {
+              const float4 x = a[8 * m], y = b[8 * m];
+              al = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, al))));
+              be = fmaf(y.x, y.x, fmaf(y.y, y.y, fmaf(y.z, y.z, fmaf(y.w, y.w, be))));
+              ga = fmaf(x.x, y.x, fmaf(x.y, y.y, fmaf(x.z, y.z, fmaf(x.w, y.w, ga))));
+            }
           }
         }
         for (int o = 4; o > 0; o >>= 1) {
@@ -447,17 +469,29 @@ __global__ void __launch_bounds__(1024) jacobi_onesided_f32_kernel(const float* 
         const float cs = 1.f / sqrtf(1.f + t * t), sn = cs * t;
         float4* ja = reinterpret_cast<float4*>(Jc + size_t(i) * ld) + sub;
         float4* jb = reinterpret_cast<float4*>(Jc + size_t(j) * ld) + sub;
-        for (int m = 0; m < nchunk; ++m) {
-          const float4 x = a[8 * m], y = b[8 * m];
-          a[8 * m] = make_float4(cs * x.x - sn * y.x, cs * x.y - sn * y.y, cs * x.z - sn * y.z,
-                                 cs * x.w - sn * y.w);
-          b[8 * m] = make_float4(sn * x.x + cs * y.x, sn * x.y + cs * y.y, sn * x.z + cs * y.z,
-                                 sn * x.w + cs * y.w);
-          const float4 u = ja[8 * m], v = jb[8 * m];
-          ja[8 * m] = make_float4(cs * u.x - sn * v.x, cs * u.y - sn * v.y, cs * u.z - sn * v.z,
-                                  cs * u.w - sn * v.w);
-          jb[8 * m] = make_float4(sn * u.x + cs * v.x, sn * u.y + cs * v.y, sn * u.z + cs * v.z,
-                                  sn * u.w + cs * v.w);
+        auto rot = [&](float4* pa, float4* pb, const float4 x, const float4 y) {
+          *pa = make_float4(cs * x.x - sn * y.x, cs * x.y - sn * y.y, cs * x.z - sn * y.z,
+                            cs * x.w - sn * y.w);
+          *pb = make_float4(sn * x.x + cs * y.x, sn * x.y + cs * y.y, sn * x.z + cs * y.z,
+                            sn * x.w + cs * y.w);
+        };
+        if (kCh > 0) {
+          float4 u[kR], v[kR];
+#pragma unroll
+          for (int m = 0; m < kR; ++m) {
+            u[m] = ja[8 * m];
+            v[m] = jb[8 * m];
+          }
+#pragma unroll
+          for (int m = 0; m < kR; ++m) {
+            rot(a + 8 * m, b + 8 * m, xa[m], xb[m]);
+            rot(ja + 8 * m, jb + 8 * m, u[m], v[m]);
+          }
+        } else {
+          for (int m = 0; m < nchunk; ++m) {
+            rot(a + 8 * m, b + 8 * m, a[8 * m], b[8 * m]);
+            rot(ja + 8 * m, jb + 8 * m, ja[8 * m], jb[8 * m]);
+          }
         }
         if (sub == 0) s_rot = 1;
       }
@@ -930,12 +964,21 @@ void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, dou
     const unsigned jthreads =
         unsigned(std::min<int64_t>(1024, ((pp / 2) * 8 + 31) / 32 * 32));
     if (jac_smem) {
-      CTM_CUDA(cudaFuncSetAttribute(jacobi_onesided_f32_kernel<true>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, int(wjac)));
-      jacobi_onesided_f32_kernel<true><<<1, jthreads, wjac, c.stream>>>(
-          Mc, int(q), int(pp), Jc, norms, 40, 4e-6f, status_flags(c), nullptr);
+      auto launch = [&](auto kern) {
+        CTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(wjac)));
+        kern<<<1, jthreads, wjac, c.stream>>>(Mc, int(q), int(pp), Jc, norms, 40, 4e-6f,
+                                             status_flags(c), nullptr);
+      };
+      switch (jacobi_ld(int(q)) / 32) {
+        case 1: launch(jacobi_onesided_f32_kernel<true, 1>); break;
+        case 2: launch(jacobi_onesided_f32_kernel<true, 2>); break;
+        case 3: launch(jacobi_onesided_f32_kernel<true, 3>); break;
+        case 4: launch(jacobi_onesided_f32_kernel<true, 4>); break;
+        case 5: launch(jacobi_onesided_f32_kernel<true, 5>); break;
+        default: launch(jacobi_onesided_f32_kernel<true, 0>); break;
+      }
     } else {
-      jacobi_onesided_f32_kernel<false><<<1, jthreads, 0, c.stream>>>(
+      jacobi_onesided_f32_kernel<false, 0><<<1, jthreads, 0, c.stream>>>(
           Mc, int(q), int(pp), Jc, norms, 40, 4e-6f, status_flags(c), Wg);
     }
     CTM_LAUNCH_CHECK();
