@@ -182,6 +182,7 @@ __global__ void __launch_bounds__(chol_threads<T>()) cholesky_kernel(
   extern __shared__ __align__(32) unsigned char chol_smem[];
   __shared__ T sh[32];
   __shared__ T s_d[kCholNb];
+  __shared__ T s_rd[kCholNb];
   __shared__ T s_mul[kCholNb][kCholNb];
   __shared__ int s_fail;
   const int q4 = chol_q4(q), ld = chol_ld(q);
@@ -231,6 +232,7 @@ __global__ void __launch_bounds__(chol_threads<T>()) cholesky_kernel(
         fail = fail || (t < jb && !ok);
         s_d[t] = ok ? dt : T(0);
         const T rinv = ok ? T(1) / dt : T(0);
+        s_rd[t] = rinv;
         T m[kCholNb];
 #pragma unroll
         for (int v = 0; v < kCholNb; ++v) {
@@ -258,8 +260,7 @@ __global__ void __launch_bounds__(chol_threads<T>()) cholesky_kernel(
 #pragma unroll
       for (int t = 0; t < kCholNb; ++t) {
         if (J + t <= k) W[(J + t) * ld + k] = x[t];
-        const T dt = s_d[t];
-        S[t * ld + k] = (k >= J + kCholNb && dt > T(0)) ? x[t] / dt : T(0);
+        S[t * ld + k] = k >= J + kCholNb ? x[t] * s_rd[t] : T(0);
       }
     }
     if (want_inv) {

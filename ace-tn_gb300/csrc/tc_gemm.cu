@@ -25,6 +25,11 @@ namespace {
 constexpr int kBM = 128;         // rows of A per CTA (MMA M)
 // K per stage: 64 BF16 (128-byte rows, 128-byte swizzle); the kernel and the
 // tensor maps also take 32 (64-byte rows, 64-byte swizzle).
+// Clusters sharing B tiles (multicast) are built and tested but off: on the
+// double-layer GEMM at D=6 they measured slower (451 us against 373 us with
+// 256-wide tiles), the lockstep of the cluster costing more than the halved
+// operand stream saves.
+constexpr bool kClusterB = false;
 constexpr int kThreads = 256;    // 8 warps: in the epilogue warp w reads TMEM lanes
                                  // 32 (w % 4) .. +31 for half (w / 4) of the columns
 constexpr uint32_t kTmemCols = 256;
@@ -59,6 +64,29 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return done != 0;
 }
 
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n"
+      " .reg .pred P1;\n"
+      " mbarrier.test_wait.parity.shared::cta.b64 P1, [%1], %2;\n"
+      " selp.b32 %0, 1, 0, P1;\n"
+      "}\n"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Bounded wait of the single producer / MMA thread on a pipeline barrier:
+// a non-blocking test in a tight loop (no suspension, so the thread resumes
+// as soon as the phase flips); gives up after about 0.1 s.
+__device__ __forceinline__ bool mbar_wait_spin(uint64_t* bar, uint32_t parity) {
+  for (int64_t i = 0; i < 8 * kSpinLimit; ++i)
+    if (mbar_test_wait(bar, parity)) return true;
+  return false;
+}
+
 // Bounded wait on an mbarrier phase; false when the limit expired.  Polls
 // without sleeping for the first few thousand tries (a pipeline stage turns
 // over in about a microsecond), then backs off.
@@ -77,6 +105,29 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
       : "memory");
+}
+
+// The same box landing at the same shared-memory offset in every CTA of
+// ctaMask (thread-block cluster), each CTA's barrier at that offset receiving
+// its bytes.
+__device__ __forceinline__ void tma_load_2d_mc(void* dst, const CUtensorMap* map, int x, int y,
+                                               uint64_t* bar, uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      ".multicast::cluster [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar)), "h"(mask)
+      : "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" :::
+                   "memory");
 }
 
 // Shared-memory matrix descriptor: K-major operand with rows of bk BF16
@@ -114,6 +165,16 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                    smem_u32(bar))
                : "memory");
+}
+
+// Completion of this CTA's MMAs signalled on the barrier at the same offset
+// in every CTA of mask.
+__device__ __forceinline__ void mma_commit_mc(uint64_t* bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64"
+      " [%0], %1;" ::"r"(smem_u32(bar)),
+      "h"(mask)
+      : "memory");
 }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
@@ -195,6 +256,7 @@ __device__ __forceinline__ void store4(const TcDest& d, int64_t off, const float
 struct GemmParams {
   int ntile;         // MMA N (multiple of 16, <= 256)
   int bk;            // K per stage (64 or 32)
+  int cx;            // CTAs per cluster along M sharing each B tile (1: no cluster)
   int kb_total;      // 64-wide K blocks
   int kb_per_split;
   int stages;
@@ -239,7 +301,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     s_fail = 0;
     for (int s = 0; s < p.stages; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
+      mbar_init(&empty[s], p.cx);  // released by the MMAs of every CTA of the cluster
     }
     mbar_init(tfull, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -253,8 +315,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
+  // every CTA of the cluster has initialised its barriers before any
+  // multicast copy or commit can reach them
+  if (p.cx > 1) cluster_sync_all();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_holder;
+  const uint32_t crank = p.cx > 1 ? cluster_rank() : 0u;
+  const uint16_t cmask = uint16_t((1u << p.cx) - 1u);
 
   const int kb0 = blockIdx.z * p.kb_per_split;
   const int kb1 = min(kb0 + p.kb_per_split, p.kb_total);
@@ -268,7 +335,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int i = 0; i < nkb; ++i) {
       const int s = i % p.stages;
       const uint32_t ph = (i / p.stages) & 1;
-      if (!mbar_wait(&empty[s], ph ^ 1)) {
+      if (!mbar_wait_spin(&empty[s], ph ^ 1)) {
         atomicOr(&s_fail, 1);
         break;
       }
@@ -276,10 +343,17 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_expect_tx(&full[s], stage_bytes);
       const int x = (kb0 + i) * bk;
       tma_load_2d(st, &tA, x, m0, &full[s]);
-      tma_load_2d(st + a_bytes, &tB, x, n0, &full[s]);
-      if (p.mode == 3) {
-        tma_load_2d(st + half_bytes, &tAl, x, m0, &full[s]);
-        tma_load_2d(st + half_bytes + a_bytes, &tBl, x, n0, &full[s]);
+      if (p.mode == 3) tma_load_2d(st + half_bytes, &tAl, x, m0, &full[s]);
+      if (p.cx == 1) {
+        tma_load_2d(st + a_bytes, &tB, x, n0, &full[s]);
+        if (p.mode == 3) tma_load_2d(st + half_bytes + a_bytes, &tBl, x, n0, &full[s]);
+      } else {
+        // this CTA's slice of the shared B tile, multicast to the cluster
+        const int rows = p.ntile / p.cx;
+        const uint32_t off = a_bytes + crank * uint32_t(rows) * uint32_t(bk) * 2u;
+        tma_load_2d_mc(st + off, &tB, x, n0 + int(crank) * rows, &full[s], cmask);
+        if (p.mode == 3)
+          tma_load_2d_mc(st + half_bytes + off, &tBl, x, n0 + int(crank) * rows, &full[s], cmask);
       }
       issued_loads = i + 1;
     }
@@ -289,7 +363,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int i = 0; i < nkb; ++i) {
       const int s = i % p.stages;
       const uint32_t ph = (i / p.stages) & 1;
-      if (!mbar_wait(&full[s], ph)) {
+      if (!mbar_wait_spin(&full[s], ph)) {
         atomicOr(&s_fail, 1);
         break;
       }
@@ -307,7 +381,8 @@ __global__ void __launch_bounds__(kThreads, 1)
           mma_bf16(tmem, al, bh, idesc, 1u);
         }
       }
-      mma_commit(&empty[s]);
+      if (p.cx == 1) mma_commit(&empty[s]);
+      else mma_commit_mc(&empty[s], cmask);
     }
     mma_commit(tfull);
   }
@@ -410,6 +485,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
+  // no CTA leaves while a peer may still copy into its shared memory or
+  // arrive on its barriers
+  if (p.cx > 1) cluster_sync_all();
   if (warp == 0) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
@@ -679,7 +757,9 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
               "tc_gemm: operand shapes");
   const int imode = static_cast<int>(mode);
   const int64_t M = A.rows, N = B.rows, K = A.k;
-  // N tiling: MMA N must be a multiple of 16 up to 256
+  // N tiling: MMA N must be a multiple of 16 up to 256 (256-wide 3xBF16
+  // tiles with two stages measured faster than 128-wide ones with three:
+  // 373 us against 551 us for the double-layer GEMM at D=6)
   const int64_t n_tiles = (N + 255) / 256;
   int ntile = static_cast<int>(((N + n_tiles - 1) / n_tiles + 15) / 16 * 16);
   ntile = std::max(ntile, 16);
@@ -706,9 +786,20 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   // dynamic shared memory: the stage ring (the kernel's static arrays take ~8 KB)
   const int stages = std::max(2, std::min(6, int((210 * 1024) / stage_bytes)));
   const size_t smem = size_t(stages) * stage_bytes + 256 + 1024;
+  // Long 3xBF16 products with a direct epilogue run in clusters of cx CTAs
+  // along M that share each B tile: every CTA loads 1/cx of it and multicasts
+  // it to the others, which divides the B operand stream from L2 by cx (the
+  // double-layer GEMMs are bound by that stream).  M tiles are padded to a
+  // multiple of cx (the padding rows read zeros and store nothing).
+  int cx = 1;
+  if (kClusterB && imode == 3 && direct && kb_total >= 8) {
+    if (m_tiles >= 4 && ntile % 32 == 0) cx = 4;
+    else if (m_tiles >= 2 && ntile % 16 == 0) cx = 2;
+  }
+  const int64_t m_grid = (m_tiles + cx - 1) / cx * cx;
   // grid x over N tiles when A is the larger operand: the CTAs that share an
   // A tile are then resident together and A streams from DRAM once
-  const bool n_fast = n_tiles > 1 && m_tiles > n_tiles && m_tiles <= 65535;
+  const bool n_fast = cx == 1 && n_tiles > 1 && m_tiles > n_tiles && m_tiles <= 65535;
   Scope scope(c);
   float* part = direct ? nullptr : c.alloc<float>(size_t(splits) * m_pad * n_pad);
   if (c.sizing()) return;
@@ -718,10 +809,10 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
               "tc_gemm: grid too large");
   CUtensorMap tA, tAl, tB, tBl;
   make_map(&tA, A.hi, A.rows, K, A.ld, kBM, bk);
-  make_map(&tB, B.hi, B.rows, K, B.ld, uint32_t(ntile), bk);
+  make_map(&tB, B.hi, B.rows, K, B.ld, uint32_t(ntile / cx), bk);
   if (imode == 3) {
     make_map(&tAl, A.lo, A.rows, K, A.ld, kBM, bk);
-    make_map(&tBl, B.lo, B.rows, K, B.ld, uint32_t(ntile), bk);
+    make_map(&tBl, B.lo, B.rows, K, B.ld, uint32_t(ntile / cx), bk);
   } else {
     tAl = tA;
     tBl = tB;
@@ -729,6 +820,7 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   GemmParams p{};
   p.ntile = ntile;
   p.bk = bk;
+  p.cx = cx;
   p.kb_total = kb_total;
   p.kb_per_split = kb_per_split;
   p.stages = stages;
@@ -750,14 +842,30 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   if (absmax != nullptr) CTM_CUDA(cudaMemsetAsync(absmax, 0, sizeof(double), c.stream));
   CTM_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(smem)));
-  const dim3 grid(static_cast<unsigned>(n_fast ? n_tiles : m_tiles),
-                  static_cast<unsigned>(n_fast ? m_tiles : n_tiles), static_cast<unsigned>(splits));
+  const dim3 grid(static_cast<unsigned>(n_fast ? n_tiles : m_grid),
+                  static_cast<unsigned>(n_fast ? m_grid : n_tiles), static_cast<unsigned>(splits));
   {
     const double work = 2.0 * double(M) * N * K * imode;
     KernelTimer timer(c.stream, kTagTcGemm, work);
     KernelTimer timer2(c.stream, out.extra_tag >= 0 ? out.extra_tag : kTagTcGemm,
                        out.extra_tag >= 0 ? work : -1.0);
-    tc_gemm_kernel<<<grid, kThreads, smem, c.stream>>>(tA, tAl, tB, tBl, p);
+    if (cx == 1) {
+      tc_gemm_kernel<<<grid, kThreads, smem, c.stream>>>(tA, tAl, tB, tBl, p);
+    } else {
+      cudaLaunchConfig_t cfg{};
+      cfg.gridDim = grid;
+      cfg.blockDim = dim3(kThreads);
+      cfg.dynamicSmemBytes = smem;
+      cfg.stream = c.stream;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = unsigned(cx);
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      CTM_CUDA(cudaLaunchKernelEx(&cfg, tc_gemm_kernel, tA, tAl, tB, tBl, p));
+    }
     CTM_LAUNCH_CHECK();
   }
   if (direct) return;
