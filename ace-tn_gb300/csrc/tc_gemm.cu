@@ -254,6 +254,7 @@ __device__ __forceinline__ void store4(const TcDest& d, int64_t off, const float
 }
 
 struct GemmParams {
+  int m_tiles, n_tiles, tiles;  // persistent kernel: the tile grid
   int ntile;         // MMA N (multiple of 16, <= 256)
   int bk;            // K per stage (64 or 32)
   int cx;            // CTAs per cluster along M sharing each B tile (1: no cluster)
@@ -492,6 +493,264 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(kTmemCols)
+                 : "memory");
+  }
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void epi_bar_sync() {
+  asm volatile("bar.sync 1, 256;" ::: "memory");  // the eight epilogue warps
+}
+
+// Persistent form for direct-epilogue products with more tiles than SMs: one
+// CTA per SM walks tiles blockIdx.x, + gridDim.x, ...; the accumulator is
+// double-buffered in tensor memory (2 x 256 columns), so while eight
+// epilogue warps drain tile i the MMA thread already accumulates tile i + 1
+// and the producer keeps the shared-memory ring full across tiles.
+// Warp 0 lane 0: TMA producer; warp 1 lane 0: MMA issuer; warps 4-11:
+// epilogue (warp w reads TMEM lanes 32 (w % 4).. for half (w - 4) / 4 of the
+// columns).  Waits are bounded as in tc_gemm_kernel; the epilogue warps
+// agree on failure through shared memory, so their named barriers are always
+// reached by all eight.
+constexpr int kPThreads = 384;
+constexpr uint32_t kPTmemCols = 512;
+
+__global__ void __launch_bounds__(kPThreads, 1)
+    tc_gemm_persistent_kernel(const __grid_constant__ CUtensorMap tA,
+                              const __grid_constant__ CUtensorMap tAl,
+                              const __grid_constant__ CUtensorMap tB,
+                              const __grid_constant__ CUtensorMap tBl, const GemmParams p) {
+  extern __shared__ uint8_t dyn_smem[];
+  uint8_t* base = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(dyn_smem) + 1023) & ~uintptr_t(1023));
+  const int bk = p.bk;
+  const uint32_t a_bytes = kBM * bk * 2;
+  const uint32_t b_bytes = uint32_t(p.ntile) * bk * 2;
+  const uint32_t half_bytes = a_bytes + b_bytes;
+  const uint32_t stage_bytes = half_bytes * (p.mode == 3 ? 2 : 1);
+  uint64_t* full = reinterpret_cast<uint64_t*>(base + size_t(p.stages) * stage_bytes);
+  uint64_t* empty = full + p.stages;
+  uint64_t* tfull = empty + p.stages;  // [2]
+  uint64_t* tempty = tfull + 2;        // [2]
+  uint64_t* mdone = tempty + 2;
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(mdone + 1);
+  __shared__ int s_fail;
+  __shared__ int s_epi_fail;
+  __shared__ int64_t s_co[4][256];
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    s_fail = 0;
+    s_epi_fail = 0;
+    for (int st = 0; st < p.stages; ++st) {
+      mbar_init(&full[st], 1);
+      mbar_init(&empty[st], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 8);  // one arrival per epilogue warp
+    }
+    mbar_init(mdone, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_holder)),
+                 "r"(kPTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_holder;
+  const int ntl = (p.tiles - int(blockIdx.x) + int(gridDim.x) - 1) / int(gridDim.x);
+  auto tile_origin = [&](int lt, int& m0, int& n0) {
+    const int t = int(blockIdx.x) + lt * int(gridDim.x);
+    int mt, nt;
+    if (p.n_fast) {
+      nt = t % p.n_tiles;
+      mt = t / p.n_tiles;
+    } else {
+      mt = t % p.m_tiles;
+      nt = t / p.m_tiles;
+    }
+    m0 = mt * kBM;
+    n0 = nt * p.ntile;
+  };
+  int issued_loads = 0;
+
+  if (threadIdx.x == 0) {
+    // ---------------- TMA producer, across tiles
+    int g = 0;
+    bool fail = false;
+    for (int lt = 0; lt < ntl && !fail; ++lt) {
+      int m0, n0;
+      tile_origin(lt, m0, n0);
+      for (int kb = 0; kb < p.kb_total; ++kb, ++g) {
+        const int st = g % p.stages;
+        const uint32_t ph = (g / p.stages) & 1;
+        if (!mbar_wait_spin(&empty[st], ph ^ 1)) {
+          atomicOr(&s_fail, 1);
+          fail = true;
+          break;
+        }
+        uint8_t* sp = base + size_t(st) * stage_bytes;
+        mbar_expect_tx(&full[st], stage_bytes);
+        const int x = kb * bk;
+        tma_load_2d(sp, &tA, x, m0, &full[st]);
+        tma_load_2d(sp + a_bytes, &tB, x, n0, &full[st]);
+        if (p.mode == 3) {
+          tma_load_2d(sp + half_bytes, &tAl, x, m0, &full[st]);
+          tma_load_2d(sp + half_bytes + a_bytes, &tBl, x, n0, &full[st]);
+        }
+        issued_loads = g + 1;
+      }
+    }
+  } else if (threadIdx.x == 32) {
+    // ---------------- MMA issuer, accumulating tile lt into buffer lt & 1
+    const uint32_t idesc = idesc_bf16(kBM, p.ntile);
+    int g = 0;
+    bool fail = false;
+    for (int lt = 0; lt < ntl && !fail; ++lt) {
+      const int b = lt & 1;
+      const uint32_t use = uint32_t(lt >> 1);
+      if (!mbar_wait_spin(&tempty[b], (use & 1) ^ 1)) {
+        atomicOr(&s_fail, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t acc = tmem + uint32_t(b) * 256u;
+      for (int kb = 0; kb < p.kb_total; ++kb, ++g) {
+        const int st = g % p.stages;
+        const uint32_t ph = (g / p.stages) & 1;
+        if (!mbar_wait_spin(&full[st], ph)) {
+          atomicOr(&s_fail, 1);
+          fail = true;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        uint8_t* sp = base + size_t(st) * stage_bytes;
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          if (kk * 16 >= bk) break;
+          const uint64_t ah = smem_desc(sp + kk * 32, bk);
+          const uint64_t bh = smem_desc(sp + a_bytes + kk * 32, bk);
+          mma_bf16(acc, ah, bh, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+          if (p.mode == 3) {
+            const uint64_t al = smem_desc(sp + half_bytes + kk * 32, bk);
+            const uint64_t bl = smem_desc(sp + half_bytes + a_bytes + kk * 32, bk);
+            mma_bf16(acc, ah, bl, idesc, 1u);
+            mma_bf16(acc, al, bh, idesc, 1u);
+          }
+        }
+        mma_commit(&empty[st]);
+      }
+      if (!fail) mma_commit(&tfull[b]);
+    }
+    // every MMA issued by this thread has completed once mdone flips
+    mma_commit(mdone);
+    (void)mbar_wait(mdone, 0);
+  } else if (warp >= 4) {
+    // ---------------- epilogue warps
+    const int etid = int(threadIdx.x) - 128;  // 0..255
+    const int lane_base = (warp & 3) * 32;
+    const uint32_t trow = uint32_t(lane_base) << 16;
+    const int slice_w = ((p.ntile + 1) / 2 + 15) / 16 * 16;
+    const int c_begin = min(p.ntile, ((warp - 4) >> 2) * slice_w);
+    const int c_end = min(p.ntile, c_begin + slice_w);
+    double scd = p.alpha;
+    if (p.scale1 != nullptr) scd /= p.scale1[0];
+    if (p.scale2 != nullptr) scd /= p.scale2[0];
+    const float sc = float(scd);
+    float amax = 0.f;
+    for (int lt = 0; lt < ntl; ++lt) {
+      const int b = lt & 1;
+      const uint32_t use = uint32_t(lt >> 1);
+      int m0, n0;
+      tile_origin(lt, m0, n0);
+      bool ok = mbar_wait(&tfull[b], use & 1);
+      __syncwarp();
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok && lane == 0) s_epi_fail = 1;
+      epi_bar_sync();  // all eight warps arrive: failure is decided together
+      if (s_epi_fail) {
+        if (etid == 0) atomicOr(&s_fail, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (int k = 0; k < p.nd; ++k)
+        for (int cc = etid; cc < p.ntile; cc += 256) {
+          const int64_t n = int64_t(n0) + cc;
+          s_co[k][cc] = n < p.N ? lay_col(p.d[k].lay, n) : int64_t(-1);
+        }
+      epi_bar_sync();
+      const int row = m0 + lane_base + lane;
+      const bool mvalid = row < p.M;
+      int64_t ro[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (k < p.nd && mvalid) ro[k] = lay_row(p.d[k].lay, row);
+      const uint32_t tb = tmem + uint32_t(b) * 256u + trow;
+      for (int c = c_begin; c < c_end; c += 16) {
+        float v[16];
+        __syncwarp();
+        tmem_ld16(tb + uint32_t(c), v);
+        if (mvalid) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            if (k >= p.nd) break;
+            const TcDest& d = p.d[k];
+#pragma unroll
+            for (int gq = 0; gq < 4; ++gq) {
+              const int cb = c + 4 * gq;
+              const int64_t c0 = s_co[k][cb];
+              const bool vec = c0 >= 0 && ((ro[k] + c0) & 3) == 0 && s_co[k][cb + 1] == c0 + 1 &&
+                               s_co[k][cb + 2] == c0 + 2 && s_co[k][cb + 3] == c0 + 3;
+              if (vec) {
+                store4(d, ro[k] + c0, v + 4 * gq, sc);
+              } else {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                  const int64_t ci = s_co[k][cb + i];
+                  if (ci >= 0) store1(d, ro[k] + ci, v[4 * gq + i], sc);
+                }
+              }
+            }
+          }
+          if (p.absmax != nullptr) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+              if (s_co[0][c + i] >= 0) amax = fmaxf(amax, fabsf(v[i] * sc));
+          }
+        }
+      }
+      // this warp's reads of buffer b are complete (tmem_ld16 waits): hand it back
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[b]);
+    }
+    if (p.absmax != nullptr) {
+      for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+      if (lane == 0 && amax > 0.f)
+        atomicMax(p.absmax, (unsigned long long)__double_as_longlong(double(amax)));
+    }
+  }
+  // on failure: let in-flight copies land before the CTA's memory goes away
+  if (threadIdx.x == 0 && s_fail) {
+    for (int i = 0; i < issued_loads; ++i) (void)mbar_wait(&full[i % p.stages], (i / p.stages) & 1);
+    atomicOr(p.status, 2);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kPTmemCols)
                  : "memory");
   }
 }
@@ -817,7 +1076,12 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
     tAl = tA;
     tBl = tB;
   }
+  // more tiles than SMs with a direct epilogue: one persistent CTA per SM
+  const bool persistent = direct && cx == 1 && base_ctas > sms;
   GemmParams p{};
+  p.m_tiles = int(m_tiles);
+  p.n_tiles = int(n_tiles);
+  p.tiles = int(m_tiles * n_tiles);
   p.ntile = ntile;
   p.bk = bk;
   p.cx = cx;
@@ -849,7 +1113,12 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
     KernelTimer timer(c.stream, kTagTcGemm, work);
     KernelTimer timer2(c.stream, out.extra_tag >= 0 ? out.extra_tag : kTagTcGemm,
                        out.extra_tag >= 0 ? work : -1.0);
-    if (cx == 1) {
+    if (persistent) {
+      CTM_CUDA(cudaFuncSetAttribute(tc_gemm_persistent_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+      tc_gemm_persistent_kernel<<<unsigned(std::min<int64_t>(base_ctas, sms)), kPThreads, smem,
+                                  c.stream>>>(tA, tAl, tB, tBl, p);
+    } else if (cx == 1) {
       tc_gemm_kernel<<<grid, kThreads, smem, c.stream>>>(tA, tAl, tB, tBl, p);
     } else {
       cudaLaunchConfig_t cfg{};

@@ -13,9 +13,11 @@ import acetn_gb300 as gb
 pytestmark = pytest.mark.gpu
 
 SHAPES = [(128, 16, 64), (256, 160, 512), (1000, 150, 777), (300, 272, 1000), (5184, 160, 5184)]
-# long products with enough tiles for a direct (no split-K) epilogue; 1300
-# rows leave a partial row tile
-CLUSTER_SHAPES = [(1024, 5120, 1000), (1300, 5120, 1000)]
+# long products with more output tiles than SMs: a direct (no split-K)
+# epilogue in the persistent kernel (one CTA per SM walking the tiles, the
+# accumulator double-buffered in tensor memory); 1300 rows leave a partial
+# row tile
+LONG_SHAPES = [(1024, 5120, 1000), (1300, 5120, 1000)]
 
 
 def _rand(m, n, seed):
@@ -23,7 +25,7 @@ def _rand(m, n, seed):
     return torch.randn(m, n, generator=g, dtype=torch.float64).cuda()
 
 
-@pytest.mark.parametrize("m,n,k", SHAPES)
+@pytest.mark.parametrize("m,n,k", SHAPES + LONG_SHAPES)
 def test_bf16_single_pass(m, n, k):
     # inputs exactly representable in BF16: the only error left is the FP32
     # accumulation of exact products
@@ -35,7 +37,7 @@ def test_bf16_single_pass(m, n, k):
     assert err < 1e-5, float(err)
 
 
-@pytest.mark.parametrize("m,n,k", SHAPES + CLUSTER_SHAPES)
+@pytest.mark.parametrize("m,n,k", SHAPES + LONG_SHAPES)
 def test_split_bf16x3(m, n, k):
     A, B = _rand(m, k, 3), _rand(k, n, 4)
     C = gb.matmul(A, B, precision="mixed")
