@@ -32,7 +32,7 @@ METRIC = "CTMRG moves/s at D=6, chi=144 (Heisenberg, 2x2, half-system rSVD os=16
 # DRAM bytes (read + write) of one launch of the double-layer contraction GEMM
 # at this workload (M = D^4 = 1296, N = chi^2 = 20736, K = 1296, 3xBF16),
 # from the ncu capture summarised in profiles/tc_gemm_double_layer_d6_chi144.md
-DL_GEMM_TRAFFIC = 118.574848e6 + 70.035968e6
+DL_GEMM_TRAFFIC = 118.590208e6 + 56.284160e6
 
 
 def move_flops(D, chi, q, d=2, ny=2, niter=2):
