@@ -10,7 +10,8 @@ documented in docs/source/input_settings.rst:45-54) and adds two fields:
 * ``mixed_svd_floor`` -- mixed precision only: singular values below this
                    fraction of the largest are dropped in addition to
                    ``svd_cutoff`` (the 3xBF16 Rayleigh-Ritz product resolves
-                   about 1e-5 of the largest).
+                   about 1e-5 of the largest); the library never keeps less
+                   than 1e-8 of the largest in mixed precision.
 
 Any object with the reference's attribute names works as a config; missing
 attributes take the defaults below.

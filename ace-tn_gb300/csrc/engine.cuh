@@ -35,12 +35,13 @@ void orthonormalize(Ctx& c, float* Y, int64_t n, int64_t q, float* R);
 // X = U diag(S) V^T, U (m x r), S (r) descending, V (n x r), r = min(m, n).
 void svd_thin(Ctx& c, const double* X, int64_t m, int64_t n, double* U, double* S,
               double* V);
-// Thin SVD of B (q x n, q <= min(n, 168)) for the mixed path: Cholesky
-// factor L of the FP64 Gram matrix B B^T, FP32 one-sided Jacobi on L^T
-// (relative accuracy for every singular value above the FP64 Gram's
-// resolution, ~1e-7 s_0), V = B^T U diag(1/s) in FP32.
-void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, double* S,
-                  float* V);
+// Thin SVD of B (q x n, q <= min(n, 1024)) for the mixed path, from
+// Bt = B^T (n x q, FP32): R of a shifted Cholesky-QR3 of Bt (B = R^T Qb^T),
+// FP32 one-sided Jacobi on the columns of R with accumulated rotations
+// (Ub = its left singular vectors; singular values to ~1e-7 s_0 absolute,
+// far below the ~1e-5 s_0 of the 3xBF16 products that form B),
+// V = B^T Ub diag(1/s) in FP32.
+void svd_via_qr(Ctx& c, const float* Bt, int64_t q, int64_t n, double* Ub, double* S, float* V);
 // Truncation of acetn/renormalization/projectors.py:163-167 on a descending
 // spectrum s (len r): chi_new = min(chi, #{s/s0 > cutoff}); f[i] = 1/sqrt(s_i/s_0)
 // for i < chi_new else 0 (i < cap).

@@ -528,11 +528,6 @@ __global__ void sort_singular_kernel(const float* Jc, const float* norms, int q,
   }
 }
 
-__global__ void f64_to_f32_kernel(const double* x, float* y, int64_t n) {
-  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
-       i += int64_t(gridDim.x) * blockDim.x)
-    y[i] = float(x[i]);
-}
 
 // Sets flag bit 1 when max |G - I| exceeds tol (NaN counts as failure).
 template <class T>
@@ -809,7 +804,7 @@ void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R) {
                   flags);
     // nxt = cur @ Linv^T
     einsum(c, "ia,ba->ib", ViewT<T>(cur, {n, q}), ViewT<T>(Li, {q, q}), ViewT<T>(nxt, {n, q}));
-    if (R != nullptr && sizeof(T) == 8) {
+    if (R != nullptr) {
       if (stage == 0) {
         if (!c.sizing())
           CTM_CUDA(cudaMemcpyAsync(Rt, Lt, sizeof(T) * q * q, cudaMemcpyDeviceToDevice,
@@ -930,72 +925,92 @@ void scale_columns_compact(Ctx& c, const double* in, int64_t rows, int64_t cap, 
 // Mixed-precision SVD of the Rayleigh-Ritz matrix.
 namespace ctm {
 
-void svd_via_gram(Ctx& c, const double* B, int64_t q, int64_t n, double* Ub, double* S,
-                  float* V) {
-  CTM_REQUIRE(q >= 1 && q <= 1024 && q <= n, CTM_ERR_UNSUPPORTED,
-              "mixed SVD: needs 1 <= q <= min(n, 1024) (chi + oversampling)");
+namespace {
+
+__global__ void transpose_f32_kernel(const float* src, int q, float* dst) {
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < q * q; idx += gridDim.x * blockDim.x) {
+    const int r = idx / q, c = idx - r * q;
+    dst[c * q + r] = src[idx];
+  }
+}
+
+__global__ void scale_columns_f32_kernel(float* x, int64_t rows, int cols, const double* f) {
+  for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < rows * cols;
+       idx += int64_t(gridDim.x) * blockDim.x)
+    x[idx] = float(double(x[idx]) * f[idx % cols]);
+}
+
+// Singular values and left singular vectors of L (q x q) given as the rows
+// of Mc (FP32): one-sided Jacobi on the columns of L^T with the rotations
+// accumulated, then sorted.  Ub (q x q FP64), S, inv_s (q).
+void jacobi_left_singular(Ctx& c, const float* Mc, int64_t q, double* Ub, double* S,
+                          double* inv_s) {
   Scope scope(c);
-  double* G = c.alloc<double>(size_t(q) * q);
-  double* Wk = c.alloc<double>(cholesky_scratch(q));
-  double* L = c.alloc<double>(size_t(q) * q);
-  float* Mc = c.alloc<float>(size_t(q) * q);
   float* Jc = c.alloc<float>(size_t(q) * q);
   float* norms = c.alloc<float>(q);
-  double* inv_s = c.alloc<double>(q);
-  int* flags = c.alloc<int>(1);
-  // the Jacobi matrices stay in shared memory up to q = 168, in global
+  // the Jacobi matrices stay in shared memory up to q = 160, in global
   // memory (L2) beyond
   const size_t wjac = size_t(2) * q * jacobi_ld(int(q)) * sizeof(float);
   const bool jac_smem = wjac <= (227 - 1) * 1024;
   float* Wg = jac_smem ? nullptr : c.alloc<float>(size_t(2) * q * jacobi_ld(int(q)));
   const int64_t pp = q + (q & 1);
-  // G = B B^T = L L^T in FP64 (B = L Qb^T with orthonormal Qb); the spectrum of
-  // B is that of L, whose singular values FP32 one-sided Jacobi resolves with
-  // relative accuracy (no squaring): L^T J = W Sigma, so B = J Sigma (Qb W)^T.
-  einsum(c, "ik,jk->ij", View(B, {q, n}), View(B, {q, n}), View(G, {q, q}));
-  if (!c.sizing()) {
-    CTM_CUDA(cudaMemsetAsync(flags, 0, sizeof(int), c.stream));
-    cholesky<double>(c.stream, G, q, n, 0, Wk, nullptr, L, nullptr, nullptr, flags);
-    // Mc rows = columns of L^T = rows of L (FP32)
-    f64_to_f32_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(L, Mc, q * q);
-    CTM_LAUNCH_CHECK();
-    // FP32 dot products of length q carry ~sqrt(q) u relative error: 4e-6
-    // is the smallest coupling the sweeps can drive below.  One group of 8
-    // threads per pair of a round (no idle warps at the round barriers).
-    const unsigned jthreads =
-        unsigned(std::min<int64_t>(1024, ((pp / 2) * 8 + 31) / 32 * 32));
-    if (jac_smem) {
-      auto launch = [&](auto kern) {
-        CTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(wjac)));
-        kern<<<1, jthreads, wjac, c.stream>>>(Mc, int(q), int(pp), Jc, norms, 40, 4e-6f,
-                                             status_flags(c), nullptr);
-      };
-      switch (jacobi_ld(int(q)) / 32) {
-        case 1: launch(jacobi_onesided_f32_kernel<true, 1>); break;
-        case 2: launch(jacobi_onesided_f32_kernel<true, 2>); break;
-        case 3: launch(jacobi_onesided_f32_kernel<true, 3>); break;
-        case 4: launch(jacobi_onesided_f32_kernel<true, 4>); break;
-        case 5: launch(jacobi_onesided_f32_kernel<true, 5>); break;
-        default: launch(jacobi_onesided_f32_kernel<true, 0>); break;
-      }
-    } else {
-      jacobi_onesided_f32_kernel<false, 0><<<1, jthreads, 0, c.stream>>>(
-          Mc, int(q), int(pp), Jc, norms, 40, 4e-6f, status_flags(c), Wg);
+  if (c.sizing()) return;
+  // FP32 dot products of length q carry ~sqrt(q) u relative error: 4e-6
+  // is the smallest coupling the sweeps can drive below.  One group of 8
+  // threads per pair of a round (no idle warps at the round barriers).
+  const unsigned jthreads = unsigned(std::min<int64_t>(1024, ((pp / 2) * 8 + 31) / 32 * 32));
+  if (jac_smem) {
+    auto launch = [&](auto kern) {
+      CTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(wjac)));
+      kern<<<1, jthreads, wjac, c.stream>>>(Mc, int(q), int(pp), Jc, norms, 40, 4e-6f,
+                                           status_flags(c), nullptr);
+    };
+    switch (jacobi_ld(int(q)) / 32) {
+      case 1: launch(jacobi_onesided_f32_kernel<true, 1>); break;
+      case 2: launch(jacobi_onesided_f32_kernel<true, 2>); break;
+      case 3: launch(jacobi_onesided_f32_kernel<true, 3>); break;
+      case 4: launch(jacobi_onesided_f32_kernel<true, 4>); break;
+      case 5: launch(jacobi_onesided_f32_kernel<true, 5>); break;
+      default: launch(jacobi_onesided_f32_kernel<true, 0>); break;
     }
-    CTM_LAUNCH_CHECK();
-    sort_singular_kernel<<<1, 256, 0, c.stream>>>(Jc, norms, int(q), Ub, S, inv_s);
+  } else {
+    jacobi_onesided_f32_kernel<false, 0><<<1, jthreads, 0, c.stream>>>(
+        Mc, int(q), int(pp), Jc, norms, 40, 4e-6f, status_flags(c), Wg);
+  }
+  CTM_LAUNCH_CHECK();
+  sort_singular_kernel<<<1, 256, 0, c.stream>>>(Jc, norms, int(q), Ub, S, inv_s);
+  CTM_LAUNCH_CHECK();
+}
+
+}  // namespace
+
+void svd_via_qr(Ctx& c, const float* Bt, int64_t q, int64_t n, double* Ub, double* S, float* V) {
+  CTM_REQUIRE(q >= 1 && q <= 1024 && q <= n, CTM_ERR_UNSUPPORTED,
+              "mixed SVD: needs 1 <= q <= min(n, 1024) (chi + oversampling)");
+  Scope scope(c);
+  float* Y = c.alloc<float>(size_t(n) * q);
+  float* R = c.alloc<float>(size_t(q) * q);
+  float* Mc = c.alloc<float>(size_t(q) * q);
+  double* inv_s = c.alloc<double>(q);
+  // B^T = Qb R (shifted Cholesky-QR3 in FP32, R backward stable to ~u |B|),
+  // so B = L Qb^T with L = R^T and the SVD of B is that of L
+  if (!c.sizing())
+    CTM_CUDA(cudaMemcpyAsync(Y, Bt, sizeof(float) * n * q, cudaMemcpyDeviceToDevice, c.stream));
+  orthonormalize(c, Y, n, q, R);
+  if (!c.sizing()) {
+    // Mc rows = rows of L = columns of R
+    transpose_f32_kernel<<<grid_for(q * q, 256), 256, 0, c.stream>>>(R, int(q), Mc);
     CTM_LAUNCH_CHECK();
   }
+  jacobi_left_singular(c, Mc, q, Ub, S, inv_s);
   // V = B^T Ub diag(1/s), FP32
-  float* bf = c.alloc<float>(size_t(q) * n);
   float* uf = c.alloc<float>(size_t(q) * q);
-  double* vd = c.alloc<double>(size_t(n) * q);
-  to_f32(c, B, bf, q * n);
   to_f32(c, Ub, uf, q * q);
-  einsum(c, "ki,kj->ij", ViewF(bf, {q, n}), ViewF(uf, {q, q}), ViewF(V, {n, q}));
-  to_f64(c, V, vd, n * q);
-  scale_columns(c, vd, n, q, q, inv_s);
-  to_f32(c, vd, V, n * q);
+  einsum(c, "ik,kj->ij", ViewF(Bt, {n, q}), ViewF(uf, {q, q}), ViewF(V, {n, q}));
+  if (!c.sizing()) {
+    scale_columns_f32_kernel<<<grid_for(n * q, 256), 256, 0, c.stream>>>(V, n, int(q), inv_s);
+    CTM_LAUNCH_CHECK();
+  }
 }
 
 }  // namespace ctm

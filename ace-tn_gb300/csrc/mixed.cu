@@ -396,8 +396,9 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
     orthonormalize(c, Y, m, q, nullptr);
   }
   delete rf_span;
-  // ---- Rayleigh-Ritz: B = (Q^T Q1) Q4 in 3xBF16, SVD from the FP64 Gram matrix
-  double* Bm = c.alloc<double>(size_t(q) * n);
+  // ---- Rayleigh-Ritz: B = (Q^T Q1) Q4 in 3xBF16 (written as B^T in FP32),
+  //      its SVD from an FP32 QR of B^T and one-sided Jacobi
+  float* Bt = c.alloc<float>(size_t(n) * q);
   double* Ub = c.alloc<double>(size_t(q) * q);
   double* s = c.alloc<double>(q);
   float* V = c.alloc<float>(size_t(n) * q);
@@ -408,12 +409,12 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
     const TcOperand qt = yt_operand_f32(c, Y, m, q, q, true);           // Q^T (q x m)
     const TcOperand w = gemm_to_operand(c, A1.t(true), qt, x3, true);    // W = Q^T Q1 (q x c1)
     TcOut out;
-    out.add(TcKind::kF64, Bm, TcLayout::cols(A4.cols, q, n));            // B (q x n)
+    out.add(TcKind::kF32, Bt, TcLayout::rows(A4.cols, q, q));            // B^T (n x q)
     out.inv_scale = A1.scale;  // normalised quarter tensors
     out.inv_scale2 = A4.scale;
     tc_gemm(c, A4.t(true), w, x3, out);
   }
-  svd_via_gram(c, Bm, q, n, Ub, s, V);
+  svd_via_qr(c, Bt, q, n, Ub, s, V);
   {
     Scope s2(c);
     float* ubf = c.alloc<float>(size_t(q) * q);
@@ -424,7 +425,10 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
   // ---- truncation (FP64 spectrum) and projector products (3xBF16)
   KernelTimer proj_span(c.stream, kTagProject, 0.0);
   double* f = c.alloc<double>(cap);
-  truncation_factors(c, s, q, o.chi, std::max(o.svd_cutoff, o.mixed_floor), f, cap, chi_new);
+  // below ~1e-8 s_0 the spectrum is the noise of the 3xBF16 products: keeping
+  // it would weight noise by s^-1/2 (and grows the environment without bound)
+  truncation_factors(c, s, q, o.chi, std::max({o.svd_cutoff, o.mixed_floor, 1e-8}), f, cap,
+                     chi_new);
   double* P1f = c.alloc<double>(size_t(c1) * cap);
   double* P2f = c.alloc<double>(size_t(r4) * cap);
   {

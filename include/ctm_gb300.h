@@ -77,7 +77,7 @@ typedef struct ctm_ctmrg_opts {
   double mixed_floor;   /* CTM_PREC_MIXED only: singular values below
                            mixed_floor * s_0 are dropped as well (they are
                            below the resolution of the 3xBF16 products);
-                           0 keeps svd_cutoff alone                        */
+                           never less than 1e-8                            */
 } ctm_ctmrg_opts;
 
 /* Library version string and message of the last failure on this thread. */
