@@ -442,13 +442,21 @@ __global__ void __launch_bounds__(kCh > 0 ? 128 * kCh : 1024) jacobi_onesided_f3
               xa[m] = a[8 * m];
               xb[m] = b[8 * m];
             }
+            // two partial sums per quantity: half the dependent-FMA chain
+            float al2 = 0.f, be2 = 0.f, ga2 = 0.f;
 #pragma unroll
             for (int m = 0; m < kR; ++m) {
               const float4 x = xa[m], y = xb[m];
-              al = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, al))));
-              be = fmaf(y.x, y.x, fmaf(y.y, y.y, fmaf(y.z, y.z, fmaf(y.w, y.w, be))));
-              ga = fmaf(x.x, y.x, fmaf(x.y, y.y, fmaf(x.z, y.z, fmaf(x.w, y.w, ga))));
+              al = fmaf(x.x, x.x, fmaf(x.y, x.y, al));
+              al2 = fmaf(x.z, x.z, fmaf(x.w, x.w, al2));
+              be = fmaf(y.x, y.x, fmaf(y.y, y.y, be));
+              be2 = fmaf(y.z, y.z, fmaf(y.w, y.w, be2));
+              ga = fmaf(x.x, y.x, fmaf(x.y, y.y, ga));
+              ga2 = fmaf(x.z, y.z, fmaf(x.w, y.w, ga2));
             }
+            al += al2;
+            be += be2;
+            ga += ga2;
           } else {
             for (int m = 0; m < nchunk; ++m) {
               const float4 x = a[8 * m], y = b[8 * m];
