@@ -23,7 +23,7 @@ from .config import CTMRGConfig
 from .ctmrg import ctmrg, sweep_order
 from .directional_mover import DirectionalMover
 from .graph import CTMRGGraph
-from .linalg import (fused_3matmul_svd_lowrank, fused_matmul_svd_lowrank, matmul, svd,
+from .linalg import (fused_3matmul_svd_lowrank, fused_matmul_svd_lowrank, matmul, qr, svd,
                      svd_lowrank)
 from .measure import measure
 from .models import HeisenbergModel, IsingModel
@@ -33,5 +33,5 @@ from .state import Bond, IpepsState, random_state
 
 __all__ = ["build", "CTMRGConfig", "ctmrg", "sweep_order", "DirectionalMover",
            "ProjectorCalculator", "CTMRGGraph", "RDM", "measure", "svd_lowrank", "fused_matmul_svd_lowrank",
-           "fused_3matmul_svd_lowrank", "svd", "matmul", "HeisenbergModel", "IsingModel",
+           "fused_3matmul_svd_lowrank", "qr", "svd", "matmul", "HeisenbergModel", "IsingModel",
            "Bond", "IpepsState", "random_state"]

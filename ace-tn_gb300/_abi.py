@@ -71,6 +71,7 @@ _SIGNATURES = {
     "ctm_fused_3matmul_svd_lowrank": ([c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_i64,
                                        c_i64, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz_p, c_vp],
                                       ctypes.c_int),
+    "ctm_qr": ([c_vp, c_i64, c_i64, c_vp, c_i32, c_vp, c_sz_p, c_vp], ctypes.c_int),
     "ctm_svd_f64": ([c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp, c_sz_p, c_vp], ctypes.c_int),
     "ctm_matmul": ([c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i32, c_vp, c_sz_p, c_vp],
                    ctypes.c_int),

@@ -755,6 +755,19 @@ int ctm_svd_f64(const double* a, int64_t m, int64_t n, double* U, double* S, dou
   });
 }
 
+int ctm_qr(void* Y, int64_t n, int64_t q, void* R, int32_t dtype, void* ws, size_t* ws_bytes,
+           ctm_stream_t stream) {
+  return with_workspace(ws, ws_bytes, as_stream(stream), [&](Ctx& c) {
+    CTM_REQUIRE(n >= q && q >= 1, CTM_ERR_INVALID, "ctm_qr: needs n >= q >= 1");
+    if (dtype == CTM_DTYPE_F64) {
+      orthonormalize(c, static_cast<double*>(Y), n, q, static_cast<double*>(R));
+    } else {
+      CTM_REQUIRE(dtype == CTM_DTYPE_F32, CTM_ERR_INVALID, "ctm_qr: bad dtype");
+      orthonormalize(c, static_cast<float*>(Y), n, q, static_cast<float*>(R));
+    }
+  });
+}
+
 int ctm_matmul(const double* A, const double* B, double* C, int64_t M, int64_t N, int64_t K,
                int32_t precision, void* ws, size_t* ws_bytes, ctm_stream_t stream) {
   return with_workspace(ws, ws_bytes, as_stream(stream), [&](Ctx& c) {

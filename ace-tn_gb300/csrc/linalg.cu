@@ -12,6 +12,7 @@
 #include "engine.cuh"
 
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 
 namespace ctm {
@@ -147,7 +148,7 @@ __global__ void __launch_bounds__(LT) householder_qr_kernel(T* Y, int64_t n, int
 // shift_mode 0: none; 1: 11 (n q + q (q + 1)) u tr(G) (Fukaya et al.);
 // 2: 1000 u tr(G) (FP32 stages of the mixed path).
 // Outputs (each may be null): Lout = L (lower, row-major), Linv = L^-1
-// (lower), Lt = L^T (upper).  Wg / Eg are cholesky_scratch(q) elements of
+// (lower), Lt = L^T (upper), LinvT = L^-T (upper).  Wg / Eg are cholesky_scratch(q) elements of
 // global scratch used for W / E when they are not in shared memory.
 constexpr int kCholThreads = 1024;
 constexpr int kCholNb = 8;
@@ -177,7 +178,7 @@ constexpr int chol_threads() { return sizeof(T) == 8 ? 512 : kCholThreads; }
 template <class T, int kPlace>
 __global__ void __launch_bounds__(chol_threads<T>()) cholesky_kernel(
     const T* G, int q, int64_t n, int shift_mode, T* Wg, T* Eg, T* Lout, T* Linv, T* Lt,
-    int* flags) {
+    T* LinvT, int* flags) {
   using V4 = typename Vec4<T>::type;
   extern __shared__ __align__(32) unsigned char chol_smem[];
   __shared__ T sh[32];
@@ -190,7 +191,7 @@ __global__ void __launch_bounds__(chol_threads<T>()) cholesky_kernel(
   T* S = dg + q4;                                        // kCholNb x ld
   T* W = kPlace >= 1 ? S + kCholNb * ld : Wg;            // q4 x ld
   T* E = kPlace == 2 ? W + size_t(q4) * ld : Eg;         // q4 x ld
-  const bool want_inv = Linv != nullptr;
+  const bool want_inv = Linv != nullptr || LinvT != nullptr;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nwarps = blockDim.x >> 5, nth = blockDim.x;
   // trace -> shift (every thread ends with the same value)
@@ -346,9 +347,13 @@ __global__ void __launch_bounds__(chol_threads<T>()) cholesky_kernel(
       const T dr = dg[r];
       Lt[idx] = c > r ? (dr > T(0) ? W[r * ld + c] / dr : T(0)) : (c == r ? dr : T(0));
     }
-    if (want_inv) {
+    if (Linv != nullptr) {
       const T dr = dg[r];
       Linv[idx] = (c <= r && dr > T(0)) ? E[r * ld + c] / dr : T(0);
+    }
+    if (LinvT != nullptr) {
+      const T dc = dg[c];
+      LinvT[idx] = (r <= c && dc > T(0)) ? E[c * ld + r] / dc : T(0);
     }
   }
 }
@@ -358,7 +363,7 @@ __global__ void __launch_bounds__(chol_threads<T>()) cholesky_kernel(
 // used otherwise.
 template <class T>
 void cholesky(cudaStream_t st, const T* G, int64_t q, int64_t n, int shift_mode, T* Wg, T* Eg,
-              T* Lout, T* Linv, T* Lt, int* flags) {
+              T* Lout, T* Linv, T* Lt, int* flags, T* LinvT = nullptr) {
   const size_t mat = cholesky_scratch(q) * sizeof(T);
   const size_t head = (size_t(chol_q4(int(q))) + size_t(kCholNb) * chol_ld(int(q))) * sizeof(T);
   const int place = (head + 2 * mat <= kSmemOptin) ? 2 : (head + mat <= kSmemOptin ? 1 : 0);
@@ -366,7 +371,7 @@ void cholesky(cudaStream_t st, const T* G, int64_t q, int64_t n, int shift_mode,
   auto launch = [&](auto kern) {
     CTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     kern<<<1, chol_threads<T>(), smem, st>>>(G, int(q), n, shift_mode, Wg, Eg, Lout, Linv, Lt,
-                                             flags);
+                                             LinvT, flags);
   };
   if (place == 2) launch(cholesky_kernel<T, 2>);
   else if (place == 1) launch(cholesky_kernel<T, 1>);
@@ -766,6 +771,254 @@ int* status_flags(Ctx& c) {
   return p;
 }
 
+// ------------------------------------------------------------- tall-skinny
+// FP32 stages of the Cholesky-QR (q <= 192): one kernel per stage applies the
+// previous stage's L^-T to a slab of rows and accumulates the slab's Gram
+// matrix; a second kernel sums the per-slab Grams in slab order.
+namespace {
+
+__device__ __forceinline__ void cp_async_f32x4(float* s, const float* g) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(s));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_f32(float* s, const float* g) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(s));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+// cnt contiguous floats g -> s, issued asynchronously by the whole CTA
+// (16-byte copies when kVec: both addresses 16-byte aligned, cnt % 4 == 0)
+template <bool kVec>
+__device__ __forceinline__ void slab_copy(float* s, const float* g, int64_t cnt) {
+  if (kVec) {
+    for (int64_t i = int64_t(threadIdx.x) * 4; i < cnt; i += int64_t(blockDim.x) * 4)
+      cp_async_f32x4(s + i, g + i);
+  } else {
+    for (int64_t i = threadIdx.x; i < cnt; i += blockDim.x) cp_async_f32(s + i, g + i);
+  }
+}
+
+constexpr int kSlabThreads = 1024;
+
+// One slab of rows [r0, r0 + nr) of Y (n x q, row-major), r0 = blockIdx.x * rpb.
+// With Ut (q x q, upper triangular L^-T): X = Y Ut for the slab (written to
+// X and kept in shared memory), then part[blockIdx.x] = X^T X over the slab;
+// without Ut: part[blockIdx.x] = Y^T Y over the slab.
+// Shared memory: the slab (rpb x q, then 32 kT floats of slack so that column
+// indices up to 32 kT - 1 stay inside the buffer) and Ut (q x q + 32 kT).
+// Columns >= q are computed from neighbouring entries and never stored.
+// Apply: warp w owns rows 4w..4w+3 (+128 per pass), lane the columns
+// lane + 32 j; the row values are warp-uniform (broadcast loads, one 16-byte
+// load per 4 columns of b when kVec) and Ut rows are read conflict-free.
+// Gram: thread (warp, lane) owns rows warp + 32 i and columns lane + 32 j.
+template <int kT, bool kVec>
+__global__ void __launch_bounds__(kSlabThreads) slab_stage_kernel(
+    const float* __restrict__ Y, int64_t n, int q, int rpb, const float* __restrict__ Ut,
+    float* __restrict__ X, float* __restrict__ part) {
+  extern __shared__ __align__(16) float slab_smem[];
+  const int pad = 32 * kT;
+  float* Ys = slab_smem;                           // rpb x q (+ pad)
+  float* Us = slab_smem + size_t(rpb) * q + pad;   // q x q (+ pad)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t r0 = int64_t(blockIdx.x) * rpb;
+  const int nr = int(n - r0 < rpb ? n - r0 : rpb);
+  slab_copy<kVec>(Ys, Y + r0 * q, int64_t(nr) * q);
+  if (Ut != nullptr) slab_copy<kVec>(Us, Ut, int64_t(q) * q);
+  // slack after the rows is read only into columns that are never stored;
+  // zero it so those lanes compute on finite values
+  for (int i = threadIdx.x; i < pad; i += blockDim.x) {
+    Ys[size_t(nr) * q + i] = 0.f;
+    Us[size_t(q) * q + i] = 0.f;
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  if (Ut != nullptr) {
+    for (int rg = warp * 4; rg < nr; rg += 4 * 32) {
+      float acc[4][kT];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < kT; ++j) acc[i][j] = 0.f;
+      // rows past nr read the zeroed slack or the next rows; they are not stored
+      const float* y0 = Ys + size_t(rg) * q;
+      int b = 0;
+      if (kVec) {
+        for (; b + 4 <= q; b += 4) {
+          float4 yv[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+            yv[i] = (rg + i < nr) ? *reinterpret_cast<const float4*>(y0 + i * q + b)
+                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            float lv[kT];
+#pragma unroll
+            for (int j = 0; j < kT; ++j) lv[j] = Us[(b + t) * q + lane + 32 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              const float yy = t == 0 ? yv[i].x : t == 1 ? yv[i].y : t == 2 ? yv[i].z : yv[i].w;
+#pragma unroll
+              for (int j = 0; j < kT; ++j) acc[i][j] = fmaf(yy, lv[j], acc[i][j]);
+            }
+          }
+        }
+      }
+      for (; b < q; ++b) {
+        float lv[kT], yv[4];
+#pragma unroll
+        for (int j = 0; j < kT; ++j) lv[j] = Us[b * q + lane + 32 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) yv[i] = (rg + i < nr) ? y0[i * q + b] : 0.f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < kT; ++j) acc[i][j] = fmaf(yv[i], lv[j], acc[i][j]);
+      }
+      // every warp reads only its own rows of Ys: overwrite them in place
+      __syncwarp();
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int r = rg + i;
+        if (r >= nr) continue;
+#pragma unroll
+        for (int j = 0; j < kT; ++j) {
+          const int a = lane + 32 * j;
+          if (a < q) {
+            Ys[size_t(r) * q + a] = acc[i][j];
+            X[(r0 + r) * q + a] = acc[i][j];
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  float g[kT][kT];
+#pragma unroll
+  for (int i = 0; i < kT; ++i)
+#pragma unroll
+    for (int j = 0; j < kT; ++j) g[i][j] = 0.f;
+  for (int r = 0; r < nr; ++r) {
+    const float* yr = Ys + size_t(r) * q;
+    float av[kT], bv[kT];
+#pragma unroll
+    for (int i = 0; i < kT; ++i) {
+      av[i] = yr[warp + 32 * i];
+      bv[i] = yr[lane + 32 * i];
+    }
+#pragma unroll
+    for (int i = 0; i < kT; ++i)
+#pragma unroll
+      for (int j = 0; j < kT; ++j) g[i][j] = fmaf(av[i], bv[j], g[i][j]);
+  }
+  float* P = part + size_t(blockIdx.x) * q * q;
+#pragma unroll
+  for (int i = 0; i < kT; ++i)
+#pragma unroll
+    for (int j = 0; j < kT; ++j) {
+      const int a = warp + 32 * i, b = lane + 32 * j;
+      if (a < q && b < q) P[a * q + b] = g[i][j];
+    }
+}
+
+__device__ __forceinline__ void add_to(float4& a, const float4& b) {
+  a.x += b.x;
+  a.y += b.y;
+  a.z += b.z;
+  a.w += b.w;
+}
+__device__ __forceinline__ void add_to(float& a, const float& b) { a += b; }
+
+// G = sum over slabs of part, in slab order.  Each CTA: 64 entries (float4
+// entries when kVec, i.e. q*q % 4 == 0) x 4 slab ranges, combined through
+// shared memory in range order.
+template <bool kVec>
+__global__ void __launch_bounds__(256) slab_reduce_kernel(const float* __restrict__ part,
+                                                          int nblk, int qq,
+                                                          float* __restrict__ G) {
+  using V = typename std::conditional<kVec, float4, float>::type;
+  __shared__ V s[4][64];
+  const int t = threadIdx.x & 63, grp = threadIdx.x >> 6;
+  const int ne = kVec ? qq / 4 : qq;
+  const int e = blockIdx.x * 64 + t;
+  const int b0 = grp * nblk / 4, b1 = (grp + 1) * nblk / 4;
+  V acc;
+  memset(&acc, 0, sizeof(V));
+  if (e < ne) {
+    const V* pv = reinterpret_cast<const V*>(part);
+#pragma unroll 8
+    for (int b = b0; b < b1; ++b) add_to(acc, pv[size_t(b) * ne + e]);
+  }
+  s[grp][t] = acc;
+  __syncthreads();
+  if (grp == 0 && e < ne) {
+    V r = s[0][t];
+#pragma unroll
+    for (int k = 1; k < 4; ++k) add_to(r, s[k][t]);
+    reinterpret_cast<V*>(G)[e] = r;
+  }
+}
+
+template <int kT, bool kVec>
+void slab_stage_launch(Ctx& c, const float* Y, int64_t n, int64_t q, int rpb, int nblk,
+                       const float* Ut, float* X, float* part) {
+  const size_t smem = (size_t(rpb) * q + size_t(q) * q + 2 * 32 * kT) * sizeof(float);
+  CTM_CUDA(cudaFuncSetAttribute(slab_stage_kernel<kT, kVec>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  slab_stage_kernel<kT, kVec><<<nblk, kSlabThreads, smem, c.stream>>>(Y, n, int(q), rpb, Ut, X,
+                                                                      part);
+}
+
+template <bool kVec>
+void slab_stage_dispatch(Ctx& c, const float* Y, int64_t n, int64_t q, int rpb, int nblk,
+                         const float* Ut, float* X, float* part) {
+  switch ((q + 31) / 32) {
+    case 1: slab_stage_launch<1, kVec>(c, Y, n, q, rpb, nblk, Ut, X, part); break;
+    case 2: slab_stage_launch<2, kVec>(c, Y, n, q, rpb, nblk, Ut, X, part); break;
+    case 3: slab_stage_launch<3, kVec>(c, Y, n, q, rpb, nblk, Ut, X, part); break;
+    case 4: slab_stage_launch<4, kVec>(c, Y, n, q, rpb, nblk, Ut, X, part); break;
+    case 5: slab_stage_launch<5, kVec>(c, Y, n, q, rpb, nblk, Ut, X, part); break;
+    default: slab_stage_launch<6, kVec>(c, Y, n, q, rpb, nblk, Ut, X, part); break;
+  }
+}
+
+// rows per slab: one slab per SM, at most 64 rows (shared memory bound)
+int slab_rows(int64_t n) {
+  const int64_t sms = sm_count_linalg();
+  int64_t rpb = (n + sms - 1) / sms;
+  rpb = std::max<int64_t>(4, std::min<int64_t>(64, rpb));
+  return int(rpb);
+}
+
+}  // namespace
+
+// G (q x q) = X^T X where X = Y Ut (Ut q x q upper triangular; written to X)
+// or X = Y when Ut is null; FP32, q <= 192, one pass over Y.
+void slab_gram(Ctx& c, const float* Y, int64_t n, int64_t q, const float* Ut, float* X,
+               float* G) {
+  CTM_REQUIRE(q >= 1 && q <= 192, CTM_ERR_INVALID, "slab_gram: needs 1 <= q <= 192");
+  const int rpb = slab_rows(n);
+  const int nblk = int((n + rpb - 1) / rpb);
+  Scope scope(c);
+  float* part = c.alloc<float>(size_t(nblk) * q * q);
+  if (c.sizing()) return;
+  const bool vec = q % 4 == 0 && (reinterpret_cast<uintptr_t>(Y) & 15) == 0 &&
+                   (Ut == nullptr || (reinterpret_cast<uintptr_t>(Ut) & 15) == 0);
+  if (vec)
+    slab_stage_dispatch<true>(c, Y, n, q, rpb, nblk, Ut, X, part);
+  else
+    slab_stage_dispatch<false>(c, Y, n, q, rpb, nblk, Ut, X, part);
+  CTM_LAUNCH_CHECK();
+  const int qq = int(q * q);
+  if (qq % 4 == 0)
+    slab_reduce_kernel<true><<<unsigned((qq / 4 + 63) / 64), 256, 0, c.stream>>>(part, nblk, qq, G);
+  else
+    slab_reduce_kernel<false><<<unsigned((qq + 63) / 64), 256, 0, c.stream>>>(part, nblk, qq, G);
+  CTM_LAUNCH_CHECK();
+}
+
 template <class T>
 void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R) {
   CTM_REQUIRE(n >= q && q >= 1, CTM_ERR_INVALID, "orthonormalize: needs n >= q >= 1");
@@ -804,28 +1057,50 @@ void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R) {
   // below catches anything else.
   const int stages = 3;
   const int shifted_stages = 1;
-  for (int stage = 0; stage < stages; ++stage) {
-    einsum(c, "ia,ib->ab", ViewT<T>(cur, {n, q}), ViewT<T>(cur, {n, q}), ViewT<T>(G, {q, q}));
-    const int mode = stage < shifted_stages ? (sizeof(T) == 8 ? 1 : 2) : 0;
-    if (!c.sizing())
-      cholesky<T>(c.stream, G, q, n, mode, Wk, Ek, nullptr, Li, R != nullptr ? Lt : nullptr,
-                  flags);
-    // nxt = cur @ Linv^T
-    einsum(c, "ia,ba->ib", ViewT<T>(cur, {n, q}), ViewT<T>(Li, {q, q}), ViewT<T>(nxt, {n, q}));
-    if (R != nullptr) {
-      if (stage == 0) {
-        if (!c.sizing())
-          CTM_CUDA(cudaMemcpyAsync(Rt, Lt, sizeof(T) * q * q, cudaMemcpyDeviceToDevice,
-                                   c.stream));
-      } else {
-        einsum(c, "ab,bc->ac", ViewT<T>(Lt, {q, q}), ViewT<T>(Rt, {q, q}), ViewT<T>(Rt2, {q, q}));
-        std::swap(Rt, Rt2);
-      }
+  // FP32 with q <= 192: one slab kernel per stage applies the previous
+  // stage's L^-T and forms the next Gram matrix in the same pass over the rows
+  const bool fast_f32 = sizeof(T) == 4 && q <= 192;
+  T* Ut = fast_f32 ? c.alloc<T>(size_t(q) * q) : nullptr;
+  auto accumulate_r = [&](int stage) {
+    if (R == nullptr) return;
+    if (stage == 0) {
+      if (!c.sizing())
+        CTM_CUDA(cudaMemcpyAsync(Rt, Lt, sizeof(T) * q * q, cudaMemcpyDeviceToDevice, c.stream));
+    } else {
+      einsum(c, "ab,bc->ac", ViewT<T>(Lt, {q, q}), ViewT<T>(Rt, {q, q}), ViewT<T>(Rt2, {q, q}));
+      std::swap(Rt, Rt2);
     }
-    std::swap(cur, nxt);
+  };
+  if (fast_f32) {
+    float* const Yf = reinterpret_cast<float*>(cur);
+    slab_gram(c, Yf, n, q, nullptr, nullptr, reinterpret_cast<float*>(G));
+    for (int stage = 0; stage < stages; ++stage) {
+      const int mode = stage < shifted_stages ? 2 : 0;
+      if (!c.sizing())
+        cholesky<T>(c.stream, G, q, n, mode, Wk, Ek, nullptr, nullptr,
+                    R != nullptr ? Lt : nullptr, flags, Ut);
+      accumulate_r(stage);
+      // nxt = cur L^-T and G = nxt^T nxt
+      slab_gram(c, reinterpret_cast<const float*>(cur), n, q, reinterpret_cast<const float*>(Ut),
+                reinterpret_cast<float*>(nxt), reinterpret_cast<float*>(G));
+      std::swap(cur, nxt);
+    }
+  } else {
+    for (int stage = 0; stage < stages; ++stage) {
+      einsum(c, "ia,ib->ab", ViewT<T>(cur, {n, q}), ViewT<T>(cur, {n, q}), ViewT<T>(G, {q, q}));
+      const int mode = stage < shifted_stages ? (sizeof(T) == 8 ? 1 : 2) : 0;
+      if (!c.sizing())
+        cholesky<T>(c.stream, G, q, n, mode, Wk, Ek, nullptr, Li, R != nullptr ? Lt : nullptr,
+                    flags);
+      // nxt = cur @ Linv^T
+      einsum(c, "ia,ba->ib", ViewT<T>(cur, {n, q}), ViewT<T>(Li, {q, q}), ViewT<T>(nxt, {n, q}));
+      accumulate_r(stage);
+      std::swap(cur, nxt);
+    }
+    einsum(c, "ia,ib->ab", ViewT<T>(cur, {n, q}), ViewT<T>(cur, {n, q}), ViewT<T>(G, {q, q}));
   }
-  // cur holds Q after the stages; check it and fall back when needed
-  einsum(c, "ia,ib->ab", ViewT<T>(cur, {n, q}), ViewT<T>(cur, {n, q}), ViewT<T>(G, {q, q}));
+  // cur holds Q after the stages and G its Gram matrix; check it and fall
+  // back when needed
   T* hv = c.alloc<T>(size_t(n) * q);
   if (c.sizing()) return;
   orthogonality_check_kernel<T><<<1, 1024, 0, c.stream>>>(G, int(q), T(sizeof(T) == 8 ? 1e-11 : 2e-4),

@@ -76,6 +76,25 @@ def fused_3matmul_svd_lowrank(A, B, C, D, q=6, niter=2, omega=None):
     return U, S, V
 
 
+def qr(A):
+    """Thin QR (Q, R) of a tall float64 or float32 CUDA matrix, in the
+    matrix's own precision: the ``torch.linalg.qr`` step of the range finders
+    (acetn/linalg/svd_lowrank.py:36,39).  float32 is the arithmetic of the
+    mixed path's range finder.  Columns of Q may differ in sign from LAPACK's."""
+    if not isinstance(A, torch.Tensor) or not A.is_cuda:
+        raise ValueError("A must be a CUDA tensor (the gb300 backend has no CPU path)")
+    if A.dtype not in (torch.float64, torch.float32):
+        raise ValueError(f"A must be float64 or float32, got {A.dtype}")
+    n, q = A.shape
+    if not n >= q >= 1:
+        raise ValueError(f"qr needs rows >= columns >= 1, got {tuple(A.shape)}")
+    Q = A.contiguous().clone()
+    R = torch.empty(q, q, dtype=A.dtype, device=A.device)
+    _abi.call("ctm_qr", [_abi.ptr(Q), n, q, _abi.ptr(R), 0 if A.dtype == torch.float64 else 1],
+              A.device)
+    return Q, R
+
+
 def svd(A):
     """Thin SVD (U, S, V) of an FP64 matrix with at most 4096 rows and columns."""
     _abi.require_cuda(A, "A")

@@ -193,6 +193,19 @@ int ctm_fused_3matmul_svd_lowrank(const double* a, const double* b, const double
                                   const double* omega, double* U, double* S, double* V,
                                   void* ws, size_t* ws_bytes, ctm_stream_t stream);
 
+/* Thin QR of a tall matrix in place: Y (n x q, row-major, n >= q >= 1) is
+ * overwritten by Q with orthonormal columns and, when R is not NULL, R
+ * (q x q, upper triangular) is written with Y = Q R.  dtype CTM_DTYPE_F64
+ * (double buffers) or CTM_DTYPE_F32 (float buffers; the arithmetic of the
+ * mixed range finder).  Signs of Q's columns may differ from LAPACK's.
+ * Reference: the torch.linalg.qr calls of the range finders,
+ * acetn/linalg/svd_lowrank.py:36,39, fused_matmul_svd_lowrank.py:38,43,
+ * fused_3matmul_svd_lowrank.py:40,43,47. */
+#define CTM_DTYPE_F64 0
+#define CTM_DTYPE_F32 1
+int ctm_qr(void* Y, int64_t n, int64_t q, void* R, int32_t dtype, void* ws, size_t* ws_bytes,
+           ctm_stream_t stream);
+
 /* Thin SVD of an (m x n) FP64 matrix, m, n <= 4096: U (m x r), S (r), V (n x r),
  * r = min(m, n), singular values descending.  Used by svd_type "full-rank"
  * (acetn/renormalization/projectors.py:219-236). */

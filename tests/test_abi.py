@@ -131,6 +131,20 @@ def test_bad_sizes_are_invalid(lib):
     assert st == _abi.CTM_ERR_INVALID
     st = lib.ctm_svd_f64(None, 5000, 10, None, None, None, None, ctypes.byref(sz), None)
     assert st == _abi.CTM_ERR_UNSUPPORTED
+    st = lib.ctm_qr(None, 10, 11, None, 0, None, ctypes.byref(sz), None)
+    assert st == _abi.CTM_ERR_INVALID
+    st = lib.ctm_qr(None, 100, 10, None, 7, None, ctypes.byref(sz), None)
+    assert st == _abi.CTM_ERR_INVALID
+
+
+def test_qr_workspace_query(lib):
+    # FP32 Cholesky-QR at the D=6, chi=144 range-finder size: the input copy,
+    # the second buffer and one q x q Gram per row slab
+    n, q = 144 * 36, 160
+    for dtype, es in ((0, 8), (1, 4)):
+        sz = ctypes.c_size_t(0)
+        st = lib.ctm_qr(ctypes.c_void_p(0x1000), n, q, None, dtype, None, ctypes.byref(sz), None)
+        assert st == 0 and sz.value >= 2 * n * q * es
 
 
 def test_no_cpu_fallback():
