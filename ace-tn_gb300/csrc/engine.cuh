@@ -28,9 +28,12 @@ void to_f64(Ctx& c, const float* x, double* y, int64_t n);
 // --- linear algebra (FP64) ---------------------------------------------------
 // Orthonormal basis of the columns of Y (n x q, row-major): Y := Q.
 // If R != nullptr it receives the q x q upper-triangular factor with Y_in = Q R.
-void orthonormalize(Ctx& c, double* Y, int64_t n, int64_t q, double* R);
+// stages: Cholesky-QR stages (3: orthonormal to working precision; 2: to
+// ~u cond^2 after the shifted stage, i.e. about 1e-3 in FP32, for bases that
+// are only multiplied again in lower precision).
+void orthonormalize(Ctx& c, double* Y, int64_t n, int64_t q, double* R, int stages = 3);
 // The same in FP32 arithmetic (mixed path).
-void orthonormalize(Ctx& c, float* Y, int64_t n, int64_t q, float* R);
+void orthonormalize(Ctx& c, float* Y, int64_t n, int64_t q, float* R, int stages = 3);
 // Thin SVD of X (m x n, row-major, m >= n is not required):
 // X = U diag(S) V^T, U (m x r), S (r) descending, V (n x r), r = min(m, n).
 void svd_thin(Ctx& c, const double* X, int64_t m, int64_t n, double* U, double* S,

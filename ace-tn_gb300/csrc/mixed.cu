@@ -366,10 +366,13 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
     out.add(TcKind::kF32, Y, TcLayout::rows(m, q, q));
     tc_gemm(c, A1.q(false), t, x1, out);
   }
+  // The bases inside the power iteration are only multiplied again in BF16
+  // (~4e-3 relative): two Cholesky-QR stages (orthonormal to ~1e-3) suffice
+  // there; the final Q, which forms B in 3xBF16, gets three.
   for (int it = 0; it < o.rsvd_niter; ++it) {
     {
       KernelTimer span(c.stream, kTagOrtho, 0.0);
-      orthonormalize(c, Y, m, q, nullptr);
+      orthonormalize(c, Y, m, q, nullptr, 2);
     }
     Scope s2(c);
     float* Z = c.alloc<float>(size_t(n) * q);
@@ -383,7 +386,7 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
     }
     {
       KernelTimer span(c.stream, kTagOrtho, 0.0);
-      orthonormalize(c, Z, n, q, nullptr);
+      orthonormalize(c, Z, n, q, nullptr, 2);
     }
     const TcOperand zt = yt_operand_f32(c, Z, n, q, q, false);
     const TcOperand z3 = gemm_to_operand(c, A4.q(false), zt, x1, false);  // (Q4 Z)^T
