@@ -73,6 +73,7 @@ _SIGNATURES = {
                                       ctypes.c_int),
     "ctm_qr": ([c_vp, c_i64, c_i64, c_vp, c_i32, c_vp, c_sz_p, c_vp], ctypes.c_int),
     "ctm_svd_f64": ([c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp, c_sz_p, c_vp], ctypes.c_int),
+    "ctm_svd_f32": ([c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp, c_sz_p, c_vp], ctypes.c_int),
     "ctm_matmul": ([c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i32, c_vp, c_sz_p, c_vp],
                    ctypes.c_int),
     "ctm_matmul_mixed_noalloc": ([c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_vp], ctypes.c_int),

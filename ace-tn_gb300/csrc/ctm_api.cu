@@ -768,6 +768,15 @@ int ctm_qr(void* Y, int64_t n, int64_t q, void* R, int32_t dtype, void* ws, size
   });
 }
 
+int ctm_svd_f32(const float* bt, int64_t n, int64_t q, double* U, double* S, float* V, void* ws,
+                size_t* ws_bytes, ctm_stream_t stream) {
+  return with_workspace(ws, ws_bytes, as_stream(stream), [&](Ctx& c) {
+    CTM_REQUIRE(q >= 1 && q <= 1024 && q <= n, CTM_ERR_UNSUPPORTED,
+                "ctm_svd_f32: 1 <= q <= min(n, 1024)");
+    svd_via_qr(c, bt, q, n, U, S, V);
+  });
+}
+
 int ctm_matmul(const double* A, const double* B, double* C, int64_t M, int64_t N, int64_t K,
                int32_t precision, void* ws, size_t* ws_bytes, ctm_stream_t stream) {
   return with_workspace(ws, ws_bytes, as_stream(stream), [&](Ctx& c) {

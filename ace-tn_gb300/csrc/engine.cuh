@@ -41,8 +41,8 @@ void svd_thin(Ctx& c, const double* X, int64_t m, int64_t n, double* U, double* 
 // Thin SVD of B (q x n, q <= min(n, 1024)) for the mixed path, from
 // Bt = B^T (n x q, FP32): R of a shifted Cholesky-QR3 of Bt (B = R^T Qb^T),
 // FP32 one-sided Jacobi on the columns of R with accumulated rotations
-// (Ub = its left singular vectors; singular values to ~1e-7 s_0 absolute,
-// far below the ~1e-5 s_0 of the 3xBF16 products that form B),
+// (Ub = its left singular vectors, orthogonal to ~1e-6; singular values to
+// ~1e-6 s_0, below the ~1e-5 s_0 of the 3xBF16 products that form B),
 // V = B^T Ub diag(1/s) in FP32.
 void svd_via_qr(Ctx& c, const float* Bt, int64_t q, int64_t n, double* Ub, double* S, float* V);
 // Truncation of acetn/renormalization/projectors.py:163-167 on a descending

@@ -11,6 +11,8 @@
 //    projectors (acetn/renormalization/projectors.py:163-167).
 #include "engine.cuh"
 
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <type_traits>
 #include <cmath>
@@ -518,14 +520,19 @@ __global__ void __launch_bounds__(kCh > 0 ? 128 * kCh : 1024) jacobi_onesided_f3
           continue;
         const float zeta = (be - al) / (2.f * ga);
         const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
-        const float cs = 1.f / sqrtf(1.f + t * t), sn = cs * t;
+        // Rutishauser's form of the rotation (x' = x - s (y + tau x),
+        // y' = y + s (x - tau y), tau = s / (1 + c)): the second-order term
+        // s tau ~ t^2 / 2 is applied explicitly; with c rounded to 1 for
+        // t^2 < 2^-24, c x - s y would lengthen the pair by a factor 1 + t^2
+        // per rotation, a bias that builds up over the sweeps
+        const float cs = 1.f / sqrtf(1.f + t * t), sn = cs * t, tau = sn / (1.f + cs);
         float4* ja = reinterpret_cast<float4*>(Jc + size_t(i) * ld) + sub;
         float4* jb = reinterpret_cast<float4*>(Jc + size_t(j) * ld) + sub;
         auto rot = [&](float4* pa, float4* pb, const float4 x, const float4 y) {
-          *pa = make_float4(cs * x.x - sn * y.x, cs * x.y - sn * y.y, cs * x.z - sn * y.z,
-                            cs * x.w - sn * y.w);
-          *pb = make_float4(sn * x.x + cs * y.x, sn * x.y + cs * y.y, sn * x.z + cs * y.z,
-                            sn * x.w + cs * y.w);
+          *pa = make_float4(fmaf(-sn, fmaf(tau, x.x, y.x), x.x), fmaf(-sn, fmaf(tau, x.y, y.y), x.y),
+                            fmaf(-sn, fmaf(tau, x.z, y.z), x.z), fmaf(-sn, fmaf(tau, x.w, y.w), x.w));
+          *pb = make_float4(fmaf(sn, fmaf(-tau, y.x, x.x), y.x), fmaf(sn, fmaf(-tau, y.y, x.y), y.y),
+                            fmaf(sn, fmaf(-tau, y.z, x.z), y.z), fmaf(sn, fmaf(-tau, y.w, x.w), y.w));
         };
         if (kCh > 0) {
           float4 u[kR], v[kR];
@@ -562,6 +569,193 @@ __global__ void __launch_bounds__(kCh > 0 ? 128 * kCh : 1024) jacobi_onesided_f3
     const int r = idx / q, c = idx - r * q;
     Jc_g[idx] = Jc[r * ld + c];
   }
+}
+
+// One plane rotation of the one-sided Jacobi on a pair of rows (ra, rb) of
+// kCh float4 chunks per thread, 8 threads per pair (thread sub owns chunks
+// sub + 8 m); the accumulated-rotation rows follow at ra + ld, rb + ld.
+// Every lane of the warp must call it (full-mask shuffles).  Returns whether
+// the pair was rotated.
+template <int kCh>
+__device__ __forceinline__ bool jacobi_rotate_pair(float* ra, float* rb, int ld, int sub,
+                                                   float tol) {
+  float4* a = reinterpret_cast<float4*>(ra) + sub;
+  float4* b = reinterpret_cast<float4*>(rb) + sub;
+  float4 xa[kCh], xb[kCh];
+#pragma unroll
+  for (int m = 0; m < kCh; ++m) {
+    xa[m] = a[8 * m];
+    xb[m] = b[8 * m];
+  }
+  float al = 0.f, be = 0.f, ga = 0.f, al2 = 0.f, be2 = 0.f, ga2 = 0.f;
+#pragma unroll
+  for (int m = 0; m < kCh; ++m) {
+    const float4 x = xa[m], y = xb[m];
+    al = fmaf(x.x, x.x, fmaf(x.y, x.y, al));
+    al2 = fmaf(x.z, x.z, fmaf(x.w, x.w, al2));
+    be = fmaf(y.x, y.x, fmaf(y.y, y.y, be));
+    be2 = fmaf(y.z, y.z, fmaf(y.w, y.w, be2));
+    ga = fmaf(x.x, y.x, fmaf(x.y, y.y, ga));
+    ga2 = fmaf(x.z, y.z, fmaf(x.w, y.w, ga2));
+  }
+  al += al2;
+  be += be2;
+  ga += ga2;
+  for (int o = 4; o > 0; o >>= 1) {
+    al += __shfl_xor_sync(0xffffffffu, al, o);
+    be += __shfl_xor_sync(0xffffffffu, be, o);
+    ga += __shfl_xor_sync(0xffffffffu, ga, o);
+  }
+  if (al == 0.f || be == 0.f || !(fabsf(ga) > tol * sqrtf(al) * sqrtf(be))) return false;
+  const float zeta = (be - al) / (2.f * ga);
+  const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+  // Rutishauser's form, as in jacobi_onesided_f32_kernel
+  const float cs = 1.f / sqrtf(1.f + t * t), sn = cs * t, tau = sn / (1.f + cs);
+  float4* ja = reinterpret_cast<float4*>(ra + ld) + sub;
+  float4* jb = reinterpret_cast<float4*>(rb + ld) + sub;
+  auto rot = [&](float4* pa, float4* pb, const float4 x, const float4 y) {
+    *pa = make_float4(fmaf(-sn, fmaf(tau, x.x, y.x), x.x), fmaf(-sn, fmaf(tau, x.y, y.y), x.y),
+                      fmaf(-sn, fmaf(tau, x.z, y.z), x.z), fmaf(-sn, fmaf(tau, x.w, y.w), x.w));
+    *pb = make_float4(fmaf(sn, fmaf(-tau, y.x, x.x), y.x), fmaf(sn, fmaf(-tau, y.y, x.y), y.y),
+                      fmaf(sn, fmaf(-tau, y.z, x.z), y.z), fmaf(sn, fmaf(-tau, y.w, x.w), y.w));
+  };
+  float4 u[kCh], v[kCh];
+#pragma unroll
+  for (int m = 0; m < kCh; ++m) {
+    u[m] = ja[8 * m];
+    v[m] = jb[8 * m];
+  }
+#pragma unroll
+  for (int m = 0; m < kCh; ++m) {
+    rot(a + 8 * m, b + 8 * m, xa[m], xb[m]);
+    rot(ja + 8 * m, jb + 8 * m, u[m], v[m]);
+  }
+  return true;
+}
+
+// Block one-sided Jacobi on a cluster of P CTAs (same rotations and
+// convergence test as jacobi_onesided_f32_kernel, another cyclic order).
+// The rows (padded with zero rows to 2 P b, b a multiple of 4) form 2 P
+// blocks of b rows; CTA k holds the blocks at tournament positions k ("top")
+// and 2P-1-k ("bottom") in shared memory, each row stored as ld floats of Mc
+// followed by ld floats of the accumulated rotations J.  A sweep is 2P-1
+// block rounds of the circle method (position 0 fixed, the others advance by
+// one per round): in a round every CTA rotates all b^2 top-bottom pairs, b
+// disjoint pairs at a time (bottom row (i + s) mod b against top row i), and
+// in the first round of a sweep also the pairs inside each of its two blocks
+// (b - 1 rounds of the circle method on b rows).  Every pair of rows is thus
+// visited once per sweep.  After a round each CTA writes the blocks that move
+// into the receiving CTAs' second buffers (distributed shared memory) and the
+// cluster synchronises; after 2P-1 rounds the blocks are back home.  The
+// sweep loop ends when no CTA rotated in a sweep: every CTA reads all CTAs'
+// per-sweep flags after the same cluster barrier, so all take the same
+// decision and arrive at the same barriers.
+template <int kCh>
+__global__ void __launch_bounds__(256) jacobi_cluster_f32_kernel(const float* Mc_g, int q, int b,
+                                                                 float* Jc_g, float* norms,
+                                                                 int max_sweeps, float tol,
+                                                                 int* flags) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int P = int(cluster.num_blocks());
+  const int k = int(cluster.block_rank());
+  extern __shared__ __align__(16) float jcl_smem[];
+  __shared__ int s_rot[64];
+  constexpr int ld = 32 * kCh;
+  constexpr int RS = 2 * ld;  // row stride: Mc, then J
+  const int blk = b * RS;     // floats per block
+  float* cur = jcl_smem;      // top block, then bottom block
+  float* nxt = jcl_smem + 2 * blk;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int g = tid >> 3, sub = tid & 7;
+  for (int half = 0; half < 2; ++half) {
+    const int beta = half == 0 ? k : 2 * P - 1 - k;
+    float* base = cur + half * blk;
+    for (int r = tid >> 5; r < b; r += nth >> 5)
+      for (int c = tid & 31; c < RS; c += 32) {
+        const int gr = beta * b + r;
+        float v = 0.f;
+        if (gr < q) v = c < ld ? (c < q ? Mc_g[size_t(gr) * q + c] : 0.f) : (c - ld == gr ? 1.f : 0.f);
+        base[r * RS + c] = v;
+      }
+  }
+  for (int i = tid; i < 64; i += nth) s_rot[i] = 0;
+  cluster.sync();
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    bool rotated = false;
+    for (int t = 0; t < 2 * P - 1; ++t) {
+      const int nin = t == 0 ? b - 1 : 0;  // rounds inside the blocks
+      for (int lr = 0; lr < nin + b; ++lr) {
+        int ia, ib;
+        if (lr < nin) {
+          const int half = g < b / 2 ? 0 : 1;
+          const int kk = half == 0 ? g : g - b / 2;
+          const int i0 = kk == 0 ? 0 : ((kk - 1 + lr) % (b - 1)) + 1;
+          const int k2 = b - 1 - kk;
+          const int j0 = k2 == 0 ? 0 : ((k2 - 1 + lr) % (b - 1)) + 1;
+          ia = half * blk + i0 * RS;
+          ib = half * blk + j0 * RS;
+        } else {
+          const int sft = lr - nin;
+          ia = g * RS;
+          ib = blk + ((g + sft) % b) * RS;
+        }
+        rotated |= jacobi_rotate_pair<kCh>(cur + ia, cur + ib, ld, sub, tol);
+        __syncthreads();
+      }
+      // move the blocks: position p -> p + 1 (2P-1 -> 1, 0 stays)
+      float* dst_top;
+      float* dst_bot;
+      if (k == 0) {
+        dst_top = nxt;
+        dst_bot = cluster.map_shared_rank(nxt, 1);
+      } else if (k < P - 1) {
+        dst_top = cluster.map_shared_rank(nxt, k + 1);
+        dst_bot = cluster.map_shared_rank(nxt + blk, k - 1);
+      } else {
+        dst_top = nxt + blk;
+        dst_bot = cluster.map_shared_rank(nxt + blk, k - 1);
+      }
+      const float4* st4 = reinterpret_cast<const float4*>(cur);
+      const float4* sb4 = reinterpret_cast<const float4*>(cur + blk);
+      for (int i = tid; i < blk / 4; i += nth) {
+        reinterpret_cast<float4*>(dst_top)[i] = st4[i];
+        reinterpret_cast<float4*>(dst_bot)[i] = sb4[i];
+      }
+      cluster.sync();
+      float* tmp = cur;
+      cur = nxt;
+      nxt = tmp;
+    }
+    if (rotated) s_rot[sweep] = 1;
+    cluster.sync();
+    int any = 0;
+    for (int r = 0; r < P; ++r) any |= *cluster.map_shared_rank(&s_rot[sweep], r);
+    if (any == 0) break;
+  }
+  if (tid == 0 && k == 0 && sweep == max_sweeps) atomicOr(flags, 2);
+  // the blocks are home: top = block k, bottom = block 2P-1-k
+  for (int rr = tid; rr < 2 * b; rr += nth) {
+    const int half = rr < b ? 0 : 1, r = rr - half * b;
+    const int gr = (half == 0 ? k : 2 * P - 1 - k) * b + r;
+    if (gr >= q) continue;
+    const float* row = cur + half * blk + r * RS;
+    float nn = 0.f;
+    for (int c = 0; c < q; ++c) nn = fmaf(row[c], row[c], nn);
+    norms[gr] = sqrtf(nn);
+  }
+  for (int half = 0; half < 2; ++half) {
+    const int beta = half == 0 ? k : 2 * P - 1 - k;
+    for (int r = tid >> 5; r < b; r += nth >> 5) {
+      const int gr = beta * b + r;
+      if (gr >= q) continue;
+      const float* jrow = cur + half * blk + r * RS + ld;
+      for (int c = tid & 31; c < q; c += 32) Jc_g[size_t(gr) * q + c] = jrow[c];
+    }
+  }
+  // no CTA may leave while others can still read its shared memory
+  cluster.sync();
 }
 
 // Ub[:, r] = J[:, order[r]] (J columns stored as rows of Jc), S[r] = norm,
@@ -1265,6 +1459,46 @@ void jacobi_left_singular(Ctx& c, const float* Mc, int64_t q, double* Ub, double
   float* Wg = jac_smem ? nullptr : c.alloc<float>(size_t(2) * q * jacobi_ld(int(q)));
   const int64_t pp = q + (q & 1);
   if (c.sizing()) return;
+  // q >= 96: the block Jacobi on a cluster of kJacobiCluster CTAs (rows
+  // padded to a multiple of 8 kJacobiCluster: b a multiple of 4, 8 b threads
+  // per CTA) when its four blocks of b rows fit in shared memory (q <= 224)
+  constexpr int kJacobiCluster = 4;
+  const int P = kJacobiCluster;
+  const int qp = int((q + 8 * P - 1) / (8 * P) * (8 * P));
+  const int b = qp / (2 * P);
+  const int ldj = jacobi_ld(int(q));
+  const size_t smem = size_t(4) * b * 2 * ldj * sizeof(float);
+  if (q >= 96 && ldj <= 256 && smem <= size_t(227) * 1024) {
+    auto launch = [&](auto kern) {
+      CTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+      cudaLaunchConfig_t cfg{};
+      cfg.gridDim = dim3(P);
+      cfg.blockDim = dim3(8 * b);
+      cfg.dynamicSmemBytes = smem;
+      cfg.stream = c.stream;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = unsigned(P);
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      CTM_CUDA(cudaLaunchKernelEx(&cfg, kern, static_cast<const float*>(Mc), int(q), b, Jc, norms,
+                                  40, 4e-6f, status_flags(c)));
+    };
+    switch (ldj / 32) {
+      case 3: launch(jacobi_cluster_f32_kernel<3>); break;
+      case 4: launch(jacobi_cluster_f32_kernel<4>); break;
+      case 5: launch(jacobi_cluster_f32_kernel<5>); break;
+      case 6: launch(jacobi_cluster_f32_kernel<6>); break;
+      case 7: launch(jacobi_cluster_f32_kernel<7>); break;
+      default: launch(jacobi_cluster_f32_kernel<8>); break;
+    }
+    CTM_LAUNCH_CHECK();
+    sort_singular_kernel<<<1, 256, 0, c.stream>>>(Jc, norms, int(q), Ub, S, inv_s);
+    CTM_LAUNCH_CHECK();
+    return;
+  }
   // FP32 dot products of length q carry ~sqrt(q) u relative error: 4e-6
   // is the smallest coupling the sweeps can drive below.  One group of 8
   // threads per pair of a round (no idle warps at the round barriers).

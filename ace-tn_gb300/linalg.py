@@ -108,6 +108,25 @@ def svd(A):
     return U, S, V
 
 
+def svd_f32(Bt):
+    """SVD (U, S, V) of B = Bt^T for a float32 CUDA matrix Bt (n x q, n >= q):
+    the FP32 Rayleigh-Ritz SVD of the mixed path (Cholesky-QR3 of Bt, then
+    one-sided Jacobi).  U (q x q) and S in float64, V (n x q) in float32,
+    B ~= U diag(S) V^T, S descending."""
+    if not isinstance(Bt, torch.Tensor) or not Bt.is_cuda or Bt.dtype != torch.float32:
+        raise ValueError("Bt must be a float32 CUDA tensor")
+    Bt = Bt.contiguous()
+    n, q = Bt.shape
+    if not n >= q >= 1:
+        raise ValueError(f"svd_f32 needs rows >= columns >= 1, got {tuple(Bt.shape)}")
+    U = torch.empty(q, q, dtype=torch.float64, device=Bt.device)
+    S = torch.empty(q, dtype=torch.float64, device=Bt.device)
+    V = torch.empty(n, q, dtype=torch.float32, device=Bt.device)
+    _abi.call("ctm_svd_f32", [_abi.ptr(Bt), n, q, _abi.ptr(U), _abi.ptr(S), _abi.ptr(V)],
+              Bt.device)
+    return U, S, V
+
+
 def matmul(A, B, precision="fp64"):
     """A @ B with the library's FP64 or mixed-precision GEMM engine."""
     _abi.require_cuda(A, "A")

@@ -212,6 +212,16 @@ int ctm_qr(void* Y, int64_t n, int64_t q, void* R, int32_t dtype, void* ws, size
 int ctm_svd_f64(const double* a, int64_t m, int64_t n, double* U, double* S, double* V,
                 void* ws, size_t* ws_bytes, ctm_stream_t stream);
 
+/* Thin SVD of the mixed path's Rayleigh-Ritz step: B = bt^T (q x n, given as
+ * bt, n x q FP32 row-major, 1 <= q <= min(n, 1024)) = U diag(S) V^T with U
+ * (q x q, FP64), S (q, descending, FP64), V (n x q, FP32).  FP32 shifted
+ * Cholesky-QR3 of bt, then FP32 one-sided Jacobi with accumulated rotations
+ * (on a 4-CTA cluster from q = 96).  Replaces the torch.linalg.svd of the
+ * projected matrix in acetn/linalg/fused_matmul_svd_lowrank.py:45-51 on the
+ * mixed path; no direct counterpart, exposed to test and measure that stage. */
+int ctm_svd_f32(const float* bt, int64_t n, int64_t q, double* U, double* S, float* V,
+                void* ws, size_t* ws_bytes, ctm_stream_t stream);
+
 /* Matrix product C = A @ B of FP64 row-major matrices, with the library's
  * arithmetic: CTM_PREC_FP64 (FP64 FMAs), CTM_PREC_MIXED (3xBF16 split
  * products on tcgen05 tensor cores, FP32 accumulation) or CTM_PREC_BF16 (one
