@@ -43,6 +43,18 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
 }
 
+// Paired FP32 FMA of Blackwell (fma.rn.f32x2): d = a * b + c in each lane,
+// rounded as fmaf, one instruction for two.
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;"
+      : "=l"(d)
+      : "l"(*reinterpret_cast<unsigned long long*>(&a)),
+        "l"(*reinterpret_cast<unsigned long long*>(&b)),
+        "l"(*reinterpret_cast<unsigned long long*>(&c)));
+  return *reinterpret_cast<float2*>(&d);
+}
+
 constexpr int LT = 256;  // threads of one-CTA linear-algebra kernels
 
 template <class T>
@@ -160,7 +172,9 @@ __global__ void __launch_bounds__(LT) householder_qr_kernel(T* Y, int64_t n, int
 // and of E on other threads) and stores the scaled multipliers
 // S[t][i] = W[J+t][i] / d_t of the rows below; (c) every thread takes 4 x 4
 // tiles of the trailing rows (W: upper-triangular tiles only) and subtracts
-// sum_t S[t][i] row_(J+t) with 128-bit shared-memory accesses.
+// sum_t S[t][i] row_(J+t) with 128-bit shared-memory accesses.  (A
+// look-ahead, warp 0 eliminating the next diagonal block during (c), saved
+// under 1% at q = 160: (a) outlasts the rest of (c) in most blocks.)
 // W and E are q4 x ld (q4 = q rounded up to kCholNb, ld = q4 + 4) with zero
 // padding, so the pivot rows of the last block and every 4 x 4 tile are in
 // bounds.
@@ -581,50 +595,64 @@ __device__ __forceinline__ bool jacobi_rotate_pair(float* ra, float* rb, int ld,
                                                    float tol) {
   float4* a = reinterpret_cast<float4*>(ra) + sub;
   float4* b = reinterpret_cast<float4*>(rb) + sub;
-  float4 xa[kCh], xb[kCh];
+  float4* ja = reinterpret_cast<float4*>(ra + ld) + sub;
+  float4* jb = reinterpret_cast<float4*>(rb + ld) + sub;
+  // the rotation rows are loaded with the data rows, ahead of the decision
+  float4 xa[kCh], xb[kCh], u[kCh], v[kCh];
 #pragma unroll
   for (int m = 0; m < kCh; ++m) {
     xa[m] = a[8 * m];
     xb[m] = b[8 * m];
   }
-  float al = 0.f, be = 0.f, ga = 0.f, al2 = 0.f, be2 = 0.f, ga2 = 0.f;
-#pragma unroll
-  for (int m = 0; m < kCh; ++m) {
-    const float4 x = xa[m], y = xb[m];
-    al = fmaf(x.x, x.x, fmaf(x.y, x.y, al));
-    al2 = fmaf(x.z, x.z, fmaf(x.w, x.w, al2));
-    be = fmaf(y.x, y.x, fmaf(y.y, y.y, be));
-    be2 = fmaf(y.z, y.z, fmaf(y.w, y.w, be2));
-    ga = fmaf(x.x, y.x, fmaf(x.y, y.y, ga));
-    ga2 = fmaf(x.z, y.z, fmaf(x.w, y.w, ga2));
-  }
-  al += al2;
-  be += be2;
-  ga += ga2;
-  for (int o = 4; o > 0; o >>= 1) {
-    al += __shfl_xor_sync(0xffffffffu, al, o);
-    be += __shfl_xor_sync(0xffffffffu, be, o);
-    ga += __shfl_xor_sync(0xffffffffu, ga, o);
-  }
-  if (al == 0.f || be == 0.f || !(fabsf(ga) > tol * sqrtf(al) * sqrtf(be))) return false;
-  const float zeta = (be - al) / (2.f * ga);
-  const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
-  // Rutishauser's form, as in jacobi_onesided_f32_kernel
-  const float cs = 1.f / sqrtf(1.f + t * t), sn = cs * t, tau = sn / (1.f + cs);
-  float4* ja = reinterpret_cast<float4*>(ra + ld) + sub;
-  float4* jb = reinterpret_cast<float4*>(rb + ld) + sub;
-  auto rot = [&](float4* pa, float4* pb, const float4 x, const float4 y) {
-    *pa = make_float4(fmaf(-sn, fmaf(tau, x.x, y.x), x.x), fmaf(-sn, fmaf(tau, x.y, y.y), x.y),
-                      fmaf(-sn, fmaf(tau, x.z, y.z), x.z), fmaf(-sn, fmaf(tau, x.w, y.w), x.w));
-    *pb = make_float4(fmaf(sn, fmaf(-tau, y.x, x.x), y.x), fmaf(sn, fmaf(-tau, y.y, x.y), y.y),
-                      fmaf(sn, fmaf(-tau, y.z, x.z), y.z), fmaf(sn, fmaf(-tau, y.w, x.w), y.w));
-  };
-  float4 u[kCh], v[kCh];
 #pragma unroll
   for (int m = 0; m < kCh; ++m) {
     u[m] = ja[8 * m];
     v[m] = jb[8 * m];
   }
+  // dot products in paired FMAs: four partial sums per quantity
+  float2 al2a = make_float2(0.f, 0.f), al2b = al2a, be2a = al2a, be2b = al2a, ga2a = al2a,
+         ga2b = al2a;
+#pragma unroll
+  for (int m = 0; m < kCh; ++m) {
+    const float2 x0 = make_float2(xa[m].x, xa[m].y), x1 = make_float2(xa[m].z, xa[m].w);
+    const float2 y0 = make_float2(xb[m].x, xb[m].y), y1 = make_float2(xb[m].z, xb[m].w);
+    al2a = fma2(x0, x0, al2a);
+    al2b = fma2(x1, x1, al2b);
+    be2a = fma2(y0, y0, be2a);
+    be2b = fma2(y1, y1, be2b);
+    ga2a = fma2(x0, y0, ga2a);
+    ga2b = fma2(x1, y1, ga2b);
+  }
+  float al = (al2a.x + al2a.y) + (al2b.x + al2b.y);
+  float be = (be2a.x + be2a.y) + (be2b.x + be2b.y);
+  float ga = (ga2a.x + ga2a.y) + (ga2b.x + ga2b.y);
+  for (int o = 4; o > 0; o >>= 1) {
+    al += __shfl_xor_sync(0xffffffffu, al, o);
+    be += __shfl_xor_sync(0xffffffffu, be, o);
+    ga += __shfl_xor_sync(0xffffffffu, ga, o);
+  }
+  // |ga| > tol sqrt(al be) without square roots
+  if (al == 0.f || be == 0.f || !(ga * ga > (tol * tol * al) * be)) return false;
+  // Rotation parameters from approximate reciprocals and square roots: in
+  // Rutishauser's form an error e in c changes the orthogonality of the
+  // rotation by only ~s^2 e, so 2-ulp parameters cost nothing, while the
+  // correctly rounded divisions and roots sat on the critical path of every
+  // round.  |zeta| is capped at 1e18 so that zeta^2 stays finite (t is then
+  // ~1/(2 zeta), a negligible rotation either way); zeta = 0 gives t = 1.
+  const float zeta = __fdividef(be - al, 2.f * ga);
+  const float az = fminf(fabsf(zeta), 1e18f);
+  const float t = copysignf(__fdividef(1.f, az + sqrtf(fmaf(az, az, 1.f))), zeta);
+  const float cs = rsqrtf(fmaf(t, t, 1.f)), sn = cs * t, tau = __fdividef(sn, 1.f + cs);
+  const float2 s2 = make_float2(sn, sn), ms2 = make_float2(-sn, -sn);
+  const float2 t2 = make_float2(tau, tau), mt2 = make_float2(-tau, -tau);
+  auto rot = [&](float4* pa, float4* pb, const float4 x, const float4 y) {
+    const float2 x0 = make_float2(x.x, x.y), x1 = make_float2(x.z, x.w);
+    const float2 y0 = make_float2(y.x, y.y), y1 = make_float2(y.z, y.w);
+    const float2 p0 = fma2(ms2, fma2(t2, x0, y0), x0), p1 = fma2(ms2, fma2(t2, x1, y1), x1);
+    const float2 q0 = fma2(s2, fma2(mt2, y0, x0), y0), q1 = fma2(s2, fma2(mt2, y1, x1), y1);
+    *pa = make_float4(p0.x, p0.y, p1.x, p1.y);
+    *pb = make_float4(q0.x, q0.y, q1.x, q1.y);
+  };
 #pragma unroll
   for (int m = 0; m < kCh; ++m) {
     rot(a + 8 * m, b + 8 * m, xa[m], xb[m]);
