@@ -48,31 +48,48 @@ def move_flops(D, chi, q, d=2, ny=2, niter=2):
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle-reason samples during the timed region."""
+    """nvidia-smi clock / throttle-reason samples during the timed region:
+    sampled every 50 ms from before the region starts (start() waits for the
+    first sample), each sample stamped on arrival; stop() keeps the samples
+    that arrived inside the window set by mark_start() / mark_end() (plus one
+    sampling interval), or the nearest one when the region is shorter than
+    the interval."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
+    INTERVAL_MS = 50
+
     def __init__(self, index):
         self.index = index
         self.proc = None
         self.lines = []
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
-                 "-i", str(self.index), "-lms", "200"],
+                 "-i", str(self.index), "-lms", str(self.INTERVAL_MS)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            deadline = time.monotonic() + 5.0
+            while not self.lines and time.monotonic() < deadline and self.proc.poll() is None:
+                time.sleep(0.01)
         except (OSError, ValueError):
             self.proc = None
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.monotonic(), line.strip()))
+
+    def mark_start(self):
+        self.t0 = time.monotonic()
+
+    def mark_end(self):
+        self.t1 = time.monotonic()
 
     def stop(self):
         if self.proc is None:
@@ -85,7 +102,16 @@ class ClockSampler:
         sm, mx, reasons = [], None, set()
         names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
                  "sw_power_cap"]
-        for line in self.lines:
+        lines = list(self.lines)
+        in_window = True
+        if self.t0 is not None and self.t1 is not None and lines:
+            slack = self.INTERVAL_MS / 1e3
+            keep = [x for x in lines if self.t0 <= x[0] <= self.t1 + slack]
+            if not keep:
+                in_window = False
+                keep = [min(lines, key=lambda x: abs(x[0] - 0.5 * (self.t0 + self.t1)))]
+            lines = keep
+        for _, line in lines:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -97,8 +123,13 @@ class ClockSampler:
             for name, val in zip(names[1:], parts[5:9]):
                 if val.lower() in ("active", "1", "yes"):
                     reasons.add(name)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        out = {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+               "reasons": sorted(reasons), "samples": len(sm),
+               "interval_ms": self.INTERVAL_MS}
+        if self.t0 is not None and self.t1 is not None:
+            out["window_ms"] = round(1e3 * (self.t1 - self.t0), 1)
+            out["in_window"] = in_window
+        return out
 
 
 def package():
@@ -229,6 +260,7 @@ def run_gb300(args, rank, world, local_rank):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
     torch.cuda.synchronize(dev)
+    clocks.mark_start()
     for i in range(args.steps):
         flush.zero_()
         k, idx = order[pos % len(order)]
@@ -237,6 +269,7 @@ def run_gb300(args, rank, world, local_rank):
         ev[i][1].record(stream)
         pos += 1
     torch.cuda.synchronize(dev)
+    clocks.mark_end()
     launches = gb._abi.kernel_launches() - launches0
     qr_fallbacks = gb._abi.qr_fallbacks(dev)
     clk = clocks.stop()
@@ -275,12 +308,14 @@ def run_gb300(args, rank, world, local_rank):
         clocks = ClockSampler(local_rank)
         clocks.start()
         torch.cuda.synchronize(dev)
+        clocks.mark_start()
         for i in range(replays):
             flush.zero_()
             gev[i][0].record(stream)
             graph.replay(1)
             gev[i][1].record(stream)
         torch.cuda.synchronize(dev)
+        clocks.mark_end()
         clk = clocks.stop()
         total_s = sum(a.elapsed_time(b) for a, b in gev) / 1e3
         graph_truncated = graph.truncated()
@@ -305,18 +340,21 @@ def run_gb300(args, rank, world, local_rank):
                       "C": [c.to(dev, non_blocking=True) for c in hs["C"]],
                       "E": [e.to(dev, non_blocking=True) for e in hs["E"]]}
         h2d = state_bytes(dst)
+        before = {s: (list(dst[s]["C"]), list(dst[s]["E"])) for s in st.site_list}
         mover.move(dst, k, idx)
-        # read back the tensors the move rewrote
+        # read back the step's result: the tensors the move replaced (two
+        # corners and one edge of each renormalised site), found by identity
         moved = 0
         for s in st.site_list:
-            outs = {"C": [c.to("cpu", non_blocking=True) for c in dst[s]["C"]],
-                    "E": [e.to("cpu", non_blocking=True) for e in dst[s]["E"]]}
-            moved += sum(c.numel() * 8 for c in outs["C"]) + sum(e.numel() * 8 for e in outs["E"])
-            host[s]["C"], host[s]["E"] = outs["C"], outs["E"]
+            for key, old_list in zip(("C", "E"), before[s]):
+                for n, t in enumerate(dst[s][key]):
+                    if t is not old_list[n]:
+                        host[s][key][n] = t.to("cpu", non_blocking=True)
+                        moved += t.numel() * t.element_size()
         torch.cuda.synchronize(dev)
         for s in st.site_list:
-            host[s]["C"] = [c.pin_memory() for c in host[s]["C"]]
-            host[s]["E"] = [e.pin_memory() for e in host[s]["E"]]
+            host[s]["C"] = [c if c.is_pinned() else c.pin_memory() for c in host[s]["C"]]
+            host[s]["E"] = [e if e.is_pinned() else e.pin_memory() for e in host[s]["E"]]
         d2h = moved
     e2e_s = time.perf_counter() - t0
     e2e_value = world * e2e_steps / e2e_s
@@ -335,7 +373,7 @@ def run_gb300(args, rank, world, local_rank):
         # the double-layer contraction GEMMs (enlarged corners and edge
         # renormalization, 3xBF16 on tcgen05) are the largest kernel class
         dom_ms, dom_work, dom_n = prof["tc_gemm_double_layer"]
-        dom = "tc_gemm_kernel (double-layer contraction, 3xBF16)"
+        dom = "tc_gemm_persistent_kernel (double-layer contraction, 3xBF16)"
         peak = peaks.get("bf16_tflops_sustained") or 1700.0
         peak_src = ("MEASURED_PEAKS.json bf16_tflops_sustained" if peaks
                     else "fallback 1.7 PF/s")

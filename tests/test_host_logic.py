@@ -68,3 +68,39 @@ def test_models_match_oracle_hamiltonians():
     m = gb.IsingModel(1.0, 3.0)
     assert np.allclose(m.two_site_hamiltonian(None).numpy(), orc.ising_model(1.0, 3.0)["two_site_ham"](None))
     assert np.allclose(m.one_site_hamiltonian((0, 0)).numpy(), -3.0 * np.array([[0, 1], [1, 0]]))
+
+
+def test_clock_sampler_keeps_samples_of_the_timed_window():
+    """bench.py's clock record: only samples that arrived inside the timed
+    window count; throttle reasons are collected from them."""
+    import importlib.util
+    import os
+    spec = importlib.util.spec_from_file_location(
+        "bench_mod", os.path.join(os.path.dirname(os.path.dirname(__file__)), "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+
+    class FakeProc:
+        def terminate(self):
+            pass
+
+        def wait(self, timeout=None):
+            return 0
+
+    s = bench.ClockSampler(0)
+    s.proc = FakeProc()
+    row = "0, {sm}, 2070, 900.0, 0x0, Not Active, Not Active, {th}, Not Active"
+    s.lines = [(0.0, row.format(sm=1000, th="Active")),     # before the window
+               (1.00, row.format(sm=2070, th="Not Active")),
+               (1.02, row.format(sm=2050, th="Not Active")),
+               (9.0, row.format(sm=500, th="Active"))]     # after the window
+    s.t0, s.t1 = 0.99, 1.01
+    out = s.stop()
+    assert out["samples"] == 2 and out["sm_mhz"] == 2060.0 and out["in_window"]
+    assert out["reasons"] == [] and out["sm_max_mhz"] == 2070.0
+    # a window shorter than the interval keeps the nearest sample
+    s.lines = [(0.0, row.format(sm=1000, th="Not Active")), (5.0, row.format(sm=1500, th="Active"))]
+    s.t0, s.t1 = 4.9, 4.91
+    out = s.stop()
+    assert out["samples"] == 1 and out["sm_mhz"] == 1500.0 and not out["in_window"]
+    assert out["reasons"] == ["sw_thermal_slowdown"]
