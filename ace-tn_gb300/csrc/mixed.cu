@@ -136,42 +136,47 @@ QOps quarter_mixed(Ctx& c, const Site& S, int k) {
   bf16* th = c.alloc<bf16>(size_t(cc) * D2 * ld2);
   bf16* tl = c.alloc<bf16>(size_t(cc) * D2 * ld2);
   split_bf16(c, t1, a, cc * D2, cc * D2, true, th, tl, ld2);
-  // X[(c,e)][(l,L,u,U)]: rows of GEMM 1 are (c,u,U), columns (e,l,L); the
-  // epilogue's lanes (rows) then store contiguous (u,U) runs
+  // X[(c,e)][(l,L,u,U)]: rows of GEMM 1 are (e,l,L), columns (c,u,U), so
+  // that each epilogue thread's consecutive columns are consecutive (u,U)
+  // in X: aligned groups of 4 (D^2 % 4 == 0) go out as one 8-byte store
+  // (with rows (c,u,U) every element was a separate 2-byte store and this
+  // K = chi GEMM ran at a few per cent of the tensor pipe)
   const int64_t K2 = D2 * D2, ldx = tc_ld(K2);
   bf16* xh = c.alloc<bf16>(size_t(cc) * E * ldx);
   bf16* xl = c.alloc<bf16>(size_t(cc) * E * ldx);
   {
     TcLayout l;
     l.nm = 3;
-    l.me[0] = cc; l.ms[0] = E * ldx;
-    l.me[1] = D;  l.ms[1] = D;
-    l.me[2] = D;  l.ms[2] = 1;
+    l.me[0] = E; l.ms[0] = ldx;
+    l.me[1] = D; l.ms[1] = D * D2;
+    l.me[2] = D; l.ms[2] = D2;
     l.nn = 3;
-    l.ne[0] = E; l.ns[0] = ldx;
-    l.ne[1] = D; l.ns[1] = D * D2;
-    l.ne[2] = D; l.ns[2] = D2;
+    l.ne[0] = cc; l.ns[0] = E * ldx;
+    l.ne[1] = D;  l.ns[1] = D;
+    l.ne[2] = D;  l.ns[2] = 1;
     TcOut out;
     out.add(TcKind::kBf16Hi, xh, l).add(TcKind::kBf16Lo, xl, l);
-    tc_gemm(c, TcOperand{th, tl, cc * D2, a, ld2}, TcOperand{eh, el, E * D2, a, ld2}, x3, out);
+    tc_gemm(c, TcOperand{eh, el, E * D2, a, ld2}, TcOperand{th, tl, cc * D2, a, ld2}, x3, out);
   }
   // GEMM 2 against the double-layer matrix -> Q[(c,r,R)][(e,d,D)] and max|Q|;
-  // rows (r,R,d,D) from DL, columns (c,e) from X
+  // rows (c,e) from X, columns (r,R,d,D) from DL: consecutive columns are
+  // consecutive (d,D) in Q, stored 4 at a time, and N = D^4 = 1296 splits
+  // into six 224-wide tiles
   const DLOp dl = double_layer(c, ak, D, d);
   {
     TcLayout lq;
-    lq.nm = 4;
-    lq.me[0] = D; lq.ms[0] = D * o.ld;
-    lq.me[1] = D; lq.ms[1] = o.ld;
-    lq.me[2] = D; lq.ms[2] = D;
-    lq.me[3] = D; lq.ms[3] = 1;
-    lq.nn = 2;
-    lq.ne[0] = cc; lq.ns[0] = D2 * o.ld;
-    lq.ne[1] = E;  lq.ns[1] = D2;
+    lq.nm = 2;
+    lq.me[0] = cc; lq.ms[0] = D2 * o.ld;
+    lq.me[1] = E;  lq.ms[1] = D2;
+    lq.nn = 4;
+    lq.ne[0] = D; lq.ns[0] = D * o.ld;
+    lq.ne[1] = D; lq.ns[1] = o.ld;
+    lq.ne[2] = D; lq.ns[2] = D;
+    lq.ne[3] = D; lq.ns[3] = 1;
     TcOut out;
     out.add(TcKind::kBf16Hi, o.q_hi, lq).add(TcKind::kBf16Lo, o.q_lo, lq);
     out.extra_tag = kTagTcDoubleLayer;
-    tc_gemm_absmax(c, dl.op(), TcOperand{xh, xl, cc * E, K2, ldx}, x3, out, o.scale);
+    tc_gemm_absmax(c, TcOperand{xh, xl, cc * E, K2, ldx}, dl.op(), x3, out, o.scale);
   }
   transpose_bf16(c, o.q_hi, o.q_lo, rows, cols, o.ld, o.t_hi, o.t_lo, o.ldt);
   return o;
@@ -256,22 +261,24 @@ void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64
     g.ke[0] = B; g.ks[0] = D2 * X;
     gather_split_bf16(c, P1j, g, b1h, b1l, ld1);
   }
-  // G1 -> X[(a,x)][(l,L,u,U)]; rows (x,u,U) from P1, columns (a,l,L) from E
+  // G1 -> X[(a,x)][(l,L,u,U)]; rows (a,l,L) from E, columns (x,u,U) from
+  // P1: consecutive columns are consecutive (u,U), stored 4 at a time (as in
+  // quarter_mixed's GEMM 1)
   const int64_t K2 = D2 * D2, ldx = tc_ld(K2);
   bf16* xh = c.alloc<bf16>(size_t(Aa) * X * ldx);
   bf16* xl = c.alloc<bf16>(size_t(Aa) * X * ldx);
   {
     TcLayout l;
-    l.nm = 2;
-    l.me[0] = X;  l.ms[0] = ldx;
-    l.me[1] = D2; l.ms[1] = 1;
-    l.nn = 3;
-    l.ne[0] = Aa; l.ns[0] = X * ldx;
-    l.ne[1] = D;  l.ns[1] = D * D2;
-    l.ne[2] = D;  l.ns[2] = D2;
+    l.nm = 3;
+    l.me[0] = Aa; l.ms[0] = X * ldx;
+    l.me[1] = D;  l.ms[1] = D * D2;
+    l.me[2] = D;  l.ms[2] = D2;
+    l.nn = 2;
+    l.ne[0] = X;  l.ns[0] = ldx;
+    l.ne[1] = D2; l.ns[1] = 1;
     TcOut out;
     out.add(TcKind::kBf16Hi, xh, l).add(TcKind::kBf16Lo, xl, l);
-    tc_gemm(c, TcOperand{b1h, b1l, X * D2, B, ld1}, TcOperand{a1h, a1l, Aa * D2, B, ld1}, x3, out);
+    tc_gemm(c, TcOperand{a1h, a1l, Aa * D2, B, ld1}, TcOperand{b1h, b1l, X * D2, B, ld1}, x3, out);
   }
   // G2 -> T[(x,r,R)][(a,d,D)]
   const DLOp dl = double_layer(c, ak, D, d);
@@ -280,19 +287,19 @@ void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64
   bf16* t3h = c.alloc<bf16>(size_t(X) * D2 * ld4);
   bf16* t3l = c.alloc<bf16>(size_t(X) * D2 * ld4);
   {
-    TcLayout l;  // rows (r,R,d,D) from DL, columns (a,x) from X
-    l.nm = 4;
-    l.me[0] = D; l.ms[0] = D * ld4;
-    l.me[1] = D; l.ms[1] = ld4;
-    l.me[2] = D; l.ms[2] = D;
-    l.me[3] = D; l.ms[3] = 1;
-    l.nn = 2;
-    l.ne[0] = Aa; l.ns[0] = D2;
-    l.ne[1] = X;  l.ns[1] = D2 * ld4;
+    TcLayout l;  // rows (a,x) from X, columns (r,R,d,D) from DL (as in quarter_mixed)
+    l.nm = 2;
+    l.me[0] = Aa; l.ms[0] = D2;
+    l.me[1] = X;  l.ms[1] = D2 * ld4;
+    l.nn = 4;
+    l.ne[0] = D; l.ns[0] = D * ld4;
+    l.ne[1] = D; l.ns[1] = ld4;
+    l.ne[2] = D; l.ns[2] = D;
+    l.ne[3] = D; l.ns[3] = 1;
     TcOut out;
     out.add(TcKind::kBf16Hi, t3h, l).add(TcKind::kBf16Lo, t3l, l);
     out.extra_tag = kTagTcDoubleLayer;
-    tc_gemm(c, dl.op(), TcOperand{xh, xl, Aa * X, K2, ldx}, x3, out);
+    tc_gemm(c, TcOperand{xh, xl, Aa * X, K2, ldx}, dl.op(), x3, out);
   }
   // G3: B4[y][(a,d,D)] = P2[a][d][D][y]
   bf16* b4h = c.alloc<bf16>(size_t(Y) * ld4);

@@ -274,6 +274,7 @@ struct GemmParams {
   const double* scale2;
   unsigned long long* absmax;  // max |output| accumulated as ordered bits when non-null
   int64_t M, N;
+  int staged;        // persistent epilogue through shared memory (BF16 destinations, nd <= 2)
   TcDest d[4];
 };
 
@@ -540,6 +541,10 @@ __global__ void __launch_bounds__(kPThreads, 1)
   __shared__ int s_fail;
   __shared__ int s_epi_fail;
   __shared__ int64_t s_co[4][256];
+  // staged epilogue: per epilogue warp and destination, 32 rows x 16 BF16
+  // columns of the tile, and the rows' destination offsets
+  __shared__ __align__(16) bf16 s_stage[8][2][32][16];
+  __shared__ int64_t s_ro[8][2][32];
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -696,11 +701,66 @@ __global__ void __launch_bounds__(kPThreads, 1)
       for (int k = 0; k < 4; ++k)
         if (k < p.nd && mvalid) ro[k] = lay_row(p.d[k].lay, row);
       const uint32_t tb = tmem + uint32_t(b) * 256u + trow;
+      const int ew = warp - 4;
+      if (p.staged) {
+        if (p.nd > 0) s_ro[ew][0][lane] = ro[0];
+        if (p.nd > 1) s_ro[ew][1][lane] = ro[1];
+      }
       for (int c = c_begin; c < c_end; c += 16) {
         float v[16];
         __syncwarp();
         tmem_ld16(tb + uint32_t(c), v);
-        if (mvalid) {
+        if (p.staged) {
+          // Staged: each lane converts its row's 16 values into shared
+          // memory; then 4 lanes cover one row's 16 columns (8 bytes each),
+          // so that one store instruction writes 8 rows x 32 bytes instead
+          // of 32 scattered 8-byte pieces
+#pragma unroll
+          for (int k = 0; k < 2; ++k) {
+            if (k >= p.nd) break;
+            const bool lo = p.d[k].kind == TcKind::kBf16Lo;
+            uint32_t w[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+              float x0 = v[2 * i] * sc, x1 = v[2 * i + 1] * sc;
+              if (lo) {
+                x0 -= __bfloat162float(__float2bfloat16(x0));
+                x1 -= __bfloat162float(__float2bfloat16(x1));
+              }
+              const __nv_bfloat162 h2 = __floats2bfloat162_rn(x0, x1);
+              w[i] = *reinterpret_cast<const uint32_t*>(&h2);
+            }
+            uint4* dst4 = reinterpret_cast<uint4*>(&s_stage[ew][k][lane][0]);
+            dst4[0] = make_uint4(w[0], w[1], w[2], w[3]);
+            dst4[1] = make_uint4(w[4], w[5], w[6], w[7]);
+          }
+          __syncwarp();
+#pragma unroll
+          for (int k = 0; k < 2; ++k) {
+            if (k >= p.nd) break;
+            bf16* dp = static_cast<bf16*>(p.d[k].p);
+#pragma unroll
+            for (int it = 0; it < 4; ++it) {
+              const int g = it * 32 + lane, r = g >> 2, c4 = (g & 3) * 4;
+              if (m0 + lane_base + r >= p.M) continue;
+              const int64_t rr = s_ro[ew][k][r];
+              const int64_t c0 = s_co[k][c + c4];
+              const bool vec = c0 >= 0 && ((rr + c0) & 3) == 0 && s_co[k][c + c4 + 1] == c0 + 1 &&
+                               s_co[k][c + c4 + 2] == c0 + 2 && s_co[k][c + c4 + 3] == c0 + 3;
+              if (vec) {
+                *reinterpret_cast<uint2*>(dp + rr + c0) =
+                    *reinterpret_cast<const uint2*>(&s_stage[ew][k][r][c4]);
+              } else {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                  const int64_t ci = s_co[k][c + c4 + i];
+                  if (ci >= 0) dp[rr + ci] = s_stage[ew][k][r][c4 + i];
+                }
+              }
+            }
+          }
+          __syncwarp();  // the staging buffer is rewritten by the next chunk
+        } else if (mvalid) {
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
             if (k >= p.nd) break;
@@ -722,6 +782,8 @@ __global__ void __launch_bounds__(kPThreads, 1)
               }
             }
           }
+        }
+        if (mvalid) {
           if (p.absmax != nullptr) {
 #pragma unroll
             for (int i = 0; i < 16; ++i)
@@ -1078,6 +1140,13 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   }
   // more tiles than SMs with a direct epilogue: one persistent CTA per SM
   const bool persistent = direct && cx == 1 && base_ctas > sms;
+  // the persistent kernel's static shared memory (offset tables and the
+  // staged epilogue, ~29 KB) leaves 196 KB for the stage ring
+  const int p_stages = std::max(2, std::min(6, int((196 * 1024) / stage_bytes)));
+  const size_t p_smem = size_t(p_stages) * stage_bytes + 256 + 1024;
+  bool bf16_dests = out.nd >= 1 && out.nd <= 2;
+  for (int i = 0; i < out.nd; ++i)
+    bf16_dests = bf16_dests && (out.d[i].kind == TcKind::kBf16Hi || out.d[i].kind == TcKind::kBf16Lo);
   GemmParams p{};
   p.m_tiles = int(m_tiles);
   p.n_tiles = int(n_tiles);
@@ -1087,7 +1156,7 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   p.cx = cx;
   p.kb_total = kb_total;
   p.kb_per_split = kb_per_split;
-  p.stages = stages;
+  p.stages = persistent ? p_stages : stages;
   p.mode = imode;
   p.part = part;
   p.m_pad = m_pad;
@@ -1102,6 +1171,7 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   p.absmax = reinterpret_cast<unsigned long long*>(absmax);
   p.M = M;
   p.N = N;
+  p.staged = (persistent && bf16_dests) ? 1 : 0;
   for (int i = 0; i < out.nd; ++i) p.d[i] = out.d[i];
   if (absmax != nullptr) CTM_CUDA(cudaMemsetAsync(absmax, 0, sizeof(double), c.stream));
   CTM_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1115,8 +1185,8 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
                        out.extra_tag >= 0 ? work : -1.0);
     if (persistent) {
       CTM_CUDA(cudaFuncSetAttribute(tc_gemm_persistent_kernel,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-      tc_gemm_persistent_kernel<<<unsigned(std::min<int64_t>(base_ctas, sms)), kPThreads, smem,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, int(p_smem)));
+      tc_gemm_persistent_kernel<<<unsigned(std::min<int64_t>(base_ctas, sms)), kPThreads, p_smem,
                                   c.stream>>>(tA, tAl, tB, tBl, p);
     } else if (cx == 1) {
       tc_gemm_kernel<<<grid, kThreads, smem, c.stream>>>(tA, tAl, tB, tBl, p);

@@ -49,6 +49,29 @@ def test_mixed_quarter_tensor_matches_fp64(grown_d4):
             assert err < 2e-5, (k, err)
 
 
+def test_mixed_quarter_tensor_d6_chi144_matches_fp64():
+    """The benchmark's size: both quarter-tensor GEMMs have more tiles than
+    SMs and run in the persistent kernel with the staged BF16 epilogue."""
+    ref = gb.random_state(6, 144, 99, device="cuda")  # environment starts at chi = D^2
+    st = gb.IpepsState(2, 2, {"phys": 2, "bond": 6, "chi": 144}, "cuda")
+    g = torch.Generator().manual_seed(99)
+
+    def rnd(*shape):
+        t = torch.randn(*shape, generator=g, dtype=torch.float64)
+        return (t / t.norm()).cuda()
+
+    for s in ref.site_list:
+        st[s] = {"A": ref[s]["A"], "C": [rnd(144, 144) for _ in range(4)],
+                 "E": [rnd(144, 144, 6, 6) for _ in range(4)]}
+    for k in (0, 3):
+        q64, sh = gb.ProjectorCalculator.make_quarter_tensor(st[(0, 0)], k)
+        qmx, sh2 = gb.ProjectorCalculator.make_quarter_tensor(st[(0, 0)], k, precision="mixed")
+        assert sh == sh2 and q64.shape == (5184, 5184)
+        err = float((q64 - qmx).abs().max() / q64.abs().max())
+        assert err < 2e-5, (k, err)
+        del q64, qmx
+
+
 @pytest.mark.parametrize("k", range(4))
 def test_mixed_move_energy_within_rsvd_noise(grown_d4, k):
     """One move from the same state with the same test matrices.  The BF16
