@@ -332,61 +332,71 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int n0 = (p.n_fast ? blockIdx.x : blockIdx.y) * p.ntile;
   int issued_loads = 0;  // producer: stages handed to TMA
 
-  if (threadIdx.x == 0) {
-    // ---------------- TMA producer
-    for (int i = 0; i < nkb; ++i) {
-      const int s = i % p.stages;
-      const uint32_t ph = (i / p.stages) & 1;
-      if (!mbar_wait_spin(&empty[s], ph ^ 1)) {
-        atomicOr(&s_fail, 1);
-        break;
-      }
-      uint8_t* st = base + size_t(s) * stage_bytes;
-      mbar_expect_tx(&full[s], stage_bytes);
-      const int x = (kb0 + i) * bk;
-      tma_load_2d(st, &tA, x, m0, &full[s]);
-      if (p.mode == 3) tma_load_2d(st + half_bytes, &tAl, x, m0, &full[s]);
-      if (p.cx == 1) {
-        tma_load_2d(st + a_bytes, &tB, x, n0, &full[s]);
-        if (p.mode == 3) tma_load_2d(st + half_bytes + a_bytes, &tBl, x, n0, &full[s]);
-      } else {
-        // this CTA's slice of the shared B tile, multicast to the cluster
-        const int rows = p.ntile / p.cx;
-        const uint32_t off = a_bytes + crank * uint32_t(rows) * uint32_t(bk) * 2u;
-        tma_load_2d_mc(st + off, &tB, x, n0 + int(crank) * rows, &full[s], cmask);
-        if (p.mode == 3)
-          tma_load_2d_mc(st + half_bytes + off, &tBl, x, n0 + int(crank) * rows, &full[s], cmask);
-      }
-      issued_loads = i + 1;
-    }
-  } else if (threadIdx.x == 32) {
-    // ---------------- MMA issuer
-    const uint32_t idesc = idesc_bf16(kBM, p.ntile);
-    for (int i = 0; i < nkb; ++i) {
-      const int s = i % p.stages;
-      const uint32_t ph = (i / p.stages) & 1;
-      if (!mbar_wait_spin(&full[s], ph)) {
-        atomicOr(&s_fail, 1);
-        break;
-      }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      uint8_t* st = base + size_t(s) * stage_bytes;
-#pragma unroll
-      for (int kk = 0; kk < bk / 16; ++kk) {
-        const uint64_t ah = smem_desc(st + kk * 32, bk);
-        const uint64_t bh = smem_desc(st + a_bytes + kk * 32, bk);
-        mma_bf16(tmem, ah, bh, idesc, (i > 0 || kk > 0) ? 1u : 0u);
-        if (p.mode == 3) {
-          const uint64_t al = smem_desc(st + half_bytes + kk * 32, bk);
-          const uint64_t bl = smem_desc(st + half_bytes + a_bytes + kk * 32, bk);
-          mma_bf16(tmem, ah, bl, idesc, 1u);
-          mma_bf16(tmem, al, bh, idesc, 1u);
+  // Lane 0 of warp 0 produces and lane 0 of warp 1 issues the MMAs; the other
+  // lanes of those two warps wait at __syncwarp for their lane 0 (spinning on
+  // the epilogue's barrier next to it, they held up the pipeline thread of
+  // their own warp) and then join the epilogue.
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- TMA producer
+      for (int i = 0; i < nkb; ++i) {
+        const int s = i % p.stages;
+        const uint32_t ph = (i / p.stages) & 1;
+        if (!mbar_wait_spin(&empty[s], ph ^ 1)) {
+          atomicOr(&s_fail, 1);
+          break;
         }
+        uint8_t* st = base + size_t(s) * stage_bytes;
+        mbar_expect_tx(&full[s], stage_bytes);
+        const int x = (kb0 + i) * bk;
+        tma_load_2d(st, &tA, x, m0, &full[s]);
+        if (p.mode == 3) tma_load_2d(st + half_bytes, &tAl, x, m0, &full[s]);
+        if (p.cx == 1) {
+          tma_load_2d(st + a_bytes, &tB, x, n0, &full[s]);
+          if (p.mode == 3) tma_load_2d(st + half_bytes + a_bytes, &tBl, x, n0, &full[s]);
+        } else {
+          // this CTA's slice of the shared B tile, multicast to the cluster
+          const int rows = p.ntile / p.cx;
+          const uint32_t off = a_bytes + crank * uint32_t(rows) * uint32_t(bk) * 2u;
+          tma_load_2d_mc(st + off, &tB, x, n0 + int(crank) * rows, &full[s], cmask);
+          if (p.mode == 3)
+            tma_load_2d_mc(st + half_bytes + off, &tBl, x, n0 + int(crank) * rows, &full[s], cmask);
+        }
+        issued_loads = i + 1;
       }
-      if (p.cx == 1) mma_commit(&empty[s]);
-      else mma_commit_mc(&empty[s], cmask);
     }
-    mma_commit(tfull);
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer
+      const uint32_t idesc = idesc_bf16(kBM, p.ntile);
+      for (int i = 0; i < nkb; ++i) {
+        const int s = i % p.stages;
+        const uint32_t ph = (i / p.stages) & 1;
+        if (!mbar_wait_spin(&full[s], ph)) {
+          atomicOr(&s_fail, 1);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        uint8_t* st = base + size_t(s) * stage_bytes;
+#pragma unroll
+        for (int kk = 0; kk < bk / 16; ++kk) {
+          const uint64_t ah = smem_desc(st + kk * 32, bk);
+          const uint64_t bh = smem_desc(st + a_bytes + kk * 32, bk);
+          mma_bf16(tmem, ah, bh, idesc, (i > 0 || kk > 0) ? 1u : 0u);
+          if (p.mode == 3) {
+            const uint64_t al = smem_desc(st + half_bytes + kk * 32, bk);
+            const uint64_t bl = smem_desc(st + half_bytes + a_bytes + kk * 32, bk);
+            mma_bf16(tmem, ah, bl, idesc, 1u);
+            mma_bf16(tmem, al, bh, idesc, 1u);
+          }
+        }
+        if (p.cx == 1) mma_commit(&empty[s]);
+        else mma_commit_mc(&empty[s], cmask);
+      }
+      mma_commit(tfull);
+    }
+    __syncwarp();
   }
 
   // ---------------- epilogue: TMEM -> FP32 partial tile
