@@ -419,8 +419,9 @@ void cholesky(cudaStream_t st, const T* G, int64_t q, int64_t n, int shift_mode,
               T* Lout, T* Linv, T* Lt, int* flags, T* LinvT = nullptr) {
   const size_t mat = cholesky_scratch(q) * sizeof(T);
   const size_t head = (2 * size_t(chol_q4(int(q))) + size_t(kCholNb) * chol_ld(int(q))) * sizeof(T);
-  const bool inv = Linv != nullptr || LinvT != nullptr;
-  const int place = (inv && head + 2 * mat <= kSmemOptin) ? 2 : (head + mat <= kSmemOptin ? 1 : 0);
+  // both scratch matrices in shared memory whenever they fit, also without
+  // the inverse (that variant of the kernel compiles without spills)
+  const int place = (head + 2 * mat <= kSmemOptin) ? 2 : (head + mat <= kSmemOptin ? 1 : 0);
   const size_t smem = head + (place >= 1 ? mat : 0) + (place == 2 ? mat : 0);
   auto launch = [&](auto kern) {
     CTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
@@ -1489,8 +1490,10 @@ void jacobi_left_singular(Ctx& c, const float* Mc, int64_t q, double* Ub, double
   if (c.sizing()) return;
   // q >= 96: the block Jacobi on a cluster of kJacobiCluster CTAs (rows
   // padded to a multiple of 8 kJacobiCluster: b a multiple of 4, 8 b threads
-  // per CTA) when its four blocks of b rows fit in shared memory (q <= 224)
-  constexpr int kJacobiCluster = 4;
+  // per CTA) when its four blocks of b rows fit in shared memory.  8 CTAs:
+  // 0.90 ms against 0.95 ms with 4 at q = 160 (16 blocks of 12 rows, the
+  // rows padded to 192)
+  constexpr int kJacobiCluster = 8;
   const int P = kJacobiCluster;
   const int qp = int((q + 8 * P - 1) / (8 * P) * (8 * P));
   const int b = qp / (2 * P);

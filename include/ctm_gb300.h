@@ -216,7 +216,7 @@ int ctm_svd_f64(const double* a, int64_t m, int64_t n, double* U, double* S, dou
  * bt, n x q FP32 row-major, 1 <= q <= min(n, 1024)) = U diag(S) V^T with U
  * (q x q, FP64), S (q, descending, FP64), V (n x q, FP32).  FP32 shifted
  * Cholesky-QR3 of bt, then FP32 one-sided Jacobi with accumulated rotations
- * (on a 4-CTA cluster from q = 96).  Replaces the torch.linalg.svd of the
+ * (on an 8-CTA cluster from q = 96).  Replaces the torch.linalg.svd of the
  * projected matrix in acetn/linalg/fused_matmul_svd_lowrank.py:45-51 on the
  * mixed path; no direct counterpart, exposed to test and measure that stage. */
 int ctm_svd_f32(const float* bt, int64_t n, int64_t q, double* U, double* S, float* V,

@@ -1,5 +1,5 @@
 """The FP32 Rayleigh-Ritz SVD of the mixed path (``svd_f32``: Cholesky-QR3 of
-B^T and one-sided Jacobi; a 4-CTA cluster Jacobi from q = 96) against
+B^T and one-sided Jacobi; an 8-CTA cluster Jacobi from q = 96) against
 numpy's float64 SVD, on matrices with the graded spectrum of a converged
 D=6, chi=144 environment (s/s0 from 1 down to ~2e-4) and on a flat one.
 The bar: singular values to 2e-6 of s0 and U orthogonal to 5e-6 (FP32
