@@ -137,6 +137,30 @@ def test_bad_sizes_are_invalid(lib):
     assert st == _abi.CTM_ERR_INVALID
 
 
+def test_svd_f32_validation_and_workspace_query(lib):
+    sz = ctypes.c_size_t(0)
+    # q > n and q > 1024 are rejected before any launch
+    st = lib.ctm_svd_f32(None, 10, 11, None, None, None, None, ctypes.byref(sz), None)
+    assert st == _abi.CTM_ERR_UNSUPPORTED
+    st = lib.ctm_svd_f32(None, 5000, 1025, None, None, None, None, ctypes.byref(sz), None)
+    assert st == _abi.CTM_ERR_UNSUPPORTED
+    # the D=6, chi=144 Rayleigh-Ritz size: B^T (5184 x 160) copy, the QR's
+    # buffers and the Jacobi scratch
+    n, q = 144 * 36, 160
+    st = lib.ctm_svd_f32(ctypes.c_void_p(0x1000), n, q, ctypes.c_void_p(0x2000),
+                         ctypes.c_void_p(0x3000), ctypes.c_void_p(0x4000), None,
+                         ctypes.byref(sz), None)
+    assert st == 0 and sz.value >= 3 * n * q * 4
+
+
+def test_linalg_wrappers_reject_cpu_tensors():
+    import torch
+    with pytest.raises(ValueError):
+        gb.linalg.qr(torch.zeros(8, 4, dtype=torch.float64))
+    with pytest.raises(ValueError):
+        gb.linalg.svd_f32(torch.zeros(8, 4, dtype=torch.float32))
+
+
 def test_qr_workspace_query(lib):
     # FP32 Cholesky-QR at the D=6, chi=144 range-finder size: the input copy,
     # the second buffer and one q x q Gram per row slab
