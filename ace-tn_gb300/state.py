@@ -8,6 +8,8 @@ instance owns its tensors.  ``site_list`` / ``bond_list`` follow
 tensor_network.py:153-193.
 """
 
+import pickle
+import types
 from dataclasses import dataclass
 
 import numpy as np
@@ -105,6 +107,78 @@ class IpepsState:
             x, y = (int(t) for t in key.split(","))
             st.set_site((x, y), v["A"], v["C"], v["E"])
         return st
+
+    @classmethod
+    def load_reference(cls, filename, device="cuda"):
+        """Reads a checkpoint written by the reference's ``TensorNetwork.save``
+        (acetn/ipeps/tensor_network.py:94-111: torch.save of
+        {"tensor_network": ..., "tensors": {site: SiteTensor}}) without
+        importing the reference.  The file is unpickled (it holds objects, not
+        only tensors), so read only checkpoints from a trusted source."""
+        data = torch.load(filename, map_location="cpu", weights_only=False,
+                          pickle_module=_REF_PICKLE)
+        if not isinstance(data, dict) or "tensors" not in data:
+            raise ValueError(f"{filename}: not a checkpoint of the reference's TensorNetwork.save")
+        tn, tensors = data.get("tensor_network"), data["tensors"]
+        sites = sorted(tuple(s) for s in tensors)
+        nx = getattr(tn, "nx", max(s[0] for s in sites) + 1)
+        ny = getattr(tn, "ny", max(s[1] for s in sites) + 1)
+        A0, C0, _ = _site_arrays(next(iter(tensors.values())))
+        dims = dict(getattr(tn, "dims", None) or
+                    {"phys": A0.shape[4], "bond": A0.shape[0], "chi": C0[0].shape[0]})
+        st = cls(nx, ny, dims, device)
+        for site, obj in tensors.items():
+            A, C, E = _site_arrays(obj)
+            st.set_site(tuple(site), A, C, E)
+        return st
+
+
+class _RefStub:
+    """Stand-in for a class of the reference while one of its checkpoints is
+    read: pickle rebuilds objects without calling __init__ and restores their
+    attributes, which is all a checkpoint needs (SiteTensor._site_tensor,
+    _corner_tensors, _edge_tensors; TensorNetwork.nx, ny, dims)."""
+
+    def __new__(cls, *args, **kwargs):
+        obj = object.__new__(cls)
+        obj._args = args
+        return obj
+
+    def __setstate__(self, state):
+        if isinstance(state, tuple) and len(state) == 2:  # (dict, slots)
+            state = {**(state[0] or {}), **(state[1] or {})}
+        if isinstance(state, dict):
+            self.__dict__.update(state)
+        else:
+            self._state = state
+
+
+class _RefUnpickler(pickle.Unpickler):
+    """Unpickler that resolves the reference's classes (module acetn.*) to
+    _RefStub subclasses of the same name, so that reading a reference
+    checkpoint needs neither the reference nor its dependencies."""
+
+    _stubs = {}
+
+    def find_class(self, module, name):
+        if module == "acetn" or module.startswith("acetn."):
+            key = (module, name)
+            if key not in self._stubs:
+                self._stubs[key] = type(name, (_RefStub,), {"__module__": module})
+            return self._stubs[key]
+        return super().find_class(module, name)
+
+
+_REF_PICKLE = types.SimpleNamespace(__name__="pickle", Unpickler=_RefUnpickler, load=pickle.load,
+                                    Pickler=pickle.Pickler, dump=pickle.dump)
+
+
+def _site_arrays(obj):
+    """(A, [C0..C3], [E0..E3]) of a reference SiteTensor (or its stand-in)."""
+    d = obj.__dict__
+    if "_site_tensor" in d:
+        return d["_site_tensor"], list(d["_corner_tensors"]), list(d["_edge_tensors"])
+    return obj["A"], list(obj["C"]), list(obj["E"])
 
 
 def _initial_environment(a):

@@ -104,3 +104,31 @@ def test_clock_sampler_keeps_samples_of_the_timed_window():
     out = s.stop()
     assert out["samples"] == 1 and out["sm_mhz"] == 1500.0 and not out["in_window"]
     assert out["reasons"] == ["sw_thermal_slowdown"]
+
+
+def test_reads_a_checkpoint_written_by_the_reference(tmp_path):
+    """tests/golden/ref_checkpoint_d2.pt was written by the reference's own
+    TensorNetwork.save (tests/golden/make_checkpoint.py); it is read without
+    the reference, tensor for tensor, and round-trips through the plain
+    checkpoint format."""
+    import os
+    import numpy as np
+    golden = os.path.join(os.path.dirname(__file__), "golden")
+    st = gb.IpepsState.load_reference(os.path.join(golden, "ref_checkpoint_d2.pt"), device="cpu")
+    z = np.load(os.path.join(golden, "ref_checkpoint_d2.npz"))
+    assert (st.nx, st.ny) == (2, 2) and st.dims == {"phys": 2, "bond": 2, "chi": 6}
+    for s in st.site_list:
+        key = f"{s[0]}_{s[1]}"
+        assert np.array_equal(st[s]["A"].numpy(), z[f"{key}_A"])
+        for k in range(4):
+            assert np.array_equal(st[s]["C"][k].numpy(), z[f"{key}_C{k}"])
+            assert np.array_equal(st[s]["E"][k].numpy(), z[f"{key}_E{k}"])
+    plain = tmp_path / "plain.pt"
+    st.save(plain)
+    back = gb.IpepsState.load(plain, device="cpu")
+    for s in st.site_list:
+        assert torch.equal(back[s]["A"], st[s]["A"])
+        assert all(torch.equal(a, b) for a, b in zip(back[s]["E"], st[s]["E"]))
+    # a plain checkpoint is not a reference checkpoint
+    with pytest.raises(ValueError):
+        gb.IpepsState.load_reference(plain, device="cpu")
