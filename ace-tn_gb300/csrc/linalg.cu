@@ -411,9 +411,9 @@ __global__ void __launch_bounds__(chol_threads<T>()) cholesky_kernel(
     }
 }
 
-// Launches cholesky_kernel with W (and E when Linv is wanted) in shared
-// memory whenever they fit.  Wg / Eg: cholesky_scratch(q) elements each,
-// used otherwise.
+// Launches cholesky_kernel with W and E in shared memory whenever both fit,
+// else W alone.  Wg / Eg: cholesky_scratch(q) elements each, used for what
+// is not in shared memory.
 template <class T>
 void cholesky(cudaStream_t st, const T* G, int64_t q, int64_t n, int shift_mode, T* Wg, T* Eg,
               T* Lout, T* Linv, T* Lt, int* flags, T* LinvT = nullptr) {
