@@ -469,6 +469,33 @@ def bond_rdm(st, s1, s2, k):
     return _ein("fcRPrp,fcRQrq->PQpq", r1, r2)
 
 
+def norm_tensor(st, bond, a1q, a2q):
+    """``build_norm_tensor`` + ``build_norm_tensor_core`` of the full update
+    (acetn/evolution/full_update.py:163-236): the environment of bond
+    (s1, s2, k) contracted with the reduced site tensors a1q (r,d,u,y) and
+    a2q (d,l,u,x) into n12[y,x,Y,X].  ``build_norm_tensor_core_blocked``
+    (full_update.py:239-268) computes the same sum in blocks of the bra legs."""
+    s1, s2, k = bond
+    t1, t2 = st[s1], st[s2]
+    c12 = t1["C"][(k + 1) % 4]; e12 = t1["E"][(k + 1) % 4]; e11 = t1["E"][k % 4]
+    c13 = t1["C"][(k + 2) % 4]; e13 = t1["E"][(k + 2) % 4]
+    c21 = t2["C"][k % 4]; e21 = t2["E"][k % 4]; e24 = t2["E"][(k + 3) % 4]
+    c24 = t2["C"][(k + 3) % 4]; e23 = t2["E"][(k + 2) % 4]
+    tmp = _ein("ab,bcrR->acrR", c12, e12)
+    tmp = _ein("acrR,eauU->crReuU", tmp, e11)
+    tmp = _ein("crReuU,RDUY->creuDY", tmp, np.conj(a1q))
+    tmp = _ein("creuDY,rduy->ceDYdy", tmp, a1q)
+    n1 = _ein("ab,bfdD->afdD", c13, e13)
+    n1 = _ein("afdD,aeDYdy->feYy", n1, tmp)
+    tmp = _ein("ab,bcuU->acuU", c21, e21)
+    tmp = _ein("acuU,ealL->cuUelL", tmp, e24)
+    tmp = _ein("cuUelL,DLUX->cuelXD", tmp, np.conj(a2q))
+    tmp = _ein("cuelXD,dlux->ceXDxd", tmp, a2q)
+    n2 = _ein("ab,fadD->bfdD", c24, e23)
+    n2 = _ein("bfdD,cbXDxd->fcXx", n2, tmp)
+    return _ein("fcYy,fcXx->yxYX", n1, n2)
+
+
 def build_site_list(nx, ny):
     """``TensorNetwork.build_site_list`` (acetn/ipeps/tensor_network.py:179-193)."""
     return [(xi, yi) for xi in range(nx) for yi in range(ny)]

@@ -130,3 +130,21 @@ def test_unknown_site_raises():
     st = orc.random_state(2, 4, seed=1)
     with pytest.raises(ValueError):
         st[(5, 5)]
+
+
+def test_norm_tensor_matches_reference():
+    """The full update's norm tensor (acetn/evolution/full_update.py:163-268),
+    both bond directions, against the reference's build_norm_tensor and its
+    blocked core (tests/golden/make_norm_tensor.py)."""
+    z = load("norm_tensor_d2.npz")
+    sites = {}
+    for x in range(2):
+        for y in range(2):
+            key = f"{x}_{y}"
+            sites[(x, y)] = {"A": z[f"{key}_A"], "C": [z[f"{key}_C{k}"] for k in range(4)],
+                             "E": [z[f"{key}_E{k}"] for k in range(4)]}
+    st = orc.OracleState(sites, 2, 2, 6)
+    for k, s2 in ((2, (1, 0)), (1, (0, 1))):
+        n12 = orc.norm_tensor(st, ((0, 0), s2, k), z[f"k{k}_a1q"], z[f"k{k}_a2q"])
+        assert rel(n12, z[f"k{k}_n12"]) < 1e-13
+        assert rel(n12, z[f"k{k}_n12_blocked"]) < 1e-13
