@@ -409,7 +409,8 @@ def run_gb300(args, rank, world, local_rank):
                          "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
                          "traffic": traffic, "launches": dom_n, "peak_source": peak_src,
                          "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum, "
-                                            "one launch, profiles/tc_gemm_double_layer_d6_chi144.md"
+                                            "one launch, profiles/tc_gemm_double_layer_d6_chi144.md "
+                                            "(captured before the operand swap of this GEMM)"
                                             if traffic else None),
                          "work_per_launch": dom_work / dom_n if dom_n else None,
                          "share_of_step": (dom_ms / prof_moves) / prof_move_ms,
