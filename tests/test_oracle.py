@@ -148,3 +148,28 @@ def test_norm_tensor_matches_reference():
         n12 = orc.norm_tensor(st, ((0, 0), s2, k), z[f"k{k}_a1q"], z[f"k{k}_a2q"])
         assert rel(n12, z[f"k{k}_n12"]) < 1e-13
         assert rel(n12, z[f"k{k}_n12_blocked"]) < 1e-13
+
+
+def test_rsvd_known_answers():
+    """The reference's known-answer tests of its randomized SVDs
+    (tests/unit/test_linalg.py of the reference: exact recovery of low-rank
+    matrices and products to 1e-10, orthonormal factors, ordered spectra),
+    applied to the oracle's restatements."""
+    rng = np.random.default_rng(3)
+    omega = orc.OmegaStream(17)
+
+    def rec(p, u, s, v):
+        return np.linalg.norm(p - (u * s) @ v.T) / np.linalg.norm(p)
+
+    low = rng.standard_normal((100, 10)) @ rng.standard_normal((10, 80))
+    u, s, v = orc.svd_lowrank(low, 15, 3, omega)
+    assert rec(low, u, s, v) < 1e-10
+    assert np.allclose(u.T @ u, np.eye(15), atol=1e-10) and np.allclose(v.T @ v, np.eye(15), atol=1e-10)
+    assert np.all(s[:-1] >= s[1:]) and np.all(s >= 0)
+    a, b = rng.standard_normal((100, 10)), rng.standard_normal((10, 80))
+    u, s, v = orc.fused_matmul_svd_lowrank(a, b, 12, 3, omega)
+    assert rec(a @ b, u, s, v) < 1e-10
+    a, b = rng.standard_normal((60, 10)), rng.standard_normal((10, 50))
+    c, d = rng.standard_normal((50, 40)), rng.standard_normal((40, 70))
+    u, s, v = orc.fused_3matmul_svd_lowrank(a, b, c, d, 10, 3, omega)
+    assert rec(a @ b @ c @ d, u, s, v) < 1e-10
