@@ -34,7 +34,7 @@ class CtmOpts(ctypes.Structure):
     _fields_ = [("chi", c_i64), ("projectors", c_i32), ("svd_type", c_i32),
                 ("svd_cutoff", ctypes.c_double), ("rsvd_niter", c_i32),
                 ("rsvd_oversampling", c_i32), ("precision", c_i32), ("fixed_width", c_i32),
-                ("mixed_floor", ctypes.c_double)]
+                ("mixed_floor", ctypes.c_double), ("mixed_flags", c_i32)]
 
 
 SITE_P = ctypes.POINTER(CtmSite)
@@ -51,6 +51,11 @@ _SIGNATURES = {
     "ctm_profile_query": ([ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)],
                           ctypes.c_int),
+    "ctm_profile_kernel_count": ([ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+    "ctm_profile_kernel": ([ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
+                            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
+                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)],
+                           ctypes.c_int),
     "ctm_quarter_tensor": ([SITE_P, c_i64, c_i64, c_i32, c_vp, ctypes.POINTER(c_i64), c_i32,
                             c_vp, c_sz_p, c_vp], ctypes.c_int),
     "ctm_calculate_projectors": ([SITES_PP, c_i64, c_i64, c_i32, ctypes.POINTER(CtmOpts), c_vp,
@@ -164,6 +169,10 @@ def call(name, args_before_ws, device, key=None, stream=None):
     lib = load()
     fn = getattr(lib, name)
     stream = stream_handle(device) if stream is None else stream
+    # workspace sizes depend on the device (its SM count sets the split-K of
+    # the tensor-core products), so the cache is keyed by device as well
+    if key is not None:
+        key = (torch.device(device).index, key)
     nbytes = _WS_CACHE.get(key) if key is not None else None
     if nbytes is None:
         sz = ctypes.c_size_t(0)
@@ -195,6 +204,23 @@ def profile_end():
         check(lib.ctm_profile_query(tag, ctypes.byref(ms), ctypes.byref(work), ctypes.byref(n)),
               "ctm_profile_query")
         out[name] = (ms.value, work.value, n.value)
+    return out
+
+
+def profile_kernels():
+    """Per-kernel table of the last profile (after ``profile_end``): a list
+    of {name, unit ("flop" or "byte"), ms, work, launches}."""
+    lib = load()
+    n = ctypes.c_int(0)
+    check(lib.ctm_profile_kernel_count(ctypes.byref(n)), "ctm_profile_kernel_count")
+    out = []
+    for i in range(n.value):
+        name, unit = ctypes.c_char_p(), ctypes.c_int()
+        ms, work, cnt = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+        check(lib.ctm_profile_kernel(i, ctypes.byref(name), ctypes.byref(unit), ctypes.byref(ms),
+                                     ctypes.byref(work), ctypes.byref(cnt)), "ctm_profile_kernel")
+        out.append({"name": name.value.decode(), "unit": "byte" if unit.value else "flop",
+                    "ms": ms.value, "work": work.value, "launches": cnt.value})
     return out
 
 
@@ -271,5 +297,6 @@ def opts_struct(config, chi, precision, fixed_width=False):
         raise ValueError(f"Invalid precision: {precision} provided.")
     o.precision = PREC[precision]
     o.mixed_floor = float(getattr(config, "mixed_svd_floor", 1e-6))
+    o.mixed_flags = int(getattr(config, "mixed_flags", 0))
     o.fixed_width = 1 if fixed_width else 0
     return o

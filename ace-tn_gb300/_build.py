@@ -45,7 +45,12 @@ def _fingerprint():
 
 
 def build(force=False, verbose=False):
-    """Builds the library unless an up-to-date copy exists.  Returns its path."""
+    """Builds the library unless an up-to-date copy exists.  Returns its path.
+    An installed copy of the package (no sources beside it) uses the library
+    it was installed with."""
+    inc = os.path.join(os.path.dirname(PKG), "include", "ctm_gb300.h")
+    if not force and os.path.exists(LIB) and not os.path.exists(inc):
+        return LIB
     os.makedirs(OUT, exist_ok=True)
     stamp = os.path.join(OUT, "build.stamp")
     fp = _fingerprint()

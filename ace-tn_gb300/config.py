@@ -33,6 +33,7 @@ class CTMRGConfig:
     backend: Literal["gb300"] = "gb300"
     precision: Literal["fp64", "mixed"] = "fp64"
     mixed_svd_floor: float = 1e-6
+    mixed_flags: int = 0
 
 
 def resolve(config):

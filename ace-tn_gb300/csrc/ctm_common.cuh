@@ -62,14 +62,21 @@ enum ProfileTag {
 };
 constexpr int kProfileTags = 10;
 
-// Brackets one launch with CUDA events while profiling is on; `work` is the
-// algorithmic FLOP (or byte) count of the launch.
+// Unit of the work figure of a named kernel class.
+enum WorkUnit { kUnitFlop = 0, kUnitByte = 1 };
+
+// Brackets one launch (or a span of launches) with CUDA events while
+// profiling is on; `work` is the algorithmic FLOP (or byte) count.  The tag
+// form adds to one of the classes above; the named form adds to a per-kernel
+// table keyed by `name` (a string literal), with its work unit.
 class KernelTimer {
  public:
   KernelTimer(cudaStream_t s, int tag, double work);
+  KernelTimer(cudaStream_t s, const char* name, int unit, double work);
   ~KernelTimer();
 
  private:
+  void start(int tag, const char* name, int unit, double work);
   cudaStream_t stream_;
   bool active_ = false;
   size_t idx_ = 0;

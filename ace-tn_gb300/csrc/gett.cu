@@ -360,12 +360,16 @@ void einsum_impl(Ctx& c, const char* spec, const ViewT<T>& A, const ViewT<T>& B,
             static_cast<unsigned>(bext * splitk));
   CTM_REQUIRE(grid.y <= 65535 && grid.z <= 65535, CTM_ERR_UNSUPPORTED, "einsum: grid too large");
   {
-    KernelTimer timer(c.stream, sizeof(T) == 8 ? kTagGettF64 : kTagGettF32,
-                      2.0 * double(p.Mt) * p.Nt * p.Kt * bext);
+    const double flops = 2.0 * double(p.Mt) * p.Nt * p.Kt * bext;
+    KernelTimer timer(c.stream, sizeof(T) == 8 ? kTagGettF64 : kTagGettF32, flops);
+    KernelTimer kt(c.stream, sizeof(T) == 8 ? "gett_kernel<double>" : "gett_kernel<float>",
+                   kUnitFlop, flops);
     gett_kernel<T><<<grid, NT, 0, c.stream>>>(p);
     CTM_LAUNCH_CHECK();
   }
   if (splitk > 1) {
+    KernelTimer kt(c.stream, "gett_splitk_reduce", kUnitByte,
+                   double(sizeof(T)) * (splitk + 1.0) * bext * p.Mt * p.Nt);
     gett_splitk_reduce<T><<<grid_for(bext * p.Mt * p.Nt, 256), 256, 0, c.stream>>>(p);
     CTM_LAUNCH_CHECK();
   }
@@ -425,8 +429,11 @@ void reduce(Ctx& c, const double* x, int64_t n, double* out, int op) {
   Scope scope(c);
   double* part = c.alloc<double>(blocks);
   if (c.sizing()) return;
-  reduce_partial<<<blocks, RT, 0, c.stream>>>(x, n, part, op);
-  CTM_LAUNCH_CHECK();
+  {
+    KernelTimer kt(c.stream, "reduce_partial", kUnitByte, 8.0 * n);
+    reduce_partial<<<blocks, RT, 0, c.stream>>>(x, n, part, op);
+    CTM_LAUNCH_CHECK();
+  }
   reduce_final<<<1, RT, 0, c.stream>>>(part, blocks, out, op);
   CTM_LAUNCH_CHECK();
 }
@@ -461,6 +468,7 @@ void sumsq(Ctx& c, const double* x, int64_t n, double* out) { reduce(c, x, n, ou
 
 void divide_by(Ctx& c, double* x, int64_t n, const double* scal, int mode) {
   if (c.sizing() || n == 0) return;
+  KernelTimer kt(c.stream, "divide_kernel", kUnitByte, 16.0 * n);
   divide_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(x, n, scal, mode);
   CTM_LAUNCH_CHECK();
 }
@@ -468,6 +476,7 @@ void divide_by(Ctx& c, double* x, int64_t n, const double* scal, int mode) {
 void copy2d(Ctx& c, const View& src, double* dst, int64_t ld_dst) {
   CTM_REQUIRE(src.nd == 2, CTM_ERR_INVALID, "copy2d: expects a 2-D view");
   if (c.sizing() || src.numel() == 0) return;
+  KernelTimer kt(c.stream, "copy2d_kernel", kUnitByte, 16.0 * src.numel());
   copy2d_kernel<<<grid_for(src.numel(), 256), 256, 0, c.stream>>>(
       src.p, src.shape[0], src.shape[1], src.stride[0], src.stride[1], dst, ld_dst);
   CTM_LAUNCH_CHECK();
@@ -488,12 +497,14 @@ __global__ void cvt_f64_kernel(const float* x, double* y, int64_t n) {
 
 void to_f32(Ctx& c, const double* x, float* y, int64_t n) {
   if (c.sizing() || n == 0) return;
+  KernelTimer kt(c.stream, "cvt_f32_kernel", kUnitByte, 12.0 * n);
   cvt_f32_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(x, y, n);
   CTM_LAUNCH_CHECK();
 }
 
 void to_f64(Ctx& c, const float* x, double* y, int64_t n) {
   if (c.sizing() || n == 0) return;
+  KernelTimer kt(c.stream, "cvt_f64_kernel", kUnitByte, 12.0 * n);
   cvt_f64_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(x, y, n);
   CTM_LAUNCH_CHECK();
 }

@@ -425,6 +425,8 @@ void cholesky(cudaStream_t st, const T* G, int64_t q, int64_t n, int shift_mode,
   const size_t smem = head + (place >= 1 ? mat : 0) + (place == 2 ? mat : 0);
   auto launch = [&](auto kern) {
     CTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    KernelTimer kt(st, sizeof(T) == 8 ? "cholesky_kernel<double>" : "cholesky_kernel<float>",
+                   kUnitFlop, double(q) * q * q / 3.0);
     kern<<<1, chol_threads<T>(), smem, st>>>(G, int(q), n, shift_mode, Wg, Eg, Lout, Linv, Lt,
                                              LinvT, flags);
   };
@@ -1216,6 +1218,8 @@ void slab_stage_launch(Ctx& c, const float* Y, int64_t n, int64_t q, int rpb, in
   const size_t smem = (size_t(rpb) * q + size_t(q) * q + 2 * 32 * kT) * sizeof(float);
   CTM_CUDA(cudaFuncSetAttribute(slab_stage_kernel<kT, kVec>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  // forward substitution (n q^2) and the slab Gram matrices (n q^2 FMA)
+  KernelTimer kt(c.stream, "slab_stage_kernel", kUnitFlop, 4.0 * double(n) * q * q);
   slab_stage_kernel<kT, kVec><<<nblk, kSlabThreads, smem, c.stream>>>(Y, n, int(q), rpb, Lt, X,
                                                                       part);
 }
@@ -1261,6 +1265,7 @@ void slab_gram(Ctx& c, const float* Y, int64_t n, int64_t q, const float* Lt, fl
     slab_stage_dispatch<false>(c, Y, n, q, rpb, nblk, Lt, X, part);
   CTM_LAUNCH_CHECK();
   const int qq = int(q * q);
+  KernelTimer kt(c.stream, "slab_reduce_kernel", kUnitByte, 4.0 * (double(nblk) + 1.0) * qq);
   if (qq % 4 == 0)
     slab_reduce_kernel<true><<<unsigned((qq / 4 + 63) / 64), 256, 0, c.stream>>>(part, nblk, qq, G);
   else
@@ -1280,6 +1285,7 @@ void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R, int stages) {
   const bool small = (sizeof(T) == 4 && q >= 32) ? false : double(n) * q * q <= 4.0e6;
   if (small) {
     if (c.sizing()) return;
+    KernelTimer kt(c.stream, "householder_qr_kernel", kUnitFlop, 4.0 * double(n) * q * q);
     householder_qr_kernel<T><<<1, LT, 0, c.stream>>>(Y, n, q, R, V, beta, nullptr, 1);
     CTM_LAUNCH_CHECK();
     return;
@@ -1354,8 +1360,11 @@ void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R, int stages) {
   T* hv = c.alloc<T>(size_t(n) * q);
   if (c.sizing()) return;
   const T tol = sizeof(T) == 8 ? T(stages == 3 ? 1e-11 : 1e-6) : T(stages == 3 ? 2e-4 : 5e-2);
-  orthogonality_check_kernel<T><<<1, 1024, 0, c.stream>>>(G, int(q), tol, flags);
-  CTM_LAUNCH_CHECK();
+  {
+    KernelTimer kt(c.stream, "orthogonality_check_kernel", kUnitByte, double(sizeof(T)) * q * q);
+    orthogonality_check_kernel<T><<<1, 1024, 0, c.stream>>>(G, int(q), tol, flags);
+    CTM_LAUNCH_CHECK();
+  }
   if (cur != Y)
     CTM_CUDA(cudaMemcpyAsync(Y, cur, sizeof(T) * n * q, cudaMemcpyDeviceToDevice, c.stream));
   if (R != nullptr)
@@ -1414,12 +1423,16 @@ void svd_thin(Ctx& c, const double* X, int64_t m, int64_t n, double* U, double* 
     blocks = std::min<int64_t>(blocks, sms);
     blocks = std::max<int64_t>(blocks, 1);
     void* args[] = {&a};
+    KernelTimer kt(c.stream, "jacobi_sweeps_kernel", kUnitFlop, 0.0);
     CTM_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(jacobi_sweeps_kernel),
                                          dim3(unsigned(blocks)), dim3(threads), args, 0, c.stream));
     CTM_LAUNCH_CHECK();
   }
-  jacobi_finish_kernel<<<unsigned(p), LT, 0, c.stream>>>(W, J, p, L, trans, U, S, V);
-  CTM_LAUNCH_CHECK();
+  {
+    KernelTimer kt(c.stream, "jacobi_finish_kernel", kUnitFlop, 2.0 * double(p) * p * L);
+    jacobi_finish_kernel<<<unsigned(p), LT, 0, c.stream>>>(W, J, p, L, trans, U, S, V);
+    CTM_LAUNCH_CHECK();
+  }
 }
 
 void truncation_factors(Ctx& c, const double* s, int64_t r, int64_t chi, double cutoff, double* f,
@@ -1440,6 +1453,7 @@ __global__ void scale_columns_kernel(double* x, int64_t rows, int64_t cols, int6
 
 void scale_columns(Ctx& c, double* x, int64_t rows, int64_t cols, int64_t ld, const double* f) {
   if (c.sizing() || rows * cols == 0) return;
+  KernelTimer kt(c.stream, "scale_columns_kernel", kUnitByte, 16.0 * rows * cols);
   scale_columns_kernel<<<grid_for(rows * cols, 256), 256, 0, c.stream>>>(x, rows, cols, ld, f);
   CTM_LAUNCH_CHECK();
 }
@@ -1447,6 +1461,7 @@ void scale_columns(Ctx& c, double* x, int64_t rows, int64_t cols, int64_t ld, co
 void scale_columns_compact(Ctx& c, const double* in, int64_t rows, int64_t cap, const double* f,
                            const int64_t* chi_new, double* out) {
   if (c.sizing() || rows * cap == 0) return;
+  KernelTimer kt(c.stream, "scale_compact_kernel", kUnitByte, 16.0 * rows * cap);
   scale_compact_kernel<<<grid_for(rows * cap, 256), 256, 0, c.stream>>>(in, rows, cap, f, chi_new,
                                                                          out);
   CTM_LAUNCH_CHECK();
@@ -1502,6 +1517,7 @@ void jacobi_left_singular(Ctx& c, const float* Mc, int64_t q, double* Ub, double
   if (q >= 96 && ldj <= 256 && smem <= size_t(227) * 1024) {
     auto launch = [&](auto kern) {
       CTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+      KernelTimer kt(c.stream, "jacobi_cluster_f32_kernel", kUnitFlop, 0.0);
       cudaLaunchConfig_t cfg{};
       cfg.gridDim = dim3(P);
       cfg.blockDim = dim3(8 * b);
@@ -1537,6 +1553,7 @@ void jacobi_left_singular(Ctx& c, const float* Mc, int64_t q, double* Ub, double
   if (jac_smem) {
     auto launch = [&](auto kern) {
       CTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(wjac)));
+      KernelTimer kt(c.stream, "jacobi_onesided_f32_kernel", kUnitFlop, 0.0);
       kern<<<1, jthreads, wjac, c.stream>>>(Mc, int(q), int(pp), Jc, norms, 40, 4e-6f,
                                            status_flags(c), nullptr);
     };
@@ -1549,6 +1566,7 @@ void jacobi_left_singular(Ctx& c, const float* Mc, int64_t q, double* Ub, double
       default: launch(jacobi_onesided_f32_kernel<true, 0>); break;
     }
   } else {
+    KernelTimer kt(c.stream, "jacobi_onesided_f32_kernel", kUnitFlop, 0.0);
     jacobi_onesided_f32_kernel<false, 0><<<1, jthreads, 0, c.stream>>>(
         Mc, int(q), int(pp), Jc, norms, 40, 4e-6f, status_flags(c), Wg);
   }

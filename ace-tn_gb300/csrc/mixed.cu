@@ -83,6 +83,7 @@ DLOp double_layer(Ctx& c, const View& ak, int64_t D, int64_t d) {
   o.hi = c.alloc<bf16>(size_t(o.n) * o.ld);
   o.lo = c.alloc<bf16>(size_t(o.n) * o.ld);
   if (!c.sizing()) {
+    KernelTimer kt(c.stream, "double_layer_kernel", kUnitByte, 4.0 * double(o.n) * o.n);
     double_layer_kernel<<<grid_for(o.n * o.n, 256), 256, 0, c.stream>>>(
         ak.p, ak.stride[0], ak.stride[1], ak.stride[2], ak.stride[3], ak.stride[4], int(D),
         int(d), o.hi, o.lo, o.ld);
@@ -101,10 +102,21 @@ DLOp double_layer(Ctx& c, const View& ak, int64_t D, int64_t d) {
 // layout the next step reads, with the GEMM rows (one per epilogue lane) on
 // the index that is contiguous in that layout; Q^T comes from a tiled
 // transpose, and max|Q| from the last epilogue.
-QOps quarter_mixed(Ctx& c, const Site& S, int k) {
+QOps quarter_mixed(Ctx& c, const Site& S, int k, bool fp64 = false) {
   int64_t sh[6], rows, cols;
   quarter_dims(S, k, rows, cols, sh);
   QOps o = alloc_ops(c, rows, cols);
+  if (fp64) {
+    // contracted in FP64 (already divided by max|Q|), then split
+    Scope s0(c);
+    double* Qd = c.alloc<double>(size_t(rows) * cols);
+    int64_t qs[6];
+    quarter_tensor(c, S, k, Qd, qs);
+    split_bf16(c, Qd, rows, cols, cols, false, o.q_hi, o.q_lo, o.ld);
+    fill(c, o.scale, 1, 1.0);
+    transpose_bf16(c, o.q_hi, o.q_lo, rows, cols, o.ld, o.t_hi, o.t_lo, o.ldt);
+    return o;
+  }
   const View ak = S.A(k), ck = S.C(k), ek1 = S.E(3 + k), ek2 = S.E(k);
   const int64_t a = ck.shape[0], cc = sh[0], E = sh[3], D = S.D, d = S.d, D2 = D * D;
   const TcMode x3 = TcMode::kBf16x3;
@@ -156,6 +168,7 @@ QOps quarter_mixed(Ctx& c, const Site& S, int k) {
     l.ne[2] = D;  l.ns[2] = 1;
     TcOut out;
     out.add(TcKind::kBf16Hi, xh, l).add(TcKind::kBf16Lo, xl, l);
+    out.name = "enlarged corner, edge step";
     tc_gemm(c, TcOperand{eh, el, E * D2, a, ld2}, TcOperand{th, tl, cc * D2, a, ld2}, x3, out);
   }
   // GEMM 2 against the double-layer matrix -> Q[(c,r,R)][(e,d,D)] and max|Q|;
@@ -176,6 +189,9 @@ QOps quarter_mixed(Ctx& c, const Site& S, int k) {
     TcOut out;
     out.add(TcKind::kBf16Hi, o.q_hi, lq).add(TcKind::kBf16Lo, o.q_lo, lq);
     out.extra_tag = kTagTcDoubleLayer;
+    out.name = "enlarged corner, double-layer step";
+    // the reference's two one-layer site-tensor steps (projectors.py:54-55)
+    out.algo_flops = 4.0 * double(cc) * E * D2 * D2 * D2 * d;
     tc_gemm_absmax(c, TcOperand{xh, xl, cc * E, K2, ldx}, dl.op(), x3, out, o.scale);
   }
   transpose_bf16(c, o.q_hi, o.q_lo, rows, cols, o.ld, o.t_hi, o.t_lo, o.ldt);
@@ -200,7 +216,8 @@ TcOperand yt_operand_f32(Ctx& c, const float* Y, int64_t n, int64_t q, int64_t l
 }
 
 // C = A @ B^T written as the next operand (C^T, BF16 hi [+ lo]).
-TcOperand gemm_to_operand(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, bool lo) {
+TcOperand gemm_to_operand(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, bool lo,
+                          const char* name = nullptr) {
   const int64_t M = A.rows, N = B.rows;
   const int64_t ld = tc_ld(M);
   bf16* hi = c.alloc<bf16>(size_t(N) * ld);
@@ -208,16 +225,19 @@ TcOperand gemm_to_operand(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode
   TcOut out;
   out.add(TcKind::kBf16Hi, hi, TcLayout::cols(M, N, ld));
   if (lo) out.add(TcKind::kBf16Lo, lw, TcLayout::cols(M, N, ld));
+  out.name = name;
   tc_gemm(c, A, B, mode, out);
   return TcOperand{hi, lw, N, M, ld};
 }
 
 void gemm_to_f64(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, double* C,
-                 int64_t ldc, bool transposed, const double* inv_scale) {
+                 int64_t ldc, bool transposed, const double* inv_scale,
+                 const char* name = nullptr) {
   TcOut out;
   out.add(TcKind::kF64, C,
           transposed ? TcLayout::cols(A.rows, B.rows, ldc) : TcLayout::rows(A.rows, B.rows, ldc));
   out.inv_scale = inv_scale;
+  out.name = name;
   tc_gemm(c, A, B, mode, out);
 }
 
@@ -278,6 +298,7 @@ void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64
     l.ne[1] = D2; l.ns[1] = 1;
     TcOut out;
     out.add(TcKind::kBf16Hi, xh, l).add(TcKind::kBf16Lo, xl, l);
+    out.name = "edge renormalization, projector step";
     tc_gemm(c, TcOperand{a1h, a1l, Aa * D2, B, ld1}, TcOperand{b1h, b1l, X * D2, B, ld1}, x3, out);
   }
   // G2 -> T[(x,r,R)][(a,d,D)]
@@ -299,6 +320,9 @@ void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64
     TcOut out;
     out.add(TcKind::kBf16Hi, t3h, l).add(TcKind::kBf16Lo, t3l, l);
     out.extra_tag = kTagTcDoubleLayer;
+    out.name = "edge renormalization, double-layer step";
+    // the reference's two one-layer site-tensor steps (directional_mover.py:363-364)
+    out.algo_flops = 4.0 * double(Aa) * X * D2 * D2 * D2 * d;
     tc_gemm(c, TcOperand{xh, xl, Aa * X, K2, ldx}, dl.op(), x3, out);
   }
   // G3: B4[y][(a,d,D)] = P2[a][d][D][y]
@@ -322,6 +346,7 @@ void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64
     l.ne[0] = Y; l.ns[0] = X * D2;
     TcOut out;
     out.add(TcKind::kF64, Eout, l);
+    out.name = "edge renormalization, last projector step";
     tc_gemm(c, TcOperand{t3h, t3l, X * D2, K4, ld4}, TcOperand{b4h, b4l, Y, K4, ld4}, x3, out);
   }
   double* nrm = c.alloc<double>(1);
@@ -348,13 +373,57 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
   const int64_t m = r1, n = c4;
   const int64_t q = std::min({o.chi + o.rsvd_oversampling, m, n});
   const int64_t cap = std::min(o.chi, q);
-  const TcMode x1 = TcMode::kBf16x1, x3 = TcMode::kBf16x3;
+  const TcMode x3 = TcMode::kBf16x3;
+  const bool rf3 = (o.mixed_flags & CTM_MIXED_RF3) != 0;
+  const bool svd64 = (o.mixed_flags & CTM_MIXED_SVD64) != 0;
+  const bool q64 = (o.mixed_flags & CTM_MIXED_Q64) != 0;
+  const bool f32 = (o.mixed_flags & CTM_MIXED_F32) != 0;
+  // range-finder products: one BF16 pass, or 3xBF16 with FP32 bases
+  // orthonormal to working precision
+  const TcMode xr = rf3 ? x3 : TcMode::kBf16x1;
+  const int inner_stages = rf3 ? 3 : 2;
+  float* Y = c.alloc<float>(size_t(m) * q);
+  float* Bt = c.alloc<float>(size_t(n) * q);
+  float *Q1f = nullptr, *Q4f = nullptr;
+  if (f32) {
+    // every product on FP32 copies of FP64 quarter tensors (SIMT FP32 FMAs):
+    // a precision reference for the tensor-core forms
+    Q1f = c.alloc<float>(size_t(m) * c1);
+    Q4f = c.alloc<float>(size_t(r4) * n);
+    {
+      Scope s0(c);
+      double* Qd = c.alloc<double>(size_t(std::max(m * c1, r4 * n)));
+      int64_t qs[6];
+      quarter_tensor(c, *S[0], k, Qd, qs);
+      to_f32(c, Qd, Q1f, m * c1);
+      quarter_tensor(c, *S[3], k + 3, Qd, qs);
+      to_f32(c, Qd, Q4f, r4 * n);
+    }
+    Scope s0(c);
+    float* T = c.alloc<float>(size_t(std::max(c1, n)) * q);
+    float* Z = c.alloc<float>(size_t(n) * q);
+    float* omf = c.alloc<float>(size_t(n) * q);
+    to_f32(c, omega, omf, n * q);
+    einsum(c, "ik,kj->ij", ViewF(Q4f, {r4, n}), ViewF(omf, {n, q}), ViewF(T, {r4, q}));
+    einsum(c, "ik,kj->ij", ViewF(Q1f, {m, c1}), ViewF(T, {c1, q}), ViewF(Y, {m, q}));
+    for (int it = 0; it < o.rsvd_niter; ++it) {
+      orthonormalize(c, Y, m, q, nullptr, 3);
+      einsum(c, "ki,kj->ij", ViewF(Q1f, {m, c1}), ViewF(Y, {m, q}), ViewF(T, {c1, q}));
+      einsum(c, "ki,kj->ij", ViewF(Q4f, {r4, n}), ViewF(T, {r4, q}), ViewF(Z, {n, q}));
+      orthonormalize(c, Z, n, q, nullptr, 3);
+      einsum(c, "ik,kj->ij", ViewF(Q4f, {r4, n}), ViewF(Z, {n, q}), ViewF(T, {r4, q}));
+      einsum(c, "ik,kj->ij", ViewF(Q1f, {m, c1}), ViewF(T, {c1, q}), ViewF(Y, {m, q}));
+    }
+    orthonormalize(c, Y, m, q, nullptr, 3);
+    einsum(c, "ki,kj->ij", ViewF(Q1f, {m, c1}), ViewF(Y, {m, q}), ViewF(T, {c1, q}));
+    einsum(c, "ki,kj->ij", ViewF(Q4f, {r4, n}), ViewF(T, {r4, q}), ViewF(Bt, {n, q}));
+  }
   // ---- quarter tensors as BF16 operands (tensor cores, 3xBF16)
   QOps A1, A4;
-  {
+  if (!f32) {
     KernelTimer span(c.stream, kTagQuarter, 0.0);
-    A1 = quarter_mixed(c, *S[0], k);
-    A4 = quarter_mixed(c, *S[3], k + 3);
+    A1 = quarter_mixed(c, *S[0], k, q64);
+    A4 = quarter_mixed(c, *S[3], k + 3, q64);
   }
   // ---- range finder in BF16 with FP32 orthonormalization (on the unscaled
   //      quarter tensors: every product is orthonormalised before use):
@@ -363,73 +432,91 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
   //      QR of the half step spans the same space in exact arithmetic and
   //      keeps the matrices that FP32 has to orthonormalise at the condition
   //      number of Q1 Q4 instead of its square.
-  float* Y = c.alloc<float>(size_t(m) * q);
   KernelTimer* rf_span = new KernelTimer(c.stream, kTagRangeFinder, 0.0);
-  {
+  if (!f32) {
     Scope s2(c);
-    const TcOperand om = yt_operand(c, omega, n, q, q, false);           // Omega^T (q x n)
-    const TcOperand t = gemm_to_operand(c, A4.q(false), om, x1, false);  // (Q4 Om)^T
+    const TcOperand om = yt_operand(c, omega, n, q, q, rf3);           // Omega^T (q x n)
+    const TcOperand t = gemm_to_operand(c, A4.q(rf3), om, xr, rf3, "range finder");  // (Q4 Om)^T
     TcOut out;
     out.add(TcKind::kF32, Y, TcLayout::rows(m, q, q));
-    tc_gemm(c, A1.q(false), t, x1, out);
+    out.name = "range finder";
+    tc_gemm(c, A1.q(rf3), t, xr, out);
   }
   // The bases inside the power iteration are only multiplied again in BF16
   // (~4e-3 relative): two Cholesky-QR stages (orthonormal to ~1e-3) suffice
   // there; the final Q, which forms B in 3xBF16, gets three.
-  for (int it = 0; it < o.rsvd_niter; ++it) {
+  for (int it = 0; it < (f32 ? 0 : o.rsvd_niter); ++it) {
     {
       KernelTimer span(c.stream, kTagOrtho, 0.0);
-      orthonormalize(c, Y, m, q, nullptr, 2);
+      orthonormalize(c, Y, m, q, nullptr, inner_stages);
     }
     Scope s2(c);
     float* Z = c.alloc<float>(size_t(n) * q);
     {
       Scope s3(c);
-      const TcOperand yt = yt_operand_f32(c, Y, m, q, q, false);
-      const TcOperand z1 = gemm_to_operand(c, A1.t(false), yt, x1, false);  // (Q1^T Y)^T
+      const TcOperand yt = yt_operand_f32(c, Y, m, q, q, rf3);
+      const TcOperand z1 = gemm_to_operand(c, A1.t(rf3), yt, xr, rf3, "range finder");  // (Q1^T Y)^T
       TcOut out;
       out.add(TcKind::kF32, Z, TcLayout::rows(n, q, q));
-      tc_gemm(c, A4.t(false), z1, x1, out);                                   // Z = Q4^T Q1^T Y
+      out.name = "range finder";
+      tc_gemm(c, A4.t(rf3), z1, xr, out);                                 // Z = Q4^T Q1^T Y
     }
     {
       KernelTimer span(c.stream, kTagOrtho, 0.0);
-      orthonormalize(c, Z, n, q, nullptr, 2);
+      orthonormalize(c, Z, n, q, nullptr, inner_stages);
     }
-    const TcOperand zt = yt_operand_f32(c, Z, n, q, q, false);
-    const TcOperand z3 = gemm_to_operand(c, A4.q(false), zt, x1, false);  // (Q4 Z)^T
+    const TcOperand zt = yt_operand_f32(c, Z, n, q, q, rf3);
+    const TcOperand z3 = gemm_to_operand(c, A4.q(rf3), zt, xr, rf3, "range finder");  // (Q4 Z)^T
     TcOut out;
     out.add(TcKind::kF32, Y, TcLayout::rows(m, q, q));
-    tc_gemm(c, A1.q(false), z3, x1, out);
+    out.name = "range finder";
+    tc_gemm(c, A1.q(rf3), z3, xr, out);
   }
-  {
+  if (!f32) {
     KernelTimer span(c.stream, kTagOrtho, 0.0);
     orthonormalize(c, Y, m, q, nullptr);
   }
   delete rf_span;
   // ---- Rayleigh-Ritz: B = (Q^T Q1) Q4 in 3xBF16 (written as B^T in FP32),
   //      its SVD from an FP32 QR of B^T and one-sided Jacobi
-  float* Bt = c.alloc<float>(size_t(n) * q);
   double* Ub = c.alloc<double>(size_t(q) * q);
   double* s = c.alloc<double>(q);
-  float* V = c.alloc<float>(size_t(n) * q);
-  float* U = c.alloc<float>(size_t(m) * q);
+  double* Ud = c.alloc<double>(size_t(m) * q);
+  double* Vd = c.alloc<double>(size_t(n) * q);
   KernelTimer* svd_span = new KernelTimer(c.stream, kTagSvd, 0.0);
-  {
+  if (!f32) {
     Scope s2(c);
     const TcOperand qt = yt_operand_f32(c, Y, m, q, q, true);           // Q^T (q x m)
-    const TcOperand w = gemm_to_operand(c, A1.t(true), qt, x3, true);    // W = Q^T Q1 (q x c1)
+    const TcOperand w = gemm_to_operand(c, A1.t(true), qt, x3, true, "Rayleigh-Ritz");  // W = Q^T Q1
     TcOut out;
     out.add(TcKind::kF32, Bt, TcLayout::rows(A4.cols, q, q));            // B^T (n x q)
     out.inv_scale = A1.scale;  // normalised quarter tensors
     out.inv_scale2 = A4.scale;
+    out.name = "Rayleigh-Ritz";
     tc_gemm(c, A4.t(true), w, x3, out);
   }
-  svd_via_qr(c, Bt, q, n, Ub, s, V);
-  {
+  if (svd64 || f32) {
+    // B (q x n) in FP64 from its FP32 transpose; FP64 one-sided Jacobi SVD;
+    // U = Q Ub in FP64
     Scope s2(c);
+    double* btd = c.alloc<double>(size_t(n) * q);
+    double* Bd = c.alloc<double>(size_t(q) * n);
+    double* Yd = c.alloc<double>(size_t(m) * q);
+    to_f64(c, Bt, btd, n * q);
+    copy2d(c, View(btd, {n, q}).permute({1, 0}), Bd, n);
+    svd_thin(c, Bd, q, n, Ub, s, Vd);
+    to_f64(c, Y, Yd, m * q);
+    einsum(c, "ik,kj->ij", View(Yd, {m, q}), View(Ub, {q, q}), View(Ud, {m, q}));
+  } else {
+    Scope s2(c);
+    float* V = c.alloc<float>(size_t(n) * q);
+    float* U = c.alloc<float>(size_t(m) * q);
+    svd_via_qr(c, Bt, q, n, Ub, s, V);
     float* ubf = c.alloc<float>(size_t(q) * q);
     to_f32(c, Ub, ubf, q * q);
     einsum(c, "ik,kj->ij", ViewF(Y, {m, q}), ViewF(ubf, {q, q}), ViewF(U, {m, q}));
+    to_f64(c, U, Ud, m * q);
+    to_f64(c, V, Vd, n * q);
   }
   delete svd_span;
   // ---- truncation (FP64 spectrum) and projector products (3xBF16)
@@ -443,16 +530,27 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
   double* P2f = c.alloc<double>(size_t(r4) * cap);
   {
     Scope s2(c);
-    double* Ud = c.alloc<double>(size_t(m) * q);
-    double* Vd = c.alloc<double>(size_t(n) * q);
-    to_f64(c, U, Ud, m * q);
-    to_f64(c, V, Vd, n * q);
     scale_columns(c, Ud, m, cap, q, f);
     scale_columns(c, Vd, n, cap, q, f);
+    if (f32) {
+      float* uf = c.alloc<float>(size_t(m) * q);
+      float* vf = c.alloc<float>(size_t(n) * q);
+      float* pf = c.alloc<float>(size_t(std::max(c1, r4)) * cap);
+      to_f32(c, Ud, uf, m * q);
+      to_f32(c, Vd, vf, n * q);
+      ViewF uv(uf, {m, cap}), vv(vf, {n, cap});
+      uv.stride[0] = q;
+      vv.stride[0] = q;
+      einsum(c, "ki,kz->iz", ViewF(Q1f, {m, c1}), uv, ViewF(pf, {c1, cap}));
+      to_f64(c, pf, P1f, c1 * cap);
+      einsum(c, "ik,kz->iz", ViewF(Q4f, {r4, n}), vv, ViewF(pf, {r4, cap}));
+      to_f64(c, pf, P2f, r4 * cap);
+    } else {
     const TcOperand ut = yt_operand(c, Ud, m, cap, q, true);  // (U f)^T (cap x m)
-    gemm_to_f64(c, A1.t(true), ut, x3, P1f, cap, false, A1.scale);  // Q1^T U f (c1 x cap)
+    gemm_to_f64(c, A1.t(true), ut, x3, P1f, cap, false, A1.scale, "projector");  // Q1^T U f (c1 x cap)
     const TcOperand vt = yt_operand(c, Vd, n, cap, q, true);  // (V f)^T (cap x n)
-    gemm_to_f64(c, A4.q(true), vt, x3, P2f, cap, false, A4.scale);  // Q4 V f (r4 x cap)
+    gemm_to_f64(c, A4.q(true), vt, x3, P2f, cap, false, A4.scale, "projector");  // Q4 V f (r4 x cap)
+    }
   }
   if (o.fixed_width) {
     if (!c.sizing()) {

@@ -1,9 +1,10 @@
 // Matrix product for callers that cannot allocate device memory.
 //
 // Some callers of this library cannot call cudaMalloc: a host framework that
-// hands a plugin only its input and output buffers and no allocator, or code
-// that runs while a CUDA stream capture in global mode is open (allocation is
-// prohibited then).  ctm_matmul_mixed_noalloc serves them: it is the 3xBF16
+// hands a plugin only its input and output buffers and no allocator, or one
+// whose own memory pool has reserved the device, so that an allocation by
+// the plugin fails or fragments that pool.  ctm_matmul_mixed_noalloc serves
+// them: it is the 3xBF16
 // tensor-core product of ctm_matmul (CTM_PREC_MIXED) with its scratch (the
 // BF16 operand copies and the split-K partial sums) placed in a file-scope
 // device array instead of a caller workspace.

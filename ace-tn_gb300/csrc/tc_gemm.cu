@@ -14,6 +14,9 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
+#include <set>
+#include <string>
 
 #include "engine.cuh"
 #include "tc_gemm.cuh"
@@ -25,11 +28,6 @@ namespace {
 constexpr int kBM = 128;         // rows of A per CTA (MMA M)
 // K per stage: 64 BF16 (128-byte rows, 128-byte swizzle); the kernel and the
 // tensor maps also take 32 (64-byte rows, 64-byte swizzle).
-// Clusters sharing B tiles (multicast) are built and tested but off: on the
-// double-layer GEMM at D=6 they measured slower (451 us against 373 us with
-// 256-wide tiles), the lockstep of the cluster costing more than the halved
-// operand stream saves.
-constexpr bool kClusterB = false;
 constexpr int kThreads = 256;    // 8 warps: in the epilogue warp w reads TMEM lanes
                                  // 32 (w % 4) .. +31 for half (w / 4) of the columns
 constexpr uint32_t kTmemCols = 256;
@@ -107,29 +105,6 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// The same box landing at the same shared-memory offset in every CTA of
-// ctaMask (thread-block cluster), each CTA's barrier at that offset receiving
-// its bytes.
-__device__ __forceinline__ void tma_load_2d_mc(void* dst, const CUtensorMap* map, int x, int y,
-                                               uint64_t* bar, uint16_t mask) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      ".multicast::cluster [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar)), "h"(mask)
-      : "memory");
-}
-
-__device__ __forceinline__ uint32_t cluster_rank() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-
-__device__ __forceinline__ void cluster_sync_all() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" :::
-                   "memory");
-}
-
 // Shared-memory matrix descriptor: K-major operand with rows of bk BF16
 // (bk = 64: 128-byte swizzle; bk = 32: 64-byte swizzle), 8-row core-matrix
 // groups 8 * 2 * bk bytes apart.
@@ -165,16 +140,6 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                    smem_u32(bar))
                : "memory");
-}
-
-// Completion of this CTA's MMAs signalled on the barrier at the same offset
-// in every CTA of mask.
-__device__ __forceinline__ void mma_commit_mc(uint64_t* bar, uint16_t mask) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64"
-      " [%0], %1;" ::"r"(smem_u32(bar)),
-      "h"(mask)
-      : "memory");
 }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
@@ -257,7 +222,6 @@ struct GemmParams {
   int m_tiles, n_tiles, tiles;  // persistent kernel: the tile grid
   int ntile;         // MMA N (multiple of 16, <= 256)
   int bk;            // K per stage (64 or 32)
-  int cx;            // CTAs per cluster along M sharing each B tile (1: no cluster)
   int kb_total;      // 64-wide K blocks
   int kb_per_split;
   int stages;
@@ -303,7 +267,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     s_fail = 0;
     for (int s = 0; s < p.stages; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], p.cx);  // released by the MMAs of every CTA of the cluster
+      mbar_init(&empty[s], 1);
     }
     mbar_init(tfull, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -317,13 +281,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  // every CTA of the cluster has initialised its barriers before any
-  // multicast copy or commit can reach them
-  if (p.cx > 1) cluster_sync_all();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_holder;
-  const uint32_t crank = p.cx > 1 ? cluster_rank() : 0u;
-  const uint16_t cmask = uint16_t((1u << p.cx) - 1u);
 
   const int kb0 = blockIdx.z * p.kb_per_split;
   const int kb1 = min(kb0 + p.kb_per_split, p.kb_total);
@@ -350,17 +309,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         mbar_expect_tx(&full[s], stage_bytes);
         const int x = (kb0 + i) * bk;
         tma_load_2d(st, &tA, x, m0, &full[s]);
-        if (p.mode == 3) tma_load_2d(st + half_bytes, &tAl, x, m0, &full[s]);
-        if (p.cx == 1) {
-          tma_load_2d(st + a_bytes, &tB, x, n0, &full[s]);
-          if (p.mode == 3) tma_load_2d(st + half_bytes + a_bytes, &tBl, x, n0, &full[s]);
-        } else {
-          // this CTA's slice of the shared B tile, multicast to the cluster
-          const int rows = p.ntile / p.cx;
-          const uint32_t off = a_bytes + crank * uint32_t(rows) * uint32_t(bk) * 2u;
-          tma_load_2d_mc(st + off, &tB, x, n0 + int(crank) * rows, &full[s], cmask);
-          if (p.mode == 3)
-            tma_load_2d_mc(st + half_bytes + off, &tBl, x, n0 + int(crank) * rows, &full[s], cmask);
+        tma_load_2d(st + a_bytes, &tB, x, n0, &full[s]);
+        if (p.mode == 3) {
+          tma_load_2d(st + half_bytes, &tAl, x, m0, &full[s]);
+          tma_load_2d(st + half_bytes + a_bytes, &tBl, x, n0, &full[s]);
         }
         issued_loads = i + 1;
       }
@@ -391,8 +343,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             mma_bf16(tmem, al, bh, idesc, 1u);
           }
         }
-        if (p.cx == 1) mma_commit(&empty[s]);
-        else mma_commit_mc(&empty[s], cmask);
+        mma_commit(&empty[s]);
       }
       mma_commit(tfull);
     }
@@ -497,9 +448,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  // no CTA leaves while a peer may still copy into its shared memory or
-  // arrive on its barriers
-  if (p.cx > 1) cluster_sync_all();
   if (warp == 0) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
@@ -950,6 +898,14 @@ void make_map(CUtensorMap* map, const bf16* ptr, int64_t rows, int64_t k, int64_
               "cuTensorMapEncodeTiled failed with code " + std::to_string(int(res)));
 }
 
+// Kernel-class names built at run time, kept for the life of the process.
+const char* intern_name(const std::string& s) {
+  static std::mutex mu;
+  static std::set<std::string> names;
+  std::lock_guard<std::mutex> lk(mu);
+  return names.insert(s).first->c_str();
+}
+
 // SM count of the current device (152 on GB300), used by both the sizing
 // pass and the launch so that they choose the same split-K; 152 when no
 // device is visible (workspace queries on a machine without a GPU).
@@ -971,6 +927,8 @@ void split_bf16_impl(Ctx& c, const S* src, int64_t rows, int64_t cols, int64_t l
   if (c.sizing() || rows * cols == 0) return;
   dim3 grid(unsigned((cols + 31) / 32), unsigned((rows + 31) / 32));
   CTM_REQUIRE(grid.y <= 65535, CTM_ERR_UNSUPPORTED, "split_bf16: too many rows");
+  KernelTimer kt(c.stream, "split_bf16_kernel", kUnitByte,
+                 double(rows) * cols * (sizeof(S) + (lo != nullptr ? 4.0 : 2.0)));
   split_bf16_kernel<S><<<grid, 256, 0, c.stream>>>(src, rows, cols, ld_src, transpose ? 1 : 0, hi,
                                                    lo, ld_dst);
   CTM_LAUNCH_CHECK();
@@ -1059,6 +1017,8 @@ void transpose_bf16(Ctx& c, const bf16* src_hi, const bf16* src_lo, int64_t rows
               "transpose_bf16: lo arrays must be given on both sides or neither");
   const dim3 grid(unsigned((cols + 63) / 64), unsigned((rows + 63) / 64), src_lo ? 2u : 1u);
   CTM_REQUIRE(grid.y <= 65535, CTM_ERR_UNSUPPORTED, "transpose_bf16: too many rows");
+  KernelTimer kt(c.stream, "transpose_bf16_kernel", kUnitByte,
+                 4.0 * double(rows) * cols * (src_lo != nullptr ? 2.0 : 1.0));
   transpose_bf16_kernel<<<grid, 256, 0, c.stream>>>(src_hi, src_lo, rows, cols, ld_src, dst_hi,
                                                     dst_lo, ld_dst);
   CTM_LAUNCH_CHECK();
@@ -1067,6 +1027,8 @@ void transpose_bf16(Ctx& c, const bf16* src_hi, const bf16* src_lo, int64_t rows
 void join_bf16(Ctx& c, const bf16* hi, const bf16* lo, int64_t rows, int64_t cols, int64_t ld,
                double* out) {
   if (c.sizing() || rows * cols == 0) return;
+  KernelTimer kt(c.stream, "join_bf16_kernel", kUnitByte,
+                 double(rows) * cols * (8.0 + (lo != nullptr ? 4.0 : 2.0)));
   join_bf16_kernel<<<grid_for(rows * cols, 256), 256, 0, c.stream>>>(hi, lo, rows, cols, ld, out);
   CTM_LAUNCH_CHECK();
 }
@@ -1076,6 +1038,8 @@ void gather_split_bf16(Ctx& c, const double* src, const Gather& g, bf16* hi, bf1
   for (int j = 0; j < g.nr; ++j) rows *= g.re[j];
   for (int j = 0; j < g.nk; ++j) K *= g.ke[j];
   if (c.sizing() || rows * K == 0) return;
+  KernelTimer kt(c.stream, "gather_split_kernel", kUnitByte,
+                 double(rows) * K * (8.0 + (lo != nullptr ? 4.0 : 2.0)));
   gather_split_kernel<<<grid_for(rows * K, 256), 256, 0, c.stream>>>(src, g, rows, K, hi, lo, ld);
   CTM_LAUNCH_CHECK();
 }
@@ -1117,20 +1081,9 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   // dynamic shared memory: the stage ring (the kernel's static arrays take ~8 KB)
   const int stages = std::max(2, std::min(6, int((210 * 1024) / stage_bytes)));
   const size_t smem = size_t(stages) * stage_bytes + 256 + 1024;
-  // Long 3xBF16 products with a direct epilogue run in clusters of cx CTAs
-  // along M that share each B tile: every CTA loads 1/cx of it and multicasts
-  // it to the others, which divides the B operand stream from L2 by cx (the
-  // double-layer GEMMs are bound by that stream).  M tiles are padded to a
-  // multiple of cx (the padding rows read zeros and store nothing).
-  int cx = 1;
-  if (kClusterB && imode == 3 && direct && kb_total >= 8) {
-    if (m_tiles >= 4 && ntile % 32 == 0) cx = 4;
-    else if (m_tiles >= 2 && ntile % 16 == 0) cx = 2;
-  }
-  const int64_t m_grid = (m_tiles + cx - 1) / cx * cx;
   // grid x over N tiles when A is the larger operand: the CTAs that share an
   // A tile are then resident together and A streams from DRAM once
-  const bool n_fast = cx == 1 && n_tiles > 1 && m_tiles > n_tiles && m_tiles <= 65535;
+  const bool n_fast = n_tiles > 1 && m_tiles > n_tiles && m_tiles <= 65535;
   Scope scope(c);
   float* part = direct ? nullptr : c.alloc<float>(size_t(splits) * m_pad * n_pad);
   if (c.sizing()) return;
@@ -1140,16 +1093,16 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
               "tc_gemm: grid too large");
   CUtensorMap tA, tAl, tB, tBl;
   make_map(&tA, A.hi, A.rows, K, A.ld, kBM, bk);
-  make_map(&tB, B.hi, B.rows, K, B.ld, uint32_t(ntile / cx), bk);
+  make_map(&tB, B.hi, B.rows, K, B.ld, uint32_t(ntile), bk);
   if (imode == 3) {
     make_map(&tAl, A.lo, A.rows, K, A.ld, kBM, bk);
-    make_map(&tBl, B.lo, B.rows, K, B.ld, uint32_t(ntile / cx), bk);
+    make_map(&tBl, B.lo, B.rows, K, B.ld, uint32_t(ntile), bk);
   } else {
     tAl = tA;
     tBl = tB;
   }
   // more tiles than SMs with a direct epilogue: one persistent CTA per SM
-  const bool persistent = direct && cx == 1 && base_ctas > sms;
+  const bool persistent = direct && base_ctas > sms;
   // the persistent kernel's static shared memory (offset tables and the
   // staged epilogue, ~29 KB) leaves 196 KB for the stage ring
   const int p_stages = std::max(2, std::min(6, int((196 * 1024) / stage_bytes)));
@@ -1163,7 +1116,6 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   p.tiles = int(m_tiles * n_tiles);
   p.ntile = ntile;
   p.bk = bk;
-  p.cx = cx;
   p.kb_total = kb_total;
   p.kb_per_split = kb_per_split;
   p.stages = persistent ? p_stages : stages;
@@ -1186,34 +1138,24 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   if (absmax != nullptr) CTM_CUDA(cudaMemsetAsync(absmax, 0, sizeof(double), c.stream));
   CTM_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(smem)));
-  const dim3 grid(static_cast<unsigned>(n_fast ? n_tiles : m_grid),
-                  static_cast<unsigned>(n_fast ? m_grid : n_tiles), static_cast<unsigned>(splits));
+  const dim3 grid(static_cast<unsigned>(n_fast ? n_tiles : m_tiles),
+                  static_cast<unsigned>(n_fast ? m_tiles : n_tiles), static_cast<unsigned>(splits));
   {
     const double work = 2.0 * double(M) * N * K * imode;
     KernelTimer timer(c.stream, kTagTcGemm, work);
     KernelTimer timer2(c.stream, out.extra_tag >= 0 ? out.extra_tag : kTagTcGemm,
                        out.extra_tag >= 0 ? work : -1.0);
+    const char* kname = persistent ? "tc_gemm_persistent_kernel" : "tc_gemm_kernel";
+    if (out.name != nullptr) kname = intern_name(std::string(kname) + " (" + out.name + ")");
+    KernelTimer timer3(c.stream, kname, kUnitFlop,
+                       out.algo_flops >= 0.0 ? out.algo_flops : 2.0 * double(M) * N * K);
     if (persistent) {
       CTM_CUDA(cudaFuncSetAttribute(tc_gemm_persistent_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, int(p_smem)));
       tc_gemm_persistent_kernel<<<unsigned(std::min<int64_t>(base_ctas, sms)), kPThreads, p_smem,
                                   c.stream>>>(tA, tAl, tB, tBl, p);
-    } else if (cx == 1) {
-      tc_gemm_kernel<<<grid, kThreads, smem, c.stream>>>(tA, tAl, tB, tBl, p);
     } else {
-      cudaLaunchConfig_t cfg{};
-      cfg.gridDim = grid;
-      cfg.blockDim = dim3(kThreads);
-      cfg.dynamicSmemBytes = smem;
-      cfg.stream = c.stream;
-      cudaLaunchAttribute attr[1];
-      attr[0].id = cudaLaunchAttributeClusterDimension;
-      attr[0].val.clusterDim.x = unsigned(cx);
-      attr[0].val.clusterDim.y = 1;
-      attr[0].val.clusterDim.z = 1;
-      cfg.attrs = attr;
-      cfg.numAttrs = 1;
-      CTM_CUDA(cudaLaunchKernelEx(&cfg, tc_gemm_kernel, tA, tAl, tB, tBl, p));
+      tc_gemm_kernel<<<grid, kThreads, smem, c.stream>>>(tA, tAl, tB, tBl, p);
     }
     CTM_LAUNCH_CHECK();
   }
@@ -1232,6 +1174,7 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   for (int i = 0; i < out.nd; ++i) r.d[i] = out.d[i];
   dim3 rg(unsigned((M + 31) / 32), unsigned((N + 31) / 32));
   CTM_REQUIRE(rg.y <= 65535, CTM_ERR_UNSUPPORTED, "tc_gemm: output too wide");
+  KernelTimer kt(c.stream, "tc_reduce_kernel", kUnitByte, 4.0 * (splits + 1.0) * double(M) * N);
   tc_reduce_kernel<<<rg, 256, 0, c.stream>>>(r);
   CTM_LAUNCH_CHECK();
 }

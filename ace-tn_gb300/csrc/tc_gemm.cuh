@@ -55,6 +55,8 @@ struct TcOut {
   const double* inv_scale = nullptr;   // device scalars: results are divided by *inv_scale
   const double* inv_scale2 = nullptr;  // and by *inv_scale2 when non-null
   int extra_tag = -1;                  // profiling class timed besides "tensor-core GEMM"
+  const char* name = nullptr;          // kernel-class name in the per-kernel profile
+  double algo_flops = -1.0;            // algorithmic FLOPs of the product (default 2 M N K)
   int nd = 0;
   TcDest d[4];
   TcOut& add(TcKind k, void* p, const TcLayout& l) {

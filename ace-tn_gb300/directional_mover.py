@@ -98,7 +98,9 @@ class DirectionalMover:
 
     # ---------------------------------------------------------------- moves
     def _projectors_all(self, ipeps, site_lists, k):
-        device = ipeps[site_lists[0][0]]["A"].device
+        a = ipeps[site_lists[0][0]]["A"]
+        _abi.require_cuda(a, "A", storage=True)  # before any stream is forked
+        device = a.device
         slots = torch.zeros(len(site_lists), dtype=torch.int64, device=device)
         streams = self._fork(device, len(site_lists))
         pend = []

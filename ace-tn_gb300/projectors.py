@@ -48,6 +48,7 @@ class ProjectorCalculator:
         self.rsvd_oversampling = self.config.rsvd_oversampling
         self.precision = self.config.precision
         self.mixed_svd_floor = self.config.mixed_svd_floor
+        self.mixed_flags = self.config.mixed_flags
         self.omega_source = omega_source or default_omega
         self.set_calculate()
 

@@ -3,9 +3,10 @@ cell, d=2, half-system rSVD projectors, oversampling 16, 2 power iterations).
 
 A step is one directional move (projectors of both rows/columns of the move,
 then the boundary renormalization of both).  The environment is first grown
-to chi (two untimed CTMRG iterations), then W untimed moves, then K timed
-moves, each bracketed by CUDA events on the launching stream with an L2
-flush (a 256 MiB write) between moves outside the events.
+for 50 untimed CTMRG iterations (the iteration count of this workload), then
+W untimed moves, then K timed moves, each bracketed by CUDA events on the
+launching stream with an L2 flush (a 256 MiB write) between moves outside the
+events.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
        [--precision fp64|mixed]
@@ -27,12 +28,17 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 D, CHI, PHYS, OVERSAMPLING, NITER, SEED = 6, 144, 2, 16, 2, 20250
+GROW_ITERS = 50
 N_Q = CHI * D * D
 METRIC = "CTMRG moves/s at D=6, chi=144 (Heisenberg, 2x2, half-system rSVD os=16 niter=2)"
-# DRAM bytes (read + write) of one launch of the double-layer contraction GEMM
-# at this workload (M = D^4 = 1296, N = chi^2 = 20736, K = 1296, 3xBF16),
-# from the ncu capture summarised in profiles/tc_gemm_double_layer_d6_chi144.md
-DL_GEMM_TRAFFIC = 118.590208e6 + 56.284160e6
+WORKLOAD = {"workload": f"heisenberg_2x2_D{D}_chi{CHI}_rsvd_os{OVERSAMPLING}_niter{NITER}",
+            "D": D, "chi": CHI, "phys": PHYS, "projectors": "half-system", "svd_type": "rsvd",
+            "seed": SEED, "iterations_before_timing": GROW_ITERS}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of a
+# kernel class at this workload, from `ncu --metrics dram__bytes_read.sum,
+# dram__bytes_write.sum --clock-control none` on `bench.py --profile-case`
+# (one launch per class); classes without a capture report null.
+NCU_DRAM_BYTES = {}
 
 
 def move_flops(D, chi, q, d=2, ny=2, niter=2):
@@ -179,7 +185,6 @@ def run_reference(args, rank):
     (numpy/LAPACK on the host cores), same config, metric and unit."""
     if rank != 0:
         return None
-    import numpy as np
     from oracle import ctm_oracle as orc
     st = orc.random_state(D, CHI, seed=SEED)
     cfg = dict(projectors="half-system", svd_type="rsvd", rsvd_oversampling=OVERSAMPLING,
@@ -197,12 +202,11 @@ def run_reference(args, rank):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"heisenberg_2x2_D{D}_chi{CHI}_rsvd_os{OVERSAMPLING}_niter{NITER}",
-                   "D": D, "chi": CHI, "phys": PHYS, "projectors": "half-system",
-                   "svd_type": "rsvd", "seed": SEED},
+        "config": dict(WORKLOAD),
         "cpu_baseline": {"value": value, "unit": "moves/s", "cores": cpu_cores(), "kind": "port",
                          "sample": f"{args.steps} moves after 2 growth iterations "
-                                   f"({grow_s:.1f} s) and {args.warmup} warm-up moves",
+                                   f"({grow_s:.1f} s; chi saturated, the per-move cost of the "
+                                   f"{GROW_ITERS}-iteration state) and {args.warmup} warm-up moves",
                          "cpu_model": cpu_model()},
         "e2e": {"value": value, "unit": "moves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -221,7 +225,6 @@ def state_bytes(st):
 
 
 def run_gb300(args, rank, world, local_rank):
-    import numpy as np
     import torch
     import torch.distributed as dist
 
@@ -240,11 +243,18 @@ def run_gb300(args, rank, world, local_rank):
         return torch.randn(n, q, dtype=torch.float64, device=device, generator=gen)
 
     st = gb.random_state(D, CHI, SEED, d=PHYS, device=dev)
-    mover = gb.DirectionalMover(cfg, omega_source=omega)
+    # the environment is grown with the mixed path (seconds; the FP64 path
+    # would take minutes), whatever --precision times afterwards
+    import dataclasses
+    grower = gb.DirectionalMover(dataclasses.replace(cfg, precision="mixed"), omega_source=omega)
     order = gb.sweep_order(2, 2)
-    for _ in range(2):  # grow the environment to chi
+    t_grow = time.perf_counter()
+    for _ in range(GROW_ITERS):
         for k, idx in order:
-            mover.move(st, k, idx)
+            grower.move(st, k, idx)
+    torch.cuda.synchronize(dev)
+    t_grow = time.perf_counter() - t_grow
+    mover = gb.DirectionalMover(cfg, omega_source=omega)
     pos = 0
     for _ in range(args.warmup):
         k, idx = order[pos % len(order)]
@@ -273,7 +283,11 @@ def run_gb300(args, rank, world, local_rank):
     launches = gb._abi.kernel_launches() - launches0
     qr_fallbacks = gb._abi.qr_fallbacks(dev)
     clk = clocks.stop()
-    # per-kernel-class timing (CUDA events inside the library) on a separate,
+    ms = [a.elapsed_time(b) for a, b in ev]
+    total_s = sum(ms) / 1e3
+    total_max, value = aggregate(total_s, args.steps, world, dev)
+
+    # per-kernel timing (CUDA events inside the library) on a separate,
     # untimed pass with the rows of each move run one after the other, so
     # that no two kernels of the pass share the GPU
     prof_moves = max(1, min(args.steps, 4))
@@ -290,37 +304,32 @@ def run_gb300(args, rank, world, local_rank):
         pos += 1
     torch.cuda.synchronize(dev)
     prof = gb._abi.profile_end()
+    kernels = gb._abi.profile_kernels()
     prof_move_ms = sum(a.elapsed_time(b) for a, b in pev) / prof_moves
     mover.concurrent = True
-    ms = [a.elapsed_time(b) for a, b in ev]
-    total_s = sum(ms) / 1e3
-    eager = None
-    if args.graph:
-        # one CTMRG iteration (8 moves) captured as a CUDA graph and replayed;
-        # the rSVD test matrices come from torch's default CUDA generator
-        eager_total, eager_value = aggregate(total_s, args.steps, world, dev)
-        eager = {"value": eager_value, "ms_per_step": 1e3 * eager_total / args.steps}
-        graph = gb.CTMRGGraph(st, cfg).capture(warmup=1)
+
+    # one CTMRG iteration (8 moves) captured as a CUDA graph and replayed
+    graph_line = None
+    if not args.no_graph:
+        gst = clone_state(gb, st)
+        graph = gb.CTMRGGraph(gst, cfg).capture(warmup=1)
         graph.replay(1)
         replays = max(1, -(-args.steps // len(order)))
         gev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                for _ in range(replays)]
-        clocks = ClockSampler(local_rank)
-        clocks.start()
         torch.cuda.synchronize(dev)
-        clocks.mark_start()
         for i in range(replays):
             flush.zero_()
             gev[i][0].record(stream)
             graph.replay(1)
             gev[i][1].record(stream)
         torch.cuda.synchronize(dev)
-        clocks.mark_end()
-        clk = clocks.stop()
-        total_s = sum(a.elapsed_time(b) for a, b in gev) / 1e3
-        graph_truncated = graph.truncated()
-        args.steps_timed = replays * len(order)
-    total_max, value = aggregate(total_s, getattr(args, "steps_timed", args.steps), world, dev)
+        g_s = sum(a.elapsed_time(b) for a, b in gev) / 1e3
+        g_total, g_value = aggregate(g_s, replays * len(order), world, dev)
+        graph_line = {"value": g_value, "unit": "moves/s",
+                      "ms_per_step": 1e3 * g_total / (replays * len(order)),
+                      "steps": replays * len(order), "truncated_below_chi": graph.truncated()}
+        del graph, gst
 
     # ---- e2e: host buffers through the public API, copies inside the timed region
     host = {s: {"A": st[s]["A"].cpu().pin_memory(),
@@ -361,7 +370,7 @@ def run_gb300(args, rank, world, local_rank):
 
     compare = None
     if rank == 0 and not args.no_compare:
-        compare = compare_paths(gb, st, cfg, dev, args.precision)
+        compare = compare_paths(gb, st, cfg, dev, args.precision, args.compare_moves)
 
     peaks = {}
     try:
@@ -369,68 +378,48 @@ def run_gb300(args, rank, world, local_rank):
             peaks = json.load(fh)
     except OSError:
         pass
-    if args.precision == "mixed":
-        # the double-layer contraction GEMMs (enlarged corners and edge
-        # renormalization, 3xBF16 on tcgen05) are the largest kernel class
-        dom_ms, dom_work, dom_n = prof["tc_gemm_double_layer"]
-        dom = "tc_gemm_persistent_kernel (double-layer contraction, 3xBF16)"
-        peak = peaks.get("bf16_tflops_sustained") or 1700.0
-        peak_src = ("MEASURED_PEAKS.json bf16_tflops_sustained" if peaks
-                    else "fallback 1.7 PF/s")
-        bound = "tensor"
-        traffic = DL_GEMM_TRAFFIC
-    else:
-        dom_ms, dom_work, dom_n = prof["gett_f64"]
-        dom = "gett_kernel<double>"
-        peak = fp64_peak_tflops(dev)
-        peak_src = ("cuBLAS DGEMM 8192^3 measured by bench.py on this GPU "
-                    "(no FP64 entry in MEASURED_PEAKS.json)")
-        bound = "fp64"
-        traffic = None
-    achieved = (dom_work / (dom_ms / 1e3)) / 1e12 if dom_ms > 0 else None
+    table = kernel_table(kernels, prof_moves, prof_move_ms, peaks, dev)
+    roof = next((k for k in table if k["bound"] in ("tensor", "hbm") and k["achieved"]), None)
     q = CHI + OVERSAMPLING
     line = None
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "moves/s", "n_gpus": world,
-            "steps": getattr(args, "steps_timed", args.steps), "warmup": args.warmup,
-            "ms_per_step": 1e3 * total_max / getattr(args, "steps_timed", args.steps),
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * total_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision == "fp64" else "bf16/3xbf16+f64",
+            "dtype": "f64" if args.precision == "fp64" else "bf16/3xbf16+f32+f64",
+            "precision": args.precision,
             "data": "synthetic",
-            "config": {"workload": f"heisenberg_2x2_D{D}_chi{CHI}_rsvd_os{OVERSAMPLING}_niter{NITER}",
-                       "D": D, "chi": CHI, "phys": PHYS, "projectors": "half-system",
-                       "svd_type": "rsvd", "precision": args.precision, "seed": SEED,
-                       "l2": "256 MiB flush between timed moves; quarter tensors 215 MB each",
-                       "parallelism": f"replicas x{world}"},
-            "tflops": move_flops(D, CHI, q) / (total_max / getattr(args, "steps_timed", args.steps))
-                      / 1e12,
-            "roofline": {"bound": bound, "kernel": dom, "achieved": achieved, "peak": peak,
-                         "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
-                         "traffic": traffic, "launches": dom_n, "peak_source": peak_src,
-                         "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum, "
-                                            "one launch, profiles/tc_gemm_double_layer_d6_chi144.md "
-                                            "(captured before the operand swap of this GEMM)"
-                                            if traffic else None),
-                         "work_per_launch": dom_work / dom_n if dom_n else None,
-                         "share_of_step": (dom_ms / prof_moves) / prof_move_ms,
-                         "timing": f"CUDA events around each launch, {prof_moves} moves with "
-                                   "the rows run serially (ms_per_step there: "
-                                   f"{prof_move_ms:.2f})"},
+            "config": dict(WORKLOAD),
+            "l2": "256 MiB flush between timed moves; quarter tensors 215 MB each",
+            "parallelism": f"replicas x{world}",
+            "tflops": move_flops(D, CHI, q) / (total_max / args.steps) / 1e12,
+            "roofline": None if roof is None else {
+                "bound": roof["bound"], "kernel": roof["name"], "achieved": roof["achieved"],
+                "peak": roof["peak"], "unit": roof["achieved_unit"], "frac": roof["frac"],
+                "traffic": NCU_DRAM_BYTES.get(roof["name"]),
+                "launches_per_step": roof["launches_per_step"],
+                "work_per_launch": roof["work_per_launch"], "work_unit": roof["unit"],
+                "share_of_step": roof["share"], "peak_source": roof["peak_source"],
+                "timing": f"CUDA events around each launch, {prof_moves} moves with the rows "
+                          f"run serially (ms_per_step there: {prof_move_ms:.2f})"},
+            "dominant_kernel_by_time": None if not table else {
+                "kernel": table[0]["name"], "share_of_step": table[0]["share"],
+                "bound": table[0]["bound"]},
+            "kernels": table[:12],
             "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
-            # graph replays run the captured launches of the eager moves
-            "gpu_launches": int(launches) if not args.graph else
-            int(round(launches / args.steps * args.steps_timed)),
-            "execution": ("cuda_graph" if args.graph else "eager"),
+            "gpu_launches": int(launches),
+            "execution": "eager",
+            "graph": graph_line,
             "qr_fallbacks_in_timed_moves": qr_fallbacks,
-            "eager": eager,
+            "grow_seconds": t_grow,
             "comparison": compare,
-            "breakdown_ms_per_step": {k: v[0] / prof_moves for k, v in prof.items() if v[2]},
+            "spans_ms_per_step": {k: v[0] / prof_moves for k, v in prof.items() if v[2]},
             "clocks": clk,
         }
         if world == 1 and not args.no_cpu_baseline:
-            st_np = type("S", (), {})
             from oracle import ctm_oracle as orc
             ost = orc.OracleState(
                 {s: {"A": st[s]["A"].cpu().numpy(), "C": [c.cpu().numpy() for c in st[s]["C"]],
@@ -439,9 +428,59 @@ def run_gb300(args, rank, world, local_rank):
             line["cpu_baseline"] = {"value": len(times) / sum(times), "unit": "moves/s",
                                     "cores": cpu_cores(), "kind": "port",
                                     "sample": f"{len(times)} oracle moves from the GPU run's "
-                                              f"saturated chi={CHI} state",
+                                              f"{GROW_ITERS}-iteration chi={CHI} state",
                                     "cpu_model": cpu_model()}
     return line
+
+
+def sm_fp32_peak_tflops(dev):
+    """FP32 FMA peak of the SIMT units: SMs x 128 lanes x 2 FLOP x max clock."""
+    import torch
+    p = torch.cuda.get_device_properties(dev)
+    mhz = 2070.0
+    try:
+        out = subprocess.run(["nvidia-smi", "--query-gpu=clocks.max.sm", "--format=csv,noheader,nounits",
+                              "-i", str(dev.index or 0)], capture_output=True, text=True, timeout=10)
+        mhz = float(out.stdout.strip().splitlines()[0])
+    except (OSError, ValueError, IndexError, subprocess.TimeoutExpired):
+        pass
+    return p.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
+
+
+def kernel_table(kernels, moves, move_ms, peaks, dev):
+    """Kernel classes of the profiled moves sorted by time: share of the
+    (serial-rows) move, launches and algorithmic work per launch, achieved
+    rate and the fraction of the roof that bounds the class: tensor cores
+    (BF16 peak; the work is the algorithmic FLOP count of the contraction the
+    launch performs, not the split-precision passes), HBM (algorithmic bytes),
+    FP64 or FP32 SIMT FMA; iterative kernels (Jacobi sweeps) have no work
+    figure and report time only."""
+    bf16 = peaks.get("bf16_tflops") or 1900.0
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    src = "MEASURED_PEAKS.json" if peaks else "fallback"
+    out = []
+    for k in kernels:
+        name = k["name"]
+        if name.startswith("tc_gemm") and k["unit"] == "flop":
+            bound, peak, unit, psrc = "tensor", bf16, "TFLOP/s", f"{src} bf16_tflops (burst)"
+        elif k["unit"] == "byte":
+            bound, peak, unit, psrc = "hbm", hbm, "GB/s", f"{src} hbm_gbs"
+        elif "double" in name:
+            bound, peak, unit, psrc = "fp64", fp64_peak_tflops(dev), "TFLOP/s", "cuBLAS DGEMM on this GPU"
+        else:
+            bound, peak, unit, psrc = "fp32", sm_fp32_peak_tflops(dev), "TFLOP/s", "SMs x 128 x 2 x max clock"
+        sec = k["ms"] / 1e3
+        achieved = None
+        if k["work"] > 0 and sec > 0:
+            achieved = k["work"] / sec / (1e9 if unit == "GB/s" else 1e12)
+        out.append({"name": name, "share": (k["ms"] / moves) / move_ms if move_ms else None,
+                    "ms_per_step": k["ms"] / moves, "launches_per_step": k["launches"] / moves,
+                    "work_per_launch": k["work"] / k["launches"] if k["launches"] else None,
+                    "unit": k["unit"], "bound": bound, "achieved": achieved,
+                    "achieved_unit": unit, "peak": peak,
+                    "frac": achieved / peak if achieved else None, "peak_source": psrc})
+    out.sort(key=lambda x: -x["ms_per_step"])
+    return out
 
 
 def clone_state(gb, st):
@@ -453,12 +492,26 @@ def clone_state(gb, st):
     return c
 
 
-def compare_paths(gb, st, cfg, dev, precision):
-    """From the benchmark's saturated state: moves/s of this library's plain
-    FP64 path (the drop-in), and the energy after one move in each precision
-    with the same rSVD test matrices, next to the FP64 path's own spread
-    between two draws of the test matrices (the rSVD's noise)."""
+def bond_energies(gb, st, model):
+    """Per-bond energies <h_b> from trace-normalised bond RDMs (FP64)."""
+    import torch
+    rdm = gb.RDM(st)
+    out = []
+    for b in st.bond_list:
+        r = rdm[b]
+        h2 = model.two_site_hamiltonian(b).reshape(2, 2, 2, 2)
+        out.append(float(torch.einsum("PQpq,pqPQ->", r, h2) / torch.einsum("pqpq->", r)))
+    return out
+
+
+def compare_paths(gb, st, cfg, dev, precision, nmoves):
+    """From the benchmark's grown state: moves/s of this library's plain FP64
+    path (the drop-in), and, for one move of each direction, the energy per
+    site and per bond after the move in each precision with the same rSVD
+    test matrices, next to the FP64 path's own spread between two draws of
+    the test matrices (the rSVD's noise).  Energies use FP64 bond RDMs."""
     import dataclasses
+    import statistics as stats
     import torch
     order = gb.sweep_order(2, 2)
     cfg64 = dataclasses.replace(cfg, precision="fp64")
@@ -482,20 +535,39 @@ def compare_paths(gb, st, cfg, dev, precision):
     torch.cuda.synchronize(dev)
     fp64_ms = a.elapsed_time(b) / 2
     del s64
-    # one-move energies
     model = gb.HeisenbergModel(1.0, device=dev)
-    energies = {}
-    for tag, c, seed in (("fp64", cfg64, 7), ("fp64_other_draw", cfg64, 8),
-                         (precision, cfg, 7)):
-        s1 = clone_state(gb, st)
-        gb.DirectionalMover(c, omega_source=seeded(seed)).move(s1, *order[0])
-        energies[tag] = float(gb.measure(s1, model, verbose=False)["Energy"])
-        del s1
-    e64 = energies["fp64"]
+    rows = []
+    # one move of each direction (left, right, up, down) from the same state
+    for k, idx in [order[i] for i in (0, 1, 2, 3)][:nmoves]:
+        e = {}
+        for tag, c, seed in (("fp64", cfg64, 7 + k), ("fp64_other_draw", cfg64, 107 + k),
+                             (precision, cfg, 7 + k)):
+            s1 = clone_state(gb, st)
+            gb.DirectionalMover(c, omega_source=seeded(seed)).move(s1, k, idx)
+            e[tag] = bond_energies(gb, s1, model)
+            del s1
+        ref = e["fp64"]
+        e_ref = sum(ref) / 4
+        scale = max(abs(x) for x in ref)
+
+        def rel(v):
+            return abs(sum(v) / 4 - e_ref) / abs(e_ref)
+
+        def per_bond(v):
+            return max(abs(x - y) for x, y in zip(v, ref)) / scale
+
+        rows.append({"move": [k, idx], "energy_fp64": e_ref,
+                     "rel_err": rel(e[precision]), "bond_err": per_bond(e[precision]),
+                     "fp64_draw_rel": rel(e["fp64_other_draw"]),
+                     "fp64_draw_bond": per_bond(e["fp64_other_draw"])})
+    errs = [r["rel_err"] for r in rows]
+    draws = [r["fp64_draw_rel"] for r in rows]
     return {"fp64_path": {"moves_per_s": 1e3 / fp64_ms, "ms_per_step": fp64_ms},
-            "one_move_energy": energies,
-            "rel_err_vs_fp64": abs(energies[precision] - e64) / abs(e64),
-            "fp64_rsvd_draw_spread": abs(energies["fp64_other_draw"] - e64) / abs(e64)}
+            "state": f"after {GROW_ITERS} iterations",
+            "rel_err_vs_fp64": stats.median(errs), "rel_err_vs_fp64_max": max(errs),
+            "fp64_rsvd_draw_spread": stats.median(draws),
+            "fp64_rsvd_draw_spread_max": max(draws),
+            "moves": rows}
 
 
 def aggregate(total_s, steps, world, device="cpu"):
@@ -582,10 +654,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
-    ap.add_argument("--graph", action="store_true",
-                    help="time replays of one CUDA-graph-captured CTMRG iteration (8 moves)")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="skip the replays of one CUDA-graph-captured CTMRG iteration")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the FP64-path timing and the one-move accuracy check")
+    ap.add_argument("--compare-moves", type=int, default=4,
+                    help="moves (one per direction) of the accuracy check")
     ap.add_argument("--cpu-moves", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-case", action="store_true",

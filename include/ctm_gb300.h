@@ -45,9 +45,20 @@ enum {
 /* Arithmetic of a projector computation. */
 enum {
   CTM_PREC_FP64 = 0,   /* every product in FP64: the drop-in path                     */
-  CTM_PREC_MIXED = 1,  /* tensor-core BF16 range finder, 3xBF16 products feeding the
-                          projectors, FP64 Rayleigh-Ritz SVD, truncation and scaling */
+  CTM_PREC_MIXED = 1,  /* tensor cores: BF16 range finder, 3xBF16 enlarged corners,
+                          Rayleigh-Ritz and projector products, FP32 Cholesky-QR and
+                          one-sided Jacobi SVD of the Rayleigh-Ritz matrix; FP64
+                          spectrum, truncation and s^-1/2 scaling (ctm_ctmrg_opts
+                          .mixed_flags selects higher precision per stage)          */
   CTM_PREC_BF16 = 2    /* ctm_matmul only: one BF16 tensor-core pass, FP32 accumulation */
+};
+
+/* Stage precision of CTM_PREC_MIXED (bits of ctm_ctmrg_opts.mixed_flags). */
+enum {
+  CTM_MIXED_RF3 = 1,    /* range-finder products in 3xBF16 (default: one BF16 pass) */
+  CTM_MIXED_SVD64 = 2,  /* SVD of the Rayleigh-Ritz matrix in FP64                  */
+  CTM_MIXED_Q64 = 8,    /* quarter tensors contracted in FP64, then split to BF16   */
+  CTM_MIXED_F32 = 16    /* FP64 quarter tensors, every product in FP32 SIMT         */
 };
 
 /* Projector construction (acetn/ipeps/ipeps_config.py:16-24 CTMRGConfig). */
@@ -78,6 +89,8 @@ typedef struct ctm_ctmrg_opts {
                            mixed_floor * s_0 are dropped as well (they are
                            below the resolution of the 3xBF16 products);
                            never less than 1e-8                            */
+  int32_t mixed_flags;  /* CTM_PREC_MIXED only: precision of its stages
+                           (CTM_MIXED_* bits, 0 = the defaults)          */
 } ctm_ctmrg_opts;
 
 /* Library version string and message of the last failure on this thread. */
@@ -113,6 +126,14 @@ int ctm_qr_fallbacks(unsigned long long* count, ctm_stream_t stream);
 void ctm_profile_begin(void);
 int ctm_profile_end(void);
 int ctm_profile_query(int tag, double* total_ms, double* total_work, long long* launches);
+/* Per-kernel table of the same profile: the number of kernel classes timed,
+ * and class i's name, work unit (0 = algorithmic FLOP, 1 = algorithmic
+ * bytes read + written), total milliseconds, total work and launch count.
+ * The name stays valid until the next ctm_profile_begin().  No counterpart
+ * in the reference. */
+int ctm_profile_kernel_count(int* count);
+int ctm_profile_kernel(int i, const char** name, int* unit, double* total_ms, double* total_work,
+                       long long* launches);
 
 /* Enlarged corner (quarter tensor) of one site in direction k, reshaped to a
  * (rows x cols) matrix, rows = (c, r, R), cols = (e, d, D), divided by its
@@ -234,8 +255,9 @@ int ctm_matmul(const double* A, const double* B, double* C, int64_t M, int64_t N
 
 /* C = A @ B (FP64 in and out, 3xBF16 tensor-core arithmetic as ctm_matmul
  * with CTM_PREC_MIXED) for callers that cannot allocate device memory: a
- * host that hands a plugin only its input and output buffers, or code that
- * runs while a global-mode stream capture forbids cudaMalloc.  No workspace:
+ * host that hands a plugin only its input and output buffers, or a host
+ * whose own memory pool has reserved the device, so that a cudaMalloc from
+ * the plugin fails or fragments that pool.  No workspace:
  * the scratch (BF16 operand copies, split-K partial sums) lives in a 32 MiB
  * file-scope device array that every GPU loading the library keeps until the
  * process exits; products needing more scratch (about M = N = K > 1000)

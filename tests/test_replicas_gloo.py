@@ -34,7 +34,9 @@ def _worker(rank, world, port, times, out):
 def test_replica_aggregation_takes_slowest_rank():
     world = 2
     times = [2.0, 3.0]
-    manager = mp.Manager()
+    # a spawned manager: forking a process that already runs threads (torch,
+    # the reference's import) can deadlock the child
+    manager = mp.get_context("spawn").Manager()
     out = manager.dict()
     mp.spawn(_worker, args=(world, _free_port(), times, out), nprocs=world, join=True)
     for rank in range(world):

@@ -2,8 +2,8 @@
 ABI, against the workspace-based ctm_matmul (CTM_PREC_MIXED).
 
 Callers that cannot allocate device memory (a plugin host that only passes
-input and output buffers, or code running under a global-mode stream
-capture) use this entry point; its scratch is a static device array shared
+input and output buffers, or one whose memory pool has reserved the device)
+use this entry point; its scratch is a static device array shared
 by all calls.  Two calls in a row must both match the existing entry point
 (same kernels, so the tolerance is the FP64 rounding of the final sum) and
 the FP64 product within the 3xBF16 tolerance of the other tensor-core tests.
