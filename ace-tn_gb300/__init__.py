@@ -1,8 +1,8 @@
 """GB300 (sm_103a) backend for the CTMRG hot path of Ace-TN.
 
-Import name: the directory is ``ace-tn_gb300``; import it with
-``importlib.import_module("ace-tn_gb300")`` (the repository's test and bench
-entry points also register the alias ``acetn_gb300``).
+Import name: ``acetn_gb300`` (``pip install .`` maps the source directory
+``ace-tn_gb300`` to it; in-tree, the repository's test and bench entry points
+import the directory and register the same alias).
 
 Drop-in replacements for the reference's CTMRG-path objects, operating on
 any iPEPS object with the reference's access pattern whose tensors are
@@ -13,6 +13,7 @@ float64 CUDA tensors:
     ProjectorCalculator(config)   acetn/renormalization/projectors.py
     RDM(ipeps), measure(...)      acetn/measurement/
     svd_lowrank, fused_*          acetn/linalg/
+    build_norm_tensor, absorb_bond  acetn/evolution/ (full_update.py, fast_full_update.py)
 
 All arithmetic runs in libctm_gb300.so; there is no CPU fallback.
 """
@@ -20,8 +21,9 @@ All arithmetic runs in libctm_gb300.so; there is no CPU fallback.
 from . import _abi
 from ._build import build
 from .config import CTMRGConfig
-from .ctmrg import ctmrg, sweep_order
+from .ctmrg import ctmrg, pair_order, sweep_order
 from .directional_mover import DirectionalMover
+from .full_update import absorb_bond, build_norm_tensor
 from .graph import CTMRGGraph
 from .linalg import (fused_3matmul_svd_lowrank, fused_matmul_svd_lowrank, matmul, qr, svd,
                      svd_lowrank)
@@ -31,7 +33,7 @@ from .projectors import ProjectorCalculator
 from .rdm import RDM
 from .state import Bond, IpepsState, random_state
 
-__all__ = ["build", "CTMRGConfig", "ctmrg", "sweep_order", "DirectionalMover",
+__all__ = ["build", "CTMRGConfig", "ctmrg", "sweep_order", "pair_order", "DirectionalMover",
            "ProjectorCalculator", "CTMRGGraph", "RDM", "measure", "svd_lowrank", "fused_matmul_svd_lowrank",
            "fused_3matmul_svd_lowrank", "qr", "svd", "matmul", "HeisenbergModel", "IsingModel",
-           "Bond", "IpepsState", "random_state"]
+           "Bond", "IpepsState", "random_state", "build_norm_tensor", "absorb_bond"]

@@ -69,6 +69,8 @@ _SIGNATURES = {
     "ctm_site_rdm": ([SITE_P, c_i64, c_i64, c_vp, c_vp, c_sz_p, c_vp], ctypes.c_int),
     "ctm_bond_rdm": ([SITE_P, SITE_P, c_i64, c_i64, c_i32, c_vp, c_vp, c_sz_p, c_vp],
                      ctypes.c_int),
+    "ctm_norm_tensor": ([SITE_P, SITE_P, c_i64, c_i64, c_i32, c_vp, c_vp, c_i64, c_vp, c_vp,
+                         c_sz_p, c_vp], ctypes.c_int),
     "ctm_svd_lowrank": ([c_vp, c_i64, c_i64, c_i64, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz_p,
                          c_vp], ctypes.c_int),
     "ctm_fused_matmul_svd_lowrank": ([c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_i32, c_vp, c_vp,
@@ -296,7 +298,7 @@ def opts_struct(config, chi, precision, fixed_width=False):
     if precision not in PREC:
         raise ValueError(f"Invalid precision: {precision} provided.")
     o.precision = PREC[precision]
-    o.mixed_floor = float(getattr(config, "mixed_svd_floor", 1e-6))
+    o.mixed_floor = float(getattr(config, "mixed_svd_floor", 1e-12))
     o.mixed_flags = int(getattr(config, "mixed_flags", 0))
     o.fixed_width = 1 if fixed_width else 0
     return o

@@ -9,9 +9,14 @@ documented in docs/source/input_settings.rst:45-54) and adds two fields:
                    products feeding the projectors (half-system rSVD only).
 * ``mixed_svd_floor`` -- mixed precision only: singular values below this
                    fraction of the largest are dropped in addition to
-                   ``svd_cutoff`` (the 3xBF16 Rayleigh-Ritz product resolves
-                   about 1e-5 of the largest); the library never keeps less
-                   than 1e-8 of the largest in mixed precision.
+                   ``svd_cutoff`` (default: the reference's cutoff 1e-12);
+                   the library never keeps singular values below 1e-8 of the
+                   largest in mixed precision, where the spectrum of the
+                   3xBF16 Rayleigh-Ritz product is rounding noise.
+* ``mixed_flags`` -- mixed precision only: CTM_MIXED_* bits of the C ABI
+                   selecting higher precision for single stages (3xBF16
+                   range finder, FP64 SVD, FP64 quarter tensors, FP32 SIMT
+                   products); 0 = the defaults.
 
 Any object with the reference's attribute names works as a config; missing
 attributes take the defaults below.
@@ -32,7 +37,7 @@ class CTMRGConfig:
     disable_progressbar: bool = False
     backend: Literal["gb300"] = "gb300"
     precision: Literal["fp64", "mixed"] = "fp64"
-    mixed_svd_floor: float = 1e-6
+    mixed_svd_floor: float = 1e-12
     mixed_flags: int = 0
 
 

@@ -564,6 +564,60 @@ void bond_rdm(Ctx& c, const Site& S1, const Site& S2, int k, double* out) {
          View(out, {d, d, d, d}));
 }
 
+// The full update's norm tensor: build_norm_tensor with
+// build_norm_tensor_core (acetn/evolution/full_update.py:163-236), the
+// environment of bond (s1, s2, k) -- the bond RDM's chain -- contracted with
+// the reduced site tensors a1q (r, d, u, y) and a2q (d, l, u, x) of width nD
+// into n12[y][x][Y][X].  Real tensors: the reference's conj() is the identity.
+void norm_tensor(Ctx& c, const Site& S1, const Site& S2, int k, const double* a1q,
+                 const double* a2q, int64_t nD, double* out) {
+  const int64_t D = S1.D;
+  const View c12 = S1.C(k + 1), e12 = S1.E(k + 1), e11 = S1.E(k), c13 = S1.C(k + 2),
+             e13 = S1.E(k + 2);
+  const View c21 = S2.C(k), e21 = S2.E(k), e24 = S2.E(k + 3), c24 = S2.C(k + 3),
+             e23 = S2.E(k + 2);
+  const View q1(a1q, {D, D, D, nD}), q2(a2q, {D, D, D, nD});
+  Scope scope(c);
+  // right half
+  const int64_t ra = c12.shape[0], rc = e12.shape[1], re = e11.shape[0];
+  double* t = c.alloc<double>(size_t(ra) * rc * D * D);
+  einsum(c, "ab,bcrR->acrR", c12, e12, View(t, {ra, rc, D, D}));
+  double* tt = c.alloc<double>(size_t(rc) * D * D * re * D * D);
+  einsum(c, "acrR,eauU->crReuU", View(t, {ra, rc, D, D}), e11, View(tt, {rc, D, D, re, D, D}));
+  double* t3 = c.alloc<double>(size_t(rc) * D * re * D * D * nD);
+  einsum(c, "crReuU,RDUY->creuDY", View(tt, {rc, D, D, re, D, D}), q1,
+         View(t3, {rc, D, re, D, D, nD}));
+  double* t4 = c.alloc<double>(size_t(rc) * re * D * nD * D * nD);
+  einsum(c, "creuDY,rduy->ceDYdy", View(t3, {rc, D, re, D, D, nD}), q1,
+         View(t4, {rc, re, D, nD, D, nD}));
+  const int64_t fa = c13.shape[0], ff = e13.shape[1];
+  double* n1a = c.alloc<double>(size_t(fa) * ff * D * D);
+  einsum(c, "ab,bfdD->afdD", c13, e13, View(n1a, {fa, ff, D, D}));
+  double* n1 = c.alloc<double>(size_t(ff) * re * nD * nD);
+  einsum(c, "afdD,aeDYdy->feYy", View(n1a, {fa, ff, D, D}), View(t4, {rc, re, D, nD, D, nD}),
+         View(n1, {ff, re, nD, nD}));
+  // left half
+  const int64_t la = c21.shape[0], lc = e21.shape[1], le = e24.shape[0];
+  double* u = c.alloc<double>(size_t(la) * lc * D * D);
+  einsum(c, "ab,bcuU->acuU", c21, e21, View(u, {la, lc, D, D}));
+  double* uu = c.alloc<double>(size_t(lc) * D * D * le * D * D);
+  einsum(c, "acuU,ealL->cuUelL", View(u, {la, lc, D, D}), e24, View(uu, {lc, D, D, le, D, D}));
+  double* u3 = c.alloc<double>(size_t(lc) * D * le * D * nD * D);
+  einsum(c, "cuUelL,DLUX->cuelXD", View(uu, {lc, D, D, le, D, D}), q2,
+         View(u3, {lc, D, le, D, nD, D}));
+  double* u4 = c.alloc<double>(size_t(lc) * le * nD * D * nD * D);
+  einsum(c, "cuelXD,dlux->ceXDxd", View(u3, {lc, D, le, D, nD, D}), q2,
+         View(u4, {lc, le, nD, D, nD, D}));
+  const int64_t bb = c24.shape[1], bf = e23.shape[0];
+  double* n2a = c.alloc<double>(size_t(bb) * bf * D * D);
+  einsum(c, "ab,fadD->bfdD", c24, e23, View(n2a, {bb, bf, D, D}));
+  double* n2 = c.alloc<double>(size_t(bf) * lc * nD * nD);
+  einsum(c, "bfdD,cbXDxd->fcXx", View(n2a, {bb, bf, D, D}), View(u4, {lc, le, nD, D, nD, D}),
+         View(n2, {bf, lc, nD, nD}));
+  einsum(c, "fcYy,fcXx->yxYX", View(n1, {ff, re, nD, nD}), View(n2, {bf, lc, nD, nD}),
+         View(out, {nD, nD, nD, nD}));
+}
+
 }  // namespace ctm
 
 // ====================================================================== C ABI
@@ -709,6 +763,21 @@ int ctm_bond_rdm(const ctm_site_f64* s1, const ctm_site_f64* s2, int64_t D, int6
     if (!c.sizing()) CTM_REQUIRE(rdm != nullptr, CTM_ERR_INVALID, "rdm is NULL");
     Site S1{s1, D, d}, S2{s2, D, d};
     bond_rdm(c, S1, S2, k, rdm);
+  });
+}
+
+int ctm_norm_tensor(const ctm_site_f64* s1, const ctm_site_f64* s2, int64_t D, int64_t d,
+                    int32_t k, const double* a1q, const double* a2q, int64_t nD, double* n12,
+                    void* ws, size_t* ws_bytes, ctm_stream_t stream) {
+  return with_workspace(ws, ws_bytes, as_stream(stream), [&](Ctx& c) {
+    check_site(s1, D, d);
+    check_site(s2, D, d);
+    CTM_REQUIRE(nD >= 1, CTM_ERR_INVALID, "nD must be >= 1");
+    if (!c.sizing())
+      CTM_REQUIRE(a1q != nullptr && a2q != nullptr && n12 != nullptr, CTM_ERR_INVALID,
+                  "a1q, a2q and n12 must not be NULL");
+    Site S1{s1, D, d}, S2{s2, D, d};
+    norm_tensor(c, S1, S2, k, a1q, a2q, nD, n12);
   });
 }
 

@@ -97,14 +97,36 @@ class DirectionalMover:
         return self.calculate_projectors(ipeps, self.down_sites(ipeps, xi, yi), k=3)
 
     # ---------------------------------------------------------------- moves
-    def _projectors_all(self, ipeps, site_lists, k):
-        a = ipeps[site_lists[0][0]]["A"]
+    def _spec(self, ipeps, k, idx):
+        """Site quadruples of every row (column) of move (k, idx) and the
+        (s1, s2, i, j) renormalization jobs (directional_mover.py:23-97)."""
+        nx, ny = ipeps.nx, ipeps.ny
+        if k == 0:
+            return (k, [self.left_sites(ipeps, idx, yi) for yi in range(ny)],
+                    [((idx, yi), ((idx + 1) % nx, yi), yi, (yi + 1) % ny) for yi in range(ny)])
+        if k == 1:
+            return (k, [self.up_sites(ipeps, xi, idx) for xi in range(nx)],
+                    [((xi, idx), (xi, (idx - 1 + ny) % ny), xi, (xi + 1) % nx)
+                     for xi in range(nx)])
+        if k == 2:
+            return (k, [self.right_sites(ipeps, idx, yi) for yi in range(ny)],
+                    [((idx, yi), ((idx - 1 + nx) % nx, yi), yi, (yi - 1 + ny) % ny)
+                     for yi in range(ny)])
+        return (k, [self.down_sites(ipeps, xi, idx) for xi in range(nx)],
+                [((xi, idx), (xi, (idx + 1) % ny), xi, (xi - 1 + nx) % nx) for xi in range(nx)])
+
+    def _projectors_all(self, ipeps, specs):
+        """Projector pairs of every row of every move in ``specs``, each on
+        its own side stream; one device-to-host read of the truncated widths
+        for all of them (none in graph mode)."""
+        rows = [(m, k, sites) for m, (k, site_lists, _) in enumerate(specs) for sites in site_lists]
+        a = ipeps[rows[0][2][0]]["A"]
         _abi.require_cuda(a, "A", storage=True)  # before any stream is forked
         device = a.device
-        slots = torch.zeros(len(site_lists), dtype=torch.int64, device=device)
-        streams = self._fork(device, len(site_lists))
+        slots = torch.zeros(len(rows), dtype=torch.int64, device=device)
+        streams = self._fork(device, len(rows))
         pend = []
-        for n, sites in enumerate(site_lists):
+        for n, (_, k, sites) in enumerate(rows):
             if streams is None:
                 pend.append(self.projector_calculator.launch(ipeps, sites, k, slots[n:n + 1],
                                                              fixed_width=self.graph_mode))
@@ -113,67 +135,86 @@ class DirectionalMover:
                 pend.append(self.projector_calculator.launch(ipeps, sites, k, slots[n:n + 1],
                                                              fixed_width=self.graph_mode))
         self._join(device, streams, [t for p in pend for t in (p.p1buf, p.p2buf)])
+        proj = [({}, {}) for _ in specs]
+        row_in_move = [0] * len(specs)
         if self.graph_mode:
             self.last_counts = slots
-            proj1, proj2 = {}, {}
-            for n, p in enumerate(pend):
-                proj1[n], proj2[n] = p.finish(p.cap)
-            return proj1, proj2
-        chis = slots.tolist()  # the move's one device-to-host read
-        proj1, proj2 = {}, {}
-        for n, (p, c) in enumerate(zip(pend, chis)):
+            widths = [p.cap for p in pend]
+        else:
+            widths = slots.tolist()  # the one device-to-host read
+        for (m, _, _), p, c in zip(rows, pend, widths):
             if c < 1:
                 raise RuntimeError("projector truncation left no singular value above the cutoff")
-            proj1[n], proj2[n] = p.finish(c)
-        return proj1, proj2
+            n = row_in_move[m]
+            proj[m][0][n], proj[m][1][n] = p.finish(c)
+            row_in_move[m] += 1
+        return proj
+
+    def _run(self, ipeps, specs):
+        proj = self._projectors_all(ipeps, specs)
+        self._renormalize_all(ipeps, [(proj[m][0], proj[m][1], job, k)
+                                      for m, (k, _, jobs) in enumerate(specs) for job in jobs])
 
     def left_move(self, ipeps, xi):
         """directional_mover.py:23-40."""
-        ny, nx = ipeps.ny, ipeps.nx
-        proj1, proj2 = self._projectors_all(
-            ipeps, [self.left_sites(ipeps, xi, yi) for yi in range(ny)], 0)
-        self._renormalize_all(ipeps, proj1, proj2,
-                              [((xi, yi), ((xi + 1) % nx, yi), yi, (yi + 1) % ny)
-                               for yi in range(ny)], 0)
+        self._run(ipeps, [self._spec(ipeps, 0, xi)])
 
     def up_move(self, ipeps, yi):
         """directional_mover.py:42-59."""
-        nx, ny = ipeps.nx, ipeps.ny
-        proj1, proj2 = self._projectors_all(
-            ipeps, [self.up_sites(ipeps, xi, yi) for xi in range(nx)], 1)
-        self._renormalize_all(ipeps, proj1, proj2,
-                              [((xi, yi), (xi, (yi - 1 + ny) % ny), xi, (xi + 1) % nx)
-                               for xi in range(nx)], 1)
+        self._run(ipeps, [self._spec(ipeps, 1, yi)])
 
     def right_move(self, ipeps, xi):
         """directional_mover.py:61-78."""
-        ny, nx = ipeps.ny, ipeps.nx
-        proj1, proj2 = self._projectors_all(
-            ipeps, [self.right_sites(ipeps, xi, yi) for yi in range(ny)], 2)
-        self._renormalize_all(ipeps, proj1, proj2,
-                              [((xi, yi), ((xi - 1 + nx) % nx, yi), yi, (yi - 1 + ny) % ny)
-                               for yi in range(ny)], 2)
+        self._run(ipeps, [self._spec(ipeps, 2, xi)])
 
     def down_move(self, ipeps, yi):
         """directional_mover.py:80-97."""
-        nx, ny = ipeps.nx, ipeps.ny
-        proj1, proj2 = self._projectors_all(
-            ipeps, [self.down_sites(ipeps, xi, yi) for xi in range(nx)], 3)
-        self._renormalize_all(ipeps, proj1, proj2,
-                              [((xi, yi), (xi, (yi + 1) % ny), xi, (xi - 1 + nx) % nx)
-                               for xi in range(nx)], 3)
+        self._run(ipeps, [self._spec(ipeps, 3, yi)])
 
     def move(self, ipeps, k, idx):
         return (self.left_move, self.up_move, self.right_move, self.down_move)[k](ipeps, idx)
 
+    def left_right_move(self, ipeps, x1, x2):
+        """The left move of column x1 and the right move of column x2 at once.
+        A left move reads C0, C3, E0, E2, E3 and writes C0, C3, E3; a right
+        move reads C1, C2, E0, E1, E2 and writes C1, C2, E1 (directional_mover.py
+        :273-366 with k = 0, 2): neither reads what the other writes, so the
+        result equals left_move(x1) followed by right_move(x2) bit for bit.
+        The reference runs the same pair on two groups of ranks
+        (left_right_move_dist, directional_mover.py:183-226); here the rows
+        of both moves run on side streams of one GPU."""
+        self._run(ipeps, [self._spec(ipeps, 0, x1), self._spec(ipeps, 2, x2)])
+
+    def up_down_move(self, ipeps, y1, y2):
+        """The up move of row y1 and the down move of row y2 at once (they
+        touch disjoint tensors as left and right do; the reference's
+        up_down_move_dist, directional_mover.py:228-271)."""
+        self._run(ipeps, [self._spec(ipeps, 1, y1), self._spec(ipeps, 3, y2)])
+
+    def moves_at_once(self, ipeps, moves):
+        """Runs data-independent moves [(k, idx), ...] together (all their
+        rows on side streams), drawing the rSVD test matrices in the listed
+        order: one left and one right move, or one up and one down move."""
+        kinds = sorted(k % 2 for k, _ in moves)
+        if len(moves) != 2 or kinds[0] != kinds[1] or moves[0][0] == moves[1][0]:
+            raise ValueError("moves_at_once takes a left/right or an up/down pair of moves")
+        self._run(ipeps, [self._spec(ipeps, k, idx) for k, idx in moves])
+
+    def move_pair(self, ipeps, k, idx1, idx2):
+        """left_right_move (k = 0) or up_down_move (k = 1)."""
+        if k == 0:
+            return self.left_right_move(ipeps, idx1, idx2)
+        return self.up_down_move(ipeps, idx1, idx2)
+
     # ---------------------------------------------------------------- renormalization
-    def _renormalize_all(self, ipeps, proj1, proj2, jobs, k):
-        """renormalize_boundary for every (s1, s2, i, j) of a move: each reads
-        site s1 and writes site s2, and no s2 of a move is an s1 of it."""
-        device = ipeps[jobs[0][0]]["A"].device
+    def _renormalize_all(self, ipeps, jobs):
+        """renormalize_boundary for every (proj1, proj2, (s1, s2, i, j), k):
+        each reads site s1 and writes site s2, no s2 of a move is an s1 of
+        it, and the moves of a pair write tensors the other does not read."""
+        device = ipeps[jobs[0][2][0]]["A"].device
         streams = self._fork(device, len(jobs))
         outs = []
-        for n, (s1, s2, i, j) in enumerate(jobs):
+        for n, (proj1, proj2, (s1, s2, i, j), k) in enumerate(jobs):
             if streams is None:
                 self.renormalize_boundary(ipeps, proj1, proj2, s1, s2, i, j, k)
                 continue

@@ -3,7 +3,8 @@
 Once the boundary dimension has saturated (every C/E at chi and every
 truncation keeping chi_cap singular values), the moves of an iteration have
 fixed shapes; ``CTMRGGraph`` captures the 2 (nx + ny) moves of one iteration
-of ``ctmrg`` (acetn/renormalization/ctmrg.py:18-31) into one CUDA graph and
+of ``ctmrg`` (acetn/renormalization/ctmrg.py:18-31), run as left/right and
+up/down pairs on side streams, into one CUDA graph and
 replays it, removing the host work and the per-move synchronisation of the
 eager path.  The projectors are written with a fixed width (zero columns
 beyond a truncation count smaller than chi), which leaves the physics
@@ -16,7 +17,7 @@ them after ``capture()`` and after every ``replay()``.
 import torch
 
 from .config import resolve
-from .ctmrg import sweep_order
+from .ctmrg import pair_order
 from .directional_mover import DirectionalMover
 
 
@@ -26,7 +27,7 @@ class CTMRGGraph:
         self.config = resolve(config)
         self.mover = DirectionalMover(self.config, omega_source)
         self.mover.graph_mode = True
-        self.order = sweep_order(ipeps.nx, ipeps.ny)
+        self.order = pair_order(ipeps.nx, ipeps.ny)
         self.graph = None
         self.static = None
         self.counts = []
@@ -41,8 +42,8 @@ class CTMRGGraph:
 
     def _iteration(self):
         counts = []
-        for k, idx in self.order:
-            self.mover.move(self.ipeps, k, idx)
+        for kind, i1, i2 in self.order:
+            self.mover.move_pair(self.ipeps, kind, i1, i2)
             counts.append(self.mover.last_counts)
         return counts
 

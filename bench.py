@@ -2,11 +2,14 @@
 cell, d=2, half-system rSVD projectors, oversampling 16, 2 power iterations).
 
 A step is one directional move (projectors of both rows/columns of the move,
-then the boundary renormalization of both).  The environment is first grown
-for 50 untimed CTMRG iterations (the iteration count of this workload), then
-W untimed moves, then K timed moves, each bracketed by CUDA events on the
-launching stream with an L2 flush (a 256 MiB write) between moves outside the
-events.
+then the boundary renormalization of both).  Moves run as the pairs of one
+CTMRG iteration (left with right, up with down: data-independent moves whose
+rows all run at once on side streams; the result equals the sequential order
+bit for bit), so K is rounded up to an even count.  The environment is first
+grown for 50 untimed CTMRG iterations (the iteration count of this
+workload), then W untimed moves, then K timed moves, each pair bracketed by
+CUDA events on the launching stream with an L2 flush (a 256 MiB write)
+between pairs outside the events.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
        [--precision fp64|mixed]
@@ -55,7 +58,7 @@ def move_flops(D, chi, q, d=2, ny=2, niter=2):
 
 class ClockSampler:
     """nvidia-smi clock / throttle-reason samples during the timed region:
-    sampled every 50 ms from before the region starts (start() waits for the
+    sampled every 20 ms from before the region starts (start() waits for the
     first sample), each sample stamped on arrival; stop() keeps the samples
     that arrived inside the window set by mark_start() / mark_end() (plus one
     sampling interval), or the nearest one when the region is shorter than
@@ -65,7 +68,7 @@ class ClockSampler:
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    INTERVAL_MS = 50
+    INTERVAL_MS = 20
 
     def __init__(self, index):
         self.index = index
@@ -180,20 +183,95 @@ def oracle_moves(st_np, moves, seed=1):
     return times
 
 
+REF_INSTALL = os.path.join(ROOT, "baseline", "_ref")
+
+
+def reference_modules():
+    """The reference itself (installed by pip into baseline/_ref, pure
+    Python), or None.  Its ``toml`` import (logging only) is served by a
+    stand-in on the standard library's ``tomllib``."""
+    if not os.path.isdir(os.path.join(REF_INSTALL, "acetn")):
+        return None
+    import tomllib
+    import types
+    if "toml" not in sys.modules:
+        mod = types.ModuleType("toml")
+        mod.load = lambda f: tomllib.load(open(f, "rb") if isinstance(f, str) else f)
+        mod.loads = tomllib.loads
+        mod.dumps = lambda d: repr(d) + "\n"
+        sys.modules["toml"] = mod
+    if REF_INSTALL not in sys.path:
+        sys.path.append(REF_INSTALL)
+    tn = importlib.import_module("acetn.ipeps.tensor_network")
+    cfgm = importlib.import_module("acetn.ipeps.ipeps_config")
+    dm = importlib.import_module("acetn.renormalization.directional_mover")
+    return tn, cfgm, dm
+
+
+def reference_network(mods, sites):
+    """A reference TensorNetwork on the CPU (float64) holding the given site
+    arrays {site: {"A", "C", "E"}} (the reference's site dictionary is
+    shared by all its networks; this one replaces its contents)."""
+    import numpy as np
+    import torch
+    tn, cfgm, _ = mods
+    net = tn.TensorNetwork(None, cfgm.TNConfig(nx=2, ny=2, dims={"phys": PHYS, "bond": D, "chi": CHI}),
+                           torch.float64, torch.device("cpu"))
+    for s, v in sites.items():
+        st = net[s]
+        st["A"] = torch.from_numpy(np.ascontiguousarray(v["A"]))
+        st["C"] = [torch.from_numpy(np.ascontiguousarray(c)) for c in v["C"]]
+        st["E"] = [torch.from_numpy(np.ascontiguousarray(e)) for e in v["E"]]
+    net.rank, net.is_distributed = 0, False
+    return net
+
+
+def reference_moves(mods, net, moves, start=0):
+    """Times ``moves`` directional moves of the reference's own CPU path
+    (DirectionalMover of acetn/renormalization/directional_mover.py, torch on
+    all host threads); returns seconds per move."""
+    import torch
+    _, cfgm, dm = mods
+    torch.set_num_threads(cpu_cores())
+    cfg = cfgm.CTMRGConfig(projectors="half-system", svd_type="rsvd",
+                           rsvd_oversampling=OVERSAMPLING, rsvd_niter=NITER, svd_cutoff=1e-12)
+    mover = dm.DirectionalMover(cfg)
+    order = [(0, 0), (2, 1), (0, 1), (2, 0), (1, 1), (3, 0), (1, 0), (3, 1)]
+    times = []
+    for i in range(moves):
+        k, idx = order[(start + i) % len(order)]
+        t0 = time.perf_counter()
+        (mover.left_move, mover.up_move, mover.right_move, mover.down_move)[k](net, idx)
+        times.append(time.perf_counter() - t0)
+    return times
+
+
 def run_reference(args, rank):
-    """--impl reference: the reference's CPU path restated by the oracle
-    (numpy/LAPACK on the host cores), same config, metric and unit."""
+    """--impl reference: the reference's own CPU path (its DirectionalMover
+    on torch CPU tensors, all host threads) when it is installed in
+    baseline/_ref, else the oracle's numpy restatement of it; same
+    workload, metric and unit."""
     if rank != 0:
         return None
     from oracle import ctm_oracle as orc
     st = orc.random_state(D, CHI, seed=SEED)
-    cfg = dict(projectors="half-system", svd_type="rsvd", rsvd_oversampling=OVERSAMPLING,
-               rsvd_niter=NITER, svd_cutoff=1e-12)
+    mods = reference_modules()
     t0 = time.perf_counter()
-    orc.ctmrg(st, cfg, orc.OmegaStream(SEED), steps=2)  # grow the environment to chi
-    grow_s = time.perf_counter() - t0
-    oracle_moves(st, args.warmup, seed=SEED + 1)
-    times = oracle_moves(st, args.steps, seed=SEED + 2)
+    if mods is not None:
+        net = reference_network(mods, st.sites)
+        reference_moves(mods, net, 16)  # two iterations: grow the environment to chi
+        grow_s = time.perf_counter() - t0
+        reference_moves(mods, net, args.warmup, start=0)
+        times = reference_moves(mods, net, args.steps, start=args.warmup)
+        kind = "reference"
+    else:
+        cfg = dict(projectors="half-system", svd_type="rsvd", rsvd_oversampling=OVERSAMPLING,
+                   rsvd_niter=NITER, svd_cutoff=1e-12)
+        orc.ctmrg(st, cfg, orc.OmegaStream(SEED), steps=2)  # grow the environment to chi
+        grow_s = time.perf_counter() - t0
+        oracle_moves(st, args.warmup, seed=SEED + 1)
+        times = oracle_moves(st, args.steps, seed=SEED + 2)
+        kind = "port"
     total = sum(times)
     value = args.steps / total
     q = CHI + OVERSAMPLING
@@ -203,11 +281,13 @@ def run_reference(args, rank):
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": dict(WORKLOAD),
-        "cpu_baseline": {"value": value, "unit": "moves/s", "cores": cpu_cores(), "kind": "port",
+        "cpu_baseline": {"value": value, "unit": "moves/s", "cores": cpu_cores(), "kind": kind,
                          "sample": f"{args.steps} moves after 2 growth iterations "
-                                   f"({grow_s:.1f} s; chi saturated, the per-move cost of the "
+                                   f"({grow_s:.1f} s; chi saturated: the per-move cost of the "
                                    f"{GROW_ITERS}-iteration state) and {args.warmup} warm-up moves",
-                         "cpu_model": cpu_model()},
+                         "cpu_model": cpu_model(),
+                         "code": ("the reference's DirectionalMover on torch CPU tensors"
+                                  if kind == "reference" else "the oracle (numpy restatement)")},
         "e2e": {"value": value, "unit": "moves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "tflops": move_flops(D, CHI, q) / (total / args.steps) / 1e12,
@@ -250,16 +330,24 @@ def run_gb300(args, rank, world, local_rank):
     order = gb.sweep_order(2, 2)
     t_grow = time.perf_counter()
     for _ in range(GROW_ITERS):
-        for k, idx in order:
-            grower.move(st, k, idx)
+        for kind, i1, i2 in gb.pair_order(2, 2):
+            grower.move_pair(st, kind, i1, i2)
     torch.cuda.synchronize(dev)
     t_grow = time.perf_counter() - t_grow
     mover = gb.DirectionalMover(cfg, omega_source=omega)
+    pairs = gb.pair_order(2, 2)
     pos = 0
-    for _ in range(args.warmup):
-        k, idx = order[pos % len(order)]
-        mover.move(st, k, idx)
+
+    def next_pair(mv, state):
+        nonlocal pos
+        kind, i1, i2 = pairs[pos % len(pairs)]
+        mv.move_pair(state, kind, i1, i2)
         pos += 1
+
+    for _ in range(max(1, -(-args.warmup // 2))):
+        next_pair(mover, st)
+    n_pairs = max(1, -(-args.steps // 2))
+    steps = 2 * n_pairs
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     torch.cuda.synchronize(dev)
     if world > 1:
@@ -268,16 +356,14 @@ def run_gb300(args, rank, world, local_rank):
     clocks.start()
     launches0 = gb._abi.kernel_launches()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
+          for _ in range(n_pairs)]
     torch.cuda.synchronize(dev)
     clocks.mark_start()
-    for i in range(args.steps):
+    for i in range(n_pairs):
         flush.zero_()
-        k, idx = order[pos % len(order)]
         ev[i][0].record(stream)
-        mover.move(st, k, idx)
+        next_pair(mover, st)
         ev[i][1].record(stream)
-        pos += 1
     torch.cuda.synchronize(dev)
     clocks.mark_end()
     launches = gb._abi.kernel_launches() - launches0
@@ -285,23 +371,22 @@ def run_gb300(args, rank, world, local_rank):
     clk = clocks.stop()
     ms = [a.elapsed_time(b) for a, b in ev]
     total_s = sum(ms) / 1e3
-    total_max, value = aggregate(total_s, args.steps, world, dev)
+    total_max, value = aggregate(total_s, steps, world, dev)
 
     # per-kernel timing (CUDA events inside the library) on a separate,
     # untimed pass with the rows of each move run one after the other, so
     # that no two kernels of the pass share the GPU
-    prof_moves = max(1, min(args.steps, 4))
+    prof_pairs = 2
+    prof_moves = 2 * prof_pairs
     mover.concurrent = False
     pev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(prof_moves)]
+           for _ in range(prof_pairs)]
     gb._abi.profile_begin()
-    for i in range(prof_moves):
+    for i in range(prof_pairs):
         flush.zero_()
-        k, idx = order[pos % len(order)]
         pev[i][0].record(stream)
-        mover.move(st, k, idx)
+        next_pair(mover, st)
         pev[i][1].record(stream)
-        pos += 1
     torch.cuda.synchronize(dev)
     prof = gb._abi.profile_end()
     kernels = gb._abi.profile_kernels()
@@ -314,7 +399,7 @@ def run_gb300(args, rank, world, local_rank):
         gst = clone_state(gb, st)
         graph = gb.CTMRGGraph(gst, cfg).capture(warmup=1)
         graph.replay(1)
-        replays = max(1, -(-args.steps // len(order)))
+        replays = max(1, -(-steps // len(order)))
         gev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                for _ in range(replays)]
         torch.cuda.synchronize(dev)
@@ -335,13 +420,12 @@ def run_gb300(args, rank, world, local_rank):
     host = {s: {"A": st[s]["A"].cpu().pin_memory(),
                 "C": [c.cpu().pin_memory() for c in st[s]["C"]],
                 "E": [e.cpu().pin_memory() for e in st[s]["E"]]} for s in st.site_list}
-    e2e_steps = max(1, min(args.steps, 4))
+    e2e_pairs = 2
+    e2e_steps = 2 * e2e_pairs
     h2d = d2h = 0
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
-    for i in range(e2e_steps):
-        k, idx = order[pos % len(order)]
-        pos += 1
+    for i in range(e2e_pairs):
         dst = gb.IpepsState(2, 2, st.dims, dev)
         for s in st.site_list:
             hs = host[s]
@@ -350,9 +434,9 @@ def run_gb300(args, rank, world, local_rank):
                       "E": [e.to(dev, non_blocking=True) for e in hs["E"]]}
         h2d = state_bytes(dst)
         before = {s: (list(dst[s]["C"]), list(dst[s]["E"])) for s in st.site_list}
-        mover.move(dst, k, idx)
-        # read back the step's result: the tensors the move replaced (two
-        # corners and one edge of each renormalised site), found by identity
+        next_pair(mover, dst)
+        # read back the step's result: the tensors the pair replaced (two
+        # corners and one edge per renormalised site and move), found by identity
         moved = 0
         for s in st.site_list:
             for key, old_list in zip(("C", "E"), before[s]):
@@ -385,8 +469,8 @@ def run_gb300(args, rank, world, local_rank):
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "moves/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * total_max / args.steps,
+            "steps": steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * total_max / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if args.precision == "fp64" else "bf16/3xbf16+f32+f64",
             "precision": args.precision,
@@ -394,7 +478,7 @@ def run_gb300(args, rank, world, local_rank):
             "config": dict(WORKLOAD),
             "l2": "256 MiB flush between timed moves; quarter tensors 215 MB each",
             "parallelism": f"replicas x{world}",
-            "tflops": move_flops(D, CHI, q) / (total_max / args.steps) / 1e12,
+            "tflops": move_flops(D, CHI, q) / (total_max / steps) / 1e12,
             "roofline": None if roof is None else {
                 "bound": roof["bound"], "kernel": roof["name"], "achieved": roof["achieved"],
                 "peak": roof["peak"], "unit": roof["achieved_unit"], "frac": roof["frac"],
@@ -408,10 +492,11 @@ def run_gb300(args, rank, world, local_rank):
                 "kernel": table[0]["name"], "share_of_step": table[0]["share"],
                 "bound": table[0]["bound"]},
             "kernels": table[:12],
-            "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+            "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": h2d / 2,
+                    "d2h_bytes_per_step": d2h / 2, "steps": e2e_steps,
+                    "note": "state copied host->device once per pair (two moves)"},
             "gpu_launches": int(launches),
-            "execution": "eager",
+            "execution": "eager, left/right and up/down pairs of moves",
             "graph": graph_line,
             "qr_fallbacks_in_timed_moves": qr_fallbacks,
             "grow_seconds": t_grow,
@@ -420,14 +505,19 @@ def run_gb300(args, rank, world, local_rank):
             "clocks": clk,
         }
         if world == 1 and not args.no_cpu_baseline:
-            from oracle import ctm_oracle as orc
-            ost = orc.OracleState(
-                {s: {"A": st[s]["A"].cpu().numpy(), "C": [c.cpu().numpy() for c in st[s]["C"]],
-                     "E": [e.cpu().numpy() for e in st[s]["E"]]} for s in st.site_list}, 2, 2, CHI)
-            times = oracle_moves(ost, args.cpu_moves)
+            arrays = {s: {"A": st[s]["A"].cpu().numpy(), "C": [c.cpu().numpy() for c in st[s]["C"]],
+                          "E": [e.cpu().numpy() for e in st[s]["E"]]} for s in st.site_list}
+            mods = reference_modules()
+            if mods is not None:
+                times = reference_moves(mods, reference_network(mods, arrays), args.cpu_moves)
+                kind, code = "reference", "the reference's DirectionalMover on torch CPU tensors"
+            else:
+                from oracle import ctm_oracle as orc
+                times = oracle_moves(orc.OracleState(arrays, 2, 2, CHI), args.cpu_moves)
+                kind, code = "port", "the oracle (numpy restatement)"
             line["cpu_baseline"] = {"value": len(times) / sum(times), "unit": "moves/s",
-                                    "cores": cpu_cores(), "kind": "port",
-                                    "sample": f"{len(times)} oracle moves from the GPU run's "
+                                    "cores": cpu_cores(), "kind": kind, "code": code,
+                                    "sample": f"{len(times)} moves from the GPU run's "
                                               f"{GROW_ITERS}-iteration chi={CHI} state",
                                     "cpu_model": cpu_model()}
     return line

@@ -195,6 +195,16 @@ int ctm_site_rdm(const ctm_site_f64* site, int64_t D, int64_t d, double* rdm,
 int ctm_bond_rdm(const ctm_site_f64* s1, const ctm_site_f64* s2, int64_t D, int64_t d,
                  int32_t k, double* rdm, void* ws, size_t* ws_bytes, ctm_stream_t stream);
 
+/* Norm tensor of the full update for bond (s1, s2, k): the bond's environment
+ * contracted with the reduced site tensors a1q (r, d, u, y) and a2q
+ * (d, l, u, x), both (D, D, D, nD) contiguous, into n12 (nD, nD, nD, nD)
+ * indexed [y][x][Y][X] (FP64).
+ * Reference: build_norm_tensor / build_norm_tensor_core,
+ * acetn/evolution/full_update.py:163-236. */
+int ctm_norm_tensor(const ctm_site_f64* s1, const ctm_site_f64* s2, int64_t D, int64_t d,
+                    int32_t k, const double* a1q, const double* a2q, int64_t nD, double* n12,
+                    void* ws, size_t* ws_bytes, ctm_stream_t stream);
+
 /* Randomized SVD of a (m x n), of a @ b (a: m x k, b: k x n), or of
  * a @ b @ c @ e (shapes chained); omega (n x q) supplied by the caller.
  * Writes U (m x q), S (q), V (n x q) with a @ ... ~= U diag(S) V^T.

@@ -1,6 +1,8 @@
 """CUDA-graph capture of a CTMRG iteration (CTMRGGraph) against the eager
 fixed-width path: with the same test matrices, replays must reproduce the
-eager iterations exactly (same kernels, deterministic reductions)."""
+eager iterations exactly (same kernels, deterministic reductions).  The
+left/right and up/down pairs of moves run at once must equal the reference's
+sequential order bit for bit."""
 
 import pytest
 import torch
@@ -50,6 +52,27 @@ def test_graph_replay_matches_eager(precision):
     e1 = float(gb.measure(graphed, gb.HeisenbergModel(1.0), verbose=False)["Energy"])
     e2 = float(gb.measure(eager, gb.HeisenbergModel(1.0), verbose=False)["Energy"])
     assert e1 == e2
+
+
+def omega_stream(seed):
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    return lambda n, q, dev: torch.randn(n, q, dtype=torch.float64, device=dev, generator=g)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_pairs_of_moves_equal_sequential_moves(precision):
+    cfg = gb.CTMRGConfig(precision=precision, rsvd_oversampling=4, steps=3,
+                         disable_progressbar=True)
+    st = gb.random_state(3, 9, 5, device="cuda")
+    a, b = clone(st), clone(st)
+    gb.ctmrg(a, cfg, omega_source=omega_stream(11), pairs=True)
+    gb.ctmrg(b, cfg, omega_source=omega_stream(11), pairs=False)
+    torch.cuda.synchronize()
+    for s in st.site_list:
+        for k in range(4):
+            assert torch.equal(a[s]["C"][k], b[s]["C"][k])
+            assert torch.equal(a[s]["E"][k], b[s]["E"][k])
 
 
 def test_graph_capture_requires_saturated_environment():
