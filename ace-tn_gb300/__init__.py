@@ -23,6 +23,7 @@ from ._build import build
 from .config import CTMRGConfig
 from .ctmrg import ctmrg, pair_order, sweep_order
 from .directional_mover import DirectionalMover
+from .batched import BatchedCTMRG
 from .full_update import absorb_bond, build_norm_tensor
 from .graph import CTMRGGraph
 from .linalg import (fused_3matmul_svd_lowrank, fused_matmul_svd_lowrank, matmul, qr, svd,
@@ -34,6 +35,6 @@ from .rdm import RDM
 from .state import Bond, IpepsState, random_state
 
 __all__ = ["build", "CTMRGConfig", "ctmrg", "sweep_order", "pair_order", "DirectionalMover",
-           "ProjectorCalculator", "CTMRGGraph", "RDM", "measure", "svd_lowrank", "fused_matmul_svd_lowrank",
+           "ProjectorCalculator", "CTMRGGraph", "BatchedCTMRG", "RDM", "measure", "svd_lowrank", "fused_matmul_svd_lowrank",
            "fused_3matmul_svd_lowrank", "qr", "svd", "matmul", "HeisenbergModel", "IsingModel",
            "Bond", "IpepsState", "random_state", "build_norm_tensor", "absorb_bond"]

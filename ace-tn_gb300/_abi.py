@@ -44,6 +44,7 @@ _SIGNATURES = {
     "ctm_version": ([], ctypes.c_char_p),
     "ctm_last_error": ([], ctypes.c_char_p),
     "ctm_device_status": ([ctypes.POINTER(ctypes.c_int), c_vp], ctypes.c_int),
+    "ctm_set_mixed_contraction": ([c_i32, ctypes.POINTER(c_i32)], ctypes.c_int),
     "ctm_kernel_launches": ([], ctypes.c_ulonglong),
     "ctm_qr_fallbacks": ([ctypes.POINTER(ctypes.c_ulonglong), c_vp], ctypes.c_int),
     "ctm_profile_begin": ([], None),
@@ -66,8 +67,8 @@ _SIGNATURES = {
     "ctm_renormalize_boundary": ([SITE_P, c_i64, c_i64, c_i32, c_vp, c_i64, c_vp, c_i64, c_vp,
                                   c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_sz_p,
                                   c_vp], ctypes.c_int),
-    "ctm_site_rdm": ([SITE_P, c_i64, c_i64, c_vp, c_vp, c_sz_p, c_vp], ctypes.c_int),
-    "ctm_bond_rdm": ([SITE_P, SITE_P, c_i64, c_i64, c_i32, c_vp, c_vp, c_sz_p, c_vp],
+    "ctm_site_rdm": ([SITE_P, c_i64, c_i64, c_i32, c_vp, c_vp, c_sz_p, c_vp], ctypes.c_int),
+    "ctm_bond_rdm": ([SITE_P, SITE_P, c_i64, c_i64, c_i32, c_i32, c_vp, c_vp, c_sz_p, c_vp],
                      ctypes.c_int),
     "ctm_norm_tensor": ([SITE_P, SITE_P, c_i64, c_i64, c_i32, c_vp, c_vp, c_i64, c_vp, c_vp,
                          c_sz_p, c_vp], ctypes.c_int),
@@ -232,6 +233,20 @@ def qr_fallbacks(device=None):
     return int(n.value)
 
 
+CONTRACTION_FORMS = {"auto": 0, "double-layer": 1, "one-layer": 2}
+
+
+def set_mixed_contraction(form):
+    """Selects how the mixed path contracts the site tensors ("auto",
+    "double-layer" or "one-layer"); returns the previous setting."""
+    if form not in CONTRACTION_FORMS:
+        raise ValueError(f"Invalid contraction form: {form} provided.")
+    prev = c_i32(0)
+    check(load().ctm_set_mixed_contraction(CONTRACTION_FORMS[form], ctypes.byref(prev)),
+          "ctm_set_mixed_contraction")
+    return {v: k for k, v in CONTRACTION_FORMS.items()}[prev.value]
+
+
 def kernel_launches():
     return int(load().ctm_kernel_launches())
 
@@ -298,7 +313,7 @@ def opts_struct(config, chi, precision, fixed_width=False):
     if precision not in PREC:
         raise ValueError(f"Invalid precision: {precision} provided.")
     o.precision = PREC[precision]
-    o.mixed_floor = float(getattr(config, "mixed_svd_floor", 1e-12))
+    o.mixed_floor = float(getattr(config, "mixed_svd_floor", 1e-6))
     o.mixed_flags = int(getattr(config, "mixed_flags", 0))
     o.fixed_width = 1 if fixed_width else 0
     return o

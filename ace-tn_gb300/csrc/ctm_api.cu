@@ -471,47 +471,84 @@ void renormalize_boundary(Ctx& c, const Site& S, int k, const double* P1i, int64
 }
 
 // ------------------------------------------------------------------ RDMs
-// RDM.build_site_rdm (acetn/measurement/rdm.py:35-67).
-void site_rdm(Ctx& c, const Site& S, double* out) {
-  const int64_t D = S.D, d = S.d;
-  const View c1 = S.C(0), c2 = S.C(1), c3 = S.C(2), c4 = S.C(3);
-  const View e1 = S.E(0), e2 = S.E(1), e3 = S.E(2), e4 = S.E(3);
-  const View a1 = S.A(0);
+namespace {
+
+// The site RDM chain of RDM.build_site_rdm on views of element type T
+// (FP64 or FP32 GETT).
+template <class T>
+void site_rdm_chain(Ctx& c, const ViewT<T>& c1, const ViewT<T>& c2, const ViewT<T>& c3,
+                    const ViewT<T>& c4, const ViewT<T>& e1, const ViewT<T>& e2,
+                    const ViewT<T>& e3, const ViewT<T>& e4, const ViewT<T>& a1, int64_t D,
+                    int64_t d, T* out) {
+  using V = ViewT<T>;
   Scope scope(c);
   // tmp1 = einsum("ab,bclL->aclL", c4, e4)
   const int64_t A4 = c4.shape[0], C4 = e4.shape[1];
-  double* t1a = c.alloc<double>(size_t(A4) * C4 * D * D);
-  einsum(c, "ab,bclL->aclL", c4, e4, View(t1a, {A4, C4, D, D}));
+  T* t1a = c.alloc<T>(size_t(A4) * C4 * D * D);
+  einsum(c, "ab,bclL->aclL", c4, e4, V(t1a, {A4, C4, D, D}));
   // einsum("aclL,eadD->clLedD", tmp1, e3)
   const int64_t E3 = e3.shape[0];
-  double* t1b = c.alloc<double>(size_t(C4) * D * D * E3 * D * D);
-  einsum(c, "aclL,eadD->clLedD", View(t1a, {A4, C4, D, D}), e3, View(t1b, {C4, D, D, E3, D, D}));
+  T* t1b = c.alloc<T>(size_t(C4) * D * D * E3 * D * D);
+  einsum(c, "aclL,eadD->clLedD", V(t1a, {A4, C4, D, D}), e3, V(t1b, {C4, D, D, E3, D, D}));
   // einsum("clLedD,LURDP->cledURP", tmp1, conj(a1))
-  double* t1c = c.alloc<double>(size_t(C4) * D * E3 * D * D * D * d);
-  einsum(c, "clLedD,LURDP->cledURP", View(t1b, {C4, D, D, E3, D, D}), a1,
-         View(t1c, {C4, D, E3, D, D, D, d}));
+  T* t1c = c.alloc<T>(size_t(C4) * D * E3 * D * D * D * d);
+  einsum(c, "clLedD,LURDP->cledURP", V(t1b, {C4, D, D, E3, D, D}), a1,
+         V(t1c, {C4, D, E3, D, D, D, d}));
   // tmp2 = einsum("ab,bcuU->acuU", c1, e1)
   const int64_t A1 = c1.shape[0], C1 = e1.shape[1];
-  double* t2 = c.alloc<double>(size_t(A1) * C1 * D * D);
-  einsum(c, "ab,bcuU->acuU", c1, e1, View(t2, {A1, C1, D, D}));
+  T* t2 = c.alloc<T>(size_t(A1) * C1 * D * D);
+  einsum(c, "ab,bcuU->acuU", c1, e1, V(t2, {A1, C1, D, D}));
   // tmp3 = einsum("ab,carR->bcrR", c3, e2)
   const int64_t B3 = c3.shape[1], CE2 = e2.shape[0];
-  double* t3a = c.alloc<double>(size_t(B3) * CE2 * D * D);
-  einsum(c, "ab,carR->bcrR", c3, e2, View(t3a, {B3, CE2, D, D}));
+  T* t3a = c.alloc<T>(size_t(B3) * CE2 * D * D);
+  einsum(c, "ab,carR->bcrR", c3, e2, V(t3a, {B3, CE2, D, D}));
   // tmp3 = einsum("ec,bcrR->ebrR", c2, tmp3)
   const int64_t E2r = c2.shape[0];
-  double* t3b = c.alloc<double>(size_t(E2r) * B3 * D * D);
-  einsum(c, "ec,bcrR->ebrR", c2, View(t3a, {B3, CE2, D, D}), View(t3b, {E2r, B3, D, D}));
+  T* t3b = c.alloc<T>(size_t(E2r) * B3 * D * D);
+  einsum(c, "ec,bcrR->ebrR", c2, V(t3a, {B3, CE2, D, D}), V(t3b, {E2r, B3, D, D}));
   // tmp3 = einsum("ebrR,aeuU->brRauU", tmp3, tmp2)
-  double* t3c = c.alloc<double>(size_t(B3) * D * D * A1 * D * D);
-  einsum(c, "ebrR,aeuU->brRauU", View(t3b, {E2r, B3, D, D}), View(t2, {A1, C1, D, D}),
-         View(t3c, {B3, D, D, A1, D, D}));
+  T* t3c = c.alloc<T>(size_t(B3) * D * D * A1 * D * D);
+  einsum(c, "ebrR,aeuU->brRauU", V(t3b, {E2r, B3, D, D}), V(t2, {A1, C1, D, D}),
+         V(t3c, {B3, D, D, A1, D, D}));
   // tmp3 = einsum("erRcuU,cledURP->ruldP", tmp3, tmp1)
-  double* t3d = c.alloc<double>(size_t(D) * D * D * D * d);
-  einsum(c, "erRcuU,cledURP->ruldP", View(t3c, {B3, D, D, A1, D, D}),
-         View(t1c, {C4, D, E3, D, D, D, d}), View(t3d, {D, D, D, D, d}));
+  T* t3d = c.alloc<T>(size_t(D) * D * D * D * d);
+  einsum(c, "erRcuU,cledURP->ruldP", V(t3c, {B3, D, D, A1, D, D}),
+         V(t1c, {C4, D, E3, D, D, D, d}), V(t3d, {D, D, D, D, d}));
   // rdm = einsum("ruldP,lurdp->Pp", tmp3, a1)
-  einsum(c, "ruldP,lurdp->Pp", View(t3d, {D, D, D, D, d}), a1, View(out, {d, d}));
+  einsum(c, "ruldP,lurdp->Pp", V(t3d, {D, D, D, D, d}), a1, V(out, {d, d}));
+}
+
+// FP32 copy of an FP64 view: the whole underlying tensor is converted and
+// the view's shape and strides are kept (a bond_permute view stays a view).
+ViewF f32_copy(Ctx& c, const View& v) {
+  int64_t n = 1;
+  for (int i = 0; i < v.nd; ++i) n += (v.shape[i] - 1) * v.stride[i];
+  float* p = c.alloc<float>(size_t(n));
+  to_f32(c, v.p, p, n);
+  ViewF out;
+  out.p = p;
+  out.nd = v.nd;
+  for (int i = 0; i < v.nd; ++i) out.shape[i] = v.shape[i], out.stride[i] = v.stride[i];
+  return out;
+}
+
+}  // namespace
+
+// RDM.build_site_rdm (acetn/measurement/rdm.py:35-67).  CTM_PREC_MIXED runs
+// the same chain with FP32 FMAs and FP32 accumulation (FP64 result).
+void site_rdm(Ctx& c, const Site& S, double* out, int precision) {
+  const int64_t D = S.D, d = S.d;
+  if (precision == CTM_PREC_FP64) {
+    site_rdm_chain<double>(c, S.C(0), S.C(1), S.C(2), S.C(3), S.E(0), S.E(1), S.E(2), S.E(3),
+                           S.A(0), D, d, out);
+    return;
+  }
+  Scope scope(c);
+  float* o = c.alloc<float>(size_t(d) * d);
+  site_rdm_chain<float>(c, f32_copy(c, S.C(0)), f32_copy(c, S.C(1)), f32_copy(c, S.C(2)),
+                        f32_copy(c, S.C(3)), f32_copy(c, S.E(0)), f32_copy(c, S.E(1)),
+                        f32_copy(c, S.E(2)), f32_copy(c, S.E(3)), f32_copy(c, S.A(0)), D, d, o);
+  to_f64(c, o, out, d * d);
 }
 
 // RDM.build_bond_rdm (acetn/measurement/rdm.py:69-99) with the unblocked core
@@ -633,6 +670,13 @@ const char* ctm_version(void) { return "ctm_gb300 0.1 (sm_103a)"; }
 
 const char* ctm_last_error(void) { return ctm::g_last_error_cstr(); }
 
+int ctm_set_mixed_contraction(int32_t form, int32_t* previous) {
+  return guarded([&] {
+    const int old = set_contraction_form(form);
+    if (previous != nullptr) *previous = old;
+  });
+}
+
 unsigned long long ctm_kernel_launches(void) { return g_launches.load(); }
 
 int ctm_qr_fallbacks(unsigned long long* count, ctm_stream_t stream) {
@@ -745,24 +789,31 @@ int ctm_renormalize_boundary(const ctm_site_f64* s1, int64_t D, int64_t d, int32
   });
 }
 
-int ctm_site_rdm(const ctm_site_f64* site, int64_t D, int64_t d, double* rdm, void* ws,
-                 size_t* ws_bytes, ctm_stream_t stream) {
+int ctm_site_rdm(const ctm_site_f64* site, int64_t D, int64_t d, int32_t precision, double* rdm,
+                 void* ws, size_t* ws_bytes, ctm_stream_t stream) {
   return with_workspace(ws, ws_bytes, as_stream(stream), [&](Ctx& c) {
     check_site(site, D, d);
+    CTM_REQUIRE(precision == CTM_PREC_FP64 || precision == CTM_PREC_MIXED, CTM_ERR_INVALID,
+                "bad precision");
     if (!c.sizing()) CTM_REQUIRE(rdm != nullptr, CTM_ERR_INVALID, "rdm is NULL");
     Site S{site, D, d};
-    site_rdm(c, S, rdm);
+    site_rdm(c, S, rdm, precision);
   });
 }
 
 int ctm_bond_rdm(const ctm_site_f64* s1, const ctm_site_f64* s2, int64_t D, int64_t d, int32_t k,
-                 double* rdm, void* ws, size_t* ws_bytes, ctm_stream_t stream) {
+                 int32_t precision, double* rdm, void* ws, size_t* ws_bytes, ctm_stream_t stream) {
   return with_workspace(ws, ws_bytes, as_stream(stream), [&](Ctx& c) {
     check_site(s1, D, d);
     check_site(s2, D, d);
+    CTM_REQUIRE(precision == CTM_PREC_FP64 || precision == CTM_PREC_MIXED, CTM_ERR_INVALID,
+                "bad precision");
     if (!c.sizing()) CTM_REQUIRE(rdm != nullptr, CTM_ERR_INVALID, "rdm is NULL");
     Site S1{s1, D, d}, S2{s2, D, d};
-    bond_rdm(c, S1, S2, k, rdm);
+    if (precision == CTM_PREC_MIXED)
+      bond_rdm_mixed(c, S1, S2, k, rdm);
+    else
+      bond_rdm(c, S1, S2, k, rdm);
   });
 }
 

@@ -83,6 +83,12 @@ void quarter_tensor_mixed_f64(Ctx& c, const Site& S, int k, double* Q);
 // renormalize_ej on tensor cores (3xBF16), FP64 output normalised in FP64.
 void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64_t Y,
                           const double* P1j, int64_t X, double* Eout);
+// Form of the site-tensor steps of the mixed path (0 automatic, 1 double
+// layer, 2 one layer); returns the previous setting.
+int set_contraction_form(int form);
+// RDM.build_bond_rdm on tensor cores (3xBF16 contractions, FP64 halves and
+// final contraction).
+void bond_rdm_mixed(Ctx& c, const Site& S1, const Site& S2, int k, double* out);
 // Half-system rSVD projectors with tensor-core arithmetic (CTM_PREC_MIXED).
 void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg_opts& o,
                                 const double* omega, double* P1, double* P2, int64_t* chi_new);

@@ -92,34 +92,133 @@ DLOp double_layer(Ctx& c, const View& ak, int64_t D, int64_t d) {
   return o;
 }
 
-// make_quarter_tensor (acetn/renormalization/projectors.py:35-60) on tensor
-// cores, 3xBF16 throughout.  The four einsums become
-//   t1 = C E_k (FP32, the small chi^3 D^2 step),
-//   X[(c,e)][(l,L,u,U)] = sum_a t1[a][(c,u,U)] E_{k+3}[e][a][l][L]      (K = chi),
-//   Q[(c,r,R)][(e,d,D)] = sum_(l,L,u,U) DL[(r,R,d,D)][(l,L,u,U)] X    (K = D^4),
-// with the double-layer matrix DL of the site tensor (the two A / A* steps
-// of the reference in one GEMM with a long K).  Each epilogue stores into the
-// layout the next step reads, with the GEMM rows (one per epilogue lane) on
-// the index that is contiguous in that layout; Q^T comes from a tiled
-// transpose, and max|Q| from the last epilogue.
-QOps quarter_mixed(Ctx& c, const Site& S, int k, bool fp64 = false) {
+// The two site-tensor steps of the enlarged corner and of the edge
+// renormalization run either as one GEMM against the double-layer matrix
+// (K = D^4: few, long products; D^8 entries) or as the reference's two
+// one-layer steps (K = D^2 and D^2 d: the algorithmic FLOP count, larger
+// intermediates).  0: double layer up to D = 6, one layer from D = 8;
+// 1: always the double layer; 2: always one layer.
+int g_contraction_form = 0;
+
+bool one_layer_for(int64_t D) {
+  return g_contraction_form == 2 || (g_contraction_form == 0 && D >= 8);
+}
+
+// Site-tensor operands of the one-layer steps (A = S.A(k), legs l u r d p):
+//   bra[(R,D,P)][(L,U)] = A[L][U][R][D][P]   (K = D^2, leading dimension ldb)
+//   ket[(r,d)][(p,l,u)] = A[l][u][r][d][p]   (K = D^2 d, leading dimension ldk)
+__global__ void site_operands_kernel(const double* A, int64_t s0, int64_t s1, int64_t s2,
+                                     int64_t s3, int64_t s4, int D, int d, bf16* bh, bf16* bl,
+                                     int64_t ldb, bf16* kh, bf16* kl, int64_t ldk) {
+  const int64_t D2 = int64_t(D) * D, nb = D2 * d * D2;
+  for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < 2 * nb;
+       idx += int64_t(gridDim.x) * blockDim.x) {
+    double v;
+    bf16 *h, *l;
+    int64_t off;
+    if (idx < nb) {
+      const int64_t n = idx / D2, k = idx - n * D2;
+      const int P = int(n % d), Dd = int((n / d) % D), R = int(n / (int64_t(d) * D));
+      const int U = int(k % D), L = int(k / D);
+      v = A[L * s0 + U * s1 + R * s2 + Dd * s3 + P * s4];
+      h = bh;
+      l = bl;
+      off = n * ldb + k;
+    } else {
+      const int64_t i = idx - nb, n = i / (D2 * d), k = i - n * (D2 * d);
+      const int dd = int(n % D), r = int(n / D);
+      const int u = int(k % D), lg = int((k / D) % D), p = int(k / D2);
+      v = A[lg * s0 + u * s1 + r * s2 + dd * s3 + p * s4];
+      h = kh;
+      l = kl;
+      off = n * ldk + k;
+    }
+    const bf16 hv = __double2bfloat16(v);
+    h[off] = hv;
+    l[off] = __double2bfloat16(v - double(__bfloat162float(hv)));
+  }
+}
+
+// The one-layer form of the two site-tensor steps (3xBF16):
+//   T1[(i,j,R,D)][(p,l,u)] = sum_(L,U) X[(i,j,l,u)][(L,U)] A*[L,U,R,D,P]
+//   out[(i,j,R,D)][(r,d)]  = sum_(p,l,u) T1 A[l,u,r,d,p]
+// X has rows (i,j,l,u) (i, j the two boundary indices) and K = (L,U) padded
+// to ldx; outB gives the layout of the result (rows (i,j,R,D), columns
+// (r,d)); with want_absmax, *absmax receives max |result|.
+void one_layer_steps(Ctx& c, const View& ak, int64_t D, int64_t d, int64_t ni, int64_t nj,
+                     const bf16* xh, const bf16* xl, int64_t ldx, TcOut outB, bool want_absmax,
+                     double* absmax, const char* step_a, const char* step_b) {
+  const int64_t D2 = D * D, Kb = D2 * d, ldb = tc_ld(D2), ldt = tc_ld(Kb);
+  const int64_t rows = ni * nj * D2;
+  const TcMode x3 = TcMode::kBf16x3;
+  Scope scope(c);
+  bf16* bh = c.alloc<bf16>(size_t(Kb) * ldb);
+  bf16* bl = c.alloc<bf16>(size_t(Kb) * ldb);
+  bf16* kh = c.alloc<bf16>(size_t(D2) * ldt);
+  bf16* kl = c.alloc<bf16>(size_t(D2) * ldt);
+  if (!c.sizing()) {
+    KernelTimer kt(c.stream, "site_operands_kernel", kUnitByte, 2.0 * 4.0 * double(Kb) * D2);
+    site_operands_kernel<<<grid_for(2 * Kb * D2, 256), 256, 0, c.stream>>>(
+        ak.p, ak.stride[0], ak.stride[1], ak.stride[2], ak.stride[3], ak.stride[4], int(D),
+        int(d), bh, bl, ldb, kh, kl, ldt);
+    CTM_LAUNCH_CHECK();
+  }
+  bf16* th = c.alloc<bf16>(size_t(rows) * ldt);
+  bf16* tl = c.alloc<bf16>(size_t(rows) * ldt);
+  {
+    TcLayout l;  // rows (i,j,l,u) of X; columns (R,D,P) of bra
+    l.nm = 4;
+    l.me[0] = ni; l.ms[0] = nj * D2 * ldt;
+    l.me[1] = nj; l.ms[1] = D2 * ldt;
+    l.me[2] = D;  l.ms[2] = D;
+    l.me[3] = D;  l.ms[3] = 1;
+    l.nn = 3;
+    l.ne[0] = D; l.ns[0] = D * ldt;
+    l.ne[1] = D; l.ns[1] = ldt;
+    l.ne[2] = d; l.ns[2] = D2;
+    TcOut out;
+    out.add(TcKind::kBf16Hi, th, l).add(TcKind::kBf16Lo, tl, l);
+    out.name = step_a;
+    tc_gemm(c, TcOperand{xh, xl, rows, D2, ldx}, TcOperand{bh, bl, Kb, D2, ldb}, x3, out);
+  }
+  outB.name = step_b;
+  outB.algo_flops = 2.0 * double(rows) * D2 * Kb;
+  if (want_absmax)
+    tc_gemm_absmax(c, TcOperand{th, tl, rows, Kb, ldt}, TcOperand{kh, kl, D2, Kb, ldt}, x3, outB,
+                   absmax);
+  else
+    tc_gemm(c, TcOperand{th, tl, rows, Kb, ldt}, TcOperand{kh, kl, D2, Kb, ldt}, x3, outB);
+}
+
+// X[(c,e)][(l,L,u,U)] = sum_a (C_k E_k)[a][(c,u,U)] E_{k+3}[e][a][l][L]: the
+// boundary part of the enlarged corner of direction k (the first two einsums
+// of make_quarter_tensor, acetn/renormalization/projectors.py:52-53), as a
+// K-major BF16 hi/lo operand (K = (l,L,u,U) = D^4).  t1 = C E_k in FP32, then
+// a K = chi tensor-core GEMM whose epilogue writes X.  For the one-layer
+// steps (one_layer) the same values are laid out as X[(c,e,l,u)][(L,U)]
+// with K = D^2 padded to 64.
+struct XOp {
+  bf16 *hi = nullptr, *lo = nullptr;
+  int64_t rows = 0, k = 0, ld = 0, cc = 0, e = 0;
+};
+
+XOp x_operand(Ctx& c, const Site& S, int k, const char* name = "enlarged corner, edge step",
+               bool one_layer = false) {
   int64_t sh[6], rows, cols;
   quarter_dims(S, k, rows, cols, sh);
-  QOps o = alloc_ops(c, rows, cols);
-  if (fp64) {
-    // contracted in FP64 (already divided by max|Q|), then split
-    Scope s0(c);
-    double* Qd = c.alloc<double>(size_t(rows) * cols);
-    int64_t qs[6];
-    quarter_tensor(c, S, k, Qd, qs);
-    split_bf16(c, Qd, rows, cols, cols, false, o.q_hi, o.q_lo, o.ld);
-    fill(c, o.scale, 1, 1.0);
-    transpose_bf16(c, o.q_hi, o.q_lo, rows, cols, o.ld, o.t_hi, o.t_lo, o.ldt);
-    return o;
-  }
-  const View ak = S.A(k), ck = S.C(k), ek1 = S.E(3 + k), ek2 = S.E(k);
-  const int64_t a = ck.shape[0], cc = sh[0], E = sh[3], D = S.D, d = S.d, D2 = D * D;
+  const View ck = S.C(k), ek1 = S.E(3 + k), ek2 = S.E(k);
+  const int64_t a = ck.shape[0], cc = sh[0], E = sh[3], D = S.D, D2 = D * D;
   const TcMode x3 = TcMode::kBf16x3;
+  XOp x;
+  x.cc = cc;
+  x.e = E;
+  x.rows = one_layer ? cc * E * D2 : cc * E;
+  x.k = one_layer ? D2 : D2 * D2;
+  x.ld = tc_ld(x.k);
+  x.hi = c.alloc<bf16>(size_t(x.rows) * x.ld);
+  x.lo = c.alloc<bf16>(size_t(x.rows) * x.ld);
+  bf16 *xh = x.hi, *xl = x.lo;
+  const int64_t ldx = x.ld;
   Scope scope(c);
   // t1 = C E_k (a x (c,u,U)), FP32
   float* t1 = c.alloc<float>(size_t(a) * cc * D2);
@@ -153,24 +252,77 @@ QOps quarter_mixed(Ctx& c, const Site& S, int k, bool fp64 = false) {
   // in X: aligned groups of 4 (D^2 % 4 == 0) go out as one 8-byte store
   // (with rows (c,u,U) every element was a separate 2-byte store and this
   // K = chi GEMM ran at a few per cent of the tensor pipe)
-  const int64_t K2 = D2 * D2, ldx = tc_ld(K2);
-  bf16* xh = c.alloc<bf16>(size_t(cc) * E * ldx);
-  bf16* xl = c.alloc<bf16>(size_t(cc) * E * ldx);
   {
     TcLayout l;
     l.nm = 3;
-    l.me[0] = E; l.ms[0] = ldx;
-    l.me[1] = D; l.ms[1] = D * D2;
-    l.me[2] = D; l.ms[2] = D2;
     l.nn = 3;
-    l.ne[0] = cc; l.ns[0] = E * ldx;
-    l.ne[1] = D;  l.ns[1] = D;
-    l.ne[2] = D;  l.ns[2] = 1;
+    l.me[0] = E;  l.me[1] = D; l.me[2] = D;
+    l.ne[0] = cc; l.ne[1] = D; l.ne[2] = D;
+    if (one_layer) {  // X[((c E + e) D + l) D + u][L D + U]
+      l.ms[0] = D2 * ldx; l.ms[1] = D * ldx; l.ms[2] = D;
+      l.ns[0] = E * D2 * ldx; l.ns[1] = ldx; l.ns[2] = 1;
+    } else {          // X[c E + e][((l D + L) D + u) D + U]
+      l.ms[0] = ldx; l.ms[1] = D * D2; l.ms[2] = D2;
+      l.ns[0] = E * ldx; l.ns[1] = D; l.ns[2] = 1;
+    }
     TcOut out;
     out.add(TcKind::kBf16Hi, xh, l).add(TcKind::kBf16Lo, xl, l);
-    out.name = "enlarged corner, edge step";
+    out.name = name;
     tc_gemm(c, TcOperand{eh, el, E * D2, a, ld2}, TcOperand{th, tl, cc * D2, a, ld2}, x3, out);
   }
+  return x;
+}
+
+// make_quarter_tensor (acetn/renormalization/projectors.py:35-60) on tensor
+// cores, 3xBF16 throughout.  The four einsums become
+//   t1 = C E_k (FP32, the small chi^3 D^2 step),
+//   X[(c,e)][(l,L,u,U)] = sum_a t1[a][(c,u,U)] E_{k+3}[e][a][l][L]      (K = chi),
+//   Q[(c,r,R)][(e,d,D)] = sum_(l,L,u,U) DL[(r,R,d,D)][(l,L,u,U)] X    (K = D^4),
+// with the double-layer matrix DL of the site tensor (the two A / A* steps
+// of the reference in one GEMM with a long K).  Each epilogue stores into the
+// layout the next step reads, with the GEMM rows (one per epilogue lane) on
+// the index that is contiguous in that layout; Q^T comes from a tiled
+// transpose, and max|Q| from the last epilogue.
+QOps quarter_mixed(Ctx& c, const Site& S, int k, bool fp64 = false) {
+  int64_t sh[6], rows, cols;
+  quarter_dims(S, k, rows, cols, sh);
+  QOps o = alloc_ops(c, rows, cols);
+  if (fp64) {
+    // contracted in FP64 (already divided by max|Q|), then split
+    Scope s0(c);
+    double* Qd = c.alloc<double>(size_t(rows) * cols);
+    int64_t qs[6];
+    quarter_tensor(c, S, k, Qd, qs);
+    split_bf16(c, Qd, rows, cols, cols, false, o.q_hi, o.q_lo, o.ld);
+    fill(c, o.scale, 1, 1.0);
+    transpose_bf16(c, o.q_hi, o.q_lo, rows, cols, o.ld, o.t_hi, o.t_lo, o.ldt);
+    return o;
+  }
+  const View ak = S.A(k);
+  const int64_t cc = sh[0], E = sh[3], D = S.D, d = S.d, D2 = D * D;
+  const TcMode x3 = TcMode::kBf16x3;
+  Scope scope(c);
+  if (one_layer_for(D)) {
+    const XOp x = x_operand(c, S, k, "enlarged corner, edge step", true);
+    TcLayout lq;  // Q[(c,r,R)][(e,d,D)] from rows (c,e,R,D), columns (r,d)
+    lq.nm = 4;
+    lq.me[0] = cc; lq.ms[0] = D2 * o.ld;
+    lq.me[1] = E;  lq.ms[1] = D2;
+    lq.me[2] = D;  lq.ms[2] = o.ld;
+    lq.me[3] = D;  lq.ms[3] = 1;
+    lq.nn = 2;
+    lq.ne[0] = D; lq.ns[0] = D * o.ld;
+    lq.ne[1] = D; lq.ns[1] = D;
+    TcOut out;
+    out.add(TcKind::kBf16Hi, o.q_hi, lq).add(TcKind::kBf16Lo, o.q_lo, lq);
+    one_layer_steps(c, ak, D, d, cc, E, x.hi, x.lo, x.ld, out, true, o.scale,
+                    "enlarged corner, bra step", "enlarged corner, ket step");
+    transpose_bf16(c, o.q_hi, o.q_lo, rows, cols, o.ld, o.t_hi, o.t_lo, o.ldt);
+    return o;
+  }
+  const XOp x = x_operand(c, S, k);
+  const bf16 *xh = x.hi, *xl = x.lo;
+  const int64_t K2 = x.k, ldx = x.ld;
   // GEMM 2 against the double-layer matrix -> Q[(c,r,R)][(e,d,D)] and max|Q|;
   // rows (c,e) from X, columns (r,R,d,D) from DL: consecutive columns are
   // consecutive (d,D) in Q, stored 4 at a time, and N = D^4 = 1296 splits
@@ -281,6 +433,46 @@ void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64
     g.ke[0] = B; g.ks[0] = D2 * X;
     gather_split_bf16(c, P1j, g, b1h, b1l, ld1);
   }
+  const int64_t K4 = Aa * D2;
+  const int64_t ld4 = tc_ld(K4);
+  bf16* t3h = c.alloc<bf16>(size_t(X) * D2 * ld4);
+  bf16* t3l = c.alloc<bf16>(size_t(X) * D2 * ld4);
+  if (one_layer_for(D)) {
+    // G1 -> X[(a,x,l,u)][(L,U)] (K = D^2 padded), then the one-layer steps
+    // -> T[(x,r,R)][(a,d,D)]
+    const int64_t ldk = tc_ld(D2);
+    bf16* xh = c.alloc<bf16>(size_t(Aa) * X * D2 * ldk);
+    bf16* xl = c.alloc<bf16>(size_t(Aa) * X * D2 * ldk);
+    {
+      TcLayout l;
+      l.nm = 3;
+      l.me[0] = Aa; l.ms[0] = X * D2 * ldk;
+      l.me[1] = D;  l.ms[1] = D * ldk;
+      l.me[2] = D;  l.ms[2] = D;
+      l.nn = 3;
+      l.ne[0] = X; l.ns[0] = D2 * ldk;
+      l.ne[1] = D; l.ns[1] = ldk;
+      l.ne[2] = D; l.ns[2] = 1;
+      TcOut out;
+      out.add(TcKind::kBf16Hi, xh, l).add(TcKind::kBf16Lo, xl, l);
+      out.name = "edge renormalization, projector step";
+      tc_gemm(c, TcOperand{a1h, a1l, Aa * D2, B, ld1}, TcOperand{b1h, b1l, X * D2, B, ld1}, x3,
+              out);
+    }
+    TcLayout l;  // T from rows (a,x,R,D), columns (r,d)
+    l.nm = 4;
+    l.me[0] = Aa; l.ms[0] = D2;
+    l.me[1] = X;  l.ms[1] = D2 * ld4;
+    l.me[2] = D;  l.ms[2] = ld4;
+    l.me[3] = D;  l.ms[3] = 1;
+    l.nn = 2;
+    l.ne[0] = D; l.ns[0] = D * ld4;
+    l.ne[1] = D; l.ns[1] = D;
+    TcOut out;
+    out.add(TcKind::kBf16Hi, t3h, l).add(TcKind::kBf16Lo, t3l, l);
+    one_layer_steps(c, ak, D, d, Aa, X, xh, xl, ldk, out, false, nullptr,
+                    "edge renormalization, bra step", "edge renormalization, ket step");
+  } else {
   // G1 -> X[(a,x)][(l,L,u,U)]; rows (a,l,L) from E, columns (x,u,U) from
   // P1: consecutive columns are consecutive (u,U), stored 4 at a time (as in
   // quarter_mixed's GEMM 1)
@@ -303,10 +495,6 @@ void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64
   }
   // G2 -> T[(x,r,R)][(a,d,D)]
   const DLOp dl = double_layer(c, ak, D, d);
-  const int64_t K4 = Aa * D2;
-  const int64_t ld4 = tc_ld(K4);
-  bf16* t3h = c.alloc<bf16>(size_t(X) * D2 * ld4);
-  bf16* t3l = c.alloc<bf16>(size_t(X) * D2 * ld4);
   {
     TcLayout l;  // rows (a,x) from X, columns (r,R,d,D) from DL (as in quarter_mixed)
     l.nm = 2;
@@ -324,6 +512,7 @@ void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64
     // the reference's two one-layer site-tensor steps (directional_mover.py:363-364)
     out.algo_flops = 4.0 * double(Aa) * X * D2 * D2 * D2 * d;
     tc_gemm(c, TcOperand{xh, xl, Aa * X, K2, ldx}, dl.op(), x3, out);
+  }
   }
   // G3: B4[y][(a,d,D)] = P2[a][d][D][y]
   bf16* b4h = c.alloc<bf16>(size_t(Y) * ld4);
@@ -352,6 +541,169 @@ void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64
   double* nrm = c.alloc<double>(1);
   sumsq(c, Eout, Y * X * D2, nrm);
   divide_by(c, Eout, Y * X * D2, nrm, 1);
+}
+
+namespace {
+
+// Double-layer matrix of one half of a bond RDM with the physical legs and
+// the two legs leaving the half open (the site tensor A = S.A(k), legs
+// l=0, u=1, r=2, d=3, p=4; ket lowercase, bra uppercase):
+//   DLo[(Bo,Bp,Ko,Kp,Kd,Bd)][(K1,B1,K2,B2)] = A[ket] A[bra]
+// where legs g1, g2 are contracted with the half's boundary operand X and
+// leg o (toward the other site) and d stay open.  No sum: every entry is
+// one product.
+__global__ void double_layer_open_kernel(const double* A, int64_t s0, int64_t s1, int64_t s2,
+                                         int64_t s3, int64_t s4, int D, int d, int g1, int g2,
+                                         int o, bf16* hi, bf16* lo, int64_t ld) {
+  const int64_t D4 = int64_t(D) * D * D * D, N = D4 * d * d;
+  const int64_t st[5] = {s0, s1, s2, s3, s4};
+  for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < N * D4;
+       idx += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t row = idx / D4, k = idx - row * D4;
+    const int B2 = int(k % D), K2 = int((k / D) % D), B1 = int((k / (D * D)) % D),
+              K1 = int(k / (D * D * D));
+    int64_t n = row;
+    const int Bd = int(n % D);
+    n /= D;
+    const int Kd = int(n % D);
+    n /= D;
+    const int Kp = int(n % d);
+    n /= d;
+    const int Ko = int(n % D);
+    n /= D;
+    const int Bp = int(n % d);
+    const int Bo = int(n / d);
+    const int64_t ket = K1 * st[g1] + K2 * st[g2] + Ko * st[o] + Kd * st[3] + Kp * st[4];
+    const int64_t bra = B1 * st[g1] + B2 * st[g2] + Bo * st[o] + Bd * st[3] + Bp * st[4];
+    const double v = A[ket] * A[bra];
+    const bf16 h = __double2bfloat16(v);
+    hi[row * ld + k] = h;
+    lo[row * ld + k] = __double2bfloat16(v - double(__bfloat162float(h)));
+  }
+}
+
+// One half of build_bond_rdm_core (acetn/measurement/rdm.py:102-120) on
+// tensor cores, r[f][(x,Bo,Bp,Ko,Kp)] in FP64:
+//   X = the boundary operand of the quarter of direction kq
+//       (rows (c,e), K = the contracted leg pairs g1, g2),
+//   Y = X DLo^T                                       (K = D^4, 3xBF16),
+//   r = Rb Y, contracted over (t, Kd, Bd)              (K = chi D^2, 3xBF16),
+// where t is c (contract_first) or e, x the other one, and Rb the corner
+// times edge that closes the half (Rb[t][f][d][D], FP32).
+void bond_rdm_half(Ctx& c, const Site& S, int kq, const View& ak, int g1, int g2, int o,
+                   const float* rb, int64_t F, bool contract_first, double* r) {
+  const int64_t D = S.D, d = S.d, D2 = D * D, D4 = D2 * D2;
+  const TcMode x3 = TcMode::kBf16x3;
+  Scope scope(c);
+  const XOp x = x_operand(c, S, kq, "bond RDM, edge step");
+  const int64_t T = contract_first ? x.cc : x.e, Xn = contract_first ? x.e : x.cc;
+  const int64_t N = D4 * d * d, ldo = tc_ld(D4);
+  bf16* oh = c.alloc<bf16>(size_t(N) * ldo);
+  bf16* ol = c.alloc<bf16>(size_t(N) * ldo);
+  if (!c.sizing()) {
+    KernelTimer kt(c.stream, "double_layer_open_kernel", kUnitByte, 4.0 * double(N) * D4);
+    double_layer_open_kernel<<<grid_for(N * D4, 256), 256, 0, c.stream>>>(
+        ak.p, ak.stride[0], ak.stride[1], ak.stride[2], ak.stride[3], ak.stride[4], int(D),
+        int(d), g1, g2, o, oh, ol, ldo);
+    CTM_LAUNCH_CHECK();
+  }
+  // Y stored K-major for the closing GEMM: rows (x,Bo,Bp,Ko,Kp), K (t,Kd,Bd)
+  const int64_t K3 = T * D2, ld3 = tc_ld(K3), rows3 = Xn * D2 * d * d;
+  bf16* yh = c.alloc<bf16>(size_t(rows3) * ld3);
+  bf16* yl = c.alloc<bf16>(size_t(rows3) * ld3);
+  {
+    TcLayout l;
+    const int64_t xs = D * d * D * d * ld3;  // stride of x in Y's rows
+    l.nm = 2;
+    l.me[0] = x.cc; l.ms[0] = contract_first ? D2 : xs;
+    l.me[1] = x.e;  l.ms[1] = contract_first ? xs : D2;
+    l.nn = 6;
+    l.ne[0] = D; l.ns[0] = d * D * d * ld3;  // Bo
+    l.ne[1] = d; l.ns[1] = D * d * ld3;      // Bp
+    l.ne[2] = D; l.ns[2] = d * ld3;          // Ko
+    l.ne[3] = d; l.ns[3] = ld3;              // Kp
+    l.ne[4] = D; l.ns[4] = D;                // Kd
+    l.ne[5] = D; l.ns[5] = 1;                // Bd
+    TcOut out;
+    out.add(TcKind::kBf16Hi, yh, l).add(TcKind::kBf16Lo, yl, l);
+    out.name = "bond RDM, double-layer step";
+    // the reference's two one-layer site-tensor steps (rdm.py:106-107)
+    out.algo_flops = 2.0 * double(x.cc) * x.e * D4 * D2 * d * (1 + d);
+    tc_gemm(c, TcOperand{x.hi, x.lo, x.rows, D4, x.ld}, TcOperand{oh, ol, N, D4, ldo}, x3, out);
+  }
+  // Rb as the A operand: [f][(t,d,D)] from rb[t][f][d][D]
+  bf16* bh = c.alloc<bf16>(size_t(F) * ld3);
+  bf16* bl = c.alloc<bf16>(size_t(F) * ld3);
+  {
+    Gather g;
+    g.nr = 1;
+    g.re[0] = F; g.rs[0] = D2;
+    g.nk = 2;
+    g.ke[0] = T;  g.ks[0] = F * D2;
+    g.ke[1] = D2; g.ks[1] = 1;
+    gather_split_bf16(c, rb, g, bh, bl, ld3);
+  }
+  TcOut out;
+  out.add(TcKind::kF64, r, TcLayout::rows(F, rows3, rows3));
+  out.name = "bond RDM, closing step";
+  tc_gemm(c, TcOperand{bh, bl, F, K3, ld3}, TcOperand{yh, yl, rows3, K3, ld3}, x3, out);
+}
+
+ViewF f32_view(Ctx& c, const View& v) {
+  CTM_REQUIRE(v.contiguous(), CTM_ERR_INVALID, "f32_view: expects a contiguous view");
+  float* p = c.alloc<float>(size_t(v.numel()));
+  to_f32(c, v.p, p, v.numel());
+  ViewF out;
+  out.p = p;
+  out.nd = v.nd;
+  for (int i = 0; i < v.nd; ++i) out.shape[i] = v.shape[i], out.stride[i] = v.stride[i];
+  return out;
+}
+
+}  // namespace
+
+// RDM.build_bond_rdm (acetn/measurement/rdm.py:69-99) with the contraction
+// of build_bond_rdm_core (rdm.py:102-120) on tensor cores.  Right half: the
+// boundary operand of site s1's quarter of direction k+1 (C12 E12 E11; its K
+// legs are u and r of A(k)), the open double layer of A(k) with leg l toward
+// s2, closed by C13 E13 over (c, d, D).  Left half: site s2's quarter
+// operand of direction k (C21 E21 E24; K legs l and u), leg r open, closed
+// by C24 E23 over (e, d, D).  Both halves come out in FP64 and the last
+// contraction over (f, c, bond legs) is an FP64 GETT.
+void bond_rdm_mixed(Ctx& c, const Site& S1, const Site& S2, int k, double* out) {
+  const int64_t D = S1.D, d = S1.d;
+  Scope scope(c);
+  const View c13 = S1.C(k + 2), e13 = S1.E(k + 2), c24 = S2.C(k + 3), e23 = S2.E(k + 2);
+  // closing tensors (FP32): r1a[a][f][d][D] = C13 E13, r2a[e][f][d][D] = C24^T E23
+  const int64_t fa = c13.shape[0], ff = e13.shape[1];
+  float* r1a = c.alloc<float>(size_t(fa) * ff * D * D);
+  const int64_t ea = c24.shape[1], ef = e23.shape[0];
+  float* r2a = c.alloc<float>(size_t(ea) * ef * D * D);
+  {
+    Scope s2(c);
+    einsum(c, "ab,bfdD->afdD", f32_view(c, c13), f32_view(c, e13), ViewF(r1a, {fa, ff, D, D}));
+    einsum(c, "ae,fadD->efdD", f32_view(c, c24), f32_view(c, e23), ViewF(r2a, {ea, ef, D, D}));
+  }
+  int64_t sh1[6], sh2[6], rr, cq;
+  quarter_dims(S1, k + 1, rr, cq, sh1);
+  quarter_dims(S2, k, rr, cq, sh2);
+  CTM_REQUIRE(sh1[0] == fa && sh2[3] == ea, CTM_ERR_INVALID,
+              "bond RDM: closing corner and edge do not chain with the halves");
+  const int64_t e1 = sh1[3], c2 = sh2[0];  // the legs that stay open in each half
+  double* r1 = c.alloc<double>(size_t(ff) * e1 * D * d * D * d);
+  double* r2 = c.alloc<double>(size_t(ef) * c2 * D * d * D * d);
+  const View a1 = S1.A(k), a2 = S2.A(k);
+  bond_rdm_half(c, S1, k + 1, a1, 1, 2, 0, r1a, ff, true, r1);
+  bond_rdm_half(c, S2, k, a2, 0, 1, 2, r2a, ef, false, r2);
+  einsum(c, "fcRPrp,fcRQrq->PQpq", View(r1, {ff, e1, D, d, D, d}), View(r2, {ef, c2, D, d, D, d}),
+         View(out, {d, d, d, d}));
+}
+
+int set_contraction_form(int form) {
+  CTM_REQUIRE(form >= 0 && form <= 2, CTM_ERR_INVALID, "contraction form must be 0, 1 or 2");
+  const int old = g_contraction_form;
+  g_contraction_form = form;
+  return old;
 }
 
 void quarter_tensor_mixed_f64(Ctx& c, const Site& S, int k, double* Q) {

@@ -946,7 +946,8 @@ void split_bf16(Ctx& c, const float* src, int64_t rows, int64_t cols, int64_t ld
 
 namespace {
 
-__global__ void gather_split_kernel(const double* src, const Gather g, int64_t rows, int64_t K,
+template <class S>
+__global__ void gather_split_kernel(const S* src, const Gather g, int64_t rows, int64_t K,
                                     bf16* hi, bf16* lo, int64_t ld) {
   const int64_t total = rows * K;
   for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < total;
@@ -962,7 +963,7 @@ __global__ void gather_split_kernel(const double* src, const Gather g, int64_t r
       off += (k % g.ke[j]) * g.ks[j];
       k /= g.ke[j];
     }
-    const double x = src[off];
+    const double x = double(src[off]);
     const bf16 h = __double2bfloat16(x);
     hi[r0 * ld + k0] = h;
     if (lo != nullptr) lo[r0 * ld + k0] = __double2bfloat16(x - double(__bfloat162float(h)));
@@ -1033,15 +1034,25 @@ void join_bf16(Ctx& c, const bf16* hi, const bf16* lo, int64_t rows, int64_t col
   CTM_LAUNCH_CHECK();
 }
 
-void gather_split_bf16(Ctx& c, const double* src, const Gather& g, bf16* hi, bf16* lo, int64_t ld) {
+template <class S>
+void gather_split_impl(Ctx& c, const S* src, const Gather& g, bf16* hi, bf16* lo, int64_t ld) {
   int64_t rows = 1, K = 1;
   for (int j = 0; j < g.nr; ++j) rows *= g.re[j];
   for (int j = 0; j < g.nk; ++j) K *= g.ke[j];
   if (c.sizing() || rows * K == 0) return;
   KernelTimer kt(c.stream, "gather_split_kernel", kUnitByte,
-                 double(rows) * K * (8.0 + (lo != nullptr ? 4.0 : 2.0)));
-  gather_split_kernel<<<grid_for(rows * K, 256), 256, 0, c.stream>>>(src, g, rows, K, hi, lo, ld);
+                 double(rows) * K * (sizeof(S) + (lo != nullptr ? 4.0 : 2.0)));
+  gather_split_kernel<S><<<grid_for(rows * K, 256), 256, 0, c.stream>>>(src, g, rows, K, hi, lo,
+                                                                       ld);
   CTM_LAUNCH_CHECK();
+}
+
+void gather_split_bf16(Ctx& c, const double* src, const Gather& g, bf16* hi, bf16* lo, int64_t ld) {
+  gather_split_impl<double>(c, src, g, hi, lo, ld);
+}
+
+void gather_split_bf16(Ctx& c, const float* src, const Gather& g, bf16* hi, bf16* lo, int64_t ld) {
+  gather_split_impl<float>(c, src, g, hi, lo, ld);
 }
 
 namespace {

@@ -24,11 +24,13 @@ struct TcOperand {
 };
 
 // Output layout: offset(m, n) = sum_j i_j(m) * ms[j] + sum_j i_j(n) * ns[j]
-// where m and n are decoded mixed-radix over (me[0..nm), last fastest).
+// where m and n are decoded mixed-radix over (me[0..nm), last fastest);
+// up to six modes each.
+constexpr int kTcModes = 6;
 struct TcLayout {
   int nm = 1, nn = 1;
-  int64_t me[4] = {1, 1, 1, 1}, ms[4] = {0, 0, 0, 0};
-  int64_t ne[4] = {1, 1, 1, 1}, ns[4] = {0, 0, 0, 0};
+  int64_t me[kTcModes] = {1, 1, 1, 1, 1, 1}, ms[kTcModes] = {0, 0, 0, 0, 0, 0};
+  int64_t ne[kTcModes] = {1, 1, 1, 1, 1, 1}, ns[kTcModes] = {0, 0, 0, 0, 0, 0};
   static TcLayout rows(int64_t M, int64_t N, int64_t ld) {  // C[m][n] at m*ld + n
     TcLayout l;
     l.me[0] = M; l.ms[0] = ld; l.ne[0] = N; l.ns[0] = 1;
@@ -96,6 +98,8 @@ struct Gather {
   int64_t ke[4] = {1, 1, 1, 1}, ks[4] = {0, 0, 0, 0};
 };
 void gather_split_bf16(Ctx& c, const double* src, const Gather& g, bf16* hi, bf16* lo,
+                       int64_t ld);
+void gather_split_bf16(Ctx& c, const float* src, const Gather& g, bf16* hi, bf16* lo,
                        int64_t ld);
 
 // src (rows x cols FP64, leading dimension ld_src) -> hi/lo BF16 split; with

@@ -17,9 +17,11 @@ def _mat(op):
     return op.mat if hasattr(op, "mat") else op
 
 
-def measure(ipeps, model, verbose=True):
+def measure(ipeps, model, verbose=True, precision="fp64"):
+    """``precision="mixed"`` builds the RDMs on tensor cores (bond) and in
+    FP32 (site); the normalisations and operator contractions stay FP64."""
     out = {"Energy": 0.0}
-    rdm = RDM(ipeps)
+    rdm = RDM(ipeps, precision)
     site_list, bond_list = ipeps.site_list, ipeps.bond_list
     dim = model.dim
     one_keys = list(model.one_site_observables((0, 0)).keys())

@@ -13,8 +13,14 @@ from .state import Bond
 
 
 class RDM:
-    def __init__(self, ipeps):
+    """``precision``: "fp64" (the drop-in) or "mixed" (bond RDMs on tensor
+    cores in 3xBF16, site RDMs in FP32; FP64 results)."""
+
+    def __init__(self, ipeps, precision="fp64"):
         self.ipeps = ipeps
+        if precision not in ("fp64", "mixed"):
+            raise ValueError(f"Invalid precision: {precision} provided.")
+        self.precision = precision
 
     def __getitem__(self, key):
         if isinstance(key, Bond) or hasattr(key, "k"):
@@ -28,8 +34,9 @@ class RDM:
             raise KeyError(site)
         ref = _abi.SiteRef(st)
         out = torch.empty(ref.d, ref.d, dtype=torch.float64, device=ref.device)
-        _abi.call("ctm_site_rdm", [ref.pointer, ref.D, ref.d, _abi.ptr(out)], ref.device,
-                  key=("site_rdm", ref.shapes()))
+        _abi.call("ctm_site_rdm", [ref.pointer, ref.D, ref.d, _abi.PREC[self.precision],
+                                   _abi.ptr(out)], ref.device,
+                  key=("site_rdm", ref.shapes(), self.precision))
         return out
 
     def build_bond_rdm(self, bond):
@@ -39,6 +46,7 @@ class RDM:
         r2 = _abi.SiteRef(self.ipeps[s2])
         d = r1.d
         out = torch.empty(d, d, d, d, dtype=torch.float64, device=r1.device)
-        _abi.call("ctm_bond_rdm", [r1.pointer, r2.pointer, r1.D, d, k, _abi.ptr(out)], r1.device,
-                  key=("bond_rdm", r1.shapes(), r2.shapes(), k))
+        _abi.call("ctm_bond_rdm", [r1.pointer, r2.pointer, r1.D, d, k, _abi.PREC[self.precision],
+                                   _abi.ptr(out)], r1.device,
+                  key=("bond_rdm", r1.shapes(), r2.shapes(), k, self.precision))
         return out

@@ -455,6 +455,15 @@ def run_gb300(args, rank, world, local_rank):
     compare = None
     if rank == 0 and not args.no_compare:
         compare = compare_paths(gb, st, cfg, dev, args.precision, args.compare_moves)
+    sweep = None
+    if rank == 0 and not args.no_batched:
+        sweep = batched_sweep(gb, dev)
+    meas = None
+    if rank == 0 and not args.no_measure:
+        meas = measure_timing(gb, st, dev)
+    large = None
+    if rank == 0 and not args.no_large:
+        large = large_instance(gb, dev)
 
     peaks = {}
     try:
@@ -501,6 +510,9 @@ def run_gb300(args, rank, world, local_rank):
             "qr_fallbacks_in_timed_moves": qr_fallbacks,
             "grow_seconds": t_grow,
             "comparison": compare,
+            "batched_sweep": sweep,
+            "measure": meas,
+            "large_instance": large,
             "spans_ms_per_step": {k: v[0] / prof_moves for k, v in prof.items() if v[2]},
             "clocks": clk,
         }
@@ -521,6 +533,190 @@ def run_gb300(args, rank, world, local_rank):
                                               f"{GROW_ITERS}-iteration chi={CHI} state",
                                     "cpu_model": cpu_model()}
     return line
+
+
+def batched_sweep(gb, dev, iterations=3):
+    """Parameter sweep of 32 independent transverse-field Ising iPEPS (hx
+    uniform in [2.5, 3.5], D from {3, 4, 5}, chi from {48, 64, 80, 100}, one
+    seeded generator; float32 storage, FP64 projectors, half-system rSVD with
+    the reference's default oversampling 2): moves/s of BatchedCTMRG (every
+    instance on its own stream, one iteration of all 32 captured as one CUDA
+    graph) against the same 32 instances solved one after another (the plain
+    eager path, the reference's move order).  Environments are first grown
+    to chi, untimed."""
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(SEED)
+    inst = [(float(rng.uniform(2.5, 3.5)), int(rng.choice([3, 4, 5])),
+             int(rng.choice([48, 64, 80, 100]))) for _ in range(32)]
+    cfg = gb.CTMRGConfig(projectors="half-system", svd_type="rsvd", rsvd_oversampling=2,
+                         rsvd_niter=2, svd_cutoff=1e-12, precision="fp64",
+                         disable_progressbar=True)
+
+    def f32_state(D, chi, seed):
+        st = gb.random_state(D, chi, seed, bias=1e-2, device=dev)
+        for s in st.site_list:
+            v = st[s]
+            st[s] = {"A": v["A"].float(), "C": [t.float() for t in v["C"]],
+                     "E": [t.float() for t in v["E"]]}
+        return st
+
+    states = [f32_state(D, chi, SEED + i) for i, (_, D, chi) in enumerate(inst)]
+    b = gb.BatchedCTMRG(states, cfg)
+    t0 = time.perf_counter()
+    b.grow()
+    grow_s = time.perf_counter() - t0
+    seq = [clone_state(gb, st) for st in states]
+    a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    a.record()
+    for st in seq:  # one iteration of each instance, one instance after another
+        gb.ctmrg(st, cfg, steps=1, pairs=False)
+    e.record()
+    torch.cuda.synchronize(dev)
+    seq_s = a.elapsed_time(e) / 1e3
+    del seq
+    t0 = time.perf_counter()
+    b.capture(warmup=1)
+    capture_s = time.perf_counter() - t0
+    b.replay(1)
+    torch.cuda.synchronize(dev)
+    a.record()
+    b.replay(iterations)
+    e.record()
+    torch.cuda.synchronize(dev)
+    bat_s = a.elapsed_time(e) / 1e3
+    moves = b.moves_per_iteration()
+    return {"instances": len(inst), "D": [x[1] for x in inst], "chi": [x[2] for x in inst],
+            "hx_range": [min(x[0] for x in inst), max(x[0] for x in inst)],
+            "storage": "float32", "projectors": "fp64 half-system rSVD os=2 niter=2",
+            "batched_moves_per_s": moves * iterations / bat_s,
+            "sequential_moves_per_s": moves / seq_s,
+            "speedup": (moves * iterations / bat_s) / (moves / seq_s),
+            "truncated_below_chi": b.truncated(),
+            "grow_seconds": grow_s, "capture_seconds": capture_s,
+            "timing": f"CUDA events; batched: {iterations} graph replays of one iteration of "
+                      "all instances; sequential: one eager iteration per instance"}
+
+
+def large_instance(gb, dev, D8=8, chi8=256, grow=3, pairs=2):
+    """The large single instance: Heisenberg, D=8, chi=256 (enlarged corner
+    16384 x 16384), half-system rSVD with oversampling 16 and 2 power
+    iterations, mixed precision (the site-tensor steps as one-layer
+    tensor-core GEMMs, no D^8 double-layer matrix), against one move of the
+    FP64 path.  The environment is grown to chi first (untimed); moves run
+    as left/right and up/down pairs."""
+    import dataclasses
+    import torch
+    cfg = gb.CTMRGConfig(projectors="half-system", svd_type="rsvd", rsvd_oversampling=16,
+                         rsvd_niter=2, svd_cutoff=1e-12, precision="mixed",
+                         disable_progressbar=True)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(SEED)
+    omega = lambda n, q, device: torch.randn(n, q, dtype=torch.float64, device=device,
+                                             generator=gen)
+    st = gb.random_state(D8, chi8, SEED, d=PHYS, device=dev)
+    mover = gb.DirectionalMover(cfg, omega_source=omega)
+    order = gb.pair_order(2, 2)
+    t0 = time.perf_counter()
+    for _ in range(grow):
+        for kind, i1, i2 in order:
+            mover.move_pair(st, kind, i1, i2)
+    torch.cuda.synchronize(dev)
+    grow_s = time.perf_counter() - t0
+    kind, i1, i2 = order[0]
+    mover.move_pair(st, kind, i1, i2)  # warm
+    a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    a.record()
+    for i in range(pairs):
+        kind, i1, i2 = order[(1 + i) % len(order)]
+        mover.move_pair(st, kind, i1, i2)
+    e.record()
+    torch.cuda.synchronize(dev)
+    ms = a.elapsed_time(e) / (2 * pairs)
+    gb._abi.profile_begin()
+    mover.concurrent = False
+    kind, i1, i2 = order[0]
+    mover.move_pair(st, kind, i1, i2)
+    torch.cuda.synchronize(dev)
+    gb._abi.profile_end()
+    mover.concurrent = True
+    kernels = gb._abi.profile_kernels()
+    tc = [k for k in kernels if k["name"].startswith("tc_gemm")]
+    tc_ms = sum(k["ms"] for k in tc) / 2
+    tc_work = sum(k["work"] for k in tc) / 2
+    # one move of the FP64 path on the same state
+    s64 = clone_state(gb, st)
+    m64 = gb.DirectionalMover(dataclasses.replace(cfg, precision="fp64"), omega_source=omega)
+    a.record()
+    m64.move(s64, 0, 0)
+    e.record()
+    torch.cuda.synchronize(dev)
+    fp64_ms = a.elapsed_time(e)
+    del s64
+    q = chi8 + 16
+    flops = move_flops(D8, chi8, q)
+    return {"workload": f"heisenberg_2x2_D{D8}_chi{chi8}_rsvd_os16_niter2", "precision": "mixed",
+            "contraction": "one-layer site-tensor steps", "moves_per_s": 1e3 / ms,
+            "ms_per_move": ms, "tflops": flops / (ms / 1e3) / 1e12,
+            "tensor_core_ms_per_move_serial": tc_ms,
+            "tensor_core_algorithmic_tflops": tc_work / (tc_ms / 1e3) / 1e12 if tc_ms else None,
+            "fp64_path_moves_per_s": 1e3 / fp64_ms, "ratio_vs_fp64": fp64_ms / ms,
+            "grow_iterations": grow, "grow_seconds": grow_s,
+            "timing": f"CUDA events over {pairs} pairs of moves after one warm pair; FP64: one move"}
+
+
+def measure_timing(gb, st, dev):
+    """Wall time of measure() (4 site RDMs, 8 bond RDMs, energy) on the
+    benchmark's state: the mixed RDMs (bond RDMs on tensor cores), the FP64
+    path, and the reference's own RDM on the host cores for one site and one
+    bond (scaled to the 4 + 8 of a measurement), with the energy difference
+    of the mixed measurement from the FP64 one."""
+    import torch
+    model = gb.HeisenbergModel(1.0, device=dev)
+    out = {}
+    for prec, reps in (("mixed", 3), ("fp64", 1)):
+        gb.measure(st, model, verbose=False, precision=prec)  # warm (workspaces)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            e = float(gb.measure(st, model, verbose=False, precision=prec)["Energy"])
+        torch.cuda.synchronize(dev)
+        out[f"{prec}_ms"] = 1e3 * (time.perf_counter() - t0) / reps
+        out[f"{prec}_energy"] = e
+    out["mixed_rel_err_vs_fp64"] = (abs(out["mixed_energy"] - out["fp64_energy"])
+                                    / abs(out["fp64_energy"]))
+    mods = reference_modules()
+    arrays = {s: {"A": st[s]["A"].cpu().numpy(), "C": [c.cpu().numpy() for c in st[s]["C"]],
+                  "E": [e.cpu().numpy() for e in st[s]["E"]]} for s in st.site_list}
+    if mods is not None:
+        net = reference_network(mods, arrays)
+        rdm_mod = importlib.import_module("acetn.measurement.rdm")
+        bond_mod = importlib.import_module("acetn.ipeps.bond")
+        torch.set_num_threads(cpu_cores())
+        r = rdm_mod.RDM(net)
+        t0 = time.perf_counter()
+        r[(0, 0)]
+        t_site = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        r[bond_mod.Bond((0, 0), (1, 0), 2)]
+        t_bond = time.perf_counter() - t0
+        kind = "reference"
+    else:
+        from oracle import ctm_oracle as orc
+        ost = orc.OracleState(arrays, 2, 2, CHI)
+        t0 = time.perf_counter()
+        orc.site_rdm(ost[(0, 0)])
+        t_site = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        orc.bond_rdm(ost, (0, 0), (1, 0), 2)
+        t_bond = time.perf_counter() - t0
+        kind = "port"
+    out["cpu_ms"] = 1e3 * (4 * t_site + 8 * t_bond)
+    out["cpu"] = {"kind": kind, "cores": cpu_cores(),
+                  "sample": "one site RDM and one bond RDM, scaled to 4 + 8"}
+    return out
 
 
 def sm_fp32_peak_tflops(dev):
@@ -748,6 +944,12 @@ def main():
                     help="skip the replays of one CUDA-graph-captured CTMRG iteration")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the FP64-path timing and the one-move accuracy check")
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip the D=8, chi=256 instance")
+    ap.add_argument("--no-measure", action="store_true",
+                    help="skip the measure() timing")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the 32-instance parameter sweep")
     ap.add_argument("--compare-moves", type=int, default=4,
                     help="moves (one per direction) of the accuracy check")
     ap.add_argument("--cpu-moves", type=int, default=2)

@@ -97,6 +97,16 @@ typedef struct ctm_ctmrg_opts {
 const char* ctm_version(void);
 const char* ctm_last_error(void);
 
+/* Form of the two site-tensor steps of CTM_PREC_MIXED (enlarged corners and
+ * edge renormalization), for the whole process: 0 = automatic (one GEMM
+ * against the double-layer site matrix, K = D^4, up to D = 6; the two
+ * one-layer GEMMs of the reference's einsum order, K = D^2 and D^2 d, from
+ * D = 8, where the double layer's D^8 entries would multiply the FLOPs by
+ * D^2 / (2 d)), 1 = always the double layer, 2 = always one layer.
+ * *previous (if not NULL) receives the former setting.  No counterpart in
+ * the reference (its einsums are always one-layer). */
+int ctm_set_mixed_contraction(int32_t form, int32_t* previous);
+
 /* Synchronizes `stream`, stores and clears the device-side failure flags of
  * the current device: bit 0 = a factorization failed and its fallback ran,
  * bit 1 = an iteration limit or a bounded wait expired.  No counterpart in
@@ -184,16 +194,23 @@ int ctm_renormalize_boundary(const ctm_site_f64* s1, int64_t D, int64_t d, int32
                              int32_t precision, void* ws, size_t* ws_bytes,
                              ctm_stream_t stream);
 
-/* Site reduced density matrix (d x d), not trace-normalised.
+/* Site reduced density matrix (d x d), not trace-normalised.  precision:
+ * CTM_PREC_FP64, or CTM_PREC_MIXED (the same contraction chain in FP32 FMAs
+ * with FP32 accumulation; FP64 result).
  * Reference: RDM.build_site_rdm, acetn/measurement/rdm.py:35-67. */
-int ctm_site_rdm(const ctm_site_f64* site, int64_t D, int64_t d, double* rdm,
-                 void* ws, size_t* ws_bytes, ctm_stream_t stream);
+int ctm_site_rdm(const ctm_site_f64* site, int64_t D, int64_t d, int32_t precision,
+                 double* rdm, void* ws, size_t* ws_bytes, ctm_stream_t stream);
 
 /* Bond reduced density matrix (d, d, d, d) of bond (s1, s2, k), not normalised.
- * Reference: RDM.build_bond_rdm / build_bond_rdm_core_blocked,
+ * precision: CTM_PREC_FP64, or CTM_PREC_MIXED (each half on tensor cores:
+ * the boundary operand, a double layer of the site tensor with the physical
+ * and the bond legs open, and the closing corner-edge product, 3xBF16 with
+ * FP32 accumulation; FP64 halves and final contraction).
+ * Reference: RDM.build_bond_rdm / build_bond_rdm_core(_blocked),
  * acetn/measurement/rdm.py:69-153. */
 int ctm_bond_rdm(const ctm_site_f64* s1, const ctm_site_f64* s2, int64_t D, int64_t d,
-                 int32_t k, double* rdm, void* ws, size_t* ws_bytes, ctm_stream_t stream);
+                 int32_t k, int32_t precision, double* rdm, void* ws, size_t* ws_bytes,
+                 ctm_stream_t stream);
 
 /* Norm tensor of the full update for bond (s1, s2, k): the bond's environment
  * contracted with the reduced site tensors a1q (r, d, u, y) and a2q

@@ -118,7 +118,9 @@ def test_tfim_d4_chi64_fp64_and_mixed():
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_fixed_width_projectors_equal_compact_ones(precision):
     z = load("ctmrg_d2_chi20_rsvd.npz")
-    st = gpu_state(z, 20, prefix="out")
+    st = gpu_state(z, 20)
+    gb.ctmrg(st, gb.CTMRGConfig(steps=4, disable_progressbar=True),
+             omega_source=omega_from(orc.OmegaStream(2)))
     # a cutoff that truncates below chi, so the fixed-width projectors carry
     # zero columns
     cfg = gb.CTMRGConfig(projectors="half-system", svd_type="rsvd", rsvd_oversampling=2,

@@ -151,15 +151,16 @@ def test_full_rank_ctmrg_matches_golden(fname, chi, proj, steps, model):
 def test_rsvd_trajectory_within_noise_floor():
     """30 rSVD iterations: FP64 implementations differing only in rounding
     order diverge to ~1e-5 relative in E (the oracle vs the reference shows
-    the same); the GPU result must stay inside that band."""
+    1.3e-5); the GPU result must stay inside 5e-5."""
     z = load("ctmrg_d2_chi20_rsvd.npz")
     st = gpu_state(z, 20)
     gb.ctmrg(st, cfg_obj(steps=30, disable_progressbar=True),
              omega_source=omega_from(orc.OmegaStream(5)))
     e = energy_and_rdms(st, gb.HeisenbergModel(1.0))
     e_ref = float(z["out_meas_Energy"])
+    # measured 1.7e-5 (the oracle differs from the reference by 1.3e-5)
     print(f"rsvd trajectory deviation: {abs(e - e_ref) / abs(e_ref):.3e}")
-    assert abs(e - e_ref) <= 1e-3 * abs(e_ref)
+    assert abs(e - e_ref) <= 5e-5 * abs(e_ref)
 
 
 @pytest.mark.parametrize("case", ["ising_dims_2_20_dtau_001_hx_295",
