@@ -19,6 +19,7 @@ All arithmetic runs in libctm_gb300.so; there is no CPU fallback.
 """
 
 from . import _abi
+from ._abi import autotune, autotune_table, set_mixed_contraction
 from ._build import build
 from .config import CTMRGConfig
 from .ctmrg import ctmrg, pair_order, sweep_order
@@ -37,4 +38,5 @@ from .state import Bond, IpepsState, random_state
 __all__ = ["build", "CTMRGConfig", "ctmrg", "sweep_order", "pair_order", "DirectionalMover",
            "ProjectorCalculator", "CTMRGGraph", "BatchedCTMRG", "RDM", "measure", "svd_lowrank", "fused_matmul_svd_lowrank",
            "fused_3matmul_svd_lowrank", "qr", "svd", "matmul", "HeisenbergModel", "IsingModel",
-           "Bond", "IpepsState", "random_state", "build_norm_tensor", "absorb_bond"]
+           "Bond", "IpepsState", "random_state", "build_norm_tensor", "absorb_bond",
+           "autotune", "autotune_table", "set_mixed_contraction"]

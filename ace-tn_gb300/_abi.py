@@ -45,6 +45,10 @@ _SIGNATURES = {
     "ctm_last_error": ([], ctypes.c_char_p),
     "ctm_device_status": ([ctypes.POINTER(ctypes.c_int), c_vp], ctypes.c_int),
     "ctm_set_mixed_contraction": ([c_i32, ctypes.POINTER(c_i32)], ctypes.c_int),
+    "ctm_autotune": ([c_i32, ctypes.POINTER(c_i32)], ctypes.c_int),
+    "ctm_autotune_entry": ([c_i32, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(c_i32),
+                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
+                           ctypes.c_int),
     "ctm_kernel_launches": ([], ctypes.c_ulonglong),
     "ctm_qr_fallbacks": ([ctypes.POINTER(ctypes.c_ulonglong), c_vp], ctypes.c_int),
     "ctm_profile_begin": ([], None),
@@ -67,6 +71,9 @@ _SIGNATURES = {
     "ctm_renormalize_boundary": ([SITE_P, c_i64, c_i64, c_i32, c_vp, c_i64, c_vp, c_i64, c_vp,
                                   c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_sz_p,
                                   c_vp], ctypes.c_int),
+    "ctm_move_batched": ([SITE_P, c_i32, c_i32, c_i64, c_i64, ctypes.POINTER(c_i32), c_i32,
+                          ctypes.POINTER(CtmOpts), ctypes.POINTER(c_vp), ctypes.POINTER(c_vp),
+                          c_vp, c_vp, c_sz_p, c_vp], ctypes.c_int),
     "ctm_site_rdm": ([SITE_P, c_i64, c_i64, c_i32, c_vp, c_vp, c_sz_p, c_vp], ctypes.c_int),
     "ctm_bond_rdm": ([SITE_P, SITE_P, c_i64, c_i64, c_i32, c_i32, c_vp, c_vp, c_sz_p, c_vp],
                      ctypes.c_int),
@@ -244,7 +251,38 @@ def set_mixed_contraction(form):
     prev = c_i32(0)
     check(load().ctm_set_mixed_contraction(CONTRACTION_FORMS[form], ctypes.byref(prev)),
           "ctm_set_mixed_contraction")
+    _WS_CACHE.clear()  # workspace sizes depend on the form
     return {v: k for k, v in CONTRACTION_FORMS.items()}[prev.value]
+
+
+def autotune(enable=True, reset=False):
+    """Turns the tile-plan autotuner of the tensor-core GEMMs on or off
+    (``reset`` also forgets the tuned shapes); returns how many shapes are
+    tuned.  Tuning happens on the first eager call of each product shape."""
+    n = c_i32(0)
+    code = -2 if reset else (1 if enable else 0)
+    check(load().ctm_autotune(code, ctypes.byref(n)), "ctm_autotune")
+    if reset and enable:
+        check(load().ctm_autotune(1, ctypes.byref(n)), "ctm_autotune")
+    return n.value
+
+
+def autotune_table():
+    """The tuned shapes: dicts with M, N, K, passes, the chosen candidate
+    (bit 0: 128-wide N tiles, bit 1: no K split) and both times in ms."""
+    lib = load()
+    n = c_i32(0)
+    check(lib.ctm_autotune(-1, ctypes.byref(n)), "ctm_autotune")
+    rows = []
+    for i in range(n.value):
+        mnk = (ctypes.c_int64 * 3)()
+        mc = (c_i32 * 2)()
+        best, dflt = ctypes.c_double(0), ctypes.c_double(0)
+        check(lib.ctm_autotune_entry(i, mnk, mc, ctypes.byref(best), ctypes.byref(dflt)),
+              "ctm_autotune_entry")
+        rows.append({"M": mnk[0], "N": mnk[1], "K": mnk[2], "passes": mc[0], "choice": mc[1],
+                     "best_ms": best.value, "default_ms": dflt.value})
+    return rows
 
 
 def kernel_launches():

@@ -789,6 +789,107 @@ int ctm_renormalize_boundary(const ctm_site_f64* s1, int64_t D, int64_t d, int32
   });
 }
 
+int ctm_move_batched(const ctm_site_f64* sites, int32_t nx, int32_t ny, int64_t D, int64_t d,
+                     const int32_t* moves, int32_t nmoves, const ctm_ctmrg_opts* opts,
+                     const double* const* omegas, double* const* out, int64_t* chi_new, void* ws,
+                     size_t* ws_bytes, ctm_stream_t stream) {
+  return with_workspace(ws, ws_bytes, as_stream(stream), [&](Ctx& c) {
+    CTM_REQUIRE(sites != nullptr && moves != nullptr && opts != nullptr, CTM_ERR_INVALID,
+                "NULL argument");
+    CTM_REQUIRE(nx >= 1 && ny >= 1 && int64_t(nx) * ny <= 1024, CTM_ERR_INVALID,
+                "unit cell must have 1 <= nx * ny <= 1024 sites");
+    CTM_REQUIRE(nmoves == 1 || nmoves == 2, CTM_ERR_INVALID, "one or two moves per call");
+    for (int m = 0; m < nmoves; ++m)
+      CTM_REQUIRE(moves[2 * m] >= 0 && moves[2 * m] <= 3, CTM_ERR_INVALID,
+                  "move direction must be 0..3");
+    if (nmoves == 2)
+      CTM_REQUIRE(moves[0] % 2 == moves[2] % 2 && moves[0] != moves[2], CTM_ERR_INVALID,
+                  "two moves must be a left/right or an up/down pair");
+    std::vector<Site> S(size_t(nx) * ny);
+    for (int i = 0; i < nx * ny; ++i) {
+      check_site(&sites[i], D, d);
+      S[size_t(i)] = Site{&sites[i], D, d};
+    }
+    auto at = [&](int x, int y) -> const Site* {
+      x = ((x % nx) + nx) % nx;
+      y = ((y % ny) + ny) % ny;
+      return &S[size_t(x) * ny + y];
+    };
+    ctm_ctmrg_opts o = *opts;
+    o.fixed_width = 1;
+    struct Row {
+      const Site* q[4];
+      int k;
+      double *P1, *P2;
+      int64_t cap;
+    };
+    std::vector<Row> rows;
+    std::vector<int> first(nmoves), count(nmoves);
+    for (int m = 0; m < nmoves; ++m) {
+      const int k = moves[2 * m], idx = moves[2 * m + 1];
+      const int nr = (k % 2 == 0) ? ny : nx;
+      first[m] = int(rows.size());
+      count[m] = nr;
+      for (int r = 0; r < nr; ++r) {
+        Row w{};
+        w.k = k;
+        // the site quadruples of calculate_{left,up,right,down}_projectors
+        // (acetn/renormalization/directional_mover.py:99-181)
+        if (k == 0) {
+          w.q[0] = at(idx, r); w.q[1] = at(idx + 1, r); w.q[2] = at(idx + 1, r - 1); w.q[3] = at(idx, r - 1);
+        } else if (k == 1) {
+          w.q[0] = at(r, idx); w.q[1] = at(r, idx - 1); w.q[2] = at(r - 1, idx - 1); w.q[3] = at(r - 1, idx);
+        } else if (k == 2) {
+          w.q[0] = at(idx, r); w.q[1] = at(idx - 1, r); w.q[2] = at(idx - 1, r + 1); w.q[3] = at(idx, r + 1);
+        } else {
+          w.q[0] = at(r, idx); w.q[1] = at(r, idx + 1); w.q[2] = at(r + 1, idx + 1); w.q[3] = at(r + 1, idx);
+        }
+        const ProjDims pd = projector_dims(w.q, k, o);
+        w.cap = pd.cap;
+        w.P1 = c.alloc<double>(size_t(pd.p1_rows) * pd.cap);
+        w.P2 = c.alloc<double>(size_t(pd.p2_rows) * pd.cap);
+        rows.push_back(w);
+      }
+    }
+    if (!c.sizing()) {
+      CTM_REQUIRE(out != nullptr && chi_new != nullptr, CTM_ERR_INVALID, "output pointer is NULL");
+      for (size_t t = 0; t < rows.size(); ++t) {
+        CTM_REQUIRE(out[3 * t] && out[3 * t + 1] && out[3 * t + 2], CTM_ERR_INVALID,
+                    "output tensor pointer is NULL");
+        CTM_REQUIRE(o.svd_type != CTM_SVD_RSVD || (omegas != nullptr && omegas[t] != nullptr),
+                    CTM_ERR_INVALID, "omega is NULL for the randomized SVD");
+      }
+    }
+    // phase A: the projector pairs of every row of every move
+    for (size_t t = 0; t < rows.size(); ++t) {
+      Row& w = rows[t];
+      const double* om = (omegas != nullptr) ? omegas[t] : nullptr;
+      if (o.precision == CTM_PREC_MIXED)
+        calculate_projectors_mixed(c, w.q, w.k, o, om, w.P1, w.P2, chi_new ? chi_new + t : nullptr);
+      else
+        calculate_projectors(c, w.q, w.k, o, om, w.P1, w.P2, chi_new ? chi_new + t : nullptr);
+    }
+    // phase B: renormalize_boundary of every row (directional_mover.py:273-303)
+    for (int m = 0; m < nmoves; ++m) {
+      const int k = moves[2 * m], idx = moves[2 * m + 1], nr = count[m];
+      for (int r = 0; r < nr; ++r) {
+        const Site* s1;
+        int i = r, j;
+        if (k == 0) { s1 = at(idx, r); j = (r + 1) % nr; }
+        else if (k == 1) { s1 = at(r, idx); j = (r + 1) % nr; }
+        else if (k == 2) { s1 = at(idx, r); j = (r - 1 + nr) % nr; }
+        else { s1 = at(r, idx); j = (r - 1 + nr) % nr; }
+        const Row& ri = rows[size_t(first[m] + i)];
+        const Row& rj = rows[size_t(first[m] + j)];
+        const size_t t = size_t(first[m] + r);
+        renormalize_boundary(c, *s1, k, ri.P1, ri.cap, rj.P2, rj.cap, ri.P2, ri.cap, rj.P1, rj.cap,
+                             out ? out[3 * t] : nullptr, out ? out[3 * t + 1] : nullptr,
+                             out ? out[3 * t + 2] : nullptr, o.precision);
+      }
+    }
+  });
+}
+
 int ctm_site_rdm(const ctm_site_f64* site, int64_t D, int64_t d, int32_t precision, double* rdm,
                  void* ws, size_t* ws_bytes, ctm_stream_t stream) {
   return with_workspace(ws, ws_bytes, as_stream(stream), [&](Ctx& c) {

@@ -42,6 +42,7 @@ struct GettArgs {
   int64_t kchunk;
   T* part;
   int kfa, kfb;  // tile loaders walk K fastest (K is the unit-stride mode of A / B)
+  int swap_xy;   // grid x runs over column tiles (more than 65535 of them)
 };
 
 __device__ __forceinline__ void decode(const Group& g, int64_t idx, int64_t& o0, int64_t& o1) {
@@ -75,8 +76,8 @@ __global__ void __launch_bounds__(NT) gett_kernel(const GettArgs<T> p) {
   constexpr int E = (BM * BK) / NT;
 
   const int tid = threadIdx.x;
-  const int64_t m0 = static_cast<int64_t>(blockIdx.x) * BM;
-  const int64_t n0 = static_cast<int64_t>(blockIdx.y) * BN;
+  const int64_t m0 = static_cast<int64_t>(p.swap_xy ? blockIdx.y : blockIdx.x) * BM;
+  const int64_t n0 = static_cast<int64_t>(p.swap_xy ? blockIdx.x : blockIdx.y) * BN;
   const int64_t z = blockIdx.z;
   const int64_t batch = z % p.bext;
   const int64_t split = z / p.bext;
@@ -185,6 +186,63 @@ __global__ void __launch_bounds__(NT) gett_kernel(const GettArgs<T> p) {
       }
     }
   }
+}
+
+// Contractions with few outputs and a long K (the last steps of the RDMs:
+// 4 x 4 outputs over chi^2 D^2 terms) would use one 64 x 64 tile of the GETT
+// kernel for a handful of outputs.  Here every CTA takes one K chunk for all
+// Mt x Nt <= 256 outputs (one per thread; Mt + Nt <= 128), staging 32 K
+// indices of both operands in shared memory per step, and writes its partial
+// sums for gett_splitk_reduce.
+constexpr int kSmallK = 32;
+
+template <class T>
+__global__ void __launch_bounds__(256) gett_small_kernel(const GettArgs<T> p) {
+  __shared__ int64_t sAm[128], sBn[128], sAk[kSmallK], sBk[kSmallK];
+  extern __shared__ __align__(16) unsigned char small_smem[];
+  const int64_t Mt = p.Mt, Nt = p.Nt;
+  T (*As)[kSmallK + 1] = reinterpret_cast<T (*)[kSmallK + 1]>(small_smem);
+  T (*Bs)[kSmallK + 1] = reinterpret_cast<T (*)[kSmallK + 1]>(small_smem) + Mt;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < Mt; i += blockDim.x) {
+    int64_t a, c;
+    decode(p.M, i, a, c);
+    sAm[i] = a;
+  }
+  for (int i = tid; i < Nt; i += blockDim.x) {
+    int64_t b, c;
+    decode(p.N, i, b, c);
+    sBn[i] = b;
+  }
+  const int64_t k0 = int64_t(blockIdx.x) * p.kchunk;
+  const int64_t k1 = min(k0 + p.kchunk, p.Kt);
+  const int m = tid / int(Nt), n = tid % int(Nt);
+  const bool owner = tid < Mt * Nt;
+  T acc = T(0);
+  for (int64_t kb = k0; kb < k1; kb += kSmallK) {
+    __syncthreads();
+    if (tid < kSmallK) {
+      int64_t a = 0, b = 0;
+      if (kb + tid < k1) decode(p.K, kb + tid, a, b);
+      sAk[tid] = a;
+      sBk[tid] = b;
+    }
+    __syncthreads();
+    for (int e = tid; e < Mt * kSmallK; e += blockDim.x) {
+      const int i = e / kSmallK, kk = e % kSmallK;
+      As[i][kk] = (kb + kk < k1) ? p.A[sAm[i] + sAk[kk]] : T(0);
+    }
+    for (int e = tid; e < Nt * kSmallK; e += blockDim.x) {
+      const int j = e / kSmallK, kk = e % kSmallK;
+      Bs[j][kk] = (kb + kk < k1) ? p.B[sBn[j] + sBk[kk]] : T(0);
+    }
+    __syncthreads();
+    if (owner) {
+#pragma unroll 8
+      for (int kk = 0; kk < kSmallK; ++kk) acc = fma(As[m][kk], Bs[n][kk], acc);
+    }
+  }
+  if (owner) p.part[(int64_t(blockIdx.x) * Mt + m) * Nt + n] = acc;
 }
 
 // Sums split-K partial tiles in a fixed order (deterministic) into C.
@@ -342,6 +400,30 @@ void einsum_impl(Ctx& c, const char* spec, const ViewT<T>& A, const ViewT<T>& B,
   p.kfb = (p.K.n > 0 && p.K.m[p.K.n - 1].s1 == 1 &&
            !(p.N.n > 0 && p.N.m[p.N.n - 1].s0 == 1)) ? 1 : 0;
 
+  if (bext == 1 && p.Mt * p.Nt <= 256 && p.Mt + p.Nt <= 128 && p.Kt >= 8192) {
+    // few outputs, long K: one K chunk per CTA for all outputs
+    int splits = static_cast<int>(std::min<int64_t>(1024, (p.Kt + 511) / 512));
+    p.kchunk = ((p.Kt + splits - 1) / splits + kSmallK - 1) / kSmallK * kSmallK;
+    splits = static_cast<int>((p.Kt + p.kchunk - 1) / p.kchunk);
+    p.splitk = splits;
+    Scope scope(c);
+    p.part = c.alloc<T>(size_t(splits) * p.Mt * p.Nt);
+    if (c.sizing()) return;
+    {
+      const double flops = 2.0 * double(p.Mt) * p.Nt * p.Kt;
+      KernelTimer timer(c.stream, sizeof(T) == 8 ? kTagGettF64 : kTagGettF32, flops);
+      KernelTimer kt(c.stream, sizeof(T) == 8 ? "gett_small_kernel<double>"
+                                             : "gett_small_kernel<float>", kUnitFlop, flops);
+      const size_t smem = size_t(p.Mt + p.Nt) * (kSmallK + 1) * sizeof(T);
+      gett_small_kernel<T><<<splits, 256, smem, c.stream>>>(p);
+      CTM_LAUNCH_CHECK();
+    }
+    KernelTimer kt(c.stream, "gett_splitk_reduce", kUnitByte,
+                   double(sizeof(T)) * (splits + 1.0) * p.Mt * p.Nt);
+    gett_splitk_reduce<T><<<grid_for(p.Mt * p.Nt, 256), 256, 0, c.stream>>>(p);
+    CTM_LAUNCH_CHECK();
+    return;
+  }
   const int64_t tiles = ((p.Mt + BM - 1) / BM) * ((p.Nt + BN - 1) / BN) * bext;
   int splitk = 1;
   const int64_t target = 2 * 152;
@@ -356,9 +438,12 @@ void einsum_impl(Ctx& c, const char* spec, const ViewT<T>& A, const ViewT<T>& B,
   Scope scope(c);
   if (splitk > 1) p.part = c.alloc<T>(size_t(splitk) * bext * p.Mt * p.Nt);
   if (c.sizing()) return;
-  dim3 grid(static_cast<unsigned>((p.Mt + BM - 1) / BM), static_cast<unsigned>((p.Nt + BN - 1) / BN),
-            static_cast<unsigned>(bext * splitk));
-  CTM_REQUIRE(grid.y <= 65535 && grid.z <= 65535, CTM_ERR_UNSUPPORTED, "einsum: grid too large");
+  const int64_t mtiles = (p.Mt + BM - 1) / BM, ntiles = (p.Nt + BN - 1) / BN;
+  p.swap_xy = ntiles > 65535 ? 1 : 0;
+  dim3 grid(static_cast<unsigned>(p.swap_xy ? ntiles : mtiles),
+            static_cast<unsigned>(p.swap_xy ? mtiles : ntiles), static_cast<unsigned>(bext * splitk));
+  CTM_REQUIRE(grid.y <= 65535 && grid.z <= 65535 && grid.x <= 0x7fffffffLL, CTM_ERR_UNSUPPORTED,
+              "einsum: grid too large");
   {
     const double flops = 2.0 * double(p.Mt) * p.Nt * p.Kt * bext;
     KernelTimer timer(c.stream, sizeof(T) == 8 ? kTagGettF64 : kTagGettF32, flops);

@@ -14,9 +14,11 @@
 
 #include <algorithm>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <set>
 #include <string>
+#include <tuple>
 
 #include "engine.cuh"
 #include "tc_gemm.cuh"
@@ -1057,86 +1059,100 @@ void gather_split_bf16(Ctx& c, const float* src, const Gather& g, bf16* hi, bf16
 
 namespace {
 
-void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, TcOut out,
-                  double* absmax) {
-  CTM_REQUIRE(A.k == B.k && A.k >= 1 && A.rows >= 1 && B.rows >= 1, CTM_ERR_INVALID,
-              "tc_gemm: operand shapes");
-  const int imode = static_cast<int>(mode);
-  const int64_t M = A.rows, N = B.rows, K = A.k;
+// Tile plan of one product.  Candidate bits: 1 = N tiles of at most 128
+// columns (default: 256), 2 = no K split (default: split K so that the grid
+// fills the SMs in one wave).
+struct TcPlan {
+  int ntile = 0, bk = 64, kb_total = 0, splits = 1, kb_per_split = 0, stages = 2, p_stages = 2;
+  int64_t n_tiles = 0, m_tiles = 0, base_ctas = 0;
+  bool direct = true, n_fast = false, persistent = false;
+  int m_pad = 0, n_pad = 0;
+  uint32_t stage_bytes = 0;
+  size_t smem = 0, p_smem = 0;
+  size_t part_elems() const { return direct ? 0 : size_t(splits) * m_pad * n_pad; }
+};
+
+constexpr int kTcCandidates = 4;
+
+TcPlan tc_plan(int64_t M, int64_t N, int64_t K, int imode, bool absmax, int cand) {
+  TcPlan pl;
   // N tiling: MMA N must be a multiple of 16 up to 256 (256-wide 3xBF16
   // tiles with two stages measured faster than 128-wide ones with three:
   // 373 us against 551 us for the double-layer GEMM at D=6)
-  const int64_t n_tiles = (N + 255) / 256;
-  int ntile = static_cast<int>(((N + n_tiles - 1) / n_tiles + 15) / 16 * 16);
-  ntile = std::max(ntile, 16);
-  const int64_t m_tiles = (M + kBM - 1) / kBM;
+  const int64_t nmax = (cand & 1) ? 128 : 256;
+  pl.n_tiles = (N + nmax - 1) / nmax;
+  pl.ntile = static_cast<int>(((N + pl.n_tiles - 1) / pl.n_tiles + 15) / 16 * 16);
+  pl.ntile = std::max(pl.ntile, 16);
+  pl.m_tiles = (M + kBM - 1) / kBM;
   // 64-wide K steps: measured faster than 32-wide ones with a deeper ring
   // (64-byte swizzle) even where only two 3xBF16 stages fit (the double-layer
   // GEMM at D=6: 373 us against 469 us)
-  const int bk = 64;
-  const int kb_total = static_cast<int>((K + bk - 1) / bk);
-  const int64_t base_ctas = m_tiles * n_tiles;
+  pl.bk = 64;
+  pl.kb_total = static_cast<int>((K + pl.bk - 1) / pl.bk);
+  pl.base_ctas = pl.m_tiles * pl.n_tiles;
   const int sms = sm_count();
   // split K so that the grid fills the SMs in one wave: a partial second wave
   // costs as much time as a full one
-  int splits = static_cast<int>(std::min<int64_t>(std::max<int64_t>(1, sms / base_ctas),
-                                                  std::max(1, kb_total / 4)));
+  int splits = static_cast<int>(std::min<int64_t>(std::max<int64_t>(1, sms / pl.base_ctas),
+                                                  std::max(1, pl.kb_total / 4)));
   splits = std::max(splits, 1);
-  if (absmax != nullptr) splits = 1;  // the maximum is taken over complete sums
-  const int kb_per_split = (kb_total + splits - 1) / splits;
-  splits = (kb_total + kb_per_split - 1) / kb_per_split;
-  const bool direct = splits == 1;
-  const int m_pad = static_cast<int>(m_tiles * kBM);
-  const int n_pad = static_cast<int>(n_tiles * ntile);
-  const uint32_t stage_bytes = uint32_t(kBM * bk * 2 + ntile * bk * 2) * (imode == 3 ? 2 : 1);
+  if (absmax || (cand & 2)) splits = 1;  // the maximum is taken over complete sums
+  pl.kb_per_split = (pl.kb_total + splits - 1) / splits;
+  pl.splits = (pl.kb_total + pl.kb_per_split - 1) / pl.kb_per_split;
+  pl.direct = pl.splits == 1;
+  pl.m_pad = static_cast<int>(pl.m_tiles * kBM);
+  pl.n_pad = static_cast<int>(pl.n_tiles * pl.ntile);
+  pl.stage_bytes = uint32_t(kBM * pl.bk * 2 + pl.ntile * pl.bk * 2) * (imode == 3 ? 2 : 1);
   // dynamic shared memory: the stage ring (the kernel's static arrays take ~8 KB)
-  const int stages = std::max(2, std::min(6, int((210 * 1024) / stage_bytes)));
-  const size_t smem = size_t(stages) * stage_bytes + 256 + 1024;
+  pl.stages = std::max(2, std::min(6, int((210 * 1024) / pl.stage_bytes)));
+  pl.smem = size_t(pl.stages) * pl.stage_bytes + 256 + 1024;
   // grid x over N tiles when A is the larger operand: the CTAs that share an
   // A tile are then resident together and A streams from DRAM once
-  const bool n_fast = n_tiles > 1 && m_tiles > n_tiles && m_tiles <= 65535;
-  Scope scope(c);
-  float* part = direct ? nullptr : c.alloc<float>(size_t(splits) * m_pad * n_pad);
-  if (c.sizing()) return;
-  CTM_REQUIRE(imode == 1 || (A.lo != nullptr && B.lo != nullptr), CTM_ERR_INVALID,
-              "tc_gemm: 3xBF16 needs lo parts");
-  CTM_REQUIRE(m_tiles <= 0x7fffffff && n_tiles <= 65535 && splits <= 65535, CTM_ERR_UNSUPPORTED,
-              "tc_gemm: grid too large");
+  pl.n_fast = pl.n_tiles > 1 && pl.m_tiles > pl.n_tiles && pl.m_tiles <= 65535;
+  // more tiles than SMs with a direct epilogue: one persistent CTA per SM;
+  // its static shared memory (offset tables and the staged epilogue, ~29 KB)
+  // leaves 196 KB for the stage ring
+  pl.persistent = pl.direct && pl.base_ctas > sms;
+  pl.p_stages = std::max(2, std::min(6, int((196 * 1024) / pl.stage_bytes)));
+  pl.p_smem = size_t(pl.p_stages) * pl.stage_bytes + 256 + 1024;
+  return pl;
+}
+
+void tc_launch(Ctx& c, const TcOperand& A, const TcOperand& B, int imode, const TcOut& out,
+               double* absmax, const TcPlan& pl, float* part) {
+  const int64_t M = A.rows, N = B.rows, K = A.k;
+  const int sms = sm_count();
+  CTM_REQUIRE(pl.m_tiles <= 0x7fffffff && pl.n_tiles <= 65535 && pl.splits <= 65535,
+              CTM_ERR_UNSUPPORTED, "tc_gemm: grid too large");
   CUtensorMap tA, tAl, tB, tBl;
-  make_map(&tA, A.hi, A.rows, K, A.ld, kBM, bk);
-  make_map(&tB, B.hi, B.rows, K, B.ld, uint32_t(ntile), bk);
+  make_map(&tA, A.hi, A.rows, K, A.ld, kBM, pl.bk);
+  make_map(&tB, B.hi, B.rows, K, B.ld, uint32_t(pl.ntile), pl.bk);
   if (imode == 3) {
-    make_map(&tAl, A.lo, A.rows, K, A.ld, kBM, bk);
-    make_map(&tBl, B.lo, B.rows, K, B.ld, uint32_t(ntile), bk);
+    make_map(&tAl, A.lo, A.rows, K, A.ld, kBM, pl.bk);
+    make_map(&tBl, B.lo, B.rows, K, B.ld, uint32_t(pl.ntile), pl.bk);
   } else {
     tAl = tA;
     tBl = tB;
   }
-  // more tiles than SMs with a direct epilogue: one persistent CTA per SM
-  const bool persistent = direct && base_ctas > sms;
-  // the persistent kernel's static shared memory (offset tables and the
-  // staged epilogue, ~29 KB) leaves 196 KB for the stage ring
-  const int p_stages = std::max(2, std::min(6, int((196 * 1024) / stage_bytes)));
-  const size_t p_smem = size_t(p_stages) * stage_bytes + 256 + 1024;
   bool bf16_dests = out.nd >= 1 && out.nd <= 2;
   for (int i = 0; i < out.nd; ++i)
     bf16_dests = bf16_dests && (out.d[i].kind == TcKind::kBf16Hi || out.d[i].kind == TcKind::kBf16Lo);
   GemmParams p{};
-  p.m_tiles = int(m_tiles);
-  p.n_tiles = int(n_tiles);
-  p.tiles = int(m_tiles * n_tiles);
-  p.ntile = ntile;
-  p.bk = bk;
-  p.kb_total = kb_total;
-  p.kb_per_split = kb_per_split;
-  p.stages = persistent ? p_stages : stages;
+  p.m_tiles = int(pl.m_tiles);
+  p.n_tiles = int(pl.n_tiles);
+  p.tiles = int(pl.m_tiles * pl.n_tiles);
+  p.ntile = pl.ntile;
+  p.bk = pl.bk;
+  p.kb_total = pl.kb_total;
+  p.kb_per_split = pl.kb_per_split;
+  p.stages = pl.persistent ? pl.p_stages : pl.stages;
   p.mode = imode;
   p.part = part;
-  p.m_pad = m_pad;
-  p.n_pad = n_pad;
+  p.m_pad = pl.m_pad;
+  p.n_pad = pl.n_pad;
   p.status = status_flags(c);
-  p.direct = direct ? 1 : 0;
-  p.n_fast = n_fast ? 1 : 0;
+  p.direct = pl.direct ? 1 : 0;
+  p.n_fast = pl.n_fast ? 1 : 0;
   p.nd = out.nd;
   p.alpha = out.alpha;
   p.scale1 = out.inv_scale;
@@ -1144,38 +1160,39 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   p.absmax = reinterpret_cast<unsigned long long*>(absmax);
   p.M = M;
   p.N = N;
-  p.staged = (persistent && bf16_dests) ? 1 : 0;
+  p.staged = (pl.persistent && bf16_dests) ? 1 : 0;
   for (int i = 0; i < out.nd; ++i) p.d[i] = out.d[i];
   if (absmax != nullptr) CTM_CUDA(cudaMemsetAsync(absmax, 0, sizeof(double), c.stream));
   CTM_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(smem)));
-  const dim3 grid(static_cast<unsigned>(n_fast ? n_tiles : m_tiles),
-                  static_cast<unsigned>(n_fast ? m_tiles : n_tiles), static_cast<unsigned>(splits));
+                                int(pl.smem)));
+  const dim3 grid(static_cast<unsigned>(pl.n_fast ? pl.n_tiles : pl.m_tiles),
+                  static_cast<unsigned>(pl.n_fast ? pl.m_tiles : pl.n_tiles),
+                  static_cast<unsigned>(pl.splits));
   {
     const double work = 2.0 * double(M) * N * K * imode;
     KernelTimer timer(c.stream, kTagTcGemm, work);
     KernelTimer timer2(c.stream, out.extra_tag >= 0 ? out.extra_tag : kTagTcGemm,
                        out.extra_tag >= 0 ? work : -1.0);
-    const char* kname = persistent ? "tc_gemm_persistent_kernel" : "tc_gemm_kernel";
+    const char* kname = pl.persistent ? "tc_gemm_persistent_kernel" : "tc_gemm_kernel";
     if (out.name != nullptr) kname = intern_name(std::string(kname) + " (" + out.name + ")");
     KernelTimer timer3(c.stream, kname, kUnitFlop,
                        out.algo_flops >= 0.0 ? out.algo_flops : 2.0 * double(M) * N * K);
-    if (persistent) {
+    if (pl.persistent) {
       CTM_CUDA(cudaFuncSetAttribute(tc_gemm_persistent_kernel,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, int(p_smem)));
-      tc_gemm_persistent_kernel<<<unsigned(std::min<int64_t>(base_ctas, sms)), kPThreads, p_smem,
-                                  c.stream>>>(tA, tAl, tB, tBl, p);
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, int(pl.p_smem)));
+      tc_gemm_persistent_kernel<<<unsigned(std::min<int64_t>(pl.base_ctas, sms)), kPThreads,
+                                  pl.p_smem, c.stream>>>(tA, tAl, tB, tBl, p);
     } else {
-      tc_gemm_kernel<<<grid, kThreads, smem, c.stream>>>(tA, tAl, tB, tBl, p);
+      tc_gemm_kernel<<<grid, kThreads, pl.smem, c.stream>>>(tA, tAl, tB, tBl, p);
     }
     CTM_LAUNCH_CHECK();
   }
-  if (direct) return;
+  if (pl.direct) return;
   ReduceParams r{};
   r.part = part;
-  r.splits = splits;
-  r.m_pad = m_pad;
-  r.n_pad = n_pad;
+  r.splits = pl.splits;
+  r.m_pad = pl.m_pad;
+  r.n_pad = pl.n_pad;
   r.M = M;
   r.N = N;
   r.alpha = out.alpha;
@@ -1185,9 +1202,106 @@ void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, T
   for (int i = 0; i < out.nd; ++i) r.d[i] = out.d[i];
   dim3 rg(unsigned((M + 31) / 32), unsigned((N + 31) / 32));
   CTM_REQUIRE(rg.y <= 65535, CTM_ERR_UNSUPPORTED, "tc_gemm: output too wide");
-  KernelTimer kt(c.stream, "tc_reduce_kernel", kUnitByte, 4.0 * (splits + 1.0) * double(M) * N);
+  KernelTimer kt(c.stream, "tc_reduce_kernel", kUnitByte, 4.0 * (pl.splits + 1.0) * double(M) * N);
   tc_reduce_kernel<<<rg, 256, 0, c.stream>>>(r);
   CTM_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------- autotuner
+// Per product shape (M, N, K, passes, epilogue) the tile plan is one of the
+// candidates above.  While tuning is on, the first eager call of a new shape
+// runs every distinct candidate twice, timed with CUDA events on its stream
+// (which synchronises that stream), keeps the fastest, and runs it again so
+// that the output is the chosen plan's; later calls use the table.  Without
+// an entry the default plan (candidate 0) runs.  Calls under stream capture
+// never tune.
+struct TuneKey {
+  int64_t M, N, K;
+  int mode, absmax, nd, kind0;
+  std::string name;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(M, N, K, mode, absmax, nd, kind0, name) <
+           std::tie(o.M, o.N, o.K, o.mode, o.absmax, o.nd, o.kind0, o.name);
+  }
+};
+struct TuneEntry {
+  int choice = 0;
+  double best_ms = 0.0, default_ms = 0.0;
+};
+std::mutex g_tune_mu;
+bool g_tuning = false;
+std::map<TuneKey, TuneEntry> g_tune;
+
+void tc_gemm_impl(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, TcOut out,
+                  double* absmax) {
+  CTM_REQUIRE(A.k == B.k && A.k >= 1 && A.rows >= 1 && B.rows >= 1, CTM_ERR_INVALID,
+              "tc_gemm: operand shapes");
+  const int imode = static_cast<int>(mode);
+  const int64_t M = A.rows, N = B.rows, K = A.k;
+  TcPlan plans[kTcCandidates];
+  size_t part_elems = 0;
+  for (int i = 0; i < kTcCandidates; ++i) {
+    plans[i] = tc_plan(M, N, K, imode, absmax != nullptr, i);
+    part_elems = std::max(part_elems, plans[i].part_elems());
+  }
+  // the split-K buffer fits every candidate, so the workspace size does not
+  // depend on what the tuner picks
+  Scope scope(c);
+  float* part = part_elems ? c.alloc<float>(part_elems) : nullptr;
+  if (c.sizing()) return;
+  CTM_REQUIRE(imode == 1 || (A.lo != nullptr && B.lo != nullptr), CTM_ERR_INVALID,
+              "tc_gemm: 3xBF16 needs lo parts");
+  const TuneKey key{M, N, K, imode, absmax != nullptr ? 1 : 0, out.nd,
+                    out.nd ? int(out.d[0].kind) : -1, out.name ? out.name : ""};
+  int choice = 0;
+  bool tune = false;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) choice = it->second.choice;
+    else tune = g_tuning;
+  }
+  if (tune) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CTM_CUDA(cudaStreamIsCapturing(c.stream, &cs));
+    tune = cs == cudaStreamCaptureStatusNone;
+  }
+  if (!tune) {
+    tc_launch(c, A, B, imode, out, absmax, plans[choice], part);
+    return;
+  }
+  TuneEntry e;
+  double best = 1e30;
+  cudaEvent_t ev0, ev1;
+  CTM_CUDA(cudaEventCreate(&ev0));
+  CTM_CUDA(cudaEventCreate(&ev1));
+  for (int i = 0; i < kTcCandidates; ++i) {
+    bool dup = false;  // identical to an earlier candidate
+    for (int j = 0; j < i; ++j)
+      dup = dup || (plans[j].ntile == plans[i].ntile && plans[j].splits == plans[i].splits);
+    if (dup) continue;
+    float ms = 1e30f;
+    for (int rep = 0; rep < 2; ++rep) {  // the first run also loads the kernel's attributes
+      CTM_CUDA(cudaEventRecord(ev0, c.stream));
+      tc_launch(c, A, B, imode, out, absmax, plans[i], part);
+      CTM_CUDA(cudaEventRecord(ev1, c.stream));
+      CTM_CUDA(cudaEventSynchronize(ev1));
+      float t = 0.f;
+      CTM_CUDA(cudaEventElapsedTime(&t, ev0, ev1));
+      ms = std::min(ms, t);
+    }
+    if (i == 0) e.default_ms = ms;
+    if (ms < best) {
+      best = ms;
+      e.choice = i;
+    }
+  }
+  CTM_CUDA(cudaEventDestroy(ev0));
+  CTM_CUDA(cudaEventDestroy(ev1));
+  e.best_ms = best;
+  tc_launch(c, A, B, imode, out, absmax, plans[e.choice], part);
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = e;
 }
 
 }  // namespace
@@ -1203,3 +1317,41 @@ void tc_gemm_absmax(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode,
 }
 
 }  // namespace ctm
+
+// ---------------------------------------------------------------- C ABI of the autotuner
+using namespace ctm;
+
+extern "C" {
+
+int ctm_autotune(int32_t enable, int32_t* entries) {
+  return guarded([&] {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    if (enable >= 0) g_tuning = enable != 0;
+    if (enable == -2) g_tune.clear();
+    if (entries != nullptr) *entries = static_cast<int32_t>(g_tune.size());
+  });
+}
+
+int ctm_autotune_entry(int32_t i, int64_t* mnk, int32_t* mode_choice, double* best_ms,
+                       double* default_ms) {
+  return guarded([&] {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    CTM_REQUIRE(i >= 0 && i < static_cast<int32_t>(g_tune.size()), CTM_ERR_INVALID,
+                "bad autotune entry");
+    auto it = g_tune.begin();
+    std::advance(it, i);
+    if (mnk != nullptr) {
+      mnk[0] = it->first.M;
+      mnk[1] = it->first.N;
+      mnk[2] = it->first.K;
+    }
+    if (mode_choice != nullptr) {
+      mode_choice[0] = it->first.mode;
+      mode_choice[1] = it->second.choice;
+    }
+    if (best_ms != nullptr) *best_ms = it->second.best_ms;
+    if (default_ms != nullptr) *default_ms = it->second.default_ms;
+  });
+}
+
+}  // extern "C"

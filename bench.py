@@ -38,10 +38,13 @@ WORKLOAD = {"workload": f"heisenberg_2x2_D{D}_chi{CHI}_rsvd_os{OVERSAMPLING}_nit
             "D": D, "chi": CHI, "phys": PHYS, "projectors": "half-system", "svd_type": "rsvd",
             "seed": SEED, "iterations_before_timing": GROW_ITERS}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of a
-# kernel class at this workload, from `ncu --metrics dram__bytes_read.sum,
-# dram__bytes_write.sum --clock-control none` on `bench.py --profile-case`
-# (one launch per class); classes without a capture report null.
-NCU_DRAM_BYTES = {}
+# kernel class at this workload, from one ncu capture of `bench.py
+# --profile-case --steps 1` (`ncu --set full --clock-control none -k
+# regex:tc_gemm_persistent -s 1 -c 1`: 125.2 MB read + 61.3 MB written);
+# classes without a capture report null.
+NCU_DRAM_BYTES = {
+    "tc_gemm_persistent_kernel (enlarged corner, double-layer step)": 125.186560e6 + 61.255424e6,
+}
 
 
 def move_flops(D, chi, q, d=2, ny=2, niter=2):
@@ -310,6 +313,7 @@ def run_gb300(args, rank, world, local_rank):
 
     gb = package()
     gb.build()
+    gb._abi.set_mixed_contraction(args.contraction)
     dev = torch.device("cuda", local_rank)
     torch.cuda.set_device(dev)
     stream = torch.cuda.current_stream(dev)
@@ -344,8 +348,20 @@ def run_gb300(args, rank, world, local_rank):
         mv.move_pair(state, kind, i1, i2)
         pos += 1
 
+    # the tile-plan autotuner, when asked for, tunes the saturated shapes in
+    # the warm-up pairs (tuning synchronises) and is off in the timed region
+    if args.autotune:
+        gb.autotune(True, reset=True)
     for _ in range(max(1, -(-args.warmup // 2))):
         next_pair(mover, st)
+    tune_line = None
+    if args.autotune:
+        gb.autotune(False)
+        table = gb.autotune_table()
+        tune_line = {"shapes": len(table),
+                     "changed": sum(1 for r in table if r["choice"] != 0),
+                     "default_ms": round(sum(r["default_ms"] for r in table), 4),
+                     "tuned_ms": round(sum(r["best_ms"] for r in table), 4)}
     n_pairs = max(1, -(-args.steps // 2))
     steps = 2 * n_pairs
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -483,6 +499,7 @@ def run_gb300(args, rank, world, local_rank):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if args.precision == "fp64" else "bf16/3xbf16+f32+f64",
             "precision": args.precision,
+            "contraction": args.contraction,
             "data": "synthetic",
             "config": dict(WORKLOAD),
             "l2": "256 MiB flush between timed moves; quarter tensors 215 MB each",
@@ -507,6 +524,7 @@ def run_gb300(args, rank, world, local_rank):
             "gpu_launches": int(launches),
             "execution": "eager, left/right and up/down pairs of moves",
             "graph": graph_line,
+            "autotune": tune_line,
             "qr_fallbacks_in_timed_moves": qr_fallbacks,
             "grow_seconds": t_grow,
             "comparison": compare,
@@ -587,13 +605,32 @@ def batched_sweep(gb, dev, iterations=3):
     torch.cuda.synchronize(dev)
     bat_s = a.elapsed_time(e) / 1e3
     moves = b.moves_per_iteration()
+    truncated = b.truncated()
+    # the same sweep with the mixed-precision contractions (FP64 spectrum,
+    # truncation and scaling), from the grown states
+    import dataclasses
+    mstates = [clone_state(gb, st) for st in states]
+    del b
+    bm = gb.BatchedCTMRG(mstates, dataclasses.replace(cfg, precision="mixed"))
+    bm.capture(warmup=1)
+    bm.replay(1)
+    torch.cuda.synchronize(dev)
+    a.record()
+    bm.replay(iterations)
+    e.record()
+    torch.cuda.synchronize(dev)
+    mix_s = a.elapsed_time(e) / 1e3
+    mixed_truncated = bm.truncated()
+    del bm, mstates
     return {"instances": len(inst), "D": [x[1] for x in inst], "chi": [x[2] for x in inst],
             "hx_range": [min(x[0] for x in inst), max(x[0] for x in inst)],
             "storage": "float32", "projectors": "fp64 half-system rSVD os=2 niter=2",
             "batched_moves_per_s": moves * iterations / bat_s,
             "sequential_moves_per_s": moves / seq_s,
             "speedup": (moves * iterations / bat_s) / (moves / seq_s),
-            "truncated_below_chi": b.truncated(),
+            "truncated_below_chi": truncated,
+            "batched_mixed_moves_per_s": moves * iterations / mix_s,
+            "mixed_truncated_below_chi": mixed_truncated,
             "grow_seconds": grow_s, "capture_seconds": capture_s,
             "timing": f"CUDA events; batched: {iterations} graph replays of one iteration of "
                       "all instances; sequential: one eager iteration per instance"}
@@ -906,6 +943,7 @@ def run_profile_case(args):
 
     gb = package()
     gb.build()
+    gb._abi.set_mixed_contraction(args.contraction)
     dev = torch.device("cuda", 0)
     g = torch.Generator().manual_seed(SEED)
     st = gb.IpepsState(2, 2, {"phys": PHYS, "bond": D, "chi": CHI}, dev)
@@ -928,9 +966,12 @@ def run_profile_case(args):
     mover.concurrent = False
     for _ in range(args.steps):
         mover.move(st, 0, 0)
+    if args.profile_measure:
+        # one mixed measurement (site RDMs in FP32, bond RDMs on tensor cores)
+        gb.measure(st, gb.HeisenbergModel(1.0, device=dev), verbose=False, precision="mixed")
     torch.cuda.synchronize(dev)
     return {"profile_case": "left move on a synthetic chi-saturated state", "moves": args.steps,
-            "device_status": gb._abi.device_status()}
+            "measure": bool(args.profile_measure), "device_status": gb._abi.device_status()}
 
 
 def main():
@@ -944,6 +985,12 @@ def main():
                     help="skip the replays of one CUDA-graph-captured CTMRG iteration")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the FP64-path timing and the one-move accuracy check")
+    ap.add_argument("--contraction", choices=["auto", "double-layer", "one-layer"],
+                    default="auto", help="form of the mixed path's site-tensor steps")
+    ap.add_argument("--profile-measure", action="store_true",
+                    help="with --profile-case: one mixed-precision measure() after the moves")
+    ap.add_argument("--autotune", action="store_true",
+                    help="tune the tensor-core GEMM tile plans in the warm-up pairs")
     ap.add_argument("--no-large", action="store_true",
                     help="skip the D=8, chi=256 instance")
     ap.add_argument("--no-measure", action="store_true",

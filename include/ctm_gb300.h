@@ -107,6 +107,23 @@ const char* ctm_last_error(void);
  * the reference (its einsums are always one-layer). */
 int ctm_set_mixed_contraction(int32_t form, int32_t* previous);
 
+/* Tile-plan autotuner of the tensor-core GEMMs.  enable = 1 turns tuning on,
+ * 0 off, -1 leaves it, -2 also forgets every tuned shape.  While it is on,
+ * the first call outside stream capture of each new product shape (M, N, K,
+ * passes, epilogue) times the candidate plans (N tiles of 256 or 128
+ * columns, K split to fill the SMs or not) with CUDA events, which
+ * synchronises that call's stream, and keeps the fastest for later calls,
+ * captured ones included.  Results do not depend on the plan up to FP32
+ * summation order inside a K split.  *entries (if not NULL) receives the
+ * number of tuned shapes.  No counterpart in the reference. */
+int ctm_autotune(int32_t enable, int32_t* entries);
+
+/* Tuned shape i (0 <= i < entries): mnk[3] = M, N, K; mode_choice[2] =
+ * passes (1 = BF16, 3 = 3xBF16) and the chosen candidate (bit 0: 128-wide
+ * N tiles, bit 1: no K split); the chosen and the default plan's times. */
+int ctm_autotune_entry(int32_t i, int64_t* mnk, int32_t* mode_choice, double* best_ms,
+                       double* default_ms);
+
 /* Synchronizes `stream`, stores and clears the device-side failure flags of
  * the current device: bit 0 = a factorization failed and its fallback ran,
  * bit 1 = an iteration limit or a bounded wait expired.  No counterpart in
@@ -193,6 +210,30 @@ int ctm_renormalize_boundary(const ctm_site_f64* s1, int64_t D, int64_t d, int32
                              double* Cout1, double* Cout2, double* Eout,
                              int32_t precision, void* ws, size_t* ws_bytes,
                              ctm_stream_t stream);
+
+/* One directional move, or a left/right or up/down pair of moves (which
+ * read and write disjoint tensors), of a whole nx x ny unit cell in one call:
+ * the projector pairs of every row (column) of the move(s), then the boundary
+ * renormalization of every row, all on `stream`.
+ * sites: nx * ny sites, site (x, y) at index x * ny + y.  moves: nmoves
+ * (direction k, index) pairs (k = 0 left, 1 up, 2 right, 3 down; index = the
+ * column of a left/right move, the row of an up/down move).  Rows of a move:
+ * ny for left/right, nx for up/down; row t (over all moves, in order) takes
+ * omegas[t] (n x q, as ctm_calculate_projectors; ignored for CTM_SVD_FULL)
+ * and writes chi_new[t] (device int64) and the three new tensors of its
+ * renormalised site: out[3t] = C[(3+k)%4] (a x cap), out[3t+1] = C[k]
+ * (cap x c), out[3t+2] = E[(3+k)%4] (cap x cap x D x D), all with the fixed
+ * width cap = min(chi, q) (rSVD) or min(chi, n) (full rank) and zero beyond
+ * the truncation count, so that every size is known before the call.  The
+ * site tensors are only read; the caller puts the new ones in place.
+ * Reference: DirectionalMover.left/up/right/down_move and
+ * calculate_*_projectors / renormalize_boundary,
+ * acetn/renormalization/directional_mover.py:23-181, 273-366 (the pair:
+ * left_right_move_dist / up_down_move_dist, :183-271). */
+int ctm_move_batched(const ctm_site_f64* sites, int32_t nx, int32_t ny, int64_t D, int64_t d,
+                     const int32_t* moves, int32_t nmoves, const ctm_ctmrg_opts* opts,
+                     const double* const* omegas, double* const* out, int64_t* chi_new,
+                     void* ws, size_t* ws_bytes, ctm_stream_t stream);
 
 /* Site reduced density matrix (d x d), not trace-normalised.  precision:
  * CTM_PREC_FP64, or CTM_PREC_MIXED (the same contraction chain in FP32 FMAs
