@@ -260,10 +260,9 @@ def autotune(enable=True, reset=False):
     (``reset`` also forgets the tuned shapes); returns how many shapes are
     tuned.  Tuning happens on the first eager call of each product shape."""
     n = c_i32(0)
-    code = -2 if reset else (1 if enable else 0)
-    check(load().ctm_autotune(code, ctypes.byref(n)), "ctm_autotune")
-    if reset and enable:
-        check(load().ctm_autotune(1, ctypes.byref(n)), "ctm_autotune")
+    if reset:
+        check(load().ctm_autotune(-2, None), "ctm_autotune")
+    check(load().ctm_autotune(1 if enable else 0, ctypes.byref(n)), "ctm_autotune")
     return n.value
 
 

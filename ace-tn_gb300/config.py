@@ -6,7 +6,8 @@ documented in docs/source/input_settings.rst:45-54) and adds two fields:
 * ``backend``   -- "gb300" selects this library (the reference keeps "torch").
 * ``precision`` -- "fp64": every product in FP64, the drop-in path;
                    "mixed": tensor-core range finder and split-precision
-                   products feeding the projectors (half-system rSVD only).
+                   products feeding the projectors (half- and full-system,
+                   rSVD; full-rank: split-precision products, FP64 SVD).
 * ``mixed_svd_floor`` -- mixed precision only: singular values below this
                    fraction of the largest are dropped in addition to
                    ``svd_cutoff`` (the reference's 1e-12, which the FP64 path

@@ -90,6 +90,28 @@ namespace {
 
 View mat(const double* p, int64_t r, int64_t c) { return View(p, {r, c}); }
 
+// C (M x N) = A (M x K) B (K x N), row-major FP64: the FP64 GETT, or (mixed)
+// tcgen05 3xBF16 products of the split operands with FP32 accumulation.
+void product(Ctx& c, const double* A, const double* B, double* C, int64_t M, int64_t N,
+             int64_t K, int prec) {
+  if (prec != CTM_PREC_MIXED) {
+    einsum(c, "ik,kj->ij", mat(A, M, K), mat(B, K, N), mat(C, M, N));
+    return;
+  }
+  const int64_t ld = tc_ld(K);
+  Scope scope(c);
+  bf16* ah = c.alloc<bf16>(size_t(M) * ld);
+  bf16* al = c.alloc<bf16>(size_t(M) * ld);
+  bf16* bh = c.alloc<bf16>(size_t(N) * ld);
+  bf16* bl = c.alloc<bf16>(size_t(N) * ld);
+  split_bf16(c, A, M, K, K, false, ah, al, ld);
+  split_bf16(c, B, K, N, N, true, bh, bl, ld);
+  TcOut out;
+  out.add(TcKind::kF64, C, TcLayout::rows(M, N, N));
+  out.name = "full-rank product";
+  tc_gemm(c, TcOperand{ah, al, M, K, ld}, TcOperand{bh, bl, N, K, ld}, TcMode::kBf16x3, out);
+}
+
 // y (f.rows x q) = f @ x (f.cols x q)
 void apply(Ctx& c, const Factor& f, const double* x, double* y, int64_t q, int prec) {
   (void)prec;
@@ -282,14 +304,26 @@ void calculate_projectors(Ctx& c, const Site* S[4], int k, const ctm_ctmrg_opts&
   const ProjDims pd = projector_dims(S, k, o);
   const int prec = o.precision;
   CTM_REQUIRE(prec == CTM_PREC_FP64 || prec == CTM_PREC_MIXED, CTM_ERR_INVALID, "bad precision");
+  // here the mixed precision is the full-rank form: quarter tensors and the
+  // products that feed the SVD in 3xBF16, the SVD and the projector products
+  // in FP64, singular values below the mixed floor dropped (the spectrum of
+  // the 3xBF16 products is noise there)
+  CTM_REQUIRE(prec == CTM_PREC_FP64 || o.svd_type == CTM_SVD_FULL, CTM_ERR_INVALID,
+              "mixed randomized-SVD projectors run in calculate_projectors_mixed");
+  ctm_ctmrg_opts om = o;
+  if (prec == CTM_PREC_MIXED) om.svd_cutoff = std::max({o.svd_cutoff, o.mixed_floor, 1e-8});
+  auto quarter = [&](const Site& site, int kk, double* Q, int64_t* qs) {
+    if (prec == CTM_PREC_MIXED) quarter_tensor_mixed_f64(c, site, kk, Q);
+    else quarter_tensor(c, site, kk, Q, qs);
+  };
   Scope scope(c);
   int64_t sh1[6], sh4[6], r1, c1, r4, c4;
   quarter_dims(*S[0], k, r1, c1, sh1);
   quarter_dims(*S[3], k + 3, r4, c4, sh4);
   double* Q1 = c.alloc<double>(size_t(r1) * c1);
   double* Q4 = c.alloc<double>(size_t(r4) * c4);
-  quarter_tensor(c, *S[0], k, Q1, sh1);
-  quarter_tensor(c, *S[3], k + 3, Q4, sh4);
+  quarter(*S[0], k, Q1, sh1);
+  quarter(*S[3], k + 3, Q4, sh4);
   const Factor F1{Q1, r1, c1}, F4{Q4, r4, c4};
   if (o.projectors == CTM_PROJ_HALF) {
     if (o.svd_type == CTM_SVD_RSVD) {
@@ -308,12 +342,12 @@ void calculate_projectors(Ctx& c, const Site* S[4], int k, const ctm_ctmrg_opts&
       double* U = c.alloc<double>(size_t(r1) * r);
       double* s = c.alloc<double>(r);
       double* V = c.alloc<double>(size_t(c4) * r);
-      einsum(c, "ik,kj->ij", mat(Q1, r1, c1), mat(Q4, r4, c4), mat(R, r1, c4));
+      product(c, Q1, Q4, R, r1, c4, c1, prec);
       absmax(c, R, r1 * c4, mx);
       divide_by(c, R, r1 * c4, mx, 0);
       svd_thin(c, R, r1, c4, U, s, V);
-      truncate_and_project(c, U, V, r1, c4, r, s, r, o, F1, nullptr, F4, nullptr, P1, P2, chi_new,
-                           CTM_PREC_FP64);
+      truncate_and_project(c, U, V, r1, c4, r, s, r, om, F1, nullptr, F4, nullptr, P1, P2,
+                           chi_new, CTM_PREC_FP64);
     }
     return;
   }
@@ -323,8 +357,8 @@ void calculate_projectors(Ctx& c, const Site* S[4], int k, const ctm_ctmrg_opts&
   quarter_dims(*S[2], k + 2, r3, c3, sh3);
   double* Q2 = c.alloc<double>(size_t(r2) * c2);
   double* Q3 = c.alloc<double>(size_t(r3) * c3);
-  quarter_tensor(c, *S[1], k + 1, Q2, sh2);
-  quarter_tensor(c, *S[2], k + 2, Q3, sh3);
+  quarter(*S[1], k + 1, Q2, sh2);
+  quarter(*S[2], k + 2, Q3, sh3);
   const Factor F2{Q2, r2, c2}, F3{Q3, r3, c3};
   if (o.svd_type == CTM_SVD_RSVD) {
     const int64_t q = pd.q;
@@ -341,13 +375,13 @@ void calculate_projectors(Ctx& c, const Site* S[4], int k, const ctm_ctmrg_opts&
   double* R2 = c.alloc<double>(size_t(r4) * c3);
   double* Fm = c.alloc<double>(size_t(r2) * c3);
   double* mx = c.alloc<double>(3);
-  einsum(c, "ik,kj->ij", mat(Q2, r2, c2), mat(Q1, r1, c1), mat(R1, r2, c1));
-  einsum(c, "ik,kj->ij", mat(Q4, r4, c4), mat(Q3, r3, c3), mat(R2, r4, c3));
+  product(c, Q2, Q1, R1, r2, c1, c2, prec);
+  product(c, Q4, Q3, R2, r4, c3, c4, prec);
   absmax(c, R1, r2 * c1, mx);
   divide_by(c, R1, r2 * c1, mx, 0);
   absmax(c, R2, r4 * c3, mx + 1);
   divide_by(c, R2, r4 * c3, mx + 1, 0);
-  einsum(c, "ik,kj->ij", mat(R1, r2, c1), mat(R2, r4, c3), mat(Fm, r2, c3));
+  product(c, R1, R2, Fm, r2, c3, c1, prec);
   absmax(c, Fm, r2 * c3, mx + 2);
   divide_by(c, Fm, r2 * c3, mx + 2, 0);
   const int64_t r = std::min(r2, c3);
@@ -355,7 +389,7 @@ void calculate_projectors(Ctx& c, const Site* S[4], int k, const ctm_ctmrg_opts&
   double* s = c.alloc<double>(r);
   double* V = c.alloc<double>(size_t(c3) * r);
   svd_thin(c, Fm, r2, c3, U, s, V);
-  truncate_and_project(c, U, V, r2, c3, r, s, r, o, Factor{R1, r2, c1}, nullptr,
+  truncate_and_project(c, U, V, r2, c3, r, s, r, om, Factor{R1, r2, c1}, nullptr,
                        Factor{R2, r4, c3}, nullptr, P1, P2, chi_new, CTM_PREC_FP64);
 }
 
@@ -761,7 +795,7 @@ int ctm_calculate_projectors(const ctm_site_f64* const* sites, int64_t D, int64_
       CTM_REQUIRE(opts->svd_type != CTM_SVD_RSVD || omega != nullptr, CTM_ERR_INVALID,
                   "omega is NULL for the randomized SVD");
     }
-    if (opts->precision == CTM_PREC_MIXED)
+    if (opts->precision == CTM_PREC_MIXED && opts->svd_type == CTM_SVD_RSVD)
       calculate_projectors_mixed(c, S, k, *opts, omega, P1, P2, chi_new);
     else
       calculate_projectors(c, S, k, *opts, omega, P1, P2, chi_new);
@@ -864,7 +898,7 @@ int ctm_move_batched(const ctm_site_f64* sites, int32_t nx, int32_t ny, int64_t 
     for (size_t t = 0; t < rows.size(); ++t) {
       Row& w = rows[t];
       const double* om = (omegas != nullptr) ? omegas[t] : nullptr;
-      if (o.precision == CTM_PREC_MIXED)
+      if (o.precision == CTM_PREC_MIXED && o.svd_type == CTM_SVD_RSVD)
         calculate_projectors_mixed(c, w.q, w.k, o, om, w.P1, w.P2, chi_new ? chi_new + t : nullptr);
       else
         calculate_projectors(c, w.q, w.k, o, om, w.P1, w.P2, chi_new ? chi_new + t : nullptr);

@@ -191,18 +191,17 @@ __global__ void __launch_bounds__(NT) gett_kernel(const GettArgs<T> p) {
 // Contractions with few outputs and a long K (the last steps of the RDMs:
 // 4 x 4 outputs over chi^2 D^2 terms) would use one 64 x 64 tile of the GETT
 // kernel for a handful of outputs.  Here every CTA takes one K chunk for all
-// Mt x Nt <= 256 outputs (one per thread; Mt + Nt <= 128), staging 32 K
-// indices of both operands in shared memory per step, and writes its partial
-// sums for gett_splitk_reduce.
-constexpr int kSmallK = 32;
-
-template <class T>
+// Mt x Nt <= 256 outputs (one per thread; Mt + Nt <= 128), staging KS K
+// indices of both operands in shared memory per step (128 when the operands
+// have at most 32 rows together, so that each thread has several loads in
+// flight), and writes its partial sums for gett_small_reduce.
+template <class T, int KS>
 __global__ void __launch_bounds__(256) gett_small_kernel(const GettArgs<T> p) {
-  __shared__ int64_t sAm[128], sBn[128], sAk[kSmallK], sBk[kSmallK];
+  __shared__ int64_t sAm[128], sBn[128], sAk[KS], sBk[KS];
   extern __shared__ __align__(16) unsigned char small_smem[];
   const int64_t Mt = p.Mt, Nt = p.Nt;
-  T (*As)[kSmallK + 1] = reinterpret_cast<T (*)[kSmallK + 1]>(small_smem);
-  T (*Bs)[kSmallK + 1] = reinterpret_cast<T (*)[kSmallK + 1]>(small_smem) + Mt;
+  T (*As)[KS + 1] = reinterpret_cast<T (*)[KS + 1]>(small_smem);
+  T (*Bs)[KS + 1] = reinterpret_cast<T (*)[KS + 1]>(small_smem) + Mt;
   const int tid = threadIdx.x;
   for (int i = tid; i < Mt; i += blockDim.x) {
     int64_t a, c;
@@ -219,30 +218,59 @@ __global__ void __launch_bounds__(256) gett_small_kernel(const GettArgs<T> p) {
   const int m = tid / int(Nt), n = tid % int(Nt);
   const bool owner = tid < Mt * Nt;
   T acc = T(0);
-  for (int64_t kb = k0; kb < k1; kb += kSmallK) {
+  for (int64_t kb = k0; kb < k1; kb += KS) {
     __syncthreads();
-    if (tid < kSmallK) {
+    if (tid < KS) {
       int64_t a = 0, b = 0;
       if (kb + tid < k1) decode(p.K, kb + tid, a, b);
       sAk[tid] = a;
       sBk[tid] = b;
     }
     __syncthreads();
-    for (int e = tid; e < Mt * kSmallK; e += blockDim.x) {
-      const int i = e / kSmallK, kk = e % kSmallK;
+#pragma unroll 4
+    for (int e = tid; e < Mt * KS; e += blockDim.x) {
+      const int i = e / KS, kk = e % KS;
       As[i][kk] = (kb + kk < k1) ? p.A[sAm[i] + sAk[kk]] : T(0);
     }
-    for (int e = tid; e < Nt * kSmallK; e += blockDim.x) {
-      const int j = e / kSmallK, kk = e % kSmallK;
+#pragma unroll 4
+    for (int e = tid; e < Nt * KS; e += blockDim.x) {
+      const int j = e / KS, kk = e % KS;
       Bs[j][kk] = (kb + kk < k1) ? p.B[sBn[j] + sBk[kk]] : T(0);
     }
     __syncthreads();
     if (owner) {
 #pragma unroll 8
-      for (int kk = 0; kk < kSmallK; ++kk) acc = fma(As[m][kk], Bs[n][kk], acc);
+      for (int kk = 0; kk < KS; ++kk) acc = fma(As[m][kk], Bs[n][kk], acc);
     }
   }
   if (owner) p.part[(int64_t(blockIdx.x) * Mt + m) * Nt + n] = acc;
+}
+
+// Sums the many partial sums of gett_small_kernel: one CTA per output, each
+// thread a strided subset of the splits, then a fixed-order tree in shared
+// memory (deterministic; a thread per output looping over ~1000 splits was
+// latency-bound at ~100 us).
+template <class T>
+__global__ void __launch_bounds__(256) gett_small_reduce(const GettArgs<T> p) {
+  __shared__ T red[256];
+  const int64_t out = blockIdx.x;
+  const int64_t outs = p.Mt * p.Nt;
+  T s = T(0);
+  for (int t = threadIdx.x; t < p.splitk; t += blockDim.x) s += p.part[t * outs + out];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    int64_t am, cm, bn, cn;
+    decode(p.M, out / p.Nt, am, cm);
+    decode(p.N, out % p.Nt, bn, cn);
+    T* c = p.C + cm + cn;
+    const T v = p.alpha * red[0];
+    *c = (p.beta != T(0)) ? fma(p.beta, *c, v) : v;
+  }
 }
 
 // Sums split-K partial tiles in a fixed order (deterministic) into C.
@@ -254,8 +282,17 @@ __global__ void gett_splitk_reduce(const GettArgs<T> p) {
     const int64_t n = idx % p.Nt;
     const int64_t m = (idx / p.Nt) % p.Mt;
     const int64_t b = idx / (p.Nt * p.Mt);
-    T s = T(0);
-    for (int t = 0; t < p.splitk; ++t) s += p.part[((t * p.bext + b) * p.Mt + m) * p.Nt + n];
+    // two interleaved partial sums in a fixed order: two loads in flight
+    T s0 = T(0), s1 = T(0);
+    const int64_t stride = p.bext * p.Mt * p.Nt;
+    const T* pt = p.part + (b * p.Mt + m) * p.Nt + n;
+    int t = 0;
+    for (; t + 1 < p.splitk; t += 2) {
+      s0 += pt[t * stride];
+      s1 += pt[(t + 1) * stride];
+    }
+    if (t < p.splitk) s0 += pt[t * stride];
+    const T s = s0 + s1;
     int64_t am, cm, bn, cn;
     decode(p.M, m, am, cm);
     decode(p.N, n, bn, cn);
@@ -403,7 +440,8 @@ void einsum_impl(Ctx& c, const char* spec, const ViewT<T>& A, const ViewT<T>& B,
   if (bext == 1 && p.Mt * p.Nt <= 256 && p.Mt + p.Nt <= 128 && p.Kt >= 8192) {
     // few outputs, long K: one K chunk per CTA for all outputs
     int splits = static_cast<int>(std::min<int64_t>(1024, (p.Kt + 511) / 512));
-    p.kchunk = ((p.Kt + splits - 1) / splits + kSmallK - 1) / kSmallK * kSmallK;
+    const int ks = (p.Mt + p.Nt <= 32) ? 128 : 32;
+    p.kchunk = ((p.Kt + splits - 1) / splits + ks - 1) / ks * ks;
     splits = static_cast<int>((p.Kt + p.kchunk - 1) / p.kchunk);
     p.splitk = splits;
     Scope scope(c);
@@ -414,13 +452,14 @@ void einsum_impl(Ctx& c, const char* spec, const ViewT<T>& A, const ViewT<T>& B,
       KernelTimer timer(c.stream, sizeof(T) == 8 ? kTagGettF64 : kTagGettF32, flops);
       KernelTimer kt(c.stream, sizeof(T) == 8 ? "gett_small_kernel<double>"
                                              : "gett_small_kernel<float>", kUnitFlop, flops);
-      const size_t smem = size_t(p.Mt + p.Nt) * (kSmallK + 1) * sizeof(T);
-      gett_small_kernel<T><<<splits, 256, smem, c.stream>>>(p);
+      const size_t smem = size_t(p.Mt + p.Nt) * (ks + 1) * sizeof(T);
+      if (ks == 128) gett_small_kernel<T, 128><<<splits, 256, smem, c.stream>>>(p);
+      else gett_small_kernel<T, 32><<<splits, 256, smem, c.stream>>>(p);
       CTM_LAUNCH_CHECK();
     }
-    KernelTimer kt(c.stream, "gett_splitk_reduce", kUnitByte,
+    KernelTimer kt(c.stream, "gett_small_reduce", kUnitByte,
                    double(sizeof(T)) * (splits + 1.0) * p.Mt * p.Nt);
-    gett_splitk_reduce<T><<<grid_for(p.Mt * p.Nt, 256), 256, 0, c.stream>>>(p);
+    gett_small_reduce<T><<<unsigned(p.Mt * p.Nt), 256, 0, c.stream>>>(p);
     CTM_LAUNCH_CHECK();
     return;
   }

@@ -230,7 +230,13 @@ __device__ __forceinline__ void chol_diag_block(const T* W, int ld, int J, int j
     const bool ok = t < jb && dt > T(0);
     fail = fail || (t < jb && !ok);
     s_d[t] = ok ? dt : T(0);
-    const T rinv = ok ? T(1) / dt : T(0);
+    // FP32: the hardware reciprocal (about 1 ulp) instead of the IEEE
+    // division sequence on this serial chain; FP64 keeps the division
+    T rinv = T(0);
+    if (ok) {
+      if constexpr (sizeof(T) == 4) rinv = __fdividef(1.f, dt);
+      else rinv = T(1) / dt;
+    }
     s_rd[t] = rinv;
     T m[kCholNb];
 #pragma unroll
@@ -589,11 +595,11 @@ __global__ void __launch_bounds__(kCh > 0 ? 128 * kCh : 1024) jacobi_onesided_f3
 }
 
 // One plane rotation of the one-sided Jacobi on a pair of rows (ra, rb) of
-// kCh float4 chunks per thread, 8 threads per pair (thread sub owns chunks
-// sub + 8 m); the accumulated-rotation rows follow at ra + ld, rb + ld.
-// Every lane of the warp must call it (full-mask shuffles).  Returns whether
-// the pair was rotated.
-template <int kCh>
+// kCh float4 chunks per thread, kTP threads per pair (thread sub owns chunks
+// sub + kTP m); the accumulated-rotation rows follow at ra + ld, rb + ld.
+// Every lane of the pair's group must call it (group-mask shuffles).
+// Returns whether the pair was rotated.
+template <int kCh, int kTP>
 __device__ __forceinline__ bool jacobi_rotate_pair(float* ra, float* rb, int ld, int sub,
                                                    float tol) {
   float4* a = reinterpret_cast<float4*>(ra) + sub;
@@ -604,13 +610,13 @@ __device__ __forceinline__ bool jacobi_rotate_pair(float* ra, float* rb, int ld,
   float4 xa[kCh], xb[kCh], u[kCh], v[kCh];
 #pragma unroll
   for (int m = 0; m < kCh; ++m) {
-    xa[m] = a[8 * m];
-    xb[m] = b[8 * m];
+    xa[m] = a[kTP * m];
+    xb[m] = b[kTP * m];
   }
 #pragma unroll
   for (int m = 0; m < kCh; ++m) {
-    u[m] = ja[8 * m];
-    v[m] = jb[8 * m];
+    u[m] = ja[kTP * m];
+    v[m] = jb[kTP * m];
   }
   // dot products in paired FMAs: four partial sums per quantity
   float2 al2a = make_float2(0.f, 0.f), al2b = al2a, be2a = al2a, be2b = al2a, ga2a = al2a,
@@ -629,10 +635,14 @@ __device__ __forceinline__ bool jacobi_rotate_pair(float* ra, float* rb, int ld,
   float al = (al2a.x + al2a.y) + (al2b.x + al2b.y);
   float be = (be2a.x + be2a.y) + (be2b.x + be2b.y);
   float ga = (ga2a.x + ga2a.y) + (ga2b.x + ga2b.y);
-  for (int o = 4; o > 0; o >>= 1) {
-    al += __shfl_xor_sync(0xffffffffu, al, o);
-    be += __shfl_xor_sync(0xffffffffu, be, o);
-    ga += __shfl_xor_sync(0xffffffffu, ga, o);
+  // the shuffles stay inside the pair's group of kTP lanes (its mask): the
+  // groups of a warp beyond the last pair may skip the call
+  const unsigned gmask =
+      kTP >= 32 ? 0xffffffffu : (((1u << kTP) - 1u) << ((threadIdx.x & 31) & ~(kTP - 1)));
+  for (int o = kTP / 2; o > 0; o >>= 1) {
+    al += __shfl_xor_sync(gmask, al, o);
+    be += __shfl_xor_sync(gmask, be, o);
+    ga += __shfl_xor_sync(gmask, ga, o);
   }
   // |ga| > tol sqrt(al be) without square roots
   if (al == 0.f || be == 0.f || !(ga * ga > (tol * tol * al) * be)) return false;
@@ -658,16 +668,17 @@ __device__ __forceinline__ bool jacobi_rotate_pair(float* ra, float* rb, int ld,
   };
 #pragma unroll
   for (int m = 0; m < kCh; ++m) {
-    rot(a + 8 * m, b + 8 * m, xa[m], xb[m]);
-    rot(ja + 8 * m, jb + 8 * m, u[m], v[m]);
+    rot(a + kTP * m, b + kTP * m, xa[m], xb[m]);
+    rot(ja + kTP * m, jb + kTP * m, u[m], v[m]);
   }
   return true;
 }
 
 // Block one-sided Jacobi on a cluster of P CTAs (same rotations and
 // convergence test as jacobi_onesided_f32_kernel, another cyclic order).
-// The rows (padded with zero rows to 2 P b, b a multiple of 4) form 2 P
-// blocks of b rows; CTA k holds the blocks at tournament positions k ("top")
+// kTP threads per pair (b groups; the CTA's threads are rounded up to whole
+// warps, the extra groups idle).  The rows (padded with zero rows to 2 P b,
+// b even) form 2 P blocks of b rows; CTA k holds the blocks at tournament positions k ("top")
 // and 2P-1-k ("bottom") in shared memory, each row stored as ld floats of Mc
 // followed by ld floats of the accumulated rotations J.  A sweep is 2P-1
 // block rounds of the circle method (position 0 fixed, the others advance by
@@ -681,7 +692,7 @@ __device__ __forceinline__ bool jacobi_rotate_pair(float* ra, float* rb, int ld,
 // sweep loop ends when no CTA rotated in a sweep: every CTA reads all CTAs'
 // per-sweep flags after the same cluster barrier, so all take the same
 // decision and arrive at the same barriers.
-template <int kCh>
+template <int kCh, int kTP>
 __global__ void __launch_bounds__(256) jacobi_cluster_f32_kernel(const float* Mc_g, int q, int b,
                                                                  float* Jc_g, float* norms,
                                                                  int max_sweeps, float tol,
@@ -692,13 +703,13 @@ __global__ void __launch_bounds__(256) jacobi_cluster_f32_kernel(const float* Mc
   const int k = int(cluster.block_rank());
   extern __shared__ __align__(16) float jcl_smem[];
   __shared__ int s_rot[64];
-  constexpr int ld = 32 * kCh;
+  constexpr int ld = 4 * kTP * kCh;
   constexpr int RS = 2 * ld;  // row stride: Mc, then J
   const int blk = b * RS;     // floats per block
   float* cur = jcl_smem;      // top block, then bottom block
   float* nxt = jcl_smem + 2 * blk;
   const int tid = threadIdx.x, nth = blockDim.x;
-  const int g = tid >> 3, sub = tid & 7;
+  const int g = tid / kTP, sub = tid % kTP;
   for (int half = 0; half < 2; ++half) {
     const int beta = half == 0 ? k : 2 * P - 1 - k;
     float* base = cur + half * blk;
@@ -732,7 +743,7 @@ __global__ void __launch_bounds__(256) jacobi_cluster_f32_kernel(const float* Mc
           ia = g * RS;
           ib = blk + ((g + sft) % b) * RS;
         }
-        rotated |= jacobi_rotate_pair<kCh>(cur + ia, cur + ib, ld, sub, tol);
+        if (g < b) rotated |= jacobi_rotate_pair<kCh, kTP>(cur + ia, cur + ib, ld, sub, tol);
         __syncthreads();
       }
       // move the blocks: position p -> p + 1 (2P-1 -> 1, 0 stays)
@@ -1182,24 +1193,28 @@ __device__ __forceinline__ void add_to(float4& a, const float4& b) {
 }
 __device__ __forceinline__ void add_to(float& a, const float& b) { a += b; }
 
-// G = sum over slabs of part, in slab order.  Each CTA: 64 entries (float4
-// entries when kVec, i.e. q*q % 4 == 0) x 4 slab ranges, combined through
-// shared memory in range order.
+// G = sum over slabs of part, in a fixed order.  Each CTA: 16 entries
+// (float4 entries when kVec, i.e. q*q % 4 == 0) x 16 slab ranges (about 9
+// slabs each at 149 slabs), combined through shared memory in range order:
+// 400 CTAs at q = 160, each thread a handful of independent loads (64
+// entries x 4 ranges left 100 CTAs waiting on ~37 dependent loads each).
+constexpr int kReduceEntries = 16, kReduceRanges = 16;
+
 template <bool kVec>
 __global__ void __launch_bounds__(256) slab_reduce_kernel(const float* __restrict__ part,
                                                           int nblk, int qq,
                                                           float* __restrict__ G) {
   using V = typename std::conditional<kVec, float4, float>::type;
-  __shared__ V s[4][64];
-  const int t = threadIdx.x & 63, grp = threadIdx.x >> 6;
+  __shared__ V s[kReduceRanges][kReduceEntries];
+  const int t = threadIdx.x % kReduceEntries, grp = threadIdx.x / kReduceEntries;
   const int ne = kVec ? qq / 4 : qq;
-  const int e = blockIdx.x * 64 + t;
-  const int b0 = grp * nblk / 4, b1 = (grp + 1) * nblk / 4;
+  const int e = blockIdx.x * kReduceEntries + t;
+  const int b0 = grp * nblk / kReduceRanges, b1 = (grp + 1) * nblk / kReduceRanges;
   V acc;
   memset(&acc, 0, sizeof(V));
   if (e < ne) {
     const V* pv = reinterpret_cast<const V*>(part);
-#pragma unroll 8
+#pragma unroll 4
     for (int b = b0; b < b1; ++b) add_to(acc, pv[size_t(b) * ne + e]);
   }
   s[grp][t] = acc;
@@ -1207,7 +1222,7 @@ __global__ void __launch_bounds__(256) slab_reduce_kernel(const float* __restric
   if (grp == 0 && e < ne) {
     V r = s[0][t];
 #pragma unroll
-    for (int k = 1; k < 4; ++k) add_to(r, s[k][t]);
+    for (int k = 1; k < kReduceRanges; ++k) add_to(r, s[k][t]);
     reinterpret_cast<V*>(G)[e] = r;
   }
 }
@@ -1266,10 +1281,12 @@ void slab_gram(Ctx& c, const float* Y, int64_t n, int64_t q, const float* Lt, fl
   CTM_LAUNCH_CHECK();
   const int qq = int(q * q);
   KernelTimer kt(c.stream, "slab_reduce_kernel", kUnitByte, 4.0 * (double(nblk) + 1.0) * qq);
+  const int ne = qq % 4 == 0 ? qq / 4 : qq;
+  const unsigned grid = unsigned((ne + kReduceEntries - 1) / kReduceEntries);
   if (qq % 4 == 0)
-    slab_reduce_kernel<true><<<unsigned((qq / 4 + 63) / 64), 256, 0, c.stream>>>(part, nblk, qq, G);
+    slab_reduce_kernel<true><<<grid, kReduceEntries * kReduceRanges, 0, c.stream>>>(part, nblk, qq, G);
   else
-    slab_reduce_kernel<false><<<unsigned((qq + 63) / 64), 256, 0, c.stream>>>(part, nblk, qq, G);
+    slab_reduce_kernel<false><<<grid, kReduceEntries * kReduceRanges, 0, c.stream>>>(part, nblk, qq, G);
   CTM_LAUNCH_CHECK();
 }
 
@@ -1503,16 +1520,19 @@ void jacobi_left_singular(Ctx& c, const float* Mc, int64_t q, double* Ub, double
   float* Wg = jac_smem ? nullptr : c.alloc<float>(size_t(2) * q * jacobi_ld(int(q)));
   const int64_t pp = q + (q & 1);
   if (c.sizing()) return;
-  // q >= 96: the block Jacobi on a cluster of kJacobiCluster CTAs (rows
-  // padded to a multiple of 8 kJacobiCluster: b a multiple of 4, 8 b threads
-  // per CTA) when its four blocks of b rows fit in shared memory.  8 CTAs:
-  // 0.90 ms against 0.95 ms with 4 at q = 160 (16 blocks of 12 rows, the
-  // rows padded to 192)
-  constexpr int kJacobiCluster = 8;
+  // q >= 96: the block Jacobi on a cluster of kJacobiCluster CTAs with
+  // kPairThreads threads per pair (rows padded to a multiple of 4
+  // kJacobiCluster: b even), when its four blocks of b rows fit in shared
+  // memory.  At q = 160: 16 blocks of 10 rows, no padding rows, 159 pair
+  // rounds per sweep (blocks of 12 rows, a multiple of 4 so that 8 b threads
+  // filled whole warps, padded q to 192 and took 191 rounds); 8 threads per
+  // pair measured faster per round than 16 (one shuffle level less)
+  constexpr int kJacobiCluster = 8, kPairThreads = 8;
   const int P = kJacobiCluster;
-  const int qp = int((q + 8 * P - 1) / (8 * P) * (8 * P));
+  const int qp = int((q + 4 * P - 1) / (4 * P) * (4 * P));
   const int b = qp / (2 * P);
-  const int ldj = jacobi_ld(int(q));
+  const int ldj = int((q + 4 * kPairThreads - 1) / (4 * kPairThreads) * (4 * kPairThreads));
+  const unsigned jthreads_c = unsigned((kPairThreads * b + 31) / 32 * 32);
   const size_t smem = size_t(4) * b * 2 * ldj * sizeof(float);
   if (q >= 96 && ldj <= 256 && smem <= size_t(227) * 1024) {
     auto launch = [&](auto kern) {
@@ -1520,7 +1540,7 @@ void jacobi_left_singular(Ctx& c, const float* Mc, int64_t q, double* Ub, double
       KernelTimer kt(c.stream, "jacobi_cluster_f32_kernel", kUnitFlop, 0.0);
       cudaLaunchConfig_t cfg{};
       cfg.gridDim = dim3(P);
-      cfg.blockDim = dim3(8 * b);
+      cfg.blockDim = dim3(jthreads_c);
       cfg.dynamicSmemBytes = smem;
       cfg.stream = c.stream;
       cudaLaunchAttribute attr[1];
@@ -1533,13 +1553,13 @@ void jacobi_left_singular(Ctx& c, const float* Mc, int64_t q, double* Ub, double
       CTM_CUDA(cudaLaunchKernelEx(&cfg, kern, static_cast<const float*>(Mc), int(q), b, Jc, norms,
                                   40, 4e-6f, status_flags(c)));
     };
-    switch (ldj / 32) {
-      case 3: launch(jacobi_cluster_f32_kernel<3>); break;
-      case 4: launch(jacobi_cluster_f32_kernel<4>); break;
-      case 5: launch(jacobi_cluster_f32_kernel<5>); break;
-      case 6: launch(jacobi_cluster_f32_kernel<6>); break;
-      case 7: launch(jacobi_cluster_f32_kernel<7>); break;
-      default: launch(jacobi_cluster_f32_kernel<8>); break;
+    switch (ldj / (4 * kPairThreads)) {
+      case 3: launch(jacobi_cluster_f32_kernel<3, kPairThreads>); break;
+      case 4: launch(jacobi_cluster_f32_kernel<4, kPairThreads>); break;
+      case 5: launch(jacobi_cluster_f32_kernel<5, kPairThreads>); break;
+      case 6: launch(jacobi_cluster_f32_kernel<6, kPairThreads>); break;
+      case 7: launch(jacobi_cluster_f32_kernel<7, kPairThreads>); break;
+      default: launch(jacobi_cluster_f32_kernel<8, kPairThreads>); break;
     }
     CTM_LAUNCH_CHECK();
     sort_singular_kernel<<<1, 256, 0, c.stream>>>(Jc, norms, int(q), Ub, S, inv_s);

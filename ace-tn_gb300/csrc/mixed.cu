@@ -369,7 +369,7 @@ TcOperand yt_operand_f32(Ctx& c, const float* Y, int64_t n, int64_t q, int64_t l
 
 // C = A @ B^T written as the next operand (C^T, BF16 hi [+ lo]).
 TcOperand gemm_to_operand(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode mode, bool lo,
-                          const char* name = nullptr) {
+                          const char* name = nullptr, const double* inv_scale = nullptr) {
   const int64_t M = A.rows, N = B.rows;
   const int64_t ld = tc_ld(M);
   bf16* hi = c.alloc<bf16>(size_t(N) * ld);
@@ -378,6 +378,7 @@ TcOperand gemm_to_operand(Ctx& c, const TcOperand& A, const TcOperand& B, TcMode
   out.add(TcKind::kBf16Hi, hi, TcLayout::cols(M, N, ld));
   if (lo) out.add(TcKind::kBf16Lo, lw, TcLayout::cols(M, N, ld));
   out.name = name;
+  out.inv_scale = inv_scale;
   tc_gemm(c, A, B, mode, out);
   return TcOperand{hi, lw, N, M, ld};
 }
@@ -713,10 +714,196 @@ void quarter_tensor_mixed_f64(Ctx& c, const Site& S, int k, double* Q) {
   divide_by(c, Q, o.rows * o.cols, o.scale, 0);
 }
 
+namespace {
+
+// SVD of the Rayleigh-Ritz matrix B (q x n, given as B^T in FP32) and
+// U = Q Ub with Q the final basis Y (m x q, FP32): Ud (m x q), s, Vd (n x q)
+// in FP64.  FP32: Cholesky-QR of B^T and one-sided Jacobi on its triangular
+// factor; fp64_svd: B in FP64 and the FP64 one-sided Jacobi.
+void rayleigh_ritz_svd(Ctx& c, const float* Bt, const float* Y, int64_t m, int64_t n, int64_t q,
+                       bool fp64_svd, double* Ud, double* s, double* Vd) {
+  Scope scope(c);
+  double* Ub = c.alloc<double>(size_t(q) * q);
+  if (fp64_svd) {
+    double* btd = c.alloc<double>(size_t(n) * q);
+    double* Bd = c.alloc<double>(size_t(q) * n);
+    double* Yd = c.alloc<double>(size_t(m) * q);
+    to_f64(c, Bt, btd, n * q);
+    copy2d(c, View(btd, {n, q}).permute({1, 0}), Bd, n);
+    svd_thin(c, Bd, q, n, Ub, s, Vd);
+    to_f64(c, Y, Yd, m * q);
+    einsum(c, "ik,kj->ij", View(Yd, {m, q}), View(Ub, {q, q}), View(Ud, {m, q}));
+    return;
+  }
+  float* V = c.alloc<float>(size_t(n) * q);
+  float* U = c.alloc<float>(size_t(m) * q);
+  svd_via_qr(c, Bt, q, n, Ub, s, V);
+  float* ubf = c.alloc<float>(size_t(q) * q);
+  to_f32(c, Ub, ubf, q * q);
+  einsum(c, "ik,kj->ij", ViewF(Y, {m, q}), ViewF(ubf, {q, q}), ViewF(U, {m, q}));
+  to_f64(c, U, Ud, m * q);
+  to_f64(c, V, Vd, n * q);
+}
+
+// The projectors' final form: fixed width (cap columns, zero past the
+// truncation count) or compact (chi_new columns).
+void store_projectors(Ctx& c, const ctm_ctmrg_opts& o, const double* P1f, int64_t rows1,
+                      const double* P2f, int64_t rows2, int64_t cap, const int64_t* chi_new,
+                      double* P1, double* P2) {
+  if (o.fixed_width) {
+    if (!c.sizing()) {
+      CTM_CUDA(cudaMemcpyAsync(P1, P1f, sizeof(double) * rows1 * cap, cudaMemcpyDeviceToDevice,
+                               c.stream));
+      CTM_CUDA(cudaMemcpyAsync(P2, P2f, sizeof(double) * rows2 * cap, cudaMemcpyDeviceToDevice,
+                               c.stream));
+    }
+  } else {
+    scale_columns_compact(c, P1f, rows1, cap, nullptr, chi_new, P1);
+    scale_columns_compact(c, P2f, rows2, cap, nullptr, chi_new, P2);
+  }
+}
+
+// ProjectorCalculator.calculate_full_system with the randomized SVD
+// (acetn/renormalization/projectors.py:196-217; the chain of
+// acetn/linalg/fused_3matmul_svd_lowrank.py:26-52) in the arithmetic of the
+// mixed half-system form: F = Q2 Q1 Q4 Q3 is never formed; every product of
+// the chain runs on tensor cores against the four quarter tensors (3xBF16
+// range finder, Rayleigh-Ritz and projector products), each step
+// divided by its quarter tensor's max |entry| (the reference's normalised
+// quarters; the intermediates stay O(1)); FP32 orthonormalization after
+// every half step (the reference's four-factor variant also
+// orthonormalises Z); SVD as in the half-system form; FP64 truncation;
+// proj1 = Q1^T (Q2^T U), proj2 = Q4 (Q3 V).
+void projectors_mixed_full_system(Ctx& c, const Site* S[4], int k, const ctm_ctmrg_opts& o,
+                                  const double* omega, double* P1, double* P2,
+                                  int64_t* chi_new) {
+  Scope scope(c);
+  // chain order: F0 = Q2 (site 1, k+1), F1 = Q1 (site 0, k), F2 = Q4
+  // (site 3, k+3), F3 = Q3 (site 2, k+2)
+  const int site_of[4] = {1, 0, 3, 2};
+  const int dir_of[4] = {k + 1, k, k + 3, k + 2};
+  int64_t sh[6], rows[4], cols[4];
+  for (int i = 0; i < 4; ++i) quarter_dims(*S[site_of[i]], dir_of[i], rows[i], cols[i], sh);
+  CTM_REQUIRE(cols[0] == rows[1] && cols[1] == rows[2] && cols[2] == rows[3], CTM_ERR_INVALID,
+              "full-system: quarter tensors do not chain");
+  const int64_t m = rows[0], n = cols[3];
+  const int64_t q = std::min({o.chi + o.rsvd_oversampling, m, n});
+  const int64_t cap = std::min(o.chi, q);
+  const TcMode x3 = TcMode::kBf16x3;
+  // the range finder is always 3xBF16 here: the spectrum of the four-factor
+  // product spans the square of the half system's range, and one BF16 pass
+  // per chain step left 5e-4 - 1.3e-3 of the largest bond energy between
+  // the mixed and the FP64 move at D=4, chi=32 / 64 (3xBF16: 3e-5 / 7e-5,
+  // the FP64 algorithm's own draw-to-draw spread 1.5e-5 / 4.4e-5)
+  const bool rf3 = true;
+  const bool svd64 = (o.mixed_flags & CTM_MIXED_SVD64) != 0;
+  const bool q64 = (o.mixed_flags & CTM_MIXED_Q64) != 0;
+  CTM_REQUIRE((o.mixed_flags & CTM_MIXED_F32) == 0, CTM_ERR_UNSUPPORTED,
+              "the FP32 reference form covers half-system projectors only");
+  const TcMode xr = rf3 ? x3 : TcMode::kBf16x1;
+  const int inner_stages = rf3 ? 3 : 2;
+  float* Y = c.alloc<float>(size_t(m) * q);
+  float* Bt = c.alloc<float>(size_t(n) * q);
+  QOps F[4];
+  {
+    KernelTimer span(c.stream, kTagQuarter, 0.0);
+    for (int i = 0; i < 4; ++i) F[i] = quarter_mixed(c, *S[site_of[i]], dir_of[i], q64);
+  }
+  // out (m x q, FP32) = F0 F1 F2 F3 x, from x^T (q x n)
+  auto forward = [&](const TcOperand& xt, TcMode mode, bool lo, float* out, const char* name) {
+    Scope s1(c);
+    TcOperand t = xt;
+    for (int i = 3; i >= 1; --i) t = gemm_to_operand(c, F[i].q(lo), t, mode, lo, name, F[i].scale);
+    TcOut to;
+    to.add(TcKind::kF32, out, TcLayout::rows(m, q, q));
+    to.inv_scale = F[0].scale;
+    to.name = name;
+    tc_gemm(c, F[0].q(lo), t, mode, to);
+  };
+  // out (n x q, FP32) = F3^T F2^T F1^T F0^T y, from y^T (q x m)
+  auto backward = [&](const TcOperand& yt, TcMode mode, bool lo, float* out, const char* name) {
+    Scope s1(c);
+    TcOperand t = yt;
+    for (int i = 0; i <= 2; ++i) t = gemm_to_operand(c, F[i].t(lo), t, mode, lo, name, F[i].scale);
+    TcOut to;
+    to.add(TcKind::kF32, out, TcLayout::rows(n, q, q));
+    to.inv_scale = F[3].scale;
+    to.name = name;
+    tc_gemm(c, F[3].t(lo), t, mode, to);
+  };
+  KernelTimer* rf_span = new KernelTimer(c.stream, kTagRangeFinder, 0.0);
+  {
+    Scope s2(c);
+    forward(yt_operand(c, omega, n, q, q, rf3), xr, rf3, Y, "range finder");
+  }
+  for (int it = 0; it < o.rsvd_niter; ++it) {
+    {
+      KernelTimer span(c.stream, kTagOrtho, 0.0);
+      orthonormalize(c, Y, m, q, nullptr, inner_stages);
+    }
+    Scope s2(c);
+    float* Z = c.alloc<float>(size_t(n) * q);
+    {
+      Scope s3(c);
+      backward(yt_operand_f32(c, Y, m, q, q, rf3), xr, rf3, Z, "range finder");
+    }
+    {
+      KernelTimer span(c.stream, kTagOrtho, 0.0);
+      orthonormalize(c, Z, n, q, nullptr, inner_stages);
+    }
+    forward(yt_operand_f32(c, Z, n, q, q, rf3), xr, rf3, Y, "range finder");
+  }
+  {
+    KernelTimer span(c.stream, kTagOrtho, 0.0);
+    orthonormalize(c, Y, m, q, nullptr);
+  }
+  delete rf_span;
+  double* s = c.alloc<double>(q);
+  double* Ud = c.alloc<double>(size_t(m) * q);
+  double* Vd = c.alloc<double>(size_t(n) * q);
+  {
+    KernelTimer span(c.stream, kTagSvd, 0.0);
+    {
+      Scope s2(c);
+      backward(yt_operand_f32(c, Y, m, q, q, true), x3, true, Bt, "Rayleigh-Ritz");
+    }
+    rayleigh_ritz_svd(c, Bt, Y, m, n, q, svd64, Ud, s, Vd);
+  }
+  KernelTimer proj_span(c.stream, kTagProject, 0.0);
+  double* f = c.alloc<double>(cap);
+  truncation_factors(c, s, q, o.chi, std::max({o.svd_cutoff, o.mixed_floor, 1e-8}), f, cap,
+                     chi_new);
+  const int64_t rows1 = cols[1], rows2 = rows[2];
+  double* P1f = c.alloc<double>(size_t(rows1) * cap);
+  double* P2f = c.alloc<double>(size_t(rows2) * cap);
+  {
+    Scope s2(c);
+    scale_columns(c, Ud, m, cap, q, f);
+    scale_columns(c, Vd, n, cap, q, f);
+    // proj1 = Q1^T (Q2^T U f)
+    const TcOperand ut = yt_operand(c, Ud, m, cap, q, true);                       // cap x m
+    const TcOperand u2 = gemm_to_operand(c, F[0].t(true), ut, x3, true, "projector", F[0].scale);
+    gemm_to_f64(c, F[1].t(true), u2, x3, P1f, cap, false, F[1].scale, "projector");
+    // proj2 = Q4 (Q3 V f)
+    const TcOperand vt = yt_operand(c, Vd, n, cap, q, true);                       // cap x n
+    const TcOperand v3 = gemm_to_operand(c, F[3].q(true), vt, x3, true, "projector", F[3].scale);
+    gemm_to_f64(c, F[2].q(true), v3, x3, P2f, cap, false, F[2].scale, "projector");
+  }
+  store_projectors(c, o, P1f, rows1, P2f, rows2, cap, chi_new, P1, P2);
+}
+
+}  // namespace
+
 void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg_opts& o,
                                 const double* omega, double* P1, double* P2, int64_t* chi_new) {
-  CTM_REQUIRE(o.projectors == CTM_PROJ_HALF && o.svd_type == CTM_SVD_RSVD, CTM_ERR_UNSUPPORTED,
-              "mixed precision is implemented for half-system rSVD projectors");
+  CTM_REQUIRE(o.svd_type == CTM_SVD_RSVD, CTM_ERR_INVALID,
+              "calculate_projectors_mixed: randomized SVD only (full-rank runs in "
+              "calculate_projectors)");
+  if (o.projectors == CTM_PROJ_FULL) {
+    projectors_mixed_full_system(c, S, k, o, omega, P1, P2, chi_new);
+    return;
+  }
+  CTM_REQUIRE(o.projectors == CTM_PROJ_HALF, CTM_ERR_INVALID, "Invalid ctmrg projector type");
   Scope scope(c);
   int64_t sh1[6], sh4[6], r1, c1, r4, c4;
   quarter_dims(*S[0], k, r1, c1, sh1);
@@ -831,7 +1018,6 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
   delete rf_span;
   // ---- Rayleigh-Ritz: B = (Q^T Q1) Q4 in 3xBF16 (written as B^T in FP32),
   //      its SVD from an FP32 QR of B^T and one-sided Jacobi
-  double* Ub = c.alloc<double>(size_t(q) * q);
   double* s = c.alloc<double>(q);
   double* Ud = c.alloc<double>(size_t(m) * q);
   double* Vd = c.alloc<double>(size_t(n) * q);
@@ -847,29 +1033,7 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
     out.name = "Rayleigh-Ritz";
     tc_gemm(c, A4.t(true), w, x3, out);
   }
-  if (svd64 || f32) {
-    // B (q x n) in FP64 from its FP32 transpose; FP64 one-sided Jacobi SVD;
-    // U = Q Ub in FP64
-    Scope s2(c);
-    double* btd = c.alloc<double>(size_t(n) * q);
-    double* Bd = c.alloc<double>(size_t(q) * n);
-    double* Yd = c.alloc<double>(size_t(m) * q);
-    to_f64(c, Bt, btd, n * q);
-    copy2d(c, View(btd, {n, q}).permute({1, 0}), Bd, n);
-    svd_thin(c, Bd, q, n, Ub, s, Vd);
-    to_f64(c, Y, Yd, m * q);
-    einsum(c, "ik,kj->ij", View(Yd, {m, q}), View(Ub, {q, q}), View(Ud, {m, q}));
-  } else {
-    Scope s2(c);
-    float* V = c.alloc<float>(size_t(n) * q);
-    float* U = c.alloc<float>(size_t(m) * q);
-    svd_via_qr(c, Bt, q, n, Ub, s, V);
-    float* ubf = c.alloc<float>(size_t(q) * q);
-    to_f32(c, Ub, ubf, q * q);
-    einsum(c, "ik,kj->ij", ViewF(Y, {m, q}), ViewF(ubf, {q, q}), ViewF(U, {m, q}));
-    to_f64(c, U, Ud, m * q);
-    to_f64(c, V, Vd, n * q);
-  }
+  rayleigh_ritz_svd(c, Bt, Y, m, n, q, svd64 || f32, Ud, s, Vd);
   delete svd_span;
   // ---- truncation (FP64 spectrum) and projector products (3xBF16)
   KernelTimer proj_span(c.stream, kTagProject, 0.0);
@@ -904,17 +1068,7 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
     gemm_to_f64(c, A4.q(true), vt, x3, P2f, cap, false, A4.scale, "projector");  // Q4 V f (r4 x cap)
     }
   }
-  if (o.fixed_width) {
-    if (!c.sizing()) {
-      CTM_CUDA(cudaMemcpyAsync(P1, P1f, sizeof(double) * c1 * cap, cudaMemcpyDeviceToDevice,
-                               c.stream));
-      CTM_CUDA(cudaMemcpyAsync(P2, P2f, sizeof(double) * r4 * cap, cudaMemcpyDeviceToDevice,
-                               c.stream));
-    }
-  } else {
-    scale_columns_compact(c, P1f, c1, cap, nullptr, chi_new, P1);
-    scale_columns_compact(c, P2f, r4, cap, nullptr, chi_new, P2);
-  }
+  store_projectors(c, o, P1f, c1, P2f, r4, cap, chi_new, P1, P2);
 }
 
 }  // namespace ctm

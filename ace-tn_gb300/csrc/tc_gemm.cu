@@ -803,13 +803,23 @@ __global__ void tc_reduce_kernel(const ReduceParams r) {
   if (r.inv_scale != nullptr) scd /= r.inv_scale[0];
   if (r.inv_scale2 != nullptr) scd /= r.inv_scale2[0];
   const float sc = float(scd);
-  for (int yy = ty; yy < 32; yy += 8) {
-    const int64_t m = m0 + yy, n = n0 + tx;
-    float s = 0.f;
-    if (m < r.M && n < r.N) {
-      for (int t = 0; t < r.splits; ++t) s += r.part[(size_t(t) * r.m_pad + m) * r.n_pad + n];
+  // the four rows of a thread are summed together, split by split, so that
+  // four independent loads are in flight (one row at a time left the
+  // kernel waiting on one memory latency per split and row)
+  {
+    const int64_t n = n0 + tx;
+    float s[4] = {0.f, 0.f, 0.f, 0.f};
+    bool in[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) in[j] = m0 + ty + 8 * j < r.M && n < r.N;
+    for (int t = 0; t < r.splits; ++t) {
+      const float* pt = r.part + (size_t(t) * r.m_pad + m0 + ty) * r.n_pad + n;
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (in[j]) s[j] += pt[size_t(8 * j) * r.n_pad];
     }
-    tile[yy][tx] = s;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) tile[ty + 8 * j][tx] = s[j];
   }
   for (int k = 0; k < r.nd; ++k) {
     const TcDest& d = r.d[k];

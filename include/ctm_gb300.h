@@ -49,7 +49,10 @@ enum {
                           Rayleigh-Ritz and projector products, FP32 Cholesky-QR and
                           one-sided Jacobi SVD of the Rayleigh-Ritz matrix; FP64
                           spectrum, truncation and s^-1/2 scaling (ctm_ctmrg_opts
-                          .mixed_flags selects higher precision per stage)          */
+                          .mixed_flags selects higher precision per stage); half-
+                          and full-system (four-factor chain) projectors.  With
+                          CTM_SVD_FULL: 3xBF16 quarter tensors and products, FP64
+                          SVD and projector products                              */
   CTM_PREC_BF16 = 2    /* ctm_matmul only: one BF16 tensor-core pass, FP32 accumulation */
 };
 

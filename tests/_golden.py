@@ -39,3 +39,20 @@ def rel(a, b):
 
 SITES_K = {0: [(0, 0), (1, 0), (1, 1), (0, 1)], 1: [(0, 0), (0, 1), (1, 1), (1, 0)],
            2: [(0, 0), (1, 0), (1, 1), (0, 1)], 3: [(0, 0), (0, 1), (1, 1), (1, 0)]}
+
+
+def bond_energies(st):
+    """Per-bond Heisenberg <h_b> from trace-normalised FP64 bond RDMs
+    (precision bars are set against the largest |<h_b>|)."""
+    import torch
+
+    import acetn_gb300 as gb
+
+    rdm = gb.RDM(st)
+    model = gb.HeisenbergModel(1.0)
+    out = []
+    for bd in st.bond_list:
+        r = rdm[bd]
+        h2 = torch.as_tensor(model.two_site_hamiltonian(bd)).reshape(2, 2, 2, 2).to(r)
+        out.append(float(torch.einsum("PQpq,pqPQ->", r, h2) / torch.einsum("pqpq->", r)))
+    return np.array(out)

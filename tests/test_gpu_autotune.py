@@ -3,9 +3,10 @@
 The tuner picks, per product shape, between 256- and 128-column N tiles and
 between a K split that fills the SMs and none.  Every candidate computes the
 same 3xBF16 product (only the FP32 summation order inside a K split
-differs), so a tuned product is checked against the FP64 product at the
-engine's own 3xBF16 tolerance (5e-5 normwise) and against the untuned plan
-at 1e-6 normwise; repeated calls with the tuned plan are bitwise equal.
+differs: ~sqrt(K) FP32 roundings), so a tuned product is checked against the
+FP64 product at the engine's own 3xBF16 tolerance (5e-5 normwise) and
+against the untuned plan at 2e-5 normwise; repeated calls with the tuned
+plan are bitwise equal.
 Calls under stream capture never tune."""
 
 import pytest
@@ -48,7 +49,7 @@ def test_tuned_product_matches(tuner, m, n, k):
     assert torch.equal(tuned, again)
     ref = A @ B
     assert float(torch.linalg.norm(tuned - ref) / torch.linalg.norm(ref)) < 5e-5
-    assert float(torch.linalg.norm(tuned - plain) / torch.linalg.norm(plain)) < 1e-6
+    assert float(torch.linalg.norm(tuned - plain) / torch.linalg.norm(plain)) < 2e-5
     assert gb._abi.device_status() == 0
 
 
@@ -75,19 +76,30 @@ def _fixed_omega():
 
 
 def test_tuned_mixed_moves(tuner):
-    """Mixed CTMRG iterations with the tuner on equal the untuned ones to FP32
-    summation order: the corner spectra agree to 1e-5 of their largest
-    entry (a wrong plan would differ at O(1))."""
-    cfg = gb.CTMRGConfig(steps=3, precision="mixed", rsvd_oversampling=4,
+    """One pair of mixed moves from a grown state with the tuner on (every
+    product shape of the move is tuned on the spot) against the same pair
+    untuned: the leading corner singular values agree to 1e-5 relative.  (The
+    trailing ones are not compared: near the truncation a 1e-7 change of a
+    product can rotate the kept subspace.)"""
+    cfg = gb.CTMRGConfig(steps=4, precision="mixed", rsvd_oversampling=4,
                          disable_progressbar=True)
+    st = gb.random_state(4, 48, 21, device="cuda")
+    gb.ctmrg(st, cfg, omega_source=_fixed_omega())
     results = []
     for tune in (False, True):
-        st = gb.random_state(4, 48, 21, device="cuda")
+        g = gb.IpepsState(st.nx, st.ny, st.dims, st.device)
+        for s in st.site_list:
+            v = st[s]
+            g[s] = {"A": v["A"].clone(), "C": [c.clone() for c in v["C"]],
+                    "E": [e.clone() for e in v["E"]]}
         gb.autotune(tune, reset=True)
-        gb.ctmrg(st, cfg, omega_source=_fixed_omega())
-        results.append([torch.linalg.svdvals(st[s]["C"][k]) for s in st.site_list
+        mover = gb.DirectionalMover(cfg, omega_source=_fixed_omega())
+        mover.move_pair(g, *gb.pair_order(2, 2)[0])
+        torch.cuda.synchronize()
+        results.append([torch.linalg.svdvals(g[s]["C"][k])[:8] for s in g.site_list
                         for k in range(4)])
         if tune:
             assert len(gb.autotune_table()) > 0
+    assert gb._abi.device_status() == 0
     for a, b in zip(*results):
-        assert float((a / a[0] - b / b[0]).abs().max()) < 1e-5
+        assert float(((a - b) / a[0]).abs().max()) < 1e-5
