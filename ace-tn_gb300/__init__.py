@@ -14,6 +14,7 @@ float64 CUDA tensors:
     RDM(ipeps), measure(...)      acetn/measurement/
     svd_lowrank, fused_*          acetn/linalg/
     build_norm_tensor, absorb_bond  acetn/evolution/ (full_update.py, fast_full_update.py)
+    ALSSolver                     acetn/evolution/als_solver.py
 
 All arithmetic runs in libctm_gb300.so; there is no CPU fallback.
 """
@@ -24,6 +25,7 @@ from ._build import build
 from .config import CTMRGConfig
 from .ctmrg import ctmrg, pair_order, sweep_order
 from .directional_mover import DirectionalMover
+from .als import ALSSolver
 from .batched import BatchedCTMRG
 from .full_update import absorb_bond, build_norm_tensor
 from .graph import CTMRGGraph
@@ -39,4 +41,4 @@ __all__ = ["build", "CTMRGConfig", "ctmrg", "sweep_order", "pair_order", "Direct
            "ProjectorCalculator", "CTMRGGraph", "BatchedCTMRG", "RDM", "measure", "svd_lowrank", "fused_matmul_svd_lowrank",
            "fused_3matmul_svd_lowrank", "qr", "svd", "matmul", "HeisenbergModel", "IsingModel",
            "Bond", "IpepsState", "random_state", "build_norm_tensor", "absorb_bond",
-           "autotune", "autotune_table", "set_mixed_contraction"]
+           "autotune", "autotune_table", "set_mixed_contraction", "ALSSolver"]

@@ -79,6 +79,11 @@ _SIGNATURES = {
                      ctypes.c_int),
     "ctm_norm_tensor": ([SITE_P, SITE_P, c_i64, c_i64, c_i32, c_vp, c_vp, c_i64, c_vp, c_vp,
                          c_sz_p, c_vp], ctypes.c_int),
+    "ctm_als_solve": ([c_vp, c_vp, c_i64, c_i64, c_i64, c_i32, ctypes.c_double, c_i32,
+                       ctypes.c_double, c_vp, c_vp, ctypes.POINTER(c_i32), c_vp,
+                       ctypes.POINTER(ctypes.c_size_t), c_vp], ctypes.c_int),
+    "ctm_als_cost": ([c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_vp, c_vp,
+                      ctypes.POINTER(ctypes.c_size_t), c_vp], ctypes.c_int),
     "ctm_svd_lowrank": ([c_vp, c_i64, c_i64, c_i64, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz_p,
                          c_vp], ctypes.c_int),
     "ctm_fused_matmul_svd_lowrank": ([c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_i32, c_vp, c_vp,

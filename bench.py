@@ -433,38 +433,57 @@ def run_gb300(args, rank, world, local_rank):
         del graph, gst
 
     # ---- e2e: host buffers through the public API, copies inside the timed region
+    # Every pair copies the whole state from pinned host memory to the device,
+    # runs the two moves and reads the tensors it replaced back into pinned
+    # host buffers (allocated once, outside the timed region: at saturation
+    # the replaced tensors keep their shapes), which become the next pair's
+    # input.  One untimed pair first; wall clock over the timed pairs.
+    def pinned(t):
+        return torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+
     host = {s: {"A": st[s]["A"].cpu().pin_memory(),
                 "C": [c.cpu().pin_memory() for c in st[s]["C"]],
                 "E": [e.cpu().pin_memory() for e in st[s]["E"]]} for s in st.site_list}
-    e2e_pairs = 2
+    spare = {s: {"C": [pinned(c) for c in host[s]["C"]], "E": [pinned(e) for e in host[s]["E"]]}
+             for s in st.site_list}
+    e2e_pairs = 6
     e2e_steps = 2 * e2e_pairs
     h2d = d2h = 0
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    for i in range(e2e_pairs):
+
+    def e2e_pair():
         dst = gb.IpepsState(2, 2, st.dims, dev)
         for s in st.site_list:
             hs = host[s]
             dst[s] = {"A": hs["A"].to(dev, non_blocking=True),
                       "C": [c.to(dev, non_blocking=True) for c in hs["C"]],
                       "E": [e.to(dev, non_blocking=True) for e in hs["E"]]}
-        h2d = state_bytes(dst)
+        nbytes_in = state_bytes(dst)
         before = {s: (list(dst[s]["C"]), list(dst[s]["E"])) for s in st.site_list}
         next_pair(mover, dst)
         # read back the step's result: the tensors the pair replaced (two
         # corners and one edge per renormalised site and move), found by identity
         moved = 0
+        swaps = []
         for s in st.site_list:
             for key, old_list in zip(("C", "E"), before[s]):
                 for n, t in enumerate(dst[s][key]):
                     if t is not old_list[n]:
-                        host[s][key][n] = t.to("cpu", non_blocking=True)
+                        buf = spare[s][key][n]
+                        if buf.shape != t.shape:
+                            buf = pinned(t)
+                        buf.copy_(t, non_blocking=True)
+                        swaps.append((s, key, n, buf))
                         moved += t.numel() * t.element_size()
         torch.cuda.synchronize(dev)
-        for s in st.site_list:
-            host[s]["C"] = [c if c.is_pinned() else c.pin_memory() for c in host[s]["C"]]
-            host[s]["E"] = [e if e.is_pinned() else e.pin_memory() for e in host[s]["E"]]
-        d2h = moved
+        for s, key, n, buf in swaps:
+            spare[s][key][n], host[s][key][n] = host[s][key][n], buf
+        return nbytes_in, moved
+
+    e2e_pair()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for i in range(e2e_pairs):
+        h2d, d2h = e2e_pair()
     e2e_s = time.perf_counter() - t0
     e2e_value = world * e2e_steps / e2e_s
 
@@ -477,6 +496,9 @@ def run_gb300(args, rank, world, local_rank):
     meas = None
     if rank == 0 and not args.no_measure:
         meas = measure_timing(gb, st, dev)
+    als = None
+    if rank == 0 and not args.no_als:
+        als = als_timing(gb, dev)
     large = None
     if rank == 0 and not args.no_large:
         large = large_instance(gb, dev)
@@ -520,7 +542,9 @@ def run_gb300(args, rank, world, local_rank):
             "kernels": table[:12],
             "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": h2d / 2,
                     "d2h_bytes_per_step": d2h / 2, "steps": e2e_steps,
-                    "note": "state copied host->device once per pair (two moves)"},
+                    "note": "whole state copied from pinned host memory once per pair (two "
+                            "moves), replaced tensors read back into pinned buffers; wall "
+                            "clock over 6 pairs after one untimed pair"},
             "gpu_launches": int(launches),
             "execution": "eager, left/right and up/down pairs of moves",
             "graph": graph_line,
@@ -530,6 +554,7 @@ def run_gb300(args, rank, world, local_rank):
             "comparison": compare,
             "batched_sweep": sweep,
             "measure": meas,
+            "full_update_als": als,
             "large_instance": large,
             "spans_ms_per_step": {k: v[0] / prof_moves for k, v in prof.items() if v[2]},
             "clocks": clk,
@@ -753,6 +778,61 @@ def measure_timing(gb, st, dev):
     out["cpu_ms"] = 1e3 * (4 * t_site + 8 * t_bond)
     out["cpu"] = {"kind": kind, "cores": cpu_cores(),
                   "sample": "one site RDM and one bond RDM, scaled to 4 + 8"}
+    return out
+
+
+def als_timing(gb, dev, nD=12, bD=6, pD=2, reps=3):
+    """One ALS solve of the full update (D=6, d=2 bond: reduced tensors
+    (12, 6, 2)) with the reference's default config (100 iterations, tol
+    1e-15, Cholesky): the GPU solver against the reference's own ALSSolver
+    on torch CPU tensors with all host cores (the oracle port without the
+    reference install), on the same seeded, positive-definite input."""
+    import torch
+    g = np.random.default_rng(77)
+    nz = g.standard_normal((nD, nD, nD * nD))
+    n12 = np.einsum("yxz,YXz->yxYX", nz, nz) + 1e-3 * np.einsum(
+        "yY,xX->yxYX", np.eye(nD), np.eye(nD))
+    a1, a2 = g.random((nD, bD, pD)), g.random((nD, bD, pD))
+    gate = (np.eye(pD * pD) + 0.3 * g.random((pD * pD, pD * pD))).reshape(pD, pD, pD, pD)
+    a12g = np.einsum("yxpq,pqrs->yxrs", np.einsum("yup,xuq->yxpq", a1, a2), gate)
+
+    class Cfg:
+        als_niter, als_tol, als_method, als_epsilon, backend = 100, 1e-15, "cholesky", 1e-12, "torch"
+
+    n12_d = torch.from_numpy(n12).to(dev)
+    a12g_d = torch.from_numpy(a12g).to(dev)
+    solver = gb.ALSSolver(n12_d, a12g_d, (nD, bD, pD), Cfg())
+    solver.solve()  # warm (workspace)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        r1, r2 = solver.solve()
+    torch.cuda.synchronize(dev)
+    gpu_ms = 1e3 * (time.perf_counter() - t0) / reps
+    cost = float(gb.ALSSolver.calculate_cost(r1, r2, a12g_d, n12_d))
+    out = {"shape": [nD, bD, pD], "method": "cholesky", "gpu_ms": gpu_ms,
+           "gpu_iterations": solver.iterations, "gpu_cost": cost}
+    mods = reference_modules()
+    if mods is not None:
+        als_mod = importlib.import_module("acetn.evolution.als_solver")
+        torch.set_num_threads(cpu_cores())
+        ref = als_mod.ALSSolver(torch.from_numpy(n12), torch.from_numpy(a12g), (nD, bD, pD), Cfg())
+        t0 = time.perf_counter()
+        q1, q2 = ref.solve()
+        cpu_ms = 1e3 * (time.perf_counter() - t0)
+        ref_cost = float(als_mod.ALSSolver.calculate_cost(q1, q2, torch.from_numpy(a12g),
+                                                          torch.from_numpy(n12)))
+        kind = "reference"
+    else:
+        from oracle import ctm_oracle as orc
+        t0 = time.perf_counter()
+        q1, q2, _ = orc.als_solve(n12, a12g, (nD, bD, pD))
+        cpu_ms = 1e3 * (time.perf_counter() - t0)
+        ref_cost = orc.als_cost(q1, q2, a12g, n12)
+        kind = "port"
+    out.update({"cpu_ms": cpu_ms, "cpu_cost": ref_cost,
+                "cost_rel_diff": abs(cost - ref_cost) / abs(ref_cost),
+                "cpu": {"kind": kind, "cores": cpu_cores()}})
     return out
 
 
@@ -993,6 +1073,8 @@ def main():
                     help="tune the tensor-core GEMM tile plans in the warm-up pairs")
     ap.add_argument("--no-large", action="store_true",
                     help="skip the D=8, chi=256 instance")
+    ap.add_argument("--no-als", action="store_true",
+                    help="skip the timing of one full-update ALS solve")
     ap.add_argument("--no-measure", action="store_true",
                     help="skip the measure() timing")
     ap.add_argument("--no-batched", action="store_true",

@@ -266,6 +266,31 @@ int ctm_norm_tensor(const ctm_site_f64* s1, const ctm_site_f64* s2, int64_t D, i
                     int32_t k, const double* a1q, const double* a2q, int64_t nD, double* n12,
                     void* ws, size_t* ws_bytes, ctm_stream_t stream);
 
+/* ALS solver of the full update for the reduced tensors a1r, a2r (nD, bD,
+ * pD) of one bond, FP64 on the device: initial guess from the truncated SVD
+ * of a12g[(y,p)][(x,q)], then up to niter alternating least-squares updates
+ * of a1r and a2r; method 0 ("cholesky"): the symmetrised system shifted by
+ * epsilon max|R| on the diagonal, Cholesky factor and two triangular solves
+ * (Gaussian elimination with partial pivoting when a pivot is not positive;
+ * needs nD bD <= 160 and pD <= 8); method 1 ("pinv"): the Hermitian
+ * pseudo-inverse with relative cutoff epsilon.  Stops when the relative
+ * change of the cost falls below tol after the second iteration.  n12 (nD^4,
+ * [y][x][Y][X]) and a12g (nD^2 pD^2, [y][x][p][q]) contiguous device arrays;
+ * *iterations (host, may be NULL) receives the iterations run.  Reads the
+ * cost to the host once per iteration (synchronises `stream`).
+ * Reference: ALSSolver.solve / solve_torch / initialize_reduced_tensors /
+ * solve_ar, acetn/evolution/als_solver.py:35-82, 120-147, 212-243. */
+int ctm_als_solve(const double* n12, const double* a12g, int64_t nD, int64_t bD, int64_t pD,
+                  int32_t niter, double tol, int32_t method, double epsilon, double* a1r,
+                  double* a2r, int32_t* iterations, void* ws, size_t* ws_bytes,
+                  ctm_stream_t stream);
+
+/* <a12n|N|a12n> - 2 <a12n|N|a12g> with a12n = a1r . a2r, into *cost (device).
+ * Reference: ALSSolver.calculate_cost, acetn/evolution/als_solver.py:253-262. */
+int ctm_als_cost(const double* a1r, const double* a2r, const double* a12g, const double* n12,
+                 int64_t nD, int64_t bD, int64_t pD, double* cost, void* ws, size_t* ws_bytes,
+                 ctm_stream_t stream);
+
 /* Randomized SVD of a (m x n), of a @ b (a: m x k, b: k x n), or of
  * a @ b @ c @ e (shapes chained); omega (n x q) supplied by the caller.
  * Writes U (m x q), S (q), V (n x q) with a @ ... ~= U diag(S) V^T.

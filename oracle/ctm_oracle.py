@@ -36,6 +36,7 @@ __all__ = [
     "calculate_full_system", "renormalize_cj1", "renormalize_cj2", "renormalize_ej",
     "OracleState", "Mover", "ctmrg", "site_rdm", "bond_rdm", "heisenberg_model",
     "ising_model", "measure", "build_bond_list", "build_site_list", "random_state",
+    "norm_tensor", "als_initialize", "als_cost", "als_solve",
 ]
 
 
@@ -494,6 +495,73 @@ def norm_tensor(st, bond, a1q, a2q):
     n2 = _ein("ab,fadD->bfdD", c24, e23)
     n2 = _ein("bfdD,cbXDxd->fcXx", n2, tmp)
     return _ein("fcYy,fcXx->yxYX", n1, n2)
+
+
+def als_initialize(a12g, shape):
+    """``ALSSolver.initialize_reduced_tensors`` (acetn/evolution/
+    als_solver.py:120-147): truncated SVD of a12g[(y,p)][(x,q)] to bD
+    values, each factor scaled by sqrt(S / S_0)."""
+    nD, bD, pD = shape
+    m = a12g.transpose(0, 2, 1, 3).reshape(nD * pD, nD * pD)
+    u, sv, vh = np.linalg.svd(m)
+    sq = np.sqrt(sv[:bD] / sv[0])
+    a1r = _ein("ypu,u->yup", u[:, :bD].reshape(nD, pD, bD), sq)
+    a2r = _ein("xqv,v->xvq", vh.T[:, :bD].reshape(nD, pD, bD), sq)
+    return a1r, a2r
+
+
+def als_cost(a1r, a2r, a12g, n12):
+    """``ALSSolver.calculate_cost`` (als_solver.py:253-262): the distance
+    <a12n|N|a12n> - 2 <a12n|N|a12g> up to a constant."""
+    a12n = _ein("yup,xuq->yxpq", a1r, a2r)
+    d2 = _ein("YXpq,YXpq->", _ein("yxYX,yxpq->YXpq", n12, a12n), a12n)
+    d3 = _ein("YXpq,YXpq->", _ein("yxYX,yxpq->YXpq", n12, a12g), a12n)
+    return float(d2 - 2.0 * d3)
+
+
+def _als_solve_ar(r, sm, method, eps):
+    """``ALSSolver.solve_ar`` (als_solver.py:212-243): R symmetrised; the
+    Cholesky of R + eps max|R| I with two triangular solves (a plain solve of
+    the shifted R when the factorisation fails), or the Hermitian
+    pseudo-inverse with cutoff eps."""
+    nD, bD, pD = sm.shape
+    sm = sm.reshape(nD * bD, pD)
+    r = r.reshape(nD * bD, nD * bD)
+    r = 0.5 * (r + r.T)
+    if method == "cholesky":
+        r = r + eps * np.abs(r).max() * np.eye(r.shape[0])
+        try:
+            low = np.linalg.cholesky(r)
+            y = np.linalg.solve(low, sm)  # triangular systems, solved densely
+            ar = np.linalg.solve(low.T, y)
+        except np.linalg.LinAlgError:
+            ar = np.linalg.solve(r, sm)
+    else:
+        ar = np.linalg.pinv(r, rcond=eps, hermitian=True) @ sm
+    return ar.reshape(nD, bD, pD)
+
+
+def als_solve(n12, a12g, shape, niter=100, tol=1e-15, method="cholesky", eps=1e-12):
+    """``ALSSolver.solve`` / ``solve_torch`` (als_solver.py:35-82): alternate
+    the least-squares updates of a1r (build_s1/build_r1, als_solver.py:
+    245-251) and a2r (build_s2/build_r2) until the relative change of the
+    cost falls below tol after the second iteration.  Returns (a1r, a2r,
+    iterations run)."""
+    a1r, a2r = als_initialize(a12g, shape)
+    n12g = _ein("yxYX,yxpq->YXpq", n12, a12g)
+    d1 = abs(als_cost(a1r, a2r, a12g, n12))
+    for i in range(niter):
+        s1 = _ein("YXpQ,XUQ->YUp", n12g, a2r)
+        r1 = _ein("yYXuQ,XUQ->YUyu", _ein("yxYX,xuq->yYXuq", n12, a2r), a2r)
+        a1r = _als_solve_ar(r1, s1, method, eps)
+        s2 = _ein("YXPq,YVP->XVq", n12g, a1r)
+        r2 = _ein("xYXvP,YVP->XVxv", _ein("yxYX,yvp->xYXvp", n12, a1r), a1r)
+        a2r = _als_solve_ar(r2, s2, method, eps)
+        d2 = als_cost(a1r, a2r, a12g, n12)
+        if abs(d2 - d1) / abs(d1) < tol and i > 1:
+            return a1r, a2r, i + 1
+        d1 = d2
+    return a1r, a2r, niter
 
 
 def build_site_list(nx, ny):
