@@ -787,6 +787,7 @@ def als_timing(gb, dev, nD=12, bD=6, pD=2, reps=3):
     1e-15, Cholesky): the GPU solver against the reference's own ALSSolver
     on torch CPU tensors with all host cores (the oracle port without the
     reference install), on the same seeded, positive-definite input."""
+    import numpy as np
     import torch
     g = np.random.default_rng(77)
     nz = g.standard_normal((nD, nD, nD * nD))
@@ -1057,7 +1058,7 @@ def run_profile_case(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
