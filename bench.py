@@ -944,8 +944,14 @@ def compare_paths(gb, st, cfg, dev, precision, nmoves):
     # one move of each direction (left, right, up, down) from the same state
     for k, idx in [order[i] for i in (0, 1, 2, 3)][:nmoves]:
         e = {}
-        for tag, c, seed in (("fp64", cfg64, 7 + k), ("fp64_other_draw", cfg64, 107 + k),
-                             (precision, cfg, 7 + k)):
+        runs = [("fp64", cfg64, 7 + k), ("fp64_other_draw", cfg64, 107 + k),
+                (precision, cfg, 7 + k)]
+        if precision == "mixed":
+            # the same mixed move with the reference's cutoff alone (no
+            # mixed_svd_floor): the truncation rule of the FP64 path
+            runs.append(("mixed_ref_cutoff",
+                         dataclasses.replace(cfg, mixed_svd_floor=cfg.svd_cutoff), 7 + k))
+        for tag, c, seed in runs:
             s1 = clone_state(gb, st)
             gb.DirectionalMover(c, omega_source=seeded(seed)).move(s1, k, idx)
             e[tag] = bond_energies(gb, s1, model)
@@ -960,10 +966,13 @@ def compare_paths(gb, st, cfg, dev, precision, nmoves):
         def per_bond(v):
             return max(abs(x - y) for x, y in zip(v, ref)) / scale
 
-        rows.append({"move": [k, idx], "energy_fp64": e_ref,
-                     "rel_err": rel(e[precision]), "bond_err": per_bond(e[precision]),
-                     "fp64_draw_rel": rel(e["fp64_other_draw"]),
-                     "fp64_draw_bond": per_bond(e["fp64_other_draw"])})
+        row = {"move": [k, idx], "energy_fp64": e_ref,
+               "rel_err": rel(e[precision]), "bond_err": per_bond(e[precision]),
+               "fp64_draw_rel": rel(e["fp64_other_draw"]),
+               "fp64_draw_bond": per_bond(e["fp64_other_draw"])}
+        if "mixed_ref_cutoff" in e:
+            row["rel_err_ref_cutoff"] = rel(e["mixed_ref_cutoff"])
+        rows.append(row)
     errs = [r["rel_err"] for r in rows]
     draws = [r["fp64_draw_rel"] for r in rows]
     return {"fp64_path": {"moves_per_s": 1e3 / fp64_ms, "ms_per_step": fp64_ms},
@@ -971,6 +980,13 @@ def compare_paths(gb, st, cfg, dev, precision, nmoves):
             "rel_err_vs_fp64": stats.median(errs), "rel_err_vs_fp64_max": max(errs),
             "fp64_rsvd_draw_spread": stats.median(draws),
             "fp64_rsvd_draw_spread_max": max(draws),
+            "rel_err_vs_fp64_ref_cutoff": (
+                stats.median(r["rel_err_ref_cutoff"] for r in rows)
+                if rows and "rel_err_ref_cutoff" in rows[0] else None),
+            "rel_err_vs_fp64_ref_cutoff_max": (
+                max(r["rel_err_ref_cutoff"] for r in rows)
+                if rows and "rel_err_ref_cutoff" in rows[0] else None),
+            "cutoffs": {"mixed_svd_floor": cfg.mixed_svd_floor, "svd_cutoff": cfg.svd_cutoff},
             "moves": rows}
 
 
