@@ -505,6 +505,9 @@ __global__ void __launch_bounds__(kPThreads, 1)
   // columns of the tile, and the rows' destination offsets
   __shared__ __align__(16) bf16 s_stage[8][2][32][16];
   __shared__ int64_t s_ro[8][2][32];
+  // staged epilogue: per destination and group of 4 columns, the offset of
+  // the first column when the 4 are contiguous and 4-aligned, else -1
+  __shared__ int64_t s_v4[2][64];
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -632,6 +635,8 @@ __global__ void __launch_bounds__(kPThreads, 1)
     if (p.scale1 != nullptr) scd /= p.scale1[0];
     if (p.scale2 != nullptr) scd /= p.scale2[0];
     const float sc = float(scd);
+    const bool hilo_pair = p.staged && p.nd == 2 && p.d[0].kind == TcKind::kBf16Hi &&
+                           p.d[1].kind == TcKind::kBf16Lo;
     float amax = 0.f;
     for (int lt = 0; lt < ntl; ++lt) {
       const int b = lt & 1;
@@ -654,6 +659,16 @@ __global__ void __launch_bounds__(kPThreads, 1)
           s_co[k][cc] = n < p.N ? lay_col(p.d[k].lay, n) : int64_t(-1);
         }
       epi_bar_sync();
+      if (p.staged) {
+        for (int k = 0; k < min(p.nd, 2); ++k)
+          for (int g4 = etid; g4 < p.ntile / 4; g4 += 256) {
+            const int64_t c0 = s_co[k][4 * g4];
+            const bool vec = c0 >= 0 && (c0 & 3) == 0 && s_co[k][4 * g4 + 1] == c0 + 1 &&
+                             s_co[k][4 * g4 + 2] == c0 + 2 && s_co[k][4 * g4 + 3] == c0 + 3;
+            s_v4[k][g4] = vec ? c0 : int64_t(-1);
+          }
+        epi_bar_sync();
+      }
       const int row = m0 + lane_base + lane;
       const bool mvalid = row < p.M;
       int64_t ro[4] = {0, 0, 0, 0};
@@ -675,24 +690,45 @@ __global__ void __launch_bounds__(kPThreads, 1)
           // memory; then 4 lanes cover one row's 16 columns (8 bytes each),
           // so that one store instruction writes 8 rows x 32 bytes instead
           // of 32 scattered 8-byte pieces
-#pragma unroll
-          for (int k = 0; k < 2; ++k) {
-            if (k >= p.nd) break;
-            const bool lo = p.d[k].kind == TcKind::kBf16Lo;
-            uint32_t w[8];
+          if (hilo_pair) {
+            // the hi / lo pair from one rounding per value (the same bits as
+            // rounding x for hi and x - hi for lo separately)
+            uint32_t wh[8], wl[8];
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
-              float x0 = v[2 * i] * sc, x1 = v[2 * i + 1] * sc;
-              if (lo) {
-                x0 -= __bfloat162float(__float2bfloat16(x0));
-                x1 -= __bfloat162float(__float2bfloat16(x1));
-              }
+              const float x0 = v[2 * i] * sc, x1 = v[2 * i + 1] * sc;
               const __nv_bfloat162 h2 = __floats2bfloat162_rn(x0, x1);
-              w[i] = *reinterpret_cast<const uint32_t*>(&h2);
+              const __nv_bfloat162 l2 = __floats2bfloat162_rn(x0 - __low2float(h2),
+                                                              x1 - __high2float(h2));
+              wh[i] = *reinterpret_cast<const uint32_t*>(&h2);
+              wl[i] = *reinterpret_cast<const uint32_t*>(&l2);
             }
-            uint4* dst4 = reinterpret_cast<uint4*>(&s_stage[ew][k][lane][0]);
-            dst4[0] = make_uint4(w[0], w[1], w[2], w[3]);
-            dst4[1] = make_uint4(w[4], w[5], w[6], w[7]);
+            uint4* dh = reinterpret_cast<uint4*>(&s_stage[ew][0][lane][0]);
+            uint4* dl = reinterpret_cast<uint4*>(&s_stage[ew][1][lane][0]);
+            dh[0] = make_uint4(wh[0], wh[1], wh[2], wh[3]);
+            dh[1] = make_uint4(wh[4], wh[5], wh[6], wh[7]);
+            dl[0] = make_uint4(wl[0], wl[1], wl[2], wl[3]);
+            dl[1] = make_uint4(wl[4], wl[5], wl[6], wl[7]);
+          } else {
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+              if (k >= p.nd) break;
+              const bool lo = p.d[k].kind == TcKind::kBf16Lo;
+              uint32_t w[8];
+#pragma unroll
+              for (int i = 0; i < 8; ++i) {
+                float x0 = v[2 * i] * sc, x1 = v[2 * i + 1] * sc;
+                if (lo) {
+                  x0 -= __bfloat162float(__float2bfloat16(x0));
+                  x1 -= __bfloat162float(__float2bfloat16(x1));
+                }
+                const __nv_bfloat162 h2 = __floats2bfloat162_rn(x0, x1);
+                w[i] = *reinterpret_cast<const uint32_t*>(&h2);
+              }
+              uint4* dst4 = reinterpret_cast<uint4*>(&s_stage[ew][k][lane][0]);
+              dst4[0] = make_uint4(w[0], w[1], w[2], w[3]);
+              dst4[1] = make_uint4(w[4], w[5], w[6], w[7]);
+            }
           }
           __syncwarp();
 #pragma unroll
@@ -704,11 +740,9 @@ __global__ void __launch_bounds__(kPThreads, 1)
               const int g = it * 32 + lane, r = g >> 2, c4 = (g & 3) * 4;
               if (m0 + lane_base + r >= p.M) continue;
               const int64_t rr = s_ro[ew][k][r];
-              const int64_t c0 = s_co[k][c + c4];
-              const bool vec = c0 >= 0 && ((rr + c0) & 3) == 0 && s_co[k][c + c4 + 1] == c0 + 1 &&
-                               s_co[k][c + c4 + 2] == c0 + 2 && s_co[k][c + c4 + 3] == c0 + 3;
-              if (vec) {
-                *reinterpret_cast<uint2*>(dp + rr + c0) =
+              const int64_t v0 = s_v4[k][(c + c4) >> 2];
+              if (v0 >= 0 && (rr & 3) == 0) {
+                *reinterpret_cast<uint2*>(dp + rr + v0) =
                     *reinterpret_cast<const uint2*>(&s_stage[ew][k][r][c4]);
               } else {
 #pragma unroll
