@@ -45,15 +45,21 @@ struct GettArgs {
   int swap_xy;   // grid x runs over column tiles (more than 65535 of them)
 };
 
+// Group index -> the two operands' offsets.  Decoded in 32-bit arithmetic
+// (every group's extent is below 2^31, checked on the host): a 64-bit
+// division by a run-time divisor is a long software sequence, and the tile
+// loaders decode 16 K indices per step.
 __device__ __forceinline__ void decode(const Group& g, int64_t idx, int64_t& o0, int64_t& o1) {
   o0 = 0;
   o1 = 0;
+  uint32_t rem = uint32_t(idx);
 #pragma unroll
   for (int j = kMaxModes - 1; j >= 0; --j) {
     if (j < g.n) {
-      const int64_t e = g.m[j].ext;
-      const int64_t r = idx % e;
-      idx /= e;
+      const uint32_t e = uint32_t(g.m[j].ext);
+      const uint32_t q = rem / e;
+      const int64_t r = int64_t(rem - q * e);
+      rem = q;
       o0 += r * g.m[j].s0;
       o1 += r * g.m[j].s1;
     }
@@ -427,6 +433,9 @@ void einsum_impl(Ctx& c, const char* spec, const ViewT<T>& A, const ViewT<T>& B,
   p.Mt = group_size(p.M);
   p.Nt = group_size(p.N);
   p.Kt = group_size(p.K);
+  CTM_REQUIRE(p.Mt < (int64_t(1) << 31) && p.Nt < (int64_t(1) << 31) &&
+                  p.Kt < (int64_t(1) << 31),
+              CTM_ERR_UNSUPPORTED, "einsum: index groups must have fewer than 2^31 entries");
   p.bext = bext; p.bsa = bsa; p.bsb = bsb; p.bsc = bsc;
   p.alpha = T(alpha);
   p.beta = T(beta);

@@ -158,20 +158,31 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Row / column offsets of a separable layout.  The indices are decoded in
+// 32-bit arithmetic (M and N are below 2^31, checked at launch; a 64-bit
+// division by a run-time divisor is a long software sequence, and the
+// epilogue decodes a tile's 256 columns and 128 rows for every destination);
+// the offsets themselves stay 64-bit.
 __device__ __forceinline__ int64_t lay_row(const TcLayout& l, int64_t m) {
   int64_t o = 0;
+  uint32_t r = uint32_t(m);
   for (int j = l.nm - 1; j >= 0; --j) {
-    o += (m % l.me[j]) * l.ms[j];
-    m /= l.me[j];
+    const uint32_t e = uint32_t(l.me[j]);
+    const uint32_t q = r / e;
+    o += int64_t(r - q * e) * l.ms[j];
+    r = q;
   }
   return o;
 }
 
 __device__ __forceinline__ int64_t lay_col(const TcLayout& l, int64_t n) {
   int64_t o = 0;
+  uint32_t r = uint32_t(n);
   for (int j = l.nn - 1; j >= 0; --j) {
-    o += (n % l.ne[j]) * l.ns[j];
-    n /= l.ne[j];
+    const uint32_t e = uint32_t(l.ne[j]);
+    const uint32_t q = r / e;
+    o += int64_t(r - q * e) * l.ns[j];
+    r = q;
   }
   return o;
 }
@@ -995,19 +1006,22 @@ namespace {
 template <class S>
 __global__ void gather_split_kernel(const S* src, const Gather g, int64_t rows, int64_t K,
                                     bf16* hi, bf16* lo, int64_t ld) {
-  const int64_t total = rows * K;
-  for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < total;
-       idx += int64_t(gridDim.x) * blockDim.x) {
-    int64_t r = idx / K, k = idx % K;
+  // 32-bit index decoding (rows K < 2^31, checked on the host)
+  const uint32_t total = uint32_t(rows * K), uk = uint32_t(K);
+  for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += gridDim.x * blockDim.x) {
+    uint32_t r = idx / uk, k = idx - (idx / uk) * uk;
     const int64_t r0 = r, k0 = k;
     int64_t off = 0;
     for (int j = g.nr - 1; j >= 0; --j) {
-      off += (r % g.re[j]) * g.rs[j];
-      r /= g.re[j];
+      const uint32_t e = uint32_t(g.re[j]), q = r / e;
+      off += int64_t(r - q * e) * g.rs[j];
+      r = q;
     }
     for (int j = g.nk - 1; j >= 0; --j) {
-      off += (k % g.ke[j]) * g.ks[j];
-      k /= g.ke[j];
+      const uint32_t e = uint32_t(g.ke[j]), q = k / e;
+      off += int64_t(k - q * e) * g.ks[j];
+      k = q;
     }
     const double x = double(src[off]);
     const bf16 h = __double2bfloat16(x);
@@ -1086,6 +1100,8 @@ void gather_split_impl(Ctx& c, const S* src, const Gather& g, bf16* hi, bf16* lo
   for (int j = 0; j < g.nr; ++j) rows *= g.re[j];
   for (int j = 0; j < g.nk; ++j) K *= g.ke[j];
   if (c.sizing() || rows * K == 0) return;
+  CTM_REQUIRE(rows * K < (int64_t(1) << 31), CTM_ERR_UNSUPPORTED,
+              "gather_split: fewer than 2^31 elements");
   KernelTimer kt(c.stream, "gather_split_kernel", kUnitByte,
                  double(rows) * K * (sizeof(S) + (lo != nullptr ? 4.0 : 2.0)));
   gather_split_kernel<S><<<grid_for(rows * K, 256), 256, 0, c.stream>>>(src, g, rows, K, hi, lo,
@@ -1168,6 +1184,13 @@ void tc_launch(Ctx& c, const TcOperand& A, const TcOperand& B, int imode, const 
   const int sms = sm_count();
   CTM_REQUIRE(pl.m_tiles <= 0x7fffffff && pl.n_tiles <= 65535 && pl.splits <= 65535,
               CTM_ERR_UNSUPPORTED, "tc_gemm: grid too large");
+  CTM_REQUIRE(M < (int64_t(1) << 31) && N < (int64_t(1) << 31), CTM_ERR_UNSUPPORTED,
+              "tc_gemm: M and N must be below 2^31");
+  for (int i = 0; i < out.nd; ++i)
+    for (int j = 0; j < kTcModes; ++j)
+      CTM_REQUIRE(out.d[i].lay.me[j] >= 1 && out.d[i].lay.me[j] < (int64_t(1) << 32) &&
+                      out.d[i].lay.ne[j] >= 1 && out.d[i].lay.ne[j] < (int64_t(1) << 32),
+                  CTM_ERR_INVALID, "tc_gemm: layout extents must be in [1, 2^32)");
   CUtensorMap tA, tAl, tB, tBl;
   make_map(&tA, A.hi, A.rows, K, A.ld, kBM, pl.bk);
   make_map(&tB, B.hi, B.rows, K, B.ld, uint32_t(pl.ntile), pl.bk);
