@@ -52,21 +52,22 @@ QOps alloc_ops(Ctx& c, int64_t rows, int64_t cols) {
 __global__ void double_layer_kernel(const double* A, int64_t s0, int64_t s1, int64_t s2,
                                     int64_t s3, int64_t s4, int D, int d, bf16* hi, bf16* lo,
                                     int64_t ld) {
-  const int64_t D4 = int64_t(D) * D * D * D;
-  for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < D4 * D4;
-       idx += int64_t(gridDim.x) * blockDim.x) {
-    const int64_t n = idx / D4, k = idx - n * D4;
-    const int DD = int(n % D), dd = int((n / D) % D), R = int((n / (D * D)) % D),
-              r = int(n / (D * D * D));
-    const int U = int(k % D), u = int((k / D) % D), L = int((k / (D * D)) % D),
-              l = int(k / (D * D * D));
+  // 32-bit index decoding (D^8 < 2^31, checked on the host)
+  const uint32_t D4 = uint32_t(D) * D * D * D, uD = uint32_t(D);
+  for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < D4 * D4;
+       idx += gridDim.x * blockDim.x) {
+    const uint32_t n = idx / D4, k = idx - n * D4;
+    const int DD = int(n % uD), dd = int((n / uD) % uD), R = int((n / (uD * uD)) % uD),
+              r = int(n / (uD * uD * uD));
+    const int U = int(k % uD), u = int((k / uD) % uD), L = int((k / (uD * uD)) % uD),
+              l = int(k / (uD * uD * uD));
     const double* ket = A + l * s0 + u * s1 + r * s2 + dd * s3;
     const double* bra = A + L * s0 + U * s1 + R * s2 + DD * s3;
     double v = 0.0;
     for (int p = 0; p < d; ++p) v = fma(ket[p * s4], bra[p * s4], v);
     const bf16 h = __double2bfloat16(v);
-    hi[n * ld + k] = h;
-    lo[n * ld + k] = __double2bfloat16(v - double(__bfloat162float(h)));
+    hi[int64_t(n) * ld + k] = h;
+    lo[int64_t(n) * ld + k] = __double2bfloat16(v - double(__bfloat162float(h)));
   }
 }
 
@@ -83,6 +84,8 @@ DLOp double_layer(Ctx& c, const View& ak, int64_t D, int64_t d) {
   o.hi = c.alloc<bf16>(size_t(o.n) * o.ld);
   o.lo = c.alloc<bf16>(size_t(o.n) * o.ld);
   if (!c.sizing()) {
+    CTM_REQUIRE(o.n * o.n < (int64_t(1) << 31), CTM_ERR_UNSUPPORTED,
+                "double layer: D^8 must be below 2^31");
     KernelTimer kt(c.stream, "double_layer_kernel", kUnitByte, 4.0 * double(o.n) * o.n);
     double_layer_kernel<<<grid_for(o.n * o.n, 256), 256, 0, c.stream>>>(
         ak.p, ak.stride[0], ak.stride[1], ak.stride[2], ak.stride[3], ak.stride[4], int(D),
@@ -474,20 +477,22 @@ void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64
     one_layer_steps(c, ak, D, d, Aa, X, xh, xl, ldk, out, false, nullptr,
                     "edge renormalization, bra step", "edge renormalization, ket step");
   } else {
-  // G1 -> X[(a,x)][(l,L,u,U)]; rows (a,l,L) from E, columns (x,u,U) from
+  // G1 -> X[(x,a)][(l,L,u,U)]; rows (a,l,L) from E, columns (x,u,U) from
   // P1: consecutive columns are consecutive (u,U), stored 4 at a time (as in
-  // quarter_mixed's GEMM 1)
+  // quarter_mixed's GEMM 1).  X's rows run over a fastest, so that the
+  // double-layer step below (its rows are X's rows) writes the rows of one
+  // tile to adjacent runs of T (a before x there as well)
   const int64_t K2 = D2 * D2, ldx = tc_ld(K2);
   bf16* xh = c.alloc<bf16>(size_t(Aa) * X * ldx);
   bf16* xl = c.alloc<bf16>(size_t(Aa) * X * ldx);
   {
     TcLayout l;
     l.nm = 3;
-    l.me[0] = Aa; l.ms[0] = X * ldx;
+    l.me[0] = Aa; l.ms[0] = ldx;
     l.me[1] = D;  l.ms[1] = D * D2;
     l.me[2] = D;  l.ms[2] = D2;
     l.nn = 2;
-    l.ne[0] = X;  l.ns[0] = ldx;
+    l.ne[0] = X;  l.ns[0] = Aa * ldx;
     l.ne[1] = D2; l.ns[1] = 1;
     TcOut out;
     out.add(TcKind::kBf16Hi, xh, l).add(TcKind::kBf16Lo, xl, l);
@@ -497,10 +502,10 @@ void renormalize_ej_mixed(Ctx& c, const Site& S, int k, const double* P2i, int64
   // G2 -> T[(x,r,R)][(a,d,D)]
   const DLOp dl = double_layer(c, ak, D, d);
   {
-    TcLayout l;  // rows (a,x) from X, columns (r,R,d,D) from DL (as in quarter_mixed)
+    TcLayout l;  // rows (x,a) from X, columns (r,R,d,D) from DL (as in quarter_mixed)
     l.nm = 2;
-    l.me[0] = Aa; l.ms[0] = D2;
-    l.me[1] = X;  l.ms[1] = D2 * ld4;
+    l.me[0] = X;  l.ms[0] = D2 * ld4;
+    l.me[1] = Aa; l.ms[1] = D2;
     l.nn = 4;
     l.ne[0] = D; l.ns[0] = D * ld4;
     l.ne[1] = D; l.ns[1] = ld4;
@@ -556,30 +561,32 @@ namespace {
 __global__ void double_layer_open_kernel(const double* A, int64_t s0, int64_t s1, int64_t s2,
                                          int64_t s3, int64_t s4, int D, int d, int g1, int g2,
                                          int o, bf16* hi, bf16* lo, int64_t ld) {
-  const int64_t D4 = int64_t(D) * D * D * D, N = D4 * d * d;
+  // 32-bit index decoding (D^8 d^2 < 2^31, checked on the host)
+  const uint32_t uD = uint32_t(D), ud = uint32_t(d);
+  const uint32_t D4 = uD * uD * uD * uD, N = D4 * ud * ud;
   const int64_t st[5] = {s0, s1, s2, s3, s4};
-  for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < N * D4;
-       idx += int64_t(gridDim.x) * blockDim.x) {
-    const int64_t row = idx / D4, k = idx - row * D4;
-    const int B2 = int(k % D), K2 = int((k / D) % D), B1 = int((k / (D * D)) % D),
-              K1 = int(k / (D * D * D));
-    int64_t n = row;
-    const int Bd = int(n % D);
-    n /= D;
-    const int Kd = int(n % D);
-    n /= D;
-    const int Kp = int(n % d);
-    n /= d;
-    const int Ko = int(n % D);
-    n /= D;
-    const int Bp = int(n % d);
-    const int Bo = int(n / d);
+  for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < N * D4;
+       idx += gridDim.x * blockDim.x) {
+    const uint32_t row = idx / D4, k = idx - row * D4;
+    const int B2 = int(k % uD), K2 = int((k / uD) % uD), B1 = int((k / (uD * uD)) % uD),
+              K1 = int(k / (uD * uD * uD));
+    uint32_t n = row;
+    const int Bd = int(n % uD);
+    n /= uD;
+    const int Kd = int(n % uD);
+    n /= uD;
+    const int Kp = int(n % ud);
+    n /= ud;
+    const int Ko = int(n % uD);
+    n /= uD;
+    const int Bp = int(n % ud);
+    const int Bo = int(n / ud);
     const int64_t ket = K1 * st[g1] + K2 * st[g2] + Ko * st[o] + Kd * st[3] + Kp * st[4];
     const int64_t bra = B1 * st[g1] + B2 * st[g2] + Bo * st[o] + Bd * st[3] + Bp * st[4];
     const double v = A[ket] * A[bra];
     const bf16 h = __double2bfloat16(v);
-    hi[row * ld + k] = h;
-    lo[row * ld + k] = __double2bfloat16(v - double(__bfloat162float(h)));
+    hi[int64_t(row) * ld + k] = h;
+    lo[int64_t(row) * ld + k] = __double2bfloat16(v - double(__bfloat162float(h)));
   }
 }
 
@@ -602,6 +609,8 @@ void bond_rdm_half(Ctx& c, const Site& S, int kq, const View& ak, int g1, int g2
   bf16* oh = c.alloc<bf16>(size_t(N) * ldo);
   bf16* ol = c.alloc<bf16>(size_t(N) * ldo);
   if (!c.sizing()) {
+    CTM_REQUIRE(N * D4 < (int64_t(1) << 31), CTM_ERR_UNSUPPORTED,
+                "open double layer: D^8 d^2 must be below 2^31");
     KernelTimer kt(c.stream, "double_layer_open_kernel", kUnitByte, 4.0 * double(N) * D4);
     double_layer_open_kernel<<<grid_for(N * D4, 256), 256, 0, c.stream>>>(
         ak.p, ak.stride[0], ak.stride[1], ak.stride[2], ak.stride[3], ak.stride[4], int(D),
