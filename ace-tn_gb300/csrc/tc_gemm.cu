@@ -884,33 +884,44 @@ __global__ void tc_reduce_kernel(const ReduceParams r) {
 template <class S>
 __global__ void split_bf16_kernel(const S* src, int64_t rows, int64_t cols, int64_t ld_src,
                                   int transpose, bf16* hi, bf16* lo, int64_t ld_dst) {
-  __shared__ double tile[32][33];
+  // the split in the source's precision: for an FP32 source x - hi is exact
+  // in FP32, so FP32 arithmetic gives the bits FP64 would (FP64 is slow here)
+  __shared__ S tile[32][33];
   const int64_t r0 = int64_t(blockIdx.y) * 32, c0 = int64_t(blockIdx.x) * 32;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  auto split = [&](S x, bf16& h, bf16& l) {
+    if constexpr (sizeof(S) == 4) {
+      h = __float2bfloat16(x);
+      l = __float2bfloat16(x - __bfloat162float(h));
+    } else {
+      h = __double2bfloat16(x);
+      l = __double2bfloat16(x - double(__bfloat162float(h)));
+    }
+  };
   if (!transpose) {
     for (int yy = ty; yy < 32; yy += 8) {
       const int64_t r = r0 + yy, c = c0 + tx;
       if (r < rows && c < cols) {
-        const double x = double(src[r * ld_src + c]);
-        const bf16 h = __double2bfloat16(x);
+        bf16 h, l;
+        split(src[r * ld_src + c], h, l);
         hi[r * ld_dst + c] = h;
-        if (lo != nullptr) lo[r * ld_dst + c] = __double2bfloat16(x - double(__bfloat162float(h)));
+        if (lo != nullptr) lo[r * ld_dst + c] = l;
       }
     }
     return;
   }
   for (int yy = ty; yy < 32; yy += 8) {
     const int64_t r = r0 + yy, c = c0 + tx;
-    tile[yy][tx] = (r < rows && c < cols) ? double(src[r * ld_src + c]) : 0.0;
+    tile[yy][tx] = (r < rows && c < cols) ? src[r * ld_src + c] : S(0);
   }
   __syncthreads();
   for (int yy = ty; yy < 32; yy += 8) {
     const int64_t c = c0 + yy, r = r0 + tx;  // destination row c, column r
     if (r < rows && c < cols) {
-      const double x = tile[tx][yy];
-      const bf16 h = __double2bfloat16(x);
+      bf16 h, l;
+      split(tile[tx][yy], h, l);
       hi[c * ld_dst + r] = h;
-      if (lo != nullptr) lo[c * ld_dst + r] = __double2bfloat16(x - double(__bfloat162float(h)));
+      if (lo != nullptr) lo[c * ld_dst + r] = l;
     }
   }
 }
@@ -1023,10 +1034,18 @@ __global__ void gather_split_kernel(const S* src, const Gather g, int64_t rows, 
       off += int64_t(k - q * e) * g.ks[j];
       k = q;
     }
-    const double x = double(src[off]);
-    const bf16 h = __double2bfloat16(x);
+    bf16 h, l;
+    if constexpr (sizeof(S) == 4) {  // exact in FP32 for an FP32 source (see split_bf16_kernel)
+      const float x = src[off];
+      h = __float2bfloat16(x);
+      l = __float2bfloat16(x - __bfloat162float(h));
+    } else {
+      const double x = src[off];
+      h = __double2bfloat16(x);
+      l = __double2bfloat16(x - double(__bfloat162float(h)));
+    }
     hi[r0 * ld + k0] = h;
-    if (lo != nullptr) lo[r0 * ld + k0] = __double2bfloat16(x - double(__bfloat162float(h)));
+    if (lo != nullptr) lo[r0 * ld + k0] = l;
   }
 }
 
@@ -1045,27 +1064,51 @@ __global__ void join_bf16_kernel(const bf16* hi, const bf16* lo, int64_t rows, i
 
 namespace {
 
-// 64 x 64 tiles through shared memory; blockIdx.z selects the hi or lo array.
-__global__ void transpose_bf16_kernel(const bf16* src_hi, const bf16* src_lo, int64_t rows,
-                                      int64_t cols, int64_t ld_src, bf16* dst_hi, bf16* dst_lo,
-                                      int64_t ld_dst) {
-  __shared__ bf16 tile[64][66];
+// 64 x 64 cells through shared memory, blockIdx.z selects the hi or lo
+// array; 16-byte loads of source rows and 16-byte stores of destination rows
+// (8 BF16 each) where the leading dimensions allow (2-byte accesses reached
+// 2.9 TB/s).  A destination row's last 16-byte piece may run into the
+// padding between its used length and its leading dimension.
+__global__ void __launch_bounds__(256) transpose_bf16_kernel(
+    const bf16* src_hi, const bf16* src_lo, int64_t rows, int64_t cols, int64_t ld_src,
+    bf16* dst_hi, bf16* dst_lo, int64_t ld_dst) {
+  __shared__ __align__(16) bf16 tile[64][72];
   const bf16* src = blockIdx.z ? src_lo : src_hi;
   bf16* dst = blockIdx.z ? dst_lo : dst_hi;
   const int64_t r0 = int64_t(blockIdx.y) * 64, c0 = int64_t(blockIdx.x) * 64;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  for (int yy = ty; yy < 64; yy += 8) {
-    const int64_t r = r0 + yy, cc = c0 + 2 * tx;
-    const bf16 z = __float2bfloat16(0.f);
-    tile[yy][2 * tx] = (r < rows && cc < cols) ? src[r * ld_src + cc] : z;
-    tile[yy][2 * tx + 1] = (r < rows && cc + 1 < cols) ? src[r * ld_src + cc + 1] : z;
+  const int tid = threadIdx.x;
+  const bool vsrc = (ld_src & 7) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0;
+  const bool vdst = (ld_dst & 7) == 0 && (reinterpret_cast<uintptr_t>(dst) & 15) == 0;
+  const bf16 z = __float2bfloat16(0.f);
+  for (int i = tid; i < 512; i += 256) {
+    const int rr = i >> 3, ch = i & 7;
+    const int64_t r = r0 + rr, cc = c0 + ch * 8;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (r < rows && cc < cols) {
+      if (vsrc && cc + 8 <= cols) {
+        v = *reinterpret_cast<const uint4*>(src + r * ld_src + cc);
+      } else {
+        __align__(16) bf16 e[8];
+        for (int j = 0; j < 8; ++j) e[j] = cc + j < cols ? src[r * ld_src + cc + j] : z;
+        v = *reinterpret_cast<const uint4*>(e);
+      }
+    }
+    *reinterpret_cast<uint4*>(&tile[rr][ch * 8]) = v;
   }
   __syncthreads();
-  for (int yy = ty; yy < 64; yy += 8) {
-    const int64_t dr = c0 + yy, dc = r0 + 2 * tx;  // destination row = source column
-    if (dr >= cols) continue;
-    if (dc < rows) dst[dr * ld_dst + dc] = tile[2 * tx][yy];
-    if (dc + 1 < rows) dst[dr * ld_dst + dc + 1] = tile[2 * tx + 1][yy];
+  for (int i = tid; i < 512; i += 256) {
+    const int cc = i >> 3, ch = i & 7;  // destination row c0 + cc, its entries r0 + ch * 8 ..
+    const int64_t dr = c0 + cc, dc = r0 + ch * 8;
+    if (dr >= cols || dc >= rows) continue;
+    __align__(16) bf16 e[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) e[j] = tile[ch * 8 + j][cc];
+    if (vdst && dc + 8 <= ld_dst) {
+      *reinterpret_cast<uint4*>(dst + dr * ld_dst + dc) = *reinterpret_cast<const uint4*>(e);
+    } else {
+      for (int j = 0; j < 8; ++j)
+        if (dc + j < rows) dst[dr * ld_dst + dc + j] = e[j];
+    }
   }
 }
 
