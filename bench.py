@@ -433,51 +433,55 @@ def run_gb300(args, rank, world, local_rank):
         del graph, gst
 
     # ---- e2e: host buffers through the public API, copies inside the timed region
-    # Every pair copies the whole state from pinned host memory to the device,
-    # runs the two moves and reads the tensors it replaced back into pinned
-    # host buffers (allocated once, outside the timed region: at saturation
-    # the replaced tensors keep their shapes), which become the next pair's
-    # input.  One untimed pair first; wall clock over the timed pairs.
-    def pinned(t):
-        return torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
-
-    host = {s: {"A": st[s]["A"].cpu().pin_memory(),
-                "C": [c.cpu().pin_memory() for c in st[s]["C"]],
-                "E": [e.cpu().pin_memory() for e in st[s]["E"]]} for s in st.site_list}
-    spare = {s: {"C": [pinned(c) for c in host[s]["C"]], "E": [pinned(e) for e in host[s]["E"]]}
-             for s in st.site_list}
+    # The state lives in one pinned host buffer (every site's A, C[0..3],
+    # E[0..3] back to back).  Every pair copies that buffer to the device in
+    # one transfer, runs the two moves on views of the device copy, and reads
+    # the tensors it replaced back into their places in the host buffer, which
+    # is the next pair's input.  One untimed pair first; wall clock over the
+    # timed pairs.
+    tensors = [(s, key, n, st[s][key] if key == "A" else st[s][key][n])
+               for s in st.site_list for key, count in (("A", 1), ("C", 4), ("E", 4))
+               for n in range(count)]
+    offsets, total = [], 0
+    for _, _, _, t in tensors:
+        offsets.append(total)
+        total += (t.numel() + 63) // 64 * 64  # every view 512-byte aligned, as allocations are
+    host_flat = torch.empty(total, dtype=torch.float64, pin_memory=True)
+    for (_, _, _, t), off in zip(tensors, offsets):
+        host_flat[off:off + t.numel()].copy_(t.reshape(-1).cpu())
+    where = {(s, key, n): (off, t.shape) for (s, key, n, t), off in zip(tensors, offsets)}
     e2e_pairs = 6
     e2e_steps = 2 * e2e_pairs
     h2d = d2h = 0
 
     def e2e_pair():
+        flat = host_flat.to(dev, non_blocking=True)
         dst = gb.IpepsState(2, 2, st.dims, dev)
+
+        def view(s, key, n):
+            off, shape = where[(s, key, n)]
+            return flat[off:off + shape.numel()].view(shape)
+
         for s in st.site_list:
-            hs = host[s]
-            dst[s] = {"A": hs["A"].to(dev, non_blocking=True),
-                      "C": [c.to(dev, non_blocking=True) for c in hs["C"]],
-                      "E": [e.to(dev, non_blocking=True) for e in hs["E"]]}
-        nbytes_in = state_bytes(dst)
+            dst[s] = {"A": view(s, "A", 0), "C": [view(s, "C", n) for n in range(4)],
+                      "E": [view(s, "E", n) for n in range(4)]}
         before = {s: (list(dst[s]["C"]), list(dst[s]["E"])) for s in st.site_list}
         next_pair(mover, dst)
         # read back the step's result: the tensors the pair replaced (two
-        # corners and one edge per renormalised site and move), found by identity
+        # corners and one edge per renormalised site and move, found by
+        # identity) into their places in the host buffer
         moved = 0
-        swaps = []
         for s in st.site_list:
             for key, old_list in zip(("C", "E"), before[s]):
                 for n, t in enumerate(dst[s][key]):
                     if t is not old_list[n]:
-                        buf = spare[s][key][n]
-                        if buf.shape != t.shape:
-                            buf = pinned(t)
-                        buf.copy_(t, non_blocking=True)
-                        swaps.append((s, key, n, buf))
+                        off, shape = where[(s, key, n)]
+                        if tuple(t.shape) != tuple(shape):
+                            raise RuntimeError("e2e: a replaced tensor changed its shape")
+                        host_flat[off:off + t.numel()].view(shape).copy_(t, non_blocking=True)
                         moved += t.numel() * t.element_size()
         torch.cuda.synchronize(dev)
-        for s, key, n, buf in swaps:
-            spare[s][key][n], host[s][key][n] = host[s][key][n], buf
-        return nbytes_in, moved
+        return total * 8, moved
 
     e2e_pair()
     torch.cuda.synchronize(dev)
@@ -542,9 +546,9 @@ def run_gb300(args, rank, world, local_rank):
             "kernels": table[:12],
             "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": h2d / 2,
                     "d2h_bytes_per_step": d2h / 2, "steps": e2e_steps,
-                    "note": "whole state copied from pinned host memory once per pair (two "
-                            "moves), replaced tensors read back into pinned buffers; wall "
-                            "clock over 6 pairs after one untimed pair"},
+                    "note": "whole state copied from one pinned host buffer in one transfer "
+                            "per pair (two moves), replaced tensors read back into their "
+                            "places in it; wall clock over 6 pairs after one untimed pair"},
             "gpu_launches": int(launches),
             "execution": "eager, left/right and up/down pairs of moves",
             "graph": graph_line,
