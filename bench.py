@@ -40,10 +40,12 @@ WORKLOAD = {"workload": f"heisenberg_2x2_D{D}_chi{CHI}_rsvd_os{OVERSAMPLING}_nit
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of a
 # kernel class at this workload, from one ncu capture of `bench.py
 # --profile-case --steps 1` (`ncu --set full --clock-control none -k
-# regex:tc_gemm_persistent -s 1 -c 1`: 125.2 MB read + 61.3 MB written);
+# regex:tc_gemm_persistent -s 0 -c 2`: the K = chi step 20.3 MB read + 60.0
+# MB written, the double-layer step 125.1 MB read + 62.7 MB written);
 # classes without a capture report null.
 NCU_DRAM_BYTES = {
-    "tc_gemm_persistent_kernel (enlarged corner, double-layer step)": 125.186560e6 + 61.255424e6,
+    "tc_gemm_persistent_kernel (enlarged corner, edge step)": 20.297472e6 + 59.953152e6,
+    "tc_gemm_persistent_kernel (enlarged corner, double-layer step)": 125.144064e6 + 62.710784e6,
 }
 
 
