@@ -10,7 +10,9 @@ gauge-fixed with the reference's
 (nD, bD, pD) = (8, 5, 3) as in that test, (12, 6, 2) (a D=6, d=2 bond) and
 (4, 2, 2); methods "cholesky" and "pinv"; 10 iterations (the convergence
 test |d2 - d1| / |d1| < 1e-15 is not reached, so the iteration count is
-fixed) and 100 iterations (the reference's default).
+fixed) and 100 iterations (the reference's default); and an indefinite norm
+tensor (``als_indefinite.npz``) on which the Cholesky fails and the
+reference falls back to a plain solve.
 
 Run in a container where the reference source tree is available:
 
@@ -71,6 +73,22 @@ def main(ref_root):
         name = f"als_{nD}_{bD}_{pD}.npz"
         np.savez(os.path.join(HERE, name), **out)
         print("wrote", name, {k: float(v) for k, v in out.items() if k.endswith("_cost")})
+
+    # an indefinite norm tensor (symmetric, not made positive): the shifted
+    # systems are indefinite, the Cholesky fails and solve_ar falls back to
+    # torch.linalg.solve (als_solver.py:232-236); three iterations
+    nD, bD, pD = 6, 3, 2
+    torch.manual_seed(31)
+    n = torch.randn(nD * nD, nD * nD, dtype=torch.float64)
+    n12 = (0.5 * (n + n.T)).reshape(nD, nD, nD, nD).contiguous()
+    a12g = torch.randn(nD, nD, pD, pD, dtype=torch.float64)
+    cfg = EvolutionConfig(als_niter=3, als_tol=1e-15, als_method="cholesky", backend="torch")
+    r1, r2 = ALSSolver(n12.clone(), a12g.clone(), (nD, bD, pD), cfg).solve()
+    out = {"n12": n12.numpy(), "a12g": a12g.numpy(), "shape": np.array([nD, bD, pD]),
+           "cholesky_3_a12": einsum("yup,xuq->yxpq", r1, r2).numpy(),
+           "cholesky_3_cost": np.array(float(ALSSolver.calculate_cost(r1, r2, a12g, n12)))}
+    np.savez(os.path.join(HERE, "als_indefinite.npz"), **out)
+    print("wrote als_indefinite.npz", float(out["cholesky_3_cost"]))
 
 
 if __name__ == "__main__":

@@ -69,3 +69,16 @@ def test_als_solver_host_checks():
     assert (s.niter, s.tol, s.method, s.epsilon) == (100, 1e-15, "cholesky", 1e-12)
     with pytest.raises(ValueError):  # CPU tensors: no CPU path
         s.solve()
+
+
+def test_als_indefinite_norm_falls_back_like_the_reference():
+    """An indefinite (symmetric, not positive) norm tensor: every shifted
+    system fails the Cholesky and the reference solves it directly
+    (als_solver.py:219-226); three iterations, products and cost to 1e-10."""
+    z = load("als_indefinite.npz")
+    shape = tuple(int(x) for x in z["shape"])
+    a1, a2, it = orc.als_solve(z["n12"], z["a12g"], shape, niter=3)
+    assert it == 3
+    assert rel(a12(a1, a2), z["cholesky_3_a12"]) < 1e-10
+    ref = float(z["cholesky_3_cost"])
+    assert abs(orc.als_cost(a1, a2, z["a12g"], z["n12"]) - ref) <= 1e-10 * abs(ref)

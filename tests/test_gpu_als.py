@@ -79,3 +79,23 @@ def test_gpu_als_converges_like_the_reference_test():
         a1r, a2r = gb.ALSSolver(n12, a12g, shape, Cfg(n, "cholesky")).solve()
         costs.append(float(gb.ALSSolver.calculate_cost(a1r, a2r, a12g, n12)))
     assert abs(costs[1] - costs[0]) < 1e-15 * abs(costs[0]) + 1e-9
+
+
+def test_gpu_als_indefinite_norm_takes_the_lu_fallback():
+    """Every shifted system of an indefinite norm tensor fails the Cholesky;
+    the kernel's pivoted-LU fallback gives the reference's plain solve
+    (als_solver.py:219-226): products and cost to 1e-9 after three
+    iterations."""
+    z = load("als_indefinite.npz")
+    shape = tuple(int(x) for x in z["shape"])
+    n12 = torch.from_numpy(z["n12"]).cuda()
+    a12g = torch.from_numpy(z["a12g"]).cuda()
+    solver = gb.ALSSolver(n12, a12g, shape, Cfg(3, "cholesky"))
+    a1r, a2r = solver.solve()
+    assert solver.iterations == 3
+    prod = torch.einsum("yup,xuq->yxpq", a1r, a2r).cpu().numpy()
+    assert rel(prod, z["cholesky_3_a12"]) < 1e-9
+    ref = float(z["cholesky_3_cost"])
+    cost = float(gb.ALSSolver.calculate_cost(a1r, a2r, a12g, n12))
+    assert abs(cost - ref) <= 1e-9 * abs(ref)
+    assert gb._abi.device_status() == 0
