@@ -55,3 +55,35 @@ def test_noalloc_rejects_products_beyond_its_scratch():
     st, _ = _noalloc(A, A)
     assert st == _abi.CTM_ERR_WORKSPACE
     assert b"static scratch" in _abi.load().ctm_last_error()
+
+
+def test_noalloc_captures_in_a_global_mode_graph():
+    """The entry point allocates nothing: a call captured in a CUDA graph with
+    capture_error_mode='global' (where a cudaMalloc, or any other call that
+    is unsafe during capture, makes the capture fail) replays to the
+    workspace entry point's result."""
+    gb.build()
+    A, B = _rand(256, 640, 5), _rand(640, 192, 6)
+    C = torch.empty(256, 192, dtype=torch.float64, device=A.device)
+    lib = _abi.load()
+
+    def call():
+        return lib.ctm_matmul_mixed_noalloc(_abi.ptr(A), _abi.ptr(B), _abi.ptr(C), 256, 192, 640,
+                                           _abi.stream_handle(A.device))
+
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        assert call() == _abi.CTM_OK, lib.ctm_last_error()  # warm-up outside the capture
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, capture_error_mode="global"):
+        st = call()
+    assert st == _abi.CTM_OK, lib.ctm_last_error()
+    C.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    ref = gb.matmul(A, B, precision="mixed")
+    assert torch.allclose(C, ref, rtol=1e-12, atol=1e-12)
+    assert gb._abi.device_status() == 0
