@@ -1065,46 +1065,93 @@ __device__ __forceinline__ void slab_copy(float* s, const float* g, int64_t cnt)
 
 constexpr int kSlabThreads = 1024;
 
+// Dynamic shared memory of a slab stage: rpb rows of q rounded up to 4
+// floats, and q rows of L^T padded to 32-float multiples.
+inline size_t slab_smem_bytes(int64_t q, int64_t rpb) {
+  const int64_t ldq = (q + 3) / 4 * 4, ldl = (q + 31) / 32 * 32;
+  return size_t(rpb * ldq + q * ldl) * sizeof(float);
+}
+
+// Tile t of the upper triangle (row-major, diagonal included) of an
+// nt4 x nt4 grid of 4 x 4 tiles: its tile row ti and tile column tj >= ti.
+__device__ __forceinline__ void slab_tri_tile(int t, int nt4, int& ti, int& tj) {
+  const int m = 2 * nt4 + 1;
+  int bi = int((float(m) - sqrtf(float(m * m - 8 * t))) * 0.5f);
+  bi = max(0, min(bi, nt4 - 1));
+  while (bi + 1 < nt4 && (bi + 1) * nt4 - (bi + 1) * bi / 2 <= t) ++bi;
+  while (bi * nt4 - bi * (bi - 1) / 2 > t) --bi;
+  ti = bi;
+  tj = bi + (t - (bi * nt4 - bi * (bi - 1) / 2));
+}
+
 // One slab of rows [r0, r0 + nr) of Y (n x q, row-major), r0 = blockIdx.x * rpb.
-// With Lt (q x q, upper triangular L^T of a Cholesky factor L): X = Y L^-T
-// for the slab by forward substitution (x L^T = y row by row; written to X
-// and kept in shared memory), then part[blockIdx.x] = X^T X over the slab;
-// without Lt: part[blockIdx.x] = Y^T Y over the slab.  A zero diagonal of L
-// (a pivot the factorisation dropped) gives a zero column of X.
-// Shared memory: the slab (rpb x q, then 32 kT floats of slack so that column
-// indices up to 32 kT - 1 stay inside the buffer) and Lt (q x q + 32 kT).
-// Columns >= q are computed from neighbouring entries and never stored.
+// With Lt (q x q, upper triangular L^T of a Cholesky factor L, zero below
+// the diagonal): X = Y L^-T for the slab by forward substitution (x L^T = y
+// row by row; written to X and kept in shared memory), then the slab's Gram
+// matrix X^T X; without Lt: Y^T Y.  A zero diagonal of L (a pivot the
+// factorisation dropped) gives a zero column of X.
+// Shared memory: the slab (rpb rows of ldq = q rounded up to 4 floats, zero
+// past column q) and Lt (q rows of 32 kT floats, zero past column q and, once
+// the reciprocal pivots are taken, on the diagonal: the update loop then
+// reads every column unconditionally).
 // Solve: warp w owns rows 4w..4w+3 (+128 per pass), lane the columns
 // lane + 32 j; column b is finished by its owner lane and broadcast with a
 // shuffle, then every lane subtracts x_b L[a][b] (row b of Lt, read
-// conflict-free) from its columns a > b.
-// Gram: thread (warp, lane) owns rows warp + 32 i and columns lane + 32 j.
+// conflict-free) from its columns, which changes only those with a > b.
+// Gram: the upper triangle of the slab's Gram matrix in 4 x 4 tiles, one
+// tile per thread (two 16-byte reads per 16 FMAs and row), written packed:
+// part[blockIdx.x][t][4][4] for tile t (slab_tri_tile order).
 template <int kT, bool kVec>
 __global__ void __launch_bounds__(kSlabThreads) slab_stage_kernel(
     const float* __restrict__ Y, int64_t n, int q, int rpb, const float* __restrict__ Lt,
     float* __restrict__ X, float* __restrict__ part) {
   extern __shared__ __align__(16) float slab_smem[];
   __shared__ float s_rdiag[32 * kT];
-  const int pad = 32 * kT;
-  float* Ys = slab_smem;                           // rpb x q (+ pad)
-  float* Us = slab_smem + size_t(rpb) * q + pad;   // q x q (+ pad)
+  constexpr int ldl = 32 * kT;
+  const int ldq = (q + 3) & ~3;
+  float* Ys = slab_smem;                      // rpb x ldq
+  float* Us = slab_smem + size_t(rpb) * ldq;  // q x ldl
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t r0 = int64_t(blockIdx.x) * rpb;
   const int nr = int(n - r0 < rpb ? n - r0 : rpb);
-  slab_copy<kVec>(Ys, Y + r0 * q, int64_t(nr) * q);
-  if (Lt != nullptr) slab_copy<kVec>(Us, Lt, int64_t(q) * q);
-  // slack after the rows is read only into columns that are never stored;
-  // zero it so those lanes compute on finite values
-  for (int i = threadIdx.x; i < pad; i += blockDim.x) {
-    Ys[size_t(nr) * q + i] = 0.f;
-    Us[size_t(q) * q + i] = 0.f;
+  if (kVec) {  // q % 4 == 0 (ldq == q: the slab is contiguous), 16-byte aligned rows
+    const int c4 = q / 4;
+    for (int i = threadIdx.x; i < nr * c4; i += blockDim.x)
+      cp_async_f32x4(Ys + 4 * i, Y + r0 * q + 4 * i);
+    if (Lt != nullptr)
+      for (int i = threadIdx.x; i < q * c4; i += blockDim.x) {
+        const int r = i / c4, c = i - r * c4;
+        cp_async_f32x4(Us + r * ldl + 4 * c, Lt + size_t(r) * q + 4 * c);
+      }
+  } else {
+    for (int i = threadIdx.x; i < nr * q; i += blockDim.x) {
+      const int r = i / q, c = i - r * q;
+      cp_async_f32(Ys + r * ldq + c, Y + (r0 + r) * q + c);
+    }
+    if (Lt != nullptr)
+      for (int i = threadIdx.x; i < q * q; i += blockDim.x) {
+        const int r = i / q, c = i - r * q;
+        cp_async_f32(Us + r * ldl + c, Lt + size_t(r) * q + c);
+      }
   }
+  // the padding columns (not touched by the copies)
+  if (ldq > q)
+    for (int i = threadIdx.x; i < nr * (ldq - q); i += blockDim.x) {
+      const int r = i / (ldq - q);
+      Ys[r * ldq + q + (i - r * (ldq - q))] = 0.f;
+    }
+  if (Lt != nullptr && ldl > q)
+    for (int i = threadIdx.x; i < q * (ldl - q); i += blockDim.x) {
+      const int r = i / (ldl - q);
+      Us[r * ldl + q + (i - r * (ldl - q))] = 0.f;
+    }
   cp_async_wait_all();
   __syncthreads();
   if (Lt != nullptr) {
     for (int b = threadIdx.x; b < q; b += blockDim.x) {
-      const float d = Us[size_t(b) * q + b];
+      const float d = Us[b * ldl + b];
       s_rdiag[b] = d > 0.f ? 1.f / d : 0.f;
+      Us[b * ldl + b] = 0.f;
     }
     __syncthreads();
     for (int rg = warp * 4; rg < nr; rg += 4 * 32) {
@@ -1114,7 +1161,7 @@ __global__ void __launch_bounds__(kSlabThreads) slab_stage_kernel(
 #pragma unroll
         for (int j = 0; j < kT; ++j) {
           const int a = lane + 32 * j;
-          y[i][j] = (rg + i < nr && a < q) ? Ys[size_t(rg + i) * q + a] : 0.f;
+          y[i][j] = (rg + i < nr && a < q) ? Ys[(rg + i) * ldq + a] : 0.f;
         }
 #pragma unroll
       for (int jb = 0; jb < kT; ++jb) {
@@ -1129,11 +1176,10 @@ __global__ void __launch_bounds__(kSlabThreads) slab_stage_kernel(
 #pragma unroll
             for (int i = 0; i < 4; ++i) y[i][jb] = xb[i];
           }
-          const float* lrow = Us + size_t(b) * q;
+          const float* lrow = Us + b * ldl + lane;
 #pragma unroll
           for (int j = jb; j < kT; ++j) {
-            const int a = lane + 32 * j;
-            const float l = (a > b && a < q) ? lrow[a] : 0.f;
+            const float l = lrow[32 * j];
 #pragma unroll
             for (int i = 0; i < 4; ++i) y[i][j] = fmaf(-xb[i], l, y[i][j]);
           }
@@ -1149,7 +1195,7 @@ __global__ void __launch_bounds__(kSlabThreads) slab_stage_kernel(
         for (int j = 0; j < kT; ++j) {
           const int a = lane + 32 * j;
           if (a < q) {
-            Ys[size_t(r) * q + a] = y[i][j];
+            Ys[r * ldq + a] = y[i][j];
             X[(r0 + r) * q + a] = y[i][j];
           }
         }
@@ -1157,84 +1203,96 @@ __global__ void __launch_bounds__(kSlabThreads) slab_stage_kernel(
     }
     __syncthreads();
   }
-  float g[kT][kT];
+  const int nt4 = ldq / 4;
+  const int ntiles = nt4 * (nt4 + 1) / 2;
+  float4* P = reinterpret_cast<float4*>(part) + size_t(blockIdx.x) * ntiles * 4;
+  for (int t = threadIdx.x; t < ntiles; t += blockDim.x) {
+    int ti, tj;
+    slab_tri_tile(t, nt4, ti, tj);
+    const float* ya = Ys + 4 * ti;
+    const float* yb = Ys + 4 * tj;
+    float g[4][4];
 #pragma unroll
-  for (int i = 0; i < kT; ++i)
+    for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < kT; ++j) g[i][j] = 0.f;
-  for (int r = 0; r < nr; ++r) {
-    const float* yr = Ys + size_t(r) * q;
-    float av[kT], bv[kT];
+      for (int j = 0; j < 4; ++j) g[i][j] = 0.f;
+#pragma unroll 2
+    for (int r = 0; r < nr; ++r) {
+      const float4 a4 = *reinterpret_cast<const float4*>(ya + r * ldq);
+      const float4 b4 = *reinterpret_cast<const float4*>(yb + r * ldq);
+      const float av[4] = {a4.x, a4.y, a4.z, a4.w}, bv[4] = {b4.x, b4.y, b4.z, b4.w};
 #pragma unroll
-    for (int i = 0; i < kT; ++i) {
-      av[i] = yr[warp + 32 * i];
-      bv[i] = yr[lane + 32 * i];
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) g[i][j] = fmaf(av[i], bv[j], g[i][j]);
     }
 #pragma unroll
-    for (int i = 0; i < kT; ++i)
-#pragma unroll
-      for (int j = 0; j < kT; ++j) g[i][j] = fmaf(av[i], bv[j], g[i][j]);
+    for (int i = 0; i < 4; ++i) P[size_t(t) * 4 + i] = make_float4(g[i][0], g[i][1], g[i][2], g[i][3]);
   }
-  float* P = part + size_t(blockIdx.x) * q * q;
-#pragma unroll
-  for (int i = 0; i < kT; ++i)
-#pragma unroll
-    for (int j = 0; j < kT; ++j) {
-      const int a = warp + 32 * i, b = lane + 32 * j;
-      if (a < q && b < q) P[a * q + b] = g[i][j];
-    }
 }
 
-__device__ __forceinline__ void add_to(float4& a, const float4& b) {
-  a.x += b.x;
-  a.y += b.y;
-  a.z += b.z;
-  a.w += b.w;
-}
-__device__ __forceinline__ void add_to(float& a, const float& b) { a += b; }
-
-// G = sum over slabs of part, in a fixed order.  Each CTA: 16 entries
-// (float4 entries when kVec, i.e. q*q % 4 == 0) x 16 slab ranges (about 9
-// slabs each at 149 slabs), combined through shared memory in range order:
-// 400 CTAs at q = 160, each thread a handful of independent loads (64
-// entries x 4 ranges left 100 CTAs waiting on ~37 dependent loads each).
+// G = sum over slabs of the packed tile partials, in a fixed order, written
+// to both triangles.  Each CTA: 16 tile rows (float4) x 16 slab ranges
+// (about 5 slabs each at 81 slabs), combined through shared memory in range
+// order; thread grp 0 writes the tile row and its mirror.
 constexpr int kReduceEntries = 16, kReduceRanges = 16;
 
-template <bool kVec>
 __global__ void __launch_bounds__(256) slab_reduce_kernel(const float* __restrict__ part,
-                                                          int nblk, int qq,
+                                                          int nblk, int q, int nt4,
                                                           float* __restrict__ G) {
-  using V = typename std::conditional<kVec, float4, float>::type;
-  __shared__ V s[kReduceRanges][kReduceEntries];
+  __shared__ float4 s[kReduceRanges][kReduceEntries];
   const int t = threadIdx.x % kReduceEntries, grp = threadIdx.x / kReduceEntries;
-  const int ne = kVec ? qq / 4 : qq;
+  const int ne = nt4 * (nt4 + 1) / 2 * 4;
   const int e = blockIdx.x * kReduceEntries + t;
   const int b0 = grp * nblk / kReduceRanges, b1 = (grp + 1) * nblk / kReduceRanges;
-  V acc;
-  memset(&acc, 0, sizeof(V));
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
   if (e < ne) {
-    const V* pv = reinterpret_cast<const V*>(part);
+    const float4* pv = reinterpret_cast<const float4*>(part);
 #pragma unroll 4
-    for (int b = b0; b < b1; ++b) add_to(acc, pv[size_t(b) * ne + e]);
+    for (int b = b0; b < b1; ++b) {
+      const float4 v = pv[size_t(b) * ne + e];
+      acc.x += v.x;
+      acc.y += v.y;
+      acc.z += v.z;
+      acc.w += v.w;
+    }
   }
   s[grp][t] = acc;
   __syncthreads();
   if (grp == 0 && e < ne) {
-    V r = s[0][t];
+    float4 r = s[0][t];
 #pragma unroll
-    for (int k = 1; k < kReduceRanges; ++k) add_to(r, s[k][t]);
-    reinterpret_cast<V*>(G)[e] = r;
+    for (int k = 1; k < kReduceRanges; ++k) {
+      r.x += s[k][t].x;
+      r.y += s[k][t].y;
+      r.z += s[k][t].z;
+      r.w += s[k][t].w;
+    }
+    int ti, tj;
+    slab_tri_tile(e / 4, nt4, ti, tj);
+    const int row = 4 * ti + (e & 3), col0 = 4 * tj;
+    if (row < q) {
+      const float v[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) {
+        const int col = col0 + cc;
+        if (col < q) {
+          G[size_t(row) * q + col] = v[cc];
+          if (ti != tj) G[size_t(col) * q + row] = v[cc];
+        }
+      }
+    }
   }
 }
 
 template <int kT, bool kVec>
 void slab_stage_launch(Ctx& c, const float* Y, int64_t n, int64_t q, int rpb, int nblk,
                        const float* Lt, float* X, float* part) {
-  const size_t smem = (size_t(rpb) * q + size_t(q) * q + 2 * 32 * kT) * sizeof(float);
+  const size_t smem = slab_smem_bytes(q, rpb);
   CTM_CUDA(cudaFuncSetAttribute(slab_stage_kernel<kT, kVec>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-  // forward substitution (n q^2) and the slab Gram matrices (n q^2 FMA)
-  KernelTimer kt(c.stream, "slab_stage_kernel", kUnitFlop, 4.0 * double(n) * q * q);
+  // forward substitution (n q^2 / 2 FMA) and the slab Gram matrices (n q^2 / 2 FMA)
+  KernelTimer kt(c.stream, "slab_stage_kernel", kUnitFlop, 2.0 * double(n) * q * q);
   slab_stage_kernel<kT, kVec><<<nblk, kSlabThreads, smem, c.stream>>>(Y, n, int(q), rpb, Lt, X,
                                                                       part);
 }
@@ -1252,11 +1310,15 @@ void slab_stage_dispatch(Ctx& c, const float* Y, int64_t n, int64_t q, int rpb, 
   }
 }
 
-// rows per slab: one slab per SM, at most 64 rows (shared memory bound)
-int slab_rows(int64_t n) {
+// rows per slab: about two slabs per SM, as the slab stages of several rows
+// of a move run concurrently (at n = 5184: 64 rows, 81 slabs, measured
+// faster in the concurrent move than one slab of 35 rows per SM); at most 64
+// rows and what shared memory holds
+int slab_rows(int64_t n, int64_t q) {
   const int64_t sms = sm_count_linalg();
-  int64_t rpb = (n + sms - 1) / sms;
+  int64_t rpb = (2 * n + sms - 1) / sms;
   rpb = std::max<int64_t>(4, std::min<int64_t>(64, rpb));
+  while (rpb > 4 && slab_smem_bytes(q, rpb) > kSmemOptin) --rpb;
   return int(rpb);
 }
 
@@ -1267,10 +1329,12 @@ int slab_rows(int64_t n) {
 void slab_gram(Ctx& c, const float* Y, int64_t n, int64_t q, const float* Lt, float* X,
                float* G) {
   CTM_REQUIRE(q >= 1 && q <= 192, CTM_ERR_INVALID, "slab_gram: needs 1 <= q <= 192");
-  const int rpb = slab_rows(n);
+  const int rpb = slab_rows(n, q);
   const int nblk = int((n + rpb - 1) / rpb);
+  const int nt4 = int((q + 3) / 4);
+  const int ne = nt4 * (nt4 + 1) / 2 * 4;  // float4 tile rows per slab
   Scope scope(c);
-  float* part = c.alloc<float>(size_t(nblk) * q * q);
+  float* part = c.alloc<float>(size_t(nblk) * ne * 4);
   if (c.sizing()) return;
   const bool vec = q % 4 == 0 && (reinterpret_cast<uintptr_t>(Y) & 15) == 0 &&
                    (Lt == nullptr || (reinterpret_cast<uintptr_t>(Lt) & 15) == 0);
@@ -1279,14 +1343,11 @@ void slab_gram(Ctx& c, const float* Y, int64_t n, int64_t q, const float* Lt, fl
   else
     slab_stage_dispatch<false>(c, Y, n, q, rpb, nblk, Lt, X, part);
   CTM_LAUNCH_CHECK();
-  const int qq = int(q * q);
-  KernelTimer kt(c.stream, "slab_reduce_kernel", kUnitByte, 4.0 * (double(nblk) + 1.0) * qq);
-  const int ne = qq % 4 == 0 ? qq / 4 : qq;
+  KernelTimer kt(c.stream, "slab_reduce_kernel", kUnitByte,
+                 16.0 * double(nblk) * ne + 4.0 * double(q) * q);
   const unsigned grid = unsigned((ne + kReduceEntries - 1) / kReduceEntries);
-  if (qq % 4 == 0)
-    slab_reduce_kernel<true><<<grid, kReduceEntries * kReduceRanges, 0, c.stream>>>(part, nblk, qq, G);
-  else
-    slab_reduce_kernel<false><<<grid, kReduceEntries * kReduceRanges, 0, c.stream>>>(part, nblk, qq, G);
+  slab_reduce_kernel<<<grid, kReduceEntries * kReduceRanges, 0, c.stream>>>(part, nblk, int(q),
+                                                                            nt4, G);
   CTM_LAUNCH_CHECK();
 }
 

