@@ -14,6 +14,9 @@ void einsum(Ctx& c, const char* spec, const ViewF& A, const ViewF& B, const View
             double alpha = 1.0, double beta = 0.0);
 
 // Deterministic reductions into a device scalar.
+// Number of SMs of the current device.
+int sm_count_linalg();
+
 void absmax(Ctx& c, const double* x, int64_t n, double* out);
 void sumsq(Ctx& c, const double* x, int64_t n, double* out);
 // x[i] = x[i] / s  (mode 0: s = *scal, mode 1: s = sqrt(*scal)) for i < n.

@@ -474,7 +474,10 @@ void einsum_impl(Ctx& c, const char* spec, const ViewT<T>& A, const ViewT<T>& B,
   }
   const int64_t tiles = ((p.Mt + BM - 1) / BM) * ((p.Nt + BN - 1) / BN) * bext;
   int splitk = 1;
-  const int64_t target = 2 * 152;
+  // split K until the grid holds about one CTA per SM: two per SM measured
+  // slower in the concurrent move (the CTAs of other rows' kernels share the
+  // SMs; the split-K partials double), far fewer lengthens the row
+  const int64_t target = sm_count_linalg();
   if (tiles < target && p.Kt >= 2 * BK) {
     splitk = static_cast<int>(std::min<int64_t>((target + tiles - 1) / tiles, p.Kt / BK));
     splitk = std::max(splitk, 1);

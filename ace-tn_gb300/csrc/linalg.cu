@@ -80,13 +80,19 @@ __device__ T block_sum(T v, T* sh) {
 // ------------------------------------------------------------- Householder QR
 // One CTA.  Y (n x q, row-major) is overwritten by the explicit Q; R (q x q)
 // receives the triangular factor when non-null.  V (n x q) and beta (q) are
-// scratch.  Runs only when (flags == nullptr) or (*flags & 1) != 0.
+// scratch.  Runs only when (flags == nullptr) or (*flags & 1) != 0, and then
+// first copies restore (n x q, when non-null) into Y.
 template <class T>
 __global__ void __launch_bounds__(LT) householder_qr_kernel(T* Y, int64_t n, int64_t q,
                                                             T* R, T* V, T* beta,
-                                                            const int* flags, int clear_bit) {
+                                                            const int* flags, int clear_bit,
+                                                            const T* restore = nullptr) {
   if (flags != nullptr && ((*flags) & clear_bit) == 0) return;
   if (flags != nullptr && threadIdx.x == 0) atomicAdd(&g_qr_fallbacks, 1ull);
+  if (restore != nullptr) {
+    for (int64_t i = threadIdx.x; i < n * q; i += LT) Y[i] = restore[i];
+    __syncthreads();
+  }
   __shared__ T sh[LT / 32];
   __shared__ T s_beta, s_alpha;
   for (int64_t j = 0; j < q; ++j) {
@@ -1012,14 +1018,6 @@ __global__ void scale_compact_kernel(const double* in, int64_t rows, int64_t cap
   }
 }
 
-template <class T>
-__global__ void restore_if_flagged_kernel(T* Y, const T* saved, int64_t n, const int* flags) {
-  if (((*flags) & 1) == 0) return;
-  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
-       i += int64_t(gridDim.x) * blockDim.x)
-    Y[i] = saved[i];
-}
-
 }  // namespace
 
 int sm_count_linalg() {
@@ -1234,12 +1232,15 @@ __global__ void __launch_bounds__(kSlabThreads) slab_stage_kernel(
 // G = sum over slabs of the packed tile partials, in a fixed order, written
 // to both triangles.  Each CTA: 16 tile rows (float4) x 16 slab ranges
 // (about 5 slabs each at 81 slabs), combined through shared memory in range
-// order; thread grp 0 writes the tile row and its mirror.
+// order; thread grp 0 writes the tile row and its mirror.  With tol > 0 it
+// also checks the orthonormality of the slab stage's result: flag bit 1
+// when an entry of G - I exceeds tol in magnitude (NaN counts as failure).
 constexpr int kReduceEntries = 16, kReduceRanges = 16;
 
 __global__ void __launch_bounds__(256) slab_reduce_kernel(const float* __restrict__ part,
                                                           int nblk, int q, int nt4,
-                                                          float* __restrict__ G) {
+                                                          float* __restrict__ G, float tol,
+                                                          int* flags) {
   __shared__ float4 s[kReduceRanges][kReduceEntries];
   const int t = threadIdx.x % kReduceEntries, grp = threadIdx.x / kReduceEntries;
   const int ne = nt4 * (nt4 + 1) / 2 * 4;
@@ -1273,14 +1274,17 @@ __global__ void __launch_bounds__(256) slab_reduce_kernel(const float* __restric
     const int row = 4 * ti + (e & 3), col0 = 4 * tj;
     if (row < q) {
       const float v[4] = {r.x, r.y, r.z, r.w};
+      bool bad = false;
 #pragma unroll
       for (int cc = 0; cc < 4; ++cc) {
         const int col = col0 + cc;
         if (col < q) {
           G[size_t(row) * q + col] = v[cc];
           if (ti != tj) G[size_t(col) * q + row] = v[cc];
+          bad = bad || !(fabsf(v[cc] - (row == col ? 1.f : 0.f)) <= tol);
         }
       }
+      if (tol > 0.f && bad) atomicOr(flags, 1);
     }
   }
 }
@@ -1326,8 +1330,9 @@ int slab_rows(int64_t n, int64_t q) {
 
 // G (q x q) = X^T X where X = Y L^-T (Lt = L^T, q x q upper triangular;
 // X written) or X = Y when Lt is null; FP32, q <= 192, one pass over Y.
+// check_tol > 0: sets bit 1 of *flags when max |G - I| > check_tol.
 void slab_gram(Ctx& c, const float* Y, int64_t n, int64_t q, const float* Lt, float* X,
-               float* G) {
+               float* G, float check_tol, int* flags) {
   CTM_REQUIRE(q >= 1 && q <= 192, CTM_ERR_INVALID, "slab_gram: needs 1 <= q <= 192");
   const int rpb = slab_rows(n, q);
   const int nblk = int((n + rpb - 1) / rpb);
@@ -1346,8 +1351,8 @@ void slab_gram(Ctx& c, const float* Y, int64_t n, int64_t q, const float* Lt, fl
   KernelTimer kt(c.stream, "slab_reduce_kernel", kUnitByte,
                  16.0 * double(nblk) * ne + 4.0 * double(q) * q);
   const unsigned grid = unsigned((ne + kReduceEntries - 1) / kReduceEntries);
-  slab_reduce_kernel<<<grid, kReduceEntries * kReduceRanges, 0, c.stream>>>(part, nblk, int(q),
-                                                                            nt4, G);
+  slab_reduce_kernel<<<grid, kReduceEntries * kReduceRanges, 0, c.stream>>>(
+      part, nblk, int(q), nt4, G, check_tol, flags);
   CTM_LAUNCH_CHECK();
 }
 
@@ -1396,6 +1401,7 @@ void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R, int stages) {
   // stage's L^-T (forward substitution with L^T) and forms the next Gram
   // matrix in the same pass over the rows; the factorisation forms no inverse
   const bool fast_f32 = sizeof(T) == 4 && q <= 192;
+  const T tol = sizeof(T) == 8 ? T(stages == 3 ? 1e-11 : 1e-6) : T(stages == 3 ? 2e-4 : 5e-2);
   auto accumulate_r = [&](int stage) {
     if (R == nullptr) return;
     if (stage == 0) {
@@ -1408,15 +1414,17 @@ void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R, int stages) {
   };
   if (fast_f32) {
     float* const Yf = reinterpret_cast<float*>(cur);
-    slab_gram(c, Yf, n, q, nullptr, nullptr, reinterpret_cast<float*>(G));
+    slab_gram(c, Yf, n, q, nullptr, nullptr, reinterpret_cast<float*>(G), -1.f, nullptr);
     for (int stage = 0; stage < stages; ++stage) {
       const int mode = stage < shifted_stages ? 2 : 0;
       if (!c.sizing())
         cholesky<T>(c.stream, G, q, n, mode, Wk, Ek, nullptr, nullptr, Lt, flags);
       accumulate_r(stage);
-      // nxt = cur L^-T and G = nxt^T nxt
+      // nxt = cur L^-T and G = nxt^T nxt; after the last stage the
+      // reduction also checks G against the identity
       slab_gram(c, reinterpret_cast<const float*>(cur), n, q, reinterpret_cast<const float*>(Lt),
-                reinterpret_cast<float*>(nxt), reinterpret_cast<float*>(G));
+                reinterpret_cast<float*>(nxt), reinterpret_cast<float*>(G),
+                stage == stages - 1 ? float(tol) : -1.f, flags);
       std::swap(cur, nxt);
     }
   } else {
@@ -1437,8 +1445,7 @@ void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R, int stages) {
   // back when needed
   T* hv = c.alloc<T>(size_t(n) * q);
   if (c.sizing()) return;
-  const T tol = sizeof(T) == 8 ? T(stages == 3 ? 1e-11 : 1e-6) : T(stages == 3 ? 2e-4 : 5e-2);
-  {
+  if (!fast_f32) {  // (the FP32 slab path checked G in its last reduction)
     KernelTimer kt(c.stream, "orthogonality_check_kernel", kUnitByte, double(sizeof(T)) * q * q);
     orthogonality_check_kernel<T><<<1, 1024, 0, c.stream>>>(G, int(q), tol, flags);
     CTM_LAUNCH_CHECK();
@@ -1447,9 +1454,8 @@ void orthonormalize_impl(Ctx& c, T* Y, int64_t n, int64_t q, T* R, int stages) {
     CTM_CUDA(cudaMemcpyAsync(Y, cur, sizeof(T) * n * q, cudaMemcpyDeviceToDevice, c.stream));
   if (R != nullptr)
     CTM_CUDA(cudaMemcpyAsync(R, Rt, sizeof(T) * q * q, cudaMemcpyDeviceToDevice, c.stream));
-  restore_if_flagged_kernel<T><<<grid_for(n * q, 256), 256, 0, c.stream>>>(Y, V, n * q, flags);
-  CTM_LAUNCH_CHECK();
-  householder_qr_kernel<T><<<1, LT, 0, c.stream>>>(Y, n, q, R, hv, beta, flags, 1);
+  // when flagged: Y = the saved input, then its Householder QR
+  householder_qr_kernel<T><<<1, LT, 0, c.stream>>>(Y, n, q, R, hv, beta, flags, 1, V);
   CTM_LAUNCH_CHECK();
 }
 

@@ -727,31 +727,35 @@ namespace {
 
 // SVD of the Rayleigh-Ritz matrix B (q x n, given as B^T in FP32) and
 // U = Q Ub with Q the final basis Y (m x q, FP32): Ud (m x q), s, Vd (n x q)
-// in FP64.  FP32: Cholesky-QR of B^T and one-sided Jacobi on its triangular
-// factor; fp64_svd: B in FP64 and the FP64 one-sided Jacobi.
+// in FP64; with Ud null, Ub itself (q x q FP64) goes to Ub_out instead.
+// FP32: Cholesky-QR of B^T and one-sided Jacobi on its triangular factor;
+// fp64_svd: B in FP64 and the FP64 one-sided Jacobi.
 void rayleigh_ritz_svd(Ctx& c, const float* Bt, const float* Y, int64_t m, int64_t n, int64_t q,
-                       bool fp64_svd, double* Ud, double* s, double* Vd) {
+                       bool fp64_svd, double* Ud, double* s, double* Vd,
+                       double* Ub_out = nullptr) {
   Scope scope(c);
-  double* Ub = c.alloc<double>(size_t(q) * q);
+  double* Ub = Ud != nullptr ? c.alloc<double>(size_t(q) * q) : Ub_out;
   if (fp64_svd) {
     double* btd = c.alloc<double>(size_t(n) * q);
     double* Bd = c.alloc<double>(size_t(q) * n);
-    double* Yd = c.alloc<double>(size_t(m) * q);
     to_f64(c, Bt, btd, n * q);
     copy2d(c, View(btd, {n, q}).permute({1, 0}), Bd, n);
     svd_thin(c, Bd, q, n, Ub, s, Vd);
+    if (Ud == nullptr) return;
+    double* Yd = c.alloc<double>(size_t(m) * q);
     to_f64(c, Y, Yd, m * q);
     einsum(c, "ik,kj->ij", View(Yd, {m, q}), View(Ub, {q, q}), View(Ud, {m, q}));
     return;
   }
   float* V = c.alloc<float>(size_t(n) * q);
-  float* U = c.alloc<float>(size_t(m) * q);
   svd_via_qr(c, Bt, q, n, Ub, s, V);
+  to_f64(c, V, Vd, n * q);
+  if (Ud == nullptr) return;
+  float* U = c.alloc<float>(size_t(m) * q);
   float* ubf = c.alloc<float>(size_t(q) * q);
   to_f32(c, Ub, ubf, q * q);
   einsum(c, "ik,kj->ij", ViewF(Y, {m, q}), ViewF(ubf, {q, q}), ViewF(U, {m, q}));
   to_f64(c, U, Ud, m * q);
-  to_f64(c, V, Vd, n * q);
 }
 
 // The projectors' final form: fixed width (cap columns, zero past the
@@ -1026,15 +1030,35 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
   }
   delete rf_span;
   // ---- Rayleigh-Ritz: B = (Q^T Q1) Q4 in 3xBF16 (written as B^T in FP32),
-  //      its SVD from an FP32 QR of B^T and one-sided Jacobi
+  //      its SVD from an FP32 QR of B^T and one-sided Jacobi.  The product
+  //      Q1^T Q is kept (c1 x q, K-major over q): the projector Q1^T U f with
+  //      U = Q Ub is then (Q1^T Q) (Ub f), a K = q product instead of K = m.
   double* s = c.alloc<double>(q);
-  double* Ud = c.alloc<double>(size_t(m) * q);
+  double* Ud = f32 ? c.alloc<double>(size_t(m) * q) : nullptr;
+  double* Ub = f32 ? nullptr : c.alloc<double>(size_t(q) * q);
   double* Vd = c.alloc<double>(size_t(n) * q);
+  const int64_t ldwt = tc_ld(q);
+  bf16* wt_hi = f32 ? nullptr : c.alloc<bf16>(size_t(c1) * ldwt);
+  bf16* wt_lo = f32 ? nullptr : c.alloc<bf16>(size_t(c1) * ldwt);
   KernelTimer* svd_span = new KernelTimer(c.stream, kTagSvd, 0.0);
   if (!f32) {
     Scope s2(c);
     const TcOperand qt = yt_operand_f32(c, Y, m, q, q, true);           // Q^T (q x m)
-    const TcOperand w = gemm_to_operand(c, A1.t(true), qt, x3, true, "Rayleigh-Ritz");  // W = Q^T Q1
+    // Q1^T Q (c1 x q): as W = Q^T Q1 (q rows, K = c1) for B and as its
+    // transpose (c1 rows, K = q) for the projector
+    const int64_t ldw = tc_ld(c1);
+    bf16* w_hi = c.alloc<bf16>(size_t(q) * ldw);
+    bf16* w_lo = c.alloc<bf16>(size_t(q) * ldw);
+    {
+      TcOut ow;
+      ow.add(TcKind::kBf16Hi, w_hi, TcLayout::cols(c1, q, ldw));
+      ow.add(TcKind::kBf16Lo, w_lo, TcLayout::cols(c1, q, ldw));
+      ow.add(TcKind::kBf16Hi, wt_hi, TcLayout::rows(c1, q, ldwt));
+      ow.add(TcKind::kBf16Lo, wt_lo, TcLayout::rows(c1, q, ldwt));
+      ow.name = "Rayleigh-Ritz";
+      tc_gemm(c, A1.t(true), qt, x3, ow);
+    }
+    const TcOperand w{w_hi, w_lo, q, c1, ldw};
     TcOut out;
     out.add(TcKind::kF32, Bt, TcLayout::rows(A4.cols, q, q));            // B^T (n x q)
     out.inv_scale = A1.scale;  // normalised quarter tensors
@@ -1042,7 +1066,7 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
     out.name = "Rayleigh-Ritz";
     tc_gemm(c, A4.t(true), w, x3, out);
   }
-  rayleigh_ritz_svd(c, Bt, Y, m, n, q, svd64 || f32, Ud, s, Vd);
+  rayleigh_ritz_svd(c, Bt, Y, m, n, q, svd64 || f32, Ud, s, Vd, Ub);
   delete svd_span;
   // ---- truncation (FP64 spectrum) and projector products (3xBF16)
   KernelTimer proj_span(c.stream, kTagProject, 0.0);
@@ -1055,7 +1079,8 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
   double* P2f = c.alloc<double>(size_t(r4) * cap);
   {
     Scope s2(c);
-    scale_columns(c, Ud, m, cap, q, f);
+    if (f32) scale_columns(c, Ud, m, cap, q, f);
+    else scale_columns(c, Ub, q, cap, q, f);
     scale_columns(c, Vd, n, cap, q, f);
     if (f32) {
       float* uf = c.alloc<float>(size_t(m) * q);
@@ -1071,8 +1096,9 @@ void calculate_projectors_mixed(Ctx& c, const Site* S[4], int k, const ctm_ctmrg
       einsum(c, "ik,kz->iz", ViewF(Q4f, {r4, n}), vv, ViewF(pf, {r4, cap}));
       to_f64(c, pf, P2f, r4 * cap);
     } else {
-    const TcOperand ut = yt_operand(c, Ud, m, cap, q, true);  // (U f)^T (cap x m)
-    gemm_to_f64(c, A1.t(true), ut, x3, P1f, cap, false, A1.scale, "projector");  // Q1^T U f (c1 x cap)
+    const TcOperand ubt = yt_operand(c, Ub, q, cap, q, true);  // (Ub f)^T (cap x q)
+    const TcOperand wt{wt_hi, wt_lo, c1, q, ldwt};               // Q1^T Q (c1 x q)
+    gemm_to_f64(c, wt, ubt, x3, P1f, cap, false, A1.scale, "projector");  // Q1^T Q Ub f (c1 x cap)
     const TcOperand vt = yt_operand(c, Vd, n, cap, q, true);  // (V f)^T (cap x n)
     gemm_to_f64(c, A4.q(true), vt, x3, P2f, cap, false, A4.scale, "projector");  // Q4 V f (r4 x cap)
     }
