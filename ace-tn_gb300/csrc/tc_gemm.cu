@@ -1064,21 +1064,24 @@ __global__ void join_bf16_kernel(const bf16* hi, const bf16* lo, int64_t rows, i
 
 namespace {
 
-// 64 x 64 cells through shared memory, blockIdx.z selects the hi or lo
-// array; 16-byte loads of source rows and 16-byte stores of destination rows
-// (8 BF16 each) where the leading dimensions allow (2-byte accesses reached
-// 2.9 TB/s).  A destination row's last 16-byte piece may run into the
-// padding between its used length and its leading dimension.
+// dst = src^T for one 64 x 64 cell of BF16 (blockIdx.z: the hi or the lo
+// array).  The cell goes through shared memory as 64 rows of 32 words (two
+// BF16 each; rows padded to 33 words, so that the 16-byte loads' four
+// words and the column reads below spread over the banks); a destination
+// word is a 2 x 2 block transposed in registers: lane i of a warp reads the
+// words of source rows 2i and 2i + 1 at one word column and writes word i of
+// the two destination rows that column holds (a warp stores 128 contiguous
+// bytes per destination row; the reads hit at most two words per bank).
 __global__ void __launch_bounds__(256) transpose_bf16_kernel(
     const bf16* src_hi, const bf16* src_lo, int64_t rows, int64_t cols, int64_t ld_src,
     bf16* dst_hi, bf16* dst_lo, int64_t ld_dst) {
-  __shared__ __align__(16) bf16 tile[64][72];
+  __shared__ uint32_t tile[64][33];
   const bf16* src = blockIdx.z ? src_lo : src_hi;
   bf16* dst = blockIdx.z ? dst_lo : dst_hi;
   const int64_t r0 = int64_t(blockIdx.y) * 64, c0 = int64_t(blockIdx.x) * 64;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const bool vsrc = (ld_src & 7) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0;
-  const bool vdst = (ld_dst & 7) == 0 && (reinterpret_cast<uintptr_t>(dst) & 15) == 0;
+  const bool vdst = (ld_dst & 1) == 0 && (reinterpret_cast<uintptr_t>(dst) & 3) == 0;
   const bf16 z = __float2bfloat16(0.f);
   for (int i = tid; i < 512; i += 256) {
     const int rr = i >> 3, ch = i & 7;
@@ -1093,21 +1096,29 @@ __global__ void __launch_bounds__(256) transpose_bf16_kernel(
         v = *reinterpret_cast<const uint4*>(e);
       }
     }
-    *reinterpret_cast<uint4*>(&tile[rr][ch * 8]) = v;
+    tile[rr][ch * 4 + 0] = v.x;
+    tile[rr][ch * 4 + 1] = v.y;
+    tile[rr][ch * 4 + 2] = v.z;
+    tile[rr][ch * 4 + 3] = v.w;
   }
   __syncthreads();
-  for (int i = tid; i < 512; i += 256) {
-    const int cc = i >> 3, ch = i & 7;  // destination row c0 + cc, its entries r0 + ch * 8 ..
-    const int64_t dr = c0 + cc, dc = r0 + ch * 8;
-    if (dr >= cols || dc >= rows) continue;
-    __align__(16) bf16 e[8];
+  const int64_t dc = r0 + 2 * lane;  // destination column of the word's first element
+  for (int wc = warp; wc < 32; wc += 8) {
+    const uint32_t a = tile[2 * lane][wc], b = tile[2 * lane + 1][wc];
+    // destination rows c0 + 2 wc (low halves) and c0 + 2 wc + 1 (high halves)
+    const uint32_t w[2] = {__byte_perm(a, b, 0x5410), __byte_perm(a, b, 0x7632)};
 #pragma unroll
-    for (int j = 0; j < 8; ++j) e[j] = tile[ch * 8 + j][cc];
-    if (vdst && dc + 8 <= ld_dst) {
-      *reinterpret_cast<uint4*>(dst + dr * ld_dst + dc) = *reinterpret_cast<const uint4*>(e);
-    } else {
-      for (int j = 0; j < 8; ++j)
-        if (dc + j < rows) dst[dr * ld_dst + dc + j] = e[j];
+    for (int h = 0; h < 2; ++h) {
+      const int64_t dr = c0 + 2 * wc + h;
+      if (dr >= cols || dc >= rows) continue;
+      bf16* p = dst + dr * ld_dst + dc;
+      if (vdst && dc + 2 <= ld_dst) {
+        *reinterpret_cast<uint32_t*>(p) = w[h];
+      } else {
+        const uint32_t x = w[h];
+        p[0] = *reinterpret_cast<const bf16*>(&x);
+        if (dc + 1 < rows) p[1] = reinterpret_cast<const bf16*>(&x)[1];
+      }
     }
   }
 }
@@ -1461,6 +1472,24 @@ int ctm_autotune_entry(int32_t i, int64_t* mnk, int32_t* mode_choice, double* be
     }
     if (best_ms != nullptr) *best_ms = it->second.best_ms;
     if (default_ms != nullptr) *default_ms = it->second.default_ms;
+  });
+}
+
+// Test hook, not part of the plugin interface (no declaration in the
+// public header): transpose_bf16 on caller-owned BF16 device arrays (src
+// rows x cols with leading dimension ld_src; dst cols x rows with ld_dst; lo
+// arrays optional), on the given stream.
+int ctm_test_transpose_bf16(const void* src_hi, const void* src_lo, int64_t rows, int64_t cols,
+                            int64_t ld_src, void* dst_hi, void* dst_lo, int64_t ld_dst,
+                            void* stream) {
+  return guarded([&] {
+    CTM_REQUIRE(rows >= 1 && cols >= 1 && ld_src >= cols && ld_dst >= rows, CTM_ERR_INVALID,
+                "transpose: bad sizes");
+    Ctx c;
+    c.stream = static_cast<cudaStream_t>(stream);
+    c.base = reinterpret_cast<char*>(16);  // not sizing; nothing is allocated
+    transpose_bf16(c, static_cast<const bf16*>(src_hi), static_cast<const bf16*>(src_lo), rows,
+                   cols, ld_src, static_cast<bf16*>(dst_hi), static_cast<bf16*>(dst_lo), ld_dst);
   });
 }
 

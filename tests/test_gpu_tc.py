@@ -53,3 +53,38 @@ def test_no_timeout_flags():
     A, B = _rand(512, 64, 5), _rand(64, 96, 6)
     gb.matmul(A, B, precision="mixed")
     assert gb._abi.device_status() == 0
+
+
+@pytest.mark.parametrize("rows,cols,ld_src,ld_dst", [
+    (64, 64, 64, 64),          # one cell
+    (5184, 160, 192, 5184),    # a quarter-tensor-like tall operand
+    (81, 81, 128, 128),        # odd sizes: ragged cells, the last word half padding
+    (100, 37, 37, 101),        # odd leading dimensions: element-wise loads and stores
+    (1, 70, 70, 2),            # a single row
+    (130, 1, 1, 130),          # a single column
+])
+def test_transpose_bf16_exact(rows, cols, ld_src, ld_dst):
+    """The BF16 transpose of the quarter-tensor operands (64 x 64 cells,
+    2 x 2 blocks transposed from 32-bit words): dst == src^T bit for bit,
+    for the hi and the lo array, and nothing written past the transposed
+    block's rows."""
+    import ctypes
+    from acetn_gb300 import _abi
+    lib = _abi.load()
+    fn = lib.ctm_test_transpose_bf16
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                   ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                   ctypes.c_void_p]
+    fn.restype = ctypes.c_int
+    g = torch.Generator().manual_seed(rows * 1000 + cols)
+    src = [torch.randn(rows, ld_src, generator=g).to(torch.bfloat16).cuda() for _ in range(2)]
+    sentinel = torch.tensor(7.0, dtype=torch.bfloat16)
+    dst = [torch.full((cols + 1, ld_dst), float(sentinel), dtype=torch.bfloat16, device="cuda")
+           for _ in range(2)]
+    st = fn(src[0].data_ptr(), src[1].data_ptr(), rows, cols, ld_src, dst[0].data_ptr(),
+            dst[1].data_ptr(), ld_dst, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0, lib.ctm_last_error()
+    torch.cuda.synchronize()
+    for s, d in zip(src, dst):
+        assert torch.equal(d[:cols, :rows], s[:, :cols].t())
+        assert torch.all(d[cols] == sentinel)  # the row after the last is untouched
