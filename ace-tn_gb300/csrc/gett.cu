@@ -574,11 +574,14 @@ void reduce(Ctx& c, const double* x, int64_t n, double* out, int op) {
   CTM_LAUNCH_CHECK();
 }
 
+// x /= s (mode 0) or x /= sqrt(s) (mode 1), as a product with the
+// reciprocal (within an ulp of the quotient; an FP64 division per entry is a
+// long sequence on the FP64 units)
 __global__ void divide_kernel(double* x, int64_t n, const double* scal, int mode) {
-  const double s = mode == 0 ? scal[0] : sqrt(scal[0]);
+  const double r = 1.0 / (mode == 0 ? scal[0] : sqrt(scal[0]));
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * blockDim.x)
-    x[i] = x[i] / s;
+    x[i] *= r;
 }
 
 __global__ void copy2d_kernel(const double* src, int64_t rows, int64_t cols, int64_t s0,

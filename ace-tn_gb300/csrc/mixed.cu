@@ -49,25 +49,61 @@ QOps alloc_ops(Ctx& c, int64_t rows, int64_t cols) {
 // Contracting a ket-bra pair of environment legs against it replaces the two
 // one-layer contractions of make_quarter_tensor / renormalize_ej, whose
 // K = D^2 and D^2 d are too short to keep the tensor cores busy.
-__global__ void double_layer_kernel(const double* A, int64_t s0, int64_t s1, int64_t s2,
-                                    int64_t s3, int64_t s4, int D, int d, bf16* hi, bf16* lo,
-                                    int64_t ld) {
-  // 32-bit index decoding (D^8 < 2^31, checked on the host)
-  const uint32_t D4 = uint32_t(D) * D * D * D, uD = uint32_t(D);
-  for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < D4 * D4;
-       idx += gridDim.x * blockDim.x) {
-    const uint32_t n = idx / D4, k = idx - n * D4;
-    const int DD = int(n % uD), dd = int((n / uD) % uD), R = int((n / (uD * uD)) % uD),
-              r = int(n / (uD * uD * uD));
-    const int U = int(k % uD), u = int((k / uD) % uD), L = int((k / (uD * uD)) % uD),
-              l = int(k / (uD * uD * uD));
-    const double* ket = A + l * s0 + u * s1 + r * s2 + dd * s3;
-    const double* bra = A + L * s0 + U * s1 + R * s2 + DD * s3;
-    double v = 0.0;
-    for (int p = 0; p < d; ++p) v = fma(ket[p * s4], bra[p * s4], v);
-    const bf16 h = __double2bfloat16(v);
-    hi[int64_t(n) * ld + k] = h;
-    lo[int64_t(n) * ld + k] = __double2bfloat16(v - double(__bfloat162float(h)));
+// Each CTA copies A into shared memory in FP32 (legs l, u, r, d, p, p
+// fastest) with the per-column offsets of the ket (l, u) and bra (L, U)
+// legs, then forms kDlRows rows: one FP32 FMA chain over p per entry (its
+// rounding, ~1e-7 of the terms, sits far below the hi/lo pair's 16 bits) and
+// the hi/lo split in FP32 (x - hi is exact).  FP64 arithmetic and the
+// per-entry index decoding made the earlier form several times slower.
+constexpr int kDlRows = 8;
+
+inline size_t double_layer_smem(int64_t D, int64_t d) {
+  const int64_t D4 = D * D * D * D;
+  return size_t(D4 * d + 2 * D4) * 4;
+}
+
+__global__ void __launch_bounds__(256) double_layer_kernel(const double* A, int64_t s0,
+                                                           int64_t s1, int64_t s2, int64_t s3,
+                                                           int64_t s4, int D, int d, bf16* hi,
+                                                           bf16* lo, int64_t ld) {
+  extern __shared__ float dl_smem[];
+  const int D2 = D * D, D4 = D2 * D2;
+  const int c1 = D2 * d, c0 = D * c1, c2 = D * d, c3 = d;  // canonical strides of l, u, r, d
+  float* As = dl_smem;                                       // D^4 d
+  int* kofs = reinterpret_cast<int*>(As + D4 * d);           // ket offset of column k
+  int* bofs = kofs + D4;                                     // bra offset of column k
+  for (int i = threadIdx.x; i < D4 * d; i += blockDim.x) {
+    int t = i;
+    const int p = t % d;
+    t /= d;
+    const int dd = t % D;
+    t /= D;
+    const int r = t % D;
+    t /= D;
+    const int u = t % D, l = t / D;
+    As[i] = float(A[l * s0 + u * s1 + r * s2 + dd * s3 + p * s4]);
+  }
+  for (int k = threadIdx.x; k < D4; k += blockDim.x) {
+    const int U = k % D, u = (k / D) % D, L = (k / D2) % D, l = k / (D2 * D);
+    kofs[k] = l * c0 + u * c1;
+    bofs[k] = L * c0 + U * c1;
+  }
+  __syncthreads();
+  const int n_end = min(D4, int(blockIdx.x + 1) * kDlRows);
+  for (int n = int(blockIdx.x) * kDlRows; n < n_end; ++n) {
+    const int DD = n % D, dd = (n / D) % D, R = (n / D2) % D, r = n / (D2 * D);
+    const int kn = r * c2 + dd * c3, bn = R * c2 + DD * c3;
+    bf16* hrow = hi + int64_t(n) * ld;
+    bf16* lrow = lo + int64_t(n) * ld;
+    for (int k = threadIdx.x; k < D4; k += blockDim.x) {
+      const float* ket = As + kofs[k] + kn;
+      const float* bra = As + bofs[k] + bn;
+      float v = 0.f;
+      for (int p = 0; p < d; ++p) v = fmaf(ket[p], bra[p], v);
+      const bf16 h = __float2bfloat16(v);
+      hrow[k] = h;
+      lrow[k] = __float2bfloat16(v - __bfloat162float(h));
+    }
   }
 }
 
@@ -84,10 +120,14 @@ DLOp double_layer(Ctx& c, const View& ak, int64_t D, int64_t d) {
   o.hi = c.alloc<bf16>(size_t(o.n) * o.ld);
   o.lo = c.alloc<bf16>(size_t(o.n) * o.ld);
   if (!c.sizing()) {
-    CTM_REQUIRE(o.n * o.n < (int64_t(1) << 31), CTM_ERR_UNSUPPORTED,
-                "double layer: D^8 must be below 2^31");
+    const size_t smem = double_layer_smem(D, d);
+    CTM_REQUIRE(o.n * o.n < (int64_t(1) << 31) && smem <= size_t(200) * 1024, CTM_ERR_UNSUPPORTED,
+                "double layer: D^4 (d + 2) floats must fit in shared memory (the one-layer "
+                "form serves larger D)");
     KernelTimer kt(c.stream, "double_layer_kernel", kUnitByte, 4.0 * double(o.n) * o.n);
-    double_layer_kernel<<<grid_for(o.n * o.n, 256), 256, 0, c.stream>>>(
+    CTM_CUDA(cudaFuncSetAttribute(double_layer_kernel,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    double_layer_kernel<<<unsigned((o.n + kDlRows - 1) / kDlRows), 256, smem, c.stream>>>(
         ak.p, ak.stride[0], ak.stride[1], ak.stride[2], ak.stride[3], ak.stride[4], int(D),
         int(d), o.hi, o.lo, o.ld);
     CTM_LAUNCH_CHECK();
@@ -583,10 +623,11 @@ __global__ void double_layer_open_kernel(const double* A, int64_t s0, int64_t s1
     const int Bo = int(n / ud);
     const int64_t ket = K1 * st[g1] + K2 * st[g2] + Ko * st[o] + Kd * st[3] + Kp * st[4];
     const int64_t bra = B1 * st[g1] + B2 * st[g2] + Bo * st[o] + Bd * st[3] + Bp * st[4];
-    const double v = A[ket] * A[bra];
-    const bf16 h = __double2bfloat16(v);
+    // one product: FP32 (~1e-7) is far inside the hi/lo pair's 16 bits
+    const float v = float(A[ket]) * float(A[bra]);
+    const bf16 h = __float2bfloat16(v);
     hi[int64_t(row) * ld + k] = h;
-    lo[int64_t(row) * ld + k] = __double2bfloat16(v - double(__bfloat162float(h)));
+    lo[int64_t(row) * ld + k] = __float2bfloat16(v - __bfloat162float(h));
   }
 }
 
