@@ -1089,13 +1089,15 @@ __device__ __forceinline__ void slab_tri_tile(int t, int nt4, int& ti, int& tj) 
 // matrix X^T X; without Lt: Y^T Y.  A zero diagonal of L (a pivot the
 // factorisation dropped) gives a zero column of X.
 // Shared memory: the slab (rpb rows of ldq = q rounded up to 4 floats, zero
-// past column q) and Lt (q rows of 32 kT floats, zero past column q and, once
-// the reciprocal pivots are taken, on the diagonal: the update loop then
-// reads every column unconditionally).
+// past column q) and Lt (q rows of 32 kT floats; once the reciprocal pivots
+// are taken, row b holds L[a][b] / L[b][b] for a > b and zeros elsewhere, so
+// the update loop reads every column unconditionally).
 // Solve: warp w owns rows 4w..4w+3 (+128 per pass), lane the columns
-// lane + 32 j; column b is finished by its owner lane and broadcast with a
-// shuffle, then every lane subtracts x_b L[a][b] (row b of Lt, read
-// conflict-free) from its columns, which changes only those with a > b.
+// lane + 32 j, which hold residuals r_a; column b's residual is broadcast
+// from its owner lane with a shuffle and every lane subtracts r_b times its
+// entry of scaled row b (read conflict-free); at the end of each block of 32
+// columns the lanes turn their residuals into x_a = r_a / L[a][a].  Full
+// blocks are unrolled (the shuffle source and the loop bounds constant).
 // Gram: the upper triangle of the slab's Gram matrix in 4 x 4 tiles, one
 // tile per thread (two 16-byte reads per 16 FMAs and row), written packed:
 // part[blockIdx.x][t][4][4] for tile t (slab_tri_tile order).
@@ -1132,16 +1134,12 @@ __global__ void __launch_bounds__(kSlabThreads) slab_stage_kernel(
         cp_async_f32(Us + r * ldl + c, Lt + size_t(r) * q + c);
       }
   }
-  // the padding columns (not touched by the copies)
+  // the slab's padding columns (not touched by the copies; those of Lt are
+  // zeroed with the scaling below)
   if (ldq > q)
     for (int i = threadIdx.x; i < nr * (ldq - q); i += blockDim.x) {
       const int r = i / (ldq - q);
       Ys[r * ldq + q + (i - r * (ldq - q))] = 0.f;
-    }
-  if (Lt != nullptr && ldl > q)
-    for (int i = threadIdx.x; i < q * (ldl - q); i += blockDim.x) {
-      const int r = i / (ldl - q);
-      Us[r * ldl + q + (i - r * (ldl - q))] = 0.f;
     }
   cp_async_wait_all();
   __syncthreads();
@@ -1149,7 +1147,13 @@ __global__ void __launch_bounds__(kSlabThreads) slab_stage_kernel(
     for (int b = threadIdx.x; b < q; b += blockDim.x) {
       const float d = Us[b * ldl + b];
       s_rdiag[b] = d > 0.f ? 1.f / d : 0.f;
-      Us[b * ldl + b] = 0.f;
+    }
+    __syncthreads();
+    // row b of L^T scaled by 1 / L[b][b], zero at and below the diagonal:
+    // the update of the residual r_a by column b is then r_a -= r_b Us[b][a]
+    for (int i = threadIdx.x; i < q * ldl; i += blockDim.x) {
+      const int b = i / ldl, a = i - b * ldl;
+      Us[i] = (a > b && a < q) ? Us[i] * s_rdiag[b] : 0.f;
     }
     __syncthreads();
     for (int rg = warp * 4; rg < nr; rg += 4 * 32) {
@@ -1161,27 +1165,35 @@ __global__ void __launch_bounds__(kSlabThreads) slab_stage_kernel(
           const int a = lane + 32 * j;
           y[i][j] = (rg + i < nr && a < q) ? Ys[(rg + i) * ldq + a] : 0.f;
         }
+      // column b: its residual (final once the columns before it are done)
+      // broadcast from its owner lane, subtracted from the columns after it
+      auto step = [&](int jb, int bl) {
+        float rb[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) rb[i] = __shfl_sync(0xffffffffu, y[i][jb], bl);
+        const float* lrow = Us + (32 * jb + bl) * ldl + lane;
+#pragma unroll
+        for (int j = 0; j < kT; ++j) {
+          if (j < jb) continue;
+          const float l = lrow[32 * j];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) y[i][j] = fmaf(-rb[i], l, y[i][j]);
+        }
+      };
 #pragma unroll
       for (int jb = 0; jb < kT; ++jb) {
         const int nb = q - 32 * jb < 32 ? q - 32 * jb : 32;
-        for (int bl = 0; bl < nb; ++bl) {
-          const int b = 32 * jb + bl;
-          const float rd = s_rdiag[b];
-          float xb[4];
+        if (nb == 32) {
 #pragma unroll
-          for (int i = 0; i < 4; ++i) xb[i] = __shfl_sync(0xffffffffu, y[i][jb], bl) * rd;
-          if (lane == bl) {
-#pragma unroll
-            for (int i = 0; i < 4; ++i) y[i][jb] = xb[i];
-          }
-          const float* lrow = Us + b * ldl + lane;
-#pragma unroll
-          for (int j = jb; j < kT; ++j) {
-            const float l = lrow[32 * j];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) y[i][j] = fmaf(-xb[i], l, y[i][j]);
-          }
+          for (int bl = 0; bl < 32; ++bl) step(jb, bl);
+        } else {
+          for (int bl = 0; bl < nb; ++bl) step(jb, bl);
         }
+        // the block's columns are final: x = r / L[b][b]
+        const int a = lane + 32 * jb;
+        const float rd = a < q ? s_rdiag[a] : 0.f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) y[i][jb] *= rd;
       }
       // every warp reads only its own rows of Ys: overwrite them in place
       __syncwarp();

@@ -1064,8 +1064,9 @@ __global__ void join_bf16_kernel(const bf16* hi, const bf16* lo, int64_t rows, i
 
 namespace {
 
-// dst = src^T for one 64 x 64 cell of BF16 (blockIdx.z: the hi or the lo
-// array).  The cell goes through shared memory as 64 rows of 32 words (two
+// dst = src^T for one 64 x 64 cell of BF16, of the hi and (when given) the
+// lo array in the same CTA, so that each thread has four 16-byte loads in
+// flight.  A cell goes through shared memory as 64 rows of 32 words (two
 // BF16 each; rows padded to 33 words, so that the 16-byte loads' four
 // words and the column reads below spread over the banks); a destination
 // word is a 2 x 2 block transposed in registers: lane i of a warp reads the
@@ -1075,49 +1076,65 @@ namespace {
 __global__ void __launch_bounds__(256) transpose_bf16_kernel(
     const bf16* src_hi, const bf16* src_lo, int64_t rows, int64_t cols, int64_t ld_src,
     bf16* dst_hi, bf16* dst_lo, int64_t ld_dst) {
-  __shared__ uint32_t tile[64][33];
-  const bf16* src = blockIdx.z ? src_lo : src_hi;
-  bf16* dst = blockIdx.z ? dst_lo : dst_hi;
+  __shared__ uint32_t tile[2][64][33];
+  const int na = src_lo != nullptr ? 2 : 1;
   const int64_t r0 = int64_t(blockIdx.y) * 64, c0 = int64_t(blockIdx.x) * 64;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const bool vsrc = (ld_src & 7) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0;
-  const bool vdst = (ld_dst & 1) == 0 && (reinterpret_cast<uintptr_t>(dst) & 3) == 0;
+  const bool vsrc = (ld_src & 7) == 0 && (reinterpret_cast<uintptr_t>(src_hi) & 15) == 0 &&
+                    (na == 1 || (reinterpret_cast<uintptr_t>(src_lo) & 15) == 0);
+  const bool vdst = (ld_dst & 1) == 0 && (reinterpret_cast<uintptr_t>(dst_hi) & 3) == 0 &&
+                    (na == 1 || (reinterpret_cast<uintptr_t>(dst_lo) & 3) == 0);
   const bf16 z = __float2bfloat16(0.f);
-  for (int i = tid; i < 512; i += 256) {
-    const int rr = i >> 3, ch = i & 7;
-    const int64_t r = r0 + rr, cc = c0 + ch * 8;
-    uint4 v = make_uint4(0u, 0u, 0u, 0u);
-    if (r < rows && cc < cols) {
-      if (vsrc && cc + 8 <= cols) {
-        v = *reinterpret_cast<const uint4*>(src + r * ld_src + cc);
-      } else {
-        __align__(16) bf16 e[8];
-        for (int j = 0; j < 8; ++j) e[j] = cc + j < cols ? src[r * ld_src + cc + j] : z;
-        v = *reinterpret_cast<const uint4*>(e);
+  uint4 v[2][2];
+#pragma unroll
+  for (int a = 0; a < 2; ++a) {
+    const bf16* src = a == 0 ? src_hi : src_lo;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int i = tid + 256 * j, rr = i >> 3, ch = i & 7;
+      const int64_t r = r0 + rr, cc = c0 + ch * 8;
+      v[a][j] = make_uint4(0u, 0u, 0u, 0u);
+      if (a < na && r < rows && cc < cols) {
+        if (vsrc && cc + 8 <= cols) {
+          v[a][j] = *reinterpret_cast<const uint4*>(src + r * ld_src + cc);
+        } else {
+          __align__(16) bf16 e[8];
+          for (int t = 0; t < 8; ++t) e[t] = cc + t < cols ? src[r * ld_src + cc + t] : z;
+          v[a][j] = *reinterpret_cast<const uint4*>(e);
+        }
       }
     }
-    tile[rr][ch * 4 + 0] = v.x;
-    tile[rr][ch * 4 + 1] = v.y;
-    tile[rr][ch * 4 + 2] = v.z;
-    tile[rr][ch * 4 + 3] = v.w;
   }
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int i = tid + 256 * j, rr = i >> 3, ch = i & 7;
+      tile[a][rr][ch * 4 + 0] = v[a][j].x;
+      tile[a][rr][ch * 4 + 1] = v[a][j].y;
+      tile[a][rr][ch * 4 + 2] = v[a][j].z;
+      tile[a][rr][ch * 4 + 3] = v[a][j].w;
+    }
   __syncthreads();
   const int64_t dc = r0 + 2 * lane;  // destination column of the word's first element
-  for (int wc = warp; wc < 32; wc += 8) {
-    const uint32_t a = tile[2 * lane][wc], b = tile[2 * lane + 1][wc];
-    // destination rows c0 + 2 wc (low halves) and c0 + 2 wc + 1 (high halves)
-    const uint32_t w[2] = {__byte_perm(a, b, 0x5410), __byte_perm(a, b, 0x7632)};
+  for (int a = 0; a < na; ++a) {
+    bf16* dst = a == 0 ? dst_hi : dst_lo;
+    for (int wc = warp; wc < 32; wc += 8) {
+      const uint32_t x0 = tile[a][2 * lane][wc], x1 = tile[a][2 * lane + 1][wc];
+      // destination rows c0 + 2 wc (low halves) and c0 + 2 wc + 1 (high halves)
+      const uint32_t w[2] = {__byte_perm(x0, x1, 0x5410), __byte_perm(x0, x1, 0x7632)};
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int64_t dr = c0 + 2 * wc + h;
-      if (dr >= cols || dc >= rows) continue;
-      bf16* p = dst + dr * ld_dst + dc;
-      if (vdst && dc + 2 <= ld_dst) {
-        *reinterpret_cast<uint32_t*>(p) = w[h];
-      } else {
-        const uint32_t x = w[h];
-        p[0] = *reinterpret_cast<const bf16*>(&x);
-        if (dc + 1 < rows) p[1] = reinterpret_cast<const bf16*>(&x)[1];
+      for (int h = 0; h < 2; ++h) {
+        const int64_t dr = c0 + 2 * wc + h;
+        if (dr >= cols || dc >= rows) continue;
+        bf16* p = dst + dr * ld_dst + dc;
+        if (vdst && dc + 2 <= ld_dst) {
+          *reinterpret_cast<uint32_t*>(p) = w[h];
+        } else {
+          const uint32_t x = w[h];
+          p[0] = *reinterpret_cast<const bf16*>(&x);
+          if (dc + 1 < rows) p[1] = reinterpret_cast<const bf16*>(&x)[1];
+        }
       }
     }
   }
@@ -1130,7 +1147,7 @@ void transpose_bf16(Ctx& c, const bf16* src_hi, const bf16* src_lo, int64_t rows
   if (c.sizing() || rows * cols == 0) return;
   CTM_REQUIRE((src_lo == nullptr) == (dst_lo == nullptr), CTM_ERR_INVALID,
               "transpose_bf16: lo arrays must be given on both sides or neither");
-  const dim3 grid(unsigned((cols + 63) / 64), unsigned((rows + 63) / 64), src_lo ? 2u : 1u);
+  const dim3 grid(unsigned((cols + 63) / 64), unsigned((rows + 63) / 64), 1u);
   CTM_REQUIRE(grid.y <= 65535, CTM_ERR_UNSUPPORTED, "transpose_bf16: too many rows");
   KernelTimer kt(c.stream, "transpose_bf16_kernel", kUnitByte,
                  4.0 * double(rows) * cols * (src_lo != nullptr ? 2.0 : 1.0));

