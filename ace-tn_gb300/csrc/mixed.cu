@@ -57,6 +57,19 @@ QOps alloc_ops(Ctx& c, int64_t rows, int64_t cols) {
 // per-entry index decoding made the earlier form several times slower.
 constexpr int kDlRows = 8;
 
+// x / d for x, d < 2^16 with m = ceil(2^32 / d) (d >= 2): q = (x m) >> 32 is
+// exact, as x (m d - 2^32) < x d < 2^32.  The double-layer kernels decode
+// every index through it instead of 32-bit division sequences.
+struct Div16 {
+  uint32_t d, m;
+};
+inline Div16 make_div16(int d) {
+  return Div16{uint32_t(d), d >= 2 ? uint32_t(((uint64_t(1) << 32) + uint64_t(d) - 1) / d) : 0u};
+}
+__device__ __forceinline__ uint32_t div16(uint32_t x, Div16 v) {
+  return v.d == 1 ? x : __umulhi(x, v.m);
+}
+
 inline size_t double_layer_smem(int64_t D, int64_t d) {
   const int64_t D4 = D * D * D * D;
   return size_t(D4 * d + 2 * D4) * 4;
@@ -64,34 +77,52 @@ inline size_t double_layer_smem(int64_t D, int64_t d) {
 
 __global__ void __launch_bounds__(256) double_layer_kernel(const double* A, int64_t s0,
                                                            int64_t s1, int64_t s2, int64_t s3,
-                                                           int64_t s4, int D, int d, bf16* hi,
-                                                           bf16* lo, int64_t ld) {
+                                                           int64_t s4, Div16 vD, Div16 vd,
+                                                           bf16* hi, bf16* lo, int64_t ld) {
   extern __shared__ float dl_smem[];
+  const int D = int(vD.d), d = int(vd.d);
   const int D2 = D * D, D4 = D2 * D2;
   const int c1 = D2 * d, c0 = D * c1, c2 = D * d, c3 = d;  // canonical strides of l, u, r, d
   float* As = dl_smem;                                       // D^4 d
   int* kofs = reinterpret_cast<int*>(As + D4 * d);           // ket offset of column k
   int* bofs = kofs + D4;                                     // bra offset of column k
   for (int i = threadIdx.x; i < D4 * d; i += blockDim.x) {
-    int t = i;
-    const int p = t % d;
-    t /= d;
-    const int dd = t % D;
-    t /= D;
-    const int r = t % D;
-    t /= D;
-    const int u = t % D, l = t / D;
+    uint32_t t = uint32_t(i), q = div16(t, vd);
+    const int p = int(t - q * d);
+    t = q;
+    q = div16(t, vD);
+    const int dd = int(t - q * D);
+    t = q;
+    q = div16(t, vD);
+    const int r = int(t - q * D);
+    t = q;
+    q = div16(t, vD);
+    const int u = int(t - q * D), l = int(q);
     As[i] = float(A[l * s0 + u * s1 + r * s2 + dd * s3 + p * s4]);
   }
   for (int k = threadIdx.x; k < D4; k += blockDim.x) {
-    const int U = k % D, u = (k / D) % D, L = (k / D2) % D, l = k / (D2 * D);
+    uint32_t t = uint32_t(k), q = div16(t, vD);
+    const int U = int(t - q * D);
+    t = q;
+    q = div16(t, vD);
+    const int u = int(t - q * D);
+    t = q;
+    q = div16(t, vD);
+    const int L = int(t - q * D), l = int(q);
     kofs[k] = l * c0 + u * c1;
     bofs[k] = L * c0 + U * c1;
   }
   __syncthreads();
   const int n_end = min(D4, int(blockIdx.x + 1) * kDlRows);
   for (int n = int(blockIdx.x) * kDlRows; n < n_end; ++n) {
-    const int DD = n % D, dd = (n / D) % D, R = (n / D2) % D, r = n / (D2 * D);
+    uint32_t t = uint32_t(n), q = div16(t, vD);
+    const int DD = int(t - q * D);
+    t = q;
+    q = div16(t, vD);
+    const int dd = int(t - q * D);
+    t = q;
+    q = div16(t, vD);
+    const int R = int(t - q * D), r = int(q);
     const int kn = r * c2 + dd * c3, bn = R * c2 + DD * c3;
     bf16* hrow = hi + int64_t(n) * ld;
     bf16* lrow = lo + int64_t(n) * ld;
@@ -121,15 +152,17 @@ DLOp double_layer(Ctx& c, const View& ak, int64_t D, int64_t d) {
   o.lo = c.alloc<bf16>(size_t(o.n) * o.ld);
   if (!c.sizing()) {
     const size_t smem = double_layer_smem(D, d);
-    CTM_REQUIRE(o.n * o.n < (int64_t(1) << 31) && smem <= size_t(200) * 1024, CTM_ERR_UNSUPPORTED,
-                "double layer: D^4 (d + 2) floats must fit in shared memory (the one-layer "
-                "form serves larger D)");
+    CTM_REQUIRE(o.n * o.n < (int64_t(1) << 31) && smem <= size_t(200) * 1024 &&
+                    o.n * d < (int64_t(1) << 16),
+                CTM_ERR_UNSUPPORTED,
+                "double layer: needs D^4 d < 2^16 and D^4 (d + 2) floats in shared memory "
+                "(the one-layer form serves larger D)");
     KernelTimer kt(c.stream, "double_layer_kernel", kUnitByte, 4.0 * double(o.n) * o.n);
     CTM_CUDA(cudaFuncSetAttribute(double_layer_kernel,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     double_layer_kernel<<<unsigned((o.n + kDlRows - 1) / kDlRows), 256, smem, c.stream>>>(
-        ak.p, ak.stride[0], ak.stride[1], ak.stride[2], ak.stride[3], ak.stride[4], int(D),
-        int(d), o.hi, o.lo, o.ld);
+        ak.p, ak.stride[0], ak.stride[1], ak.stride[2], ak.stride[3], ak.stride[4],
+        make_div16(int(D)), make_div16(int(d)), o.hi, o.lo, o.ld);
     CTM_LAUNCH_CHECK();
   }
   return o;
