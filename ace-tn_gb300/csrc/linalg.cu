@@ -1084,7 +1084,7 @@ __device__ __forceinline__ void slab_tri_tile(int t, int nt4, int& ti, int& tj) 
 
 // One slab of rows [r0, r0 + nr) of Y (n x q, row-major), r0 = blockIdx.x * rpb.
 // With Lt (q x q, the upper triangular L^T of a Cholesky factor L; entries
-// below the diagonal are not read): X = Y L^-T for the slab by forward substitution (x L^T = y
+// below the diagonal do not matter): X = Y L^-T for the slab by forward substitution (x L^T = y
 // row by row; written to X and kept in shared memory), then the slab's Gram
 // matrix X^T X; without Lt: Y^T Y.  A zero diagonal of L (a pivot the
 // factorisation dropped) gives a zero column of X.
