@@ -808,16 +808,32 @@ __global__ void __launch_bounds__(256) jacobi_cluster_f32_kernel(const float* Mc
 
 // Ub[:, r] = J[:, order[r]] (J columns stored as rows of Jc), S[r] = norm,
 // inv_s[r] = 1 / S[r] (0 for a zero norm); order by descending norm.
-__global__ void sort_singular_kernel(const float* Jc, const float* norms, int q, double* Ub,
-                                     double* S, double* inv_s) {
+// One CTA (q <= 1024): the rank of every row norm (descending, ties by
+// index) from a shared-memory copy of the norms, then Ub[t][rank[j]] =
+// Jc[j][t] by all threads (each thread's copies independent: the row-per-
+// thread loop waited on one load at a time).
+constexpr int kSortThreads = 1024;
+__global__ void __launch_bounds__(kSortThreads) sort_singular_kernel(const float* Jc,
+                                                                     const float* norms, int q,
+                                                                     double* Ub, double* S,
+                                                                     double* inv_s) {
+  __shared__ float s_norm[kSortThreads];
+  __shared__ int s_rank[kSortThreads];
+  for (int j = threadIdx.x; j < q; j += blockDim.x) s_norm[j] = norms[j];
+  __syncthreads();
   for (int j = threadIdx.x; j < q; j += blockDim.x) {
     int rank = 0;
-    const float nj = norms[j];
+    const float nj = s_norm[j];
     for (int i = 0; i < q; ++i)
-      if (norms[i] > nj || (norms[i] == nj && i < j)) ++rank;
+      if (s_norm[i] > nj || (s_norm[i] == nj && i < j)) ++rank;
+    s_rank[j] = rank;
     S[rank] = double(nj);
     inv_s[rank] = nj > 0.f ? 1.0 / double(nj) : 0.0;
-    for (int t = 0; t < q; ++t) Ub[t * q + rank] = double(Jc[j * q + t]);
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
+    const int j = idx / q, t = idx - j * q;
+    Ub[size_t(t) * q + s_rank[j]] = double(Jc[idx]);
   }
 }
 
@@ -1011,6 +1027,16 @@ __global__ void scale_compact_kernel(const double* in, int64_t rows, int64_t cap
                                      const int64_t* chi_new, double* out) {
   const int64_t cn = *chi_new;
   const int64_t total = rows * cn;
+  if (total < (int64_t(1) << 31)) {  // 32-bit decoding (a 64-bit division is a long sequence)
+    const uint32_t ucn = uint32_t(cn);
+    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < uint32_t(total);
+         idx += gridDim.x * blockDim.x) {
+      const uint32_t r = idx / ucn, c = idx - r * ucn;
+      const double v = in[int64_t(r) * cap + c];
+      out[idx] = f != nullptr ? v * f[c] : v;
+    }
+    return;
+  }
   for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < total;
        idx += int64_t(gridDim.x) * blockDim.x) {
     const int64_t r = idx / cn, c = idx % cn;
@@ -1540,6 +1566,15 @@ void truncation_factors(Ctx& c, const double* s, int64_t r, int64_t chi, double 
 
 __global__ void scale_columns_kernel(double* x, int64_t rows, int64_t cols, int64_t ld,
                                      const double* f) {
+  if (rows * cols < (int64_t(1) << 31)) {  // 32-bit decoding
+    const uint32_t uc = uint32_t(cols), total = uint32_t(rows * cols);
+    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += gridDim.x * blockDim.x) {
+      const uint32_t r = idx / uc, c = idx - r * uc;
+      x[int64_t(r) * ld + c] *= f[c];
+    }
+    return;
+  }
   for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < rows * cols;
        idx += int64_t(gridDim.x) * blockDim.x) {
     const int64_t r = idx / cols, c = idx % cols;
@@ -1641,7 +1676,7 @@ void jacobi_left_singular(Ctx& c, const float* Mc, int64_t q, double* Ub, double
       default: launch(jacobi_cluster_f32_kernel<8, kPairThreads>); break;
     }
     CTM_LAUNCH_CHECK();
-    sort_singular_kernel<<<1, 256, 0, c.stream>>>(Jc, norms, int(q), Ub, S, inv_s);
+    sort_singular_kernel<<<1, kSortThreads, 0, c.stream>>>(Jc, norms, int(q), Ub, S, inv_s);
     CTM_LAUNCH_CHECK();
     return;
   }
@@ -1670,7 +1705,7 @@ void jacobi_left_singular(Ctx& c, const float* Mc, int64_t q, double* Ub, double
         Mc, int(q), int(pp), Jc, norms, 40, 4e-6f, status_flags(c), Wg);
   }
   CTM_LAUNCH_CHECK();
-  sort_singular_kernel<<<1, 256, 0, c.stream>>>(Jc, norms, int(q), Ub, S, inv_s);
+  sort_singular_kernel<<<1, kSortThreads, 0, c.stream>>>(Jc, norms, int(q), Ub, S, inv_s);
   CTM_LAUNCH_CHECK();
 }
 
