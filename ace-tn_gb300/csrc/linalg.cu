@@ -1614,6 +1614,13 @@ __global__ void transpose_f32_kernel(const float* src, int q, float* dst) {
 }
 
 __global__ void scale_columns_f32_kernel(float* x, int64_t rows, int cols, const double* f) {
+  if (rows * cols < (int64_t(1) << 31)) {  // 32-bit decoding
+    const uint32_t total = uint32_t(rows * cols), uc = uint32_t(cols);
+    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += gridDim.x * blockDim.x)
+      x[idx] = float(double(x[idx]) * f[idx - (idx / uc) * uc]);
+    return;
+  }
   for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < rows * cols;
        idx += int64_t(gridDim.x) * blockDim.x)
     x[idx] = float(double(x[idx]) * f[idx % cols]);
