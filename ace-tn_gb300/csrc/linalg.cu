@@ -810,31 +810,55 @@ __global__ void __launch_bounds__(256) jacobi_cluster_f32_kernel(const float* Mc
 // inv_s[r] = 1 / S[r] (0 for a zero norm); order by descending norm.
 // One CTA (q <= 1024): the rank of every row norm (descending, ties by
 // index) from a shared-memory copy of the norms, then Ub[t][rank[j]] =
-// Jc[j][t] by all threads (each thread's copies independent: the row-per-
-// thread loop waited on one load at a time).
+// Jc[j][t].  With kStaged (q <= kSortStagedMax) Jc goes through shared
+// memory first and Ub is written row by row, contiguously (scattered
+// 8-byte stores of one CTA bound the direct form).
 constexpr int kSortThreads = 1024;
+constexpr int kSortStagedMax = 224;
+template <bool kStaged>
 __global__ void __launch_bounds__(kSortThreads) sort_singular_kernel(const float* Jc,
                                                                      const float* norms, int q,
                                                                      double* Ub, double* S,
                                                                      double* inv_s) {
+  extern __shared__ float jc_s[];  // kStaged: q rows of q + 1 floats
   __shared__ float s_norm[kSortThreads];
   __shared__ int s_rank[kSortThreads];
   for (int j = threadIdx.x; j < q; j += blockDim.x) s_norm[j] = norms[j];
+  if (kStaged)
+    for (int idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
+      const int j = idx / q, t = idx - j * q;
+      jc_s[j * (q + 1) + t] = Jc[idx];
+    }
   __syncthreads();
   for (int j = threadIdx.x; j < q; j += blockDim.x) {
     int rank = 0;
     const float nj = s_norm[j];
     for (int i = 0; i < q; ++i)
       if (s_norm[i] > nj || (s_norm[i] == nj && i < j)) ++rank;
-    s_rank[j] = rank;
+    if (kStaged) s_rank[rank] = j;  // the inverse permutation
+    else s_rank[j] = rank;
     S[rank] = double(nj);
     inv_s[rank] = nj > 0.f ? 1.0 / double(nj) : 0.0;
   }
   __syncthreads();
   for (int idx = threadIdx.x; idx < q * q; idx += blockDim.x) {
-    const int j = idx / q, t = idx - j * q;
-    Ub[size_t(t) * q + s_rank[j]] = double(Jc[idx]);
+    const int a = idx / q, b = idx - a * q;
+    if (kStaged) Ub[idx] = double(jc_s[s_rank[b] * (q + 1) + a]);  // Ub[a][b], row-major
+    else Ub[size_t(b) * q + s_rank[a]] = double(Jc[idx]);          // a = j, b = t
   }
+}
+
+void sort_singular(cudaStream_t st, const float* Jc, const float* norms, int64_t q, double* Ub,
+                   double* S, double* inv_s) {
+  if (q <= kSortStagedMax) {
+    const size_t smem = size_t(q) * (q + 1) * sizeof(float);
+    CTM_CUDA(cudaFuncSetAttribute(sort_singular_kernel<true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    sort_singular_kernel<true><<<1, kSortThreads, smem, st>>>(Jc, norms, int(q), Ub, S, inv_s);
+  } else {
+    sort_singular_kernel<false><<<1, kSortThreads, 0, st>>>(Jc, norms, int(q), Ub, S, inv_s);
+  }
+  CTM_LAUNCH_CHECK();
 }
 
 
@@ -1683,8 +1707,7 @@ void jacobi_left_singular(Ctx& c, const float* Mc, int64_t q, double* Ub, double
       default: launch(jacobi_cluster_f32_kernel<8, kPairThreads>); break;
     }
     CTM_LAUNCH_CHECK();
-    sort_singular_kernel<<<1, kSortThreads, 0, c.stream>>>(Jc, norms, int(q), Ub, S, inv_s);
-    CTM_LAUNCH_CHECK();
+    sort_singular(c.stream, Jc, norms, q, Ub, S, inv_s);
     return;
   }
   // FP32 dot products of length q carry ~sqrt(q) u relative error: 4e-6
@@ -1712,8 +1735,7 @@ void jacobi_left_singular(Ctx& c, const float* Mc, int64_t q, double* Ub, double
         Mc, int(q), int(pp), Jc, norms, 40, 4e-6f, status_flags(c), Wg);
   }
   CTM_LAUNCH_CHECK();
-  sort_singular_kernel<<<1, kSortThreads, 0, c.stream>>>(Jc, norms, int(q), Ub, S, inv_s);
-  CTM_LAUNCH_CHECK();
+  sort_singular(c.stream, Jc, norms, q, Ub, S, inv_s);
 }
 
 }  // namespace
